@@ -1,0 +1,314 @@
+"""Benchmark of the Gaussian kernel-sum hot path on one GB300 (or N replicas under torchrun).
+
+Workload (default): forward + full adjoint of a Gaussian kernel sum at N = M = 1e6, d = 3
+(the large kernel-sum sweep's biggest size): points from a mixture of 8 Gaussians (std 0.05,
+means ~ U[0.15, 0.85]^3, clipped to [0,1]), weights and adjoint seeds ~ N(0,1), sigma = 0.1,
+seed 3. One step = gbk_forward_adjoint: the target-side pass (Convolve + alpha-gradient, fused)
+and the source-side pass (dL/dy, dL/dw, fused), every pair's distance and exp recomputed.
+Metric: kernel pairs per second, pairs = N * M per step (each evaluated in both passes).
+
+Prints ONE JSON line (rank 0). `--impl reference` times the reference's CPU algorithm instead
+(the FP64 oracle restating ExactKernel; oracle/_ref when it was built on this host).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "kernel pairs/s fwd+adjoint"
+UNIT = "pairs/s"
+FLOPS_PER_PAIR_PASS = 27  # FP32 flops of one fused pass per pair (FMA = 2), see the design doc
+SMS = 152
+FP32_LANES = 128
+
+
+def make_workload(n: int, m: int, d: int = 3, seed: int = 3):
+    rng = np.random.default_rng(seed)
+    means = rng.uniform(0.15, 0.85, size=(8, d))
+
+    def pts(k):
+        comp = rng.integers(0, 8, size=k)
+        p = means[comp] + 0.05 * rng.standard_normal((k, d))
+        return np.clip(p, 0.0, 1.0)
+
+    x = pts(n)
+    y = pts(m)
+    w = rng.standard_normal((m, d))
+    a = rng.standard_normal((n, d))
+    return x, y, w, a
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks/throttle reasons every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = float(s[2])
+                for nm, v in zip(names, s[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except Exception:
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(sample: int, kind_pref: str = "port"):
+    """Times the FP64 oracle's forward+adjoint on a bounded sample (sample x sample pairs)."""
+    import oracle
+    kind = "port"
+    lib = None
+    if kind_pref == "reference":
+        try:
+            lib = oracle.load("reference")
+            kind = "reference"
+        except Exception:
+            lib = None
+    if lib is None:
+        lib = oracle.load("port")
+    x, y, w, a = make_workload(sample, sample, seed=33)
+    t0 = time.perf_counter()
+    lib.fwd_adjoint(x, y, w, 0.1, a)
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    if kind == "reference":
+        cores = 1  # the reference's ExactKernel is single-threaded per call
+    return {"value": sample * sample / dt, "unit": UNIT, "cores": cores,
+            "kind": "reference" if kind == "reference" else "port",
+            "sample": f"fwd+adjoint of {sample}x{sample} pairs (d=3, sigma=0.1), FP64, {dt:.2f} s"}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    sample = args.cpu_sample
+    x, y, w, a = make_workload(sample, sample, seed=33)
+    import oracle
+    lib = oracle.load("port")
+    kind = "port"
+    try:
+        lib = oracle.load("reference")
+        kind = "reference"
+    except Exception:
+        pass
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        lib.fwd_adjoint(x[:256], y[:256], w[:256], 0.1, a[:256])
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        lib.fwd_adjoint(x, y, w, 0.1, a)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times)
+    value = sample * sample / (ms / 1e3)
+    cores = 1 if kind == "reference" else int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"fwd+adjoint Gaussian kernel sum, bounded CPU sample {sample}x{sample}"
+                                   f" of the N=M=1e6 d=3 mixture workload", "d": 3, "dv": 3, "sigma": 0.1},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"{sample}x{sample} pairs per step, FP64"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000, help="targets = sources per step")
+    ap.add_argument("--sigma", type=float, default=0.1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=32768)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+
+    import torch
+    import deformetrica_code_gb300 as g
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    n = m = args.n
+    d = dv = 3
+    x, y, w, a = make_workload(n, m, seed=3 + rank)
+    dev = lambda arr: torch.from_numpy(arr).cuda()
+    X, Y, W, A = dev(x), dev(y), dev(w), dev(a)
+    V = torch.empty((n, dv), dtype=torch.float64, device="cuda")
+    GX = torch.empty((n, d), dtype=torch.float64, device="cuda")
+    GY = torch.empty((m, d), dtype=torch.float64, device="cuda")
+    GW = torch.empty((m, dv), dtype=torch.float64, device="cuda")
+    ctx = g.Context(local_rank)
+    lib = ctx.lib
+    stream = torch.cuda.current_stream()
+    lib.gbk_set_stream(ctx.h, ctypes.c_void_p(stream.cuda_stream))
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+    def step():
+        ctx.check(lib.gbk_forward_adjoint(ctx.h, d, dv, p(X), n, p(Y), p(W), m, args.sigma, p(A),
+                                          p(V), p(GX), p(GY), p(GW)))
+
+    def one_side():  # the dominant kernel alone: one fused target-side pass
+        ctx.check(lib.gbk_convolve_and_gradient_alpha(ctx.h, d, dv, p(X), n, p(Y), p(W), m,
+                                                      args.sigma, p(A), p(V), p(GX)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, L2 flushed between steps (outside the events) ----
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launch_count()
+    with ClockSampler(local_rank) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        launches = ctx.launch_count() - l0
+        step_ms = [s.elapsed_time(e) for s, e in evs]
+        # dominant kernel: one fused pass, averaged over launches
+        kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for s, e in kev:
+            flush.zero_()
+            s.record(stream)
+            one_side()
+            e.record(stream)
+        torch.cuda.synchronize()
+    kernel_ms = statistics.mean(s.elapsed_time(e) for s, e in kev)
+    ms = sum(step_ms) / len(step_ms)
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+        dist.barrier()
+
+    pairs = float(n) * m
+    value = pairs * world / (ms / 1e3)
+
+    # ---- end to end through the public API with pinned host buffers ----
+    pin = lambda arr: torch.from_numpy(arr).pin_memory()
+    hx, hy, hw, ha = pin(x), pin(y), pin(w), pin(a)
+    hv = torch.empty((n, dv), dtype=torch.float64).pin_memory()
+    hgx = torch.empty((n, d), dtype=torch.float64).pin_memory()
+    hgy = torch.empty((m, d), dtype=torch.float64).pin_memory()
+    hgw = torch.empty((m, dv), dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        ctx.check(lib.gbk_forward_adjoint(ctx.h, d, dv, p(hx), n, p(hy), p(hw), m, args.sigma, p(ha),
+                                          p(hv), p(hgx), p(hgy), p(hgw)))
+
+    e2e_step()
+    e2e_t = []
+    for _ in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        e2e_step()  # synchronous: returns with results in host memory
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+    h2d = 8 * (n * d + m * d + m * dv + n * dv)
+    d2h = 8 * (n * dv + n * d + m * d + m * dv)
+
+    clocks = clk.summary()
+    sm_mhz = clocks["sm_mhz"] or 2070.0
+    peak_tflops = SMS * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
+    achieved = FLOPS_PER_PAIR_PASS * pairs / (kernel_ms / 1e3) / 1e12
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32c", "data": "synthetic",
+            "config": {"workload": f"fwd+adjoint Gaussian kernel sum N=M={n} d=3 dv=3 sigma={args.sigma}"
+                                   " (8-Gaussian mixture, std 0.05, seed 3)",
+                       "N": n, "M": m, "d": d, "dv": dv, "sigma": args.sigma,
+                       "pairs_per_step": pairs, "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": f"replicas{world}"},
+            "gpu_launches": launches,
+            "e2e": {"value": pairs * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+                         "frac": achieved / peak_tflops, "traffic": None,
+                         "kernel": "pair_kernel<OpConvGradAlpha<3,3,true>, float> (one fused pass)",
+                         "kernel_ms": kernel_ms,
+                         "peak_source": f"nominal FP32 {SMS} SMs x {FP32_LANES} lanes x 2 flops x median sampled SM clock {sm_mhz:.0f} MHz"},
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,13 @@
+"""GB300-native Gaussian kernel sums for Deformetrica (sm_103a CUDA behind a C ABI).
+
+The compute path is libgbkernel.so (include/gbk.h). Importing this package loads it and raises
+if it has not been built: there is no CPU or PyTorch fallback.
+"""
+from . import _lib
+from ._lib import GBKError, GBK_MODE_F32C, GBK_MODE_F64
+
+_lib.load()
+
+from .kernel import Context, GB300ExactKernel  # noqa: E402
+
+__all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64"]

@@ -1,0 +1,103 @@
+"""ctypes binding of libgbkernel.so (declared in include/gbk.h).
+
+The library is the only compute path: if it is missing this module raises at import time.
+There is no CPU or PyTorch fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbkernel.so")
+
+GBK_OK = 0
+GBK_ERR_ARG = 1
+GBK_ERR_UNSUPPORTED = 2
+GBK_ERR_CUDA = 3
+GBK_ERR_ALLOC = 4
+GBK_ERR_TIMEOUT = 5
+GBK_ERR_STATE = 6
+
+GBK_MODE_F32C = 0
+GBK_MODE_F64 = 1
+
+OPS = {
+    "convolve": 0,
+    "convolve_gradient_alpha_fused": 1,
+    "gradient_alpha": 2,
+    "gradient_varlin": 3,
+    "gradient_dim": 4,
+    "hessian": 5,
+    "hessian_rowcol": 6,
+    "special_hessian": 7,
+}
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_L = ctypes.c_long
+_D = ctypes.c_double
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "gbk_version": (_I, []),
+    "gbk_create": (_I, [_I, ctypes.POINTER(_P)]),
+    "gbk_destroy": (None, [_P]),
+    "gbk_last_error": (ctypes.c_char_p, [_P]),
+    "gbk_set_stream": (_I, [_P, _P]),
+    "gbk_get_stream": (_P, [_P]),
+    "gbk_set_mode": (_I, [_P, _I]),
+    "gbk_get_mode": (_I, [_P]),
+    "gbk_synchronize": (_I, [_P]),
+    "gbk_launch_count": (ctypes.c_longlong, [_P]),
+    "gbk_convolve": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P]),
+    "gbk_convolve_gradient_alpha": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P]),
+    "gbk_convolve_and_gradient_alpha": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P]),
+    "gbk_convolve_gradient": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P]),
+    "gbk_convolve_gradient_dim": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _I, _P]),
+    "gbk_convolve_gradient_kdp": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _I, _I, _P]),
+    "gbk_convolve_hessian": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P]),
+    "gbk_convolve_hessian_rowcol": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _I, _I, _P]),
+    "gbk_convolve_hessian_kdpdq": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _I, _I, _I, _P]),
+    "gbk_convolve_special_hessian": (_I, [_P, _I, _P, _P, _L, _D, _P, _P]),
+    "gbk_forward_adjoint": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P, _P]),
+    "gbk_kernel_norm": (_I, [_P, _I, _I, _P, _P, _L, _D, _P]),
+    "gbk_autotune": (_I, [_P, _I, _I, _I, _L, _L, _D]),
+    "gbk_tune_save": (_I, [_P, ctypes.c_char_p]),
+    "gbk_tune_load": (_I, [_P, ctypes.c_char_p]),
+    "gbk_set_split": (_I, [_P, _I]),
+}
+
+_lib = None
+
+
+def exported_symbols() -> list[str]:
+    return sorted(SIGNATURES)
+
+
+def load(path: str | None = None) -> ctypes.CDLL:
+    """Loads libgbkernel.so and declares every signature. Raises if the library is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(the CUDA library is the only implementation; there is no fallback)")
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class GBKError(RuntimeError):
+    """A failed library call (the reference throws std::runtime_error for the same cases)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[gbk error {code}] {msg}")
+        self.code = code

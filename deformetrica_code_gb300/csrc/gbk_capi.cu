@@ -1,0 +1,678 @@
+// C ABI of libgbkernel.so: contexts, argument checks, host/device pointer staging, column
+// chunking, the source-split heuristic and the autotuner. The entry points are declared (with
+// the reference method each replaces) in include/gbk.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/gbk.h"
+#include "gbk_ctx.h"
+#include "gbk_dispatch.h"
+
+using namespace gbk;
+
+// =============================================================================================
+// kernel table
+// =============================================================================================
+namespace gbk {
+
+int op_outputs(int op, int d, int dv) {
+  switch (op) {
+    case OP_CONV: return dv;
+    case OP_CONV_GRADA: return dv + d;
+    case OP_GRADA: return d;
+    case OP_VARLIN: return dv * d;
+    case OP_GRADDIM: return dv;
+    case OP_HESSFULL: return dv * (d * (d + 1) / 2 + 1);
+    case OP_HESSRC: return 2 * dv;
+    case OP_SPECIAL: return 2 * d;
+  }
+  return 0;
+}
+
+bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
+  switch (op) {
+    case OP_CONV:
+    case OP_CONV_GRADA:
+    case OP_GRADA: return find_kernel_conv(op, mode, d, dv, variant, e);
+    case OP_VARLIN:
+    case OP_GRADDIM: return find_kernel_grad(op, mode, d, dv, variant, e);
+    case OP_HESSFULL:
+    case OP_HESSRC:
+    case OP_SPECIAL: return find_kernel_hess(op, mode, d, dv, variant, e);
+  }
+  return false;
+}
+
+int num_variants(int op, int mode, int d, int dv) {
+  bool hot_op = op == OP_CONV || op == OP_CONV_GRADA || op == OP_GRADA;
+  bool hot_shape = (d == 3 && dv == 3) || (d == 2 && dv == 2);
+  return (mode == MODE_F32C && hot_op && hot_shape) ? 4 : 1;
+}
+
+const int *supported_dv(int d, int *count) {
+  static const int dv2[] = {4, 3, 2, 1};
+  static const int dv3[] = {6, 3, 2, 1};
+  *count = 4;
+  return d == 2 ? dv2 : dv3;
+}
+
+}  // namespace gbk
+
+// =============================================================================================
+// context helpers
+// =============================================================================================
+int gbk_ctx::fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  err = buf;
+  return code;
+}
+
+int gbk_ctx::cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return GBK_OK;
+  cudaGetLastError();
+  return fail(e == cudaErrorMemoryAllocation ? GBK_ERR_ALLOC : GBK_ERR_CUDA, "%s: %s", what,
+              cudaGetErrorString(e));
+}
+
+bool gbk_ctx::capturing() const {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &st) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return st != cudaStreamCaptureStatusNone;
+}
+
+int gbk_ctx::ensure(DevBuf &b, size_t bytes, const char *what) {
+  if (b.cap >= bytes) return GBK_OK;
+  if (capturing())
+    return fail(GBK_ERR_STATE, "%s: needs %zu bytes of device scratch while the stream is being captured; "
+                "run the call once before capture", what, bytes);
+  if (b.p) {
+    int rc = cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    if (rc) return rc;
+    cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  size_t want = std::max(bytes, b.cap + b.cap / 2);
+  want = (want + 255) & ~(size_t)255;
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&p, bytes);
+    want = bytes;
+  }
+  if (e != cudaSuccess) return cuda(e, what);
+  b.p = p;
+  b.cap = want;
+  return GBK_OK;
+}
+
+static bool is_device_pointer(const void *p) {
+  if (!p) return true;
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Stages host arguments through the context's device buffers.
+struct HostIO {
+  gbk_ctx *c;
+  int slot = 0;
+  int rc = GBK_OK;
+  bool any_host = false;
+  struct Out {
+    double *host;
+    double *dev;
+    size_t n;
+  };
+  std::vector<Out> outs;
+  explicit HostIO(gbk_ctx *ctx) : c(ctx) {}
+
+  const double *in(const double *p, size_t n, const char *name) {
+    if (rc || !p || n == 0 || is_device_pointer(p)) return p;
+    any_host = true;
+    if (slot >= gbk_ctx::kStageSlots) {
+      rc = c->fail(GBK_ERR_ARG, "too many host arguments");
+      return nullptr;
+    }
+    gbk_ctx::DevBuf &b = c->stage[slot++];
+    rc = c->ensure(b, n * sizeof(double), name);
+    if (rc) return nullptr;
+    rc = c->cuda(cudaMemcpyAsync(b.p, p, n * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+                 "cudaMemcpyAsync H2D");
+    return rc ? nullptr : (const double *)b.p;
+  }
+  double *out(double *p, size_t n, const char *name) {
+    if (rc || !p || n == 0 || is_device_pointer(p)) return p;
+    any_host = true;
+    if (slot >= gbk_ctx::kStageSlots) {
+      rc = c->fail(GBK_ERR_ARG, "too many host arguments");
+      return nullptr;
+    }
+    gbk_ctx::DevBuf &b = c->stage[slot++];
+    rc = c->ensure(b, n * sizeof(double), name);
+    if (rc) return nullptr;
+    outs.push_back({p, (double *)b.p, n});
+    return (double *)b.p;
+  }
+  int finish() {
+    if (rc) return rc;
+    for (auto &o : outs) {
+      rc = c->cuda(cudaMemcpyAsync(o.host, o.dev, o.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                   "cudaMemcpyAsync D2H");
+      if (rc) return rc;
+    }
+    if (any_host) rc = c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    return rc;
+  }
+};
+
+// Tuning-table key: operation, precision, shape and size buckets (powers of two).
+static int bucket(long n) {
+  int b = 0;
+  while (n > 1) {
+    n >>= 1;
+    ++b;
+  }
+  return b;
+}
+
+gbk_ctx::TuneKey gbk_ctx::key(int op, int d, int dv, long nx, long ny) const {
+  return TuneKey{op, mode, d, dv, bucket(nx), bucket(ny)};
+}
+
+int gbk_ctx::occupancy(const KernelEntry &e, int) {
+  auto it = occ_cache.find(e.kernel);
+  if (it != occ_cache.end()) return it->second;
+  int blocks = 0;
+  if (e.smem > 48 * 1024)
+    cudaFuncSetAttribute(e.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, e.kernel, e.block, e.smem) != cudaSuccess)
+    blocks = 1;
+  cudaGetLastError();
+  if (blocks < 1) blocks = 1;
+  occ_cache[e.kernel] = blocks;
+  return blocks;
+}
+
+// Source splits: enough CTAs to fill every SM with a small tail, each split >= 2 source tiles.
+int gbk_ctx::choose_split(const KernelEntry &e, int d, long nx, long ny) {
+  if (force_split > 0) return force_split;
+  long per_cta = (long)e.block * e.r;
+  long itiles = (nx + per_cta - 1) / per_cta;
+  long slots = (long)num_sms * occupancy(e, d);
+  long max_split = std::max(1L, ny / (2L * e.tj));
+  max_split = std::min(max_split, 64L);
+  // partial buffer limit: 512 MiB
+  long cap = std::max(1L, (long)((512L << 20) / (8L * e.no * std::max(nx, 1L))));
+  max_split = std::min(max_split, cap);
+  double best = 1e300;
+  int best_s = 1;
+  for (long s = 1; s <= max_split; ++s) {
+    long ctas = itiles * s;
+    double waves = std::ceil((double)ctas / (double)slots);
+    double t = waves / (double)s + 0.002 * s;  // per-CTA work ~ 1/s, small per-split overhead
+    if (t < best - 1e-9) {
+      best = t;
+      best_s = (int)s;
+    }
+  }
+  return best_s;
+}
+
+int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
+  int variant = 0, ns = 0;
+  auto it = tune.find(key(op, d, dv, a.nx, a.ny));
+  if (it != tune.end()) {
+    variant = it->second.first;
+    ns = it->second.second;
+  }
+  KernelEntry e;
+  if (!find_kernel(op, mode, d, dv, variant, &e) && !find_kernel(op, mode, d, dv, 0, &e))
+    return fail(GBK_ERR_UNSUPPORTED, "no kernel for op %d, d=%d, dv=%d", op, d, dv);
+  if (force_split > 0) ns = force_split;
+  if (ns <= 0) ns = choose_split(e, d, a.nx, a.ny);
+  if (ns > 1) {
+    // launch_pairs rounds the split count; size the buffer for the requested count
+    int rc = ensure(partial, (size_t)ns * e.no * std::max(a.nx, 1L) * sizeof(double), "split partials");
+    if (rc) return rc;
+    a.partial = (double *)partial.p;
+  }
+  int rc = cuda(e.fn(a, ns, stream), "kernel launch");
+  if (rc) return rc;
+  launches += (ns > 1) ? 2 : 1;
+  return GBK_OK;
+}
+
+// Splits dv weight columns into compiled chunk widths (largest first).
+static std::vector<std::pair<int, int>> column_chunks(int d, int dv) {
+  int cnt;
+  const int *sup = supported_dv(d, &cnt);
+  std::vector<std::pair<int, int>> ch;
+  int c0 = 0, rem = dv;
+  while (rem > 0) {
+    for (int k = 0; k < cnt; ++k)
+      if (sup[k] <= rem) {
+        ch.push_back({c0, sup[k]});
+        c0 += sup[k];
+        rem -= sup[k];
+        break;
+      }
+  }
+  return ch;
+}
+
+static double clamp_sigma(double s) { return s < 1e-10 ? 1e-10 : s; }  // AbstractKernel.h:87-89
+
+#define GBK_GUARD(ctx)                                                     \
+  do {                                                                     \
+    if (!(ctx)) return GBK_ERR_ARG;                                        \
+    (ctx)->err.clear();                                                    \
+    if (cudaSetDevice((ctx)->device) != cudaSuccess) {                     \
+      cudaGetLastError();                                                  \
+      return (ctx)->fail(GBK_ERR_CUDA, "cudaSetDevice(%d)", (ctx)->device); \
+    }                                                                      \
+  } while (0)
+
+static int check_common(gbk_ctx *c, int d, int dv, long nx, long ny, double sigma) {
+  if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d not supported (2 or 3)", d);
+  if (dv <= 0) return c->fail(GBK_ERR_ARG, "weights need at least one column (dv=%d)", dv);
+  if (nx < 0 || ny < 0) return c->fail(GBK_ERR_ARG, "negative row count");
+  if (!(sigma == sigma)) return c->fail(GBK_ERR_ARG, "kernel width is NaN");
+  if (nx > (1L << 31) || ny > (1L << 31)) return c->fail(GBK_ERR_ARG, "row count above 2^31");
+  return GBK_OK;
+}
+
+static PairArgs base_args(long nx, long ny, double sigma) {
+  PairArgs a;
+  memset(&a, 0, sizeof a);
+  a.nx = nx;
+  a.ny = ny;
+  a.sigma = clamp_sigma(sigma);
+  a.nsplit = 1;
+  return a;
+}
+
+// Runs a weight-linear op over column chunks. out0 per-column stride `ocol` (elements per weight
+// column in one output row) and row stride dv*ocol; out1 (gradient) accumulates over chunks.
+static int run_chunked(gbk_ctx *c, int op, int d, int dv, PairArgs a, const double *w,
+                       const double *alpha, double *out0, int ocol, double *out1) {
+  auto ch = column_chunks(d, dv);
+  for (size_t q = 0; q < ch.size(); ++q) {
+    int c0 = ch[q].first, cw = ch[q].second;
+    PairArgs b = a;
+    b.w = w + c0;
+    b.w_ld = dv;
+    if (alpha) {
+      b.ta = alpha + c0;
+      b.ta_ld = dv;
+    }
+    b.out0 = out0 ? out0 + (long)c0 * ocol : nullptr;
+    b.out0_ld = dv * ocol;
+    b.out1 = out1;
+    b.out1_ld = d;
+    b.acc0 = 0;
+    b.acc1 = q > 0 ? 1 : 0;
+    int rc = c->launch(op, d, cw, b);
+    if (rc) return rc;
+  }
+  return GBK_OK;
+}
+
+// =============================================================================================
+// entry points
+// =============================================================================================
+extern "C" {
+
+int gbk_version(void) { return 10000; }
+
+static thread_local std::string g_create_err;
+
+int gbk_create(int device, gbk_ctx **out) {
+  if (!out) return GBK_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    g_create_err = "no CUDA device " + std::to_string(device);
+    return GBK_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    cudaGetLastError();
+    return GBK_ERR_CUDA;
+  }
+  gbk_ctx *c = new gbk_ctx();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return GBK_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  *out = c;
+  return GBK_OK;
+}
+
+void gbk_destroy(gbk_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->release();
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  cudaGetLastError();
+  delete c;
+}
+
+const char *gbk_last_error(const gbk_ctx *c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+int gbk_set_stream(gbk_ctx *c, void *stream) {
+  if (!c) return GBK_ERR_ARG;
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return GBK_OK;
+}
+
+void *gbk_get_stream(const gbk_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int gbk_set_mode(gbk_ctx *c, int mode) {
+  if (!c) return GBK_ERR_ARG;
+  if (mode != GBK_MODE_F32C && mode != GBK_MODE_F64) return c->fail(GBK_ERR_ARG, "unknown mode %d", mode);
+  c->mode = mode;
+  return GBK_OK;
+}
+
+int gbk_get_mode(const gbk_ctx *c) { return c ? c->mode : -1; }
+
+int gbk_synchronize(gbk_ctx *c) {
+  GBK_GUARD(c);
+  return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+}
+
+long long gbk_launch_count(const gbk_ctx *c) { return c ? c->launches : 0; }
+
+int gbk_set_split(gbk_ctx *c, int nsplit) {
+  if (!c || nsplit < 0) return GBK_ERR_ARG;
+  c->force_split = nsplit;
+  return GBK_OK;
+}
+
+int gbk_convolve(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                 const double *w, long ny, double sigma, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  double *dout = io.out(out, (size_t)nx * dv, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  if (int rc = run_chunked(c, OP_CONV, d, dv, a, dw, nullptr, dout, 1, nullptr)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_gradient_alpha(gbk_ctx *c, int d, int dv, const double *x, long nx,
+                                const double *y, const double *w, long ny, double sigma,
+                                const double *alpha, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if ((nx && (!x || !out || !alpha)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  const double *da = io.in(alpha, (size_t)nx * dv, "alpha");
+  double *dout = io.out(out, (size_t)nx * d, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  if (int rc = run_chunked(c, OP_GRADA, d, dv, a, dw, da, nullptr, 1, dout)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_and_gradient_alpha(gbk_ctx *c, int d, int dv, const double *x, long nx,
+                                    const double *y, const double *w, long ny, double sigma,
+                                    const double *alpha, double *out_v, double *out_g) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if ((nx && (!x || !out_v || !out_g || !alpha)) || (ny && (!y || !w)))
+    return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  const double *da = io.in(alpha, (size_t)nx * dv, "alpha");
+  double *dv_ = io.out(out_v, (size_t)nx * dv, "out_v");
+  double *dg = io.out(out_g, (size_t)nx * d, "out_g");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  if (int rc = run_chunked(c, OP_CONV_GRADA, d, dv, a, dw, da, dv_, 1, dg)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_gradient(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                          const double *w, long ny, double sigma, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  double *dout = io.out(out, (size_t)nx * dv * d, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  if (int rc = run_chunked(c, OP_VARLIN, d, dv, a, dw, nullptr, dout, d, nullptr)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_gradient_dim(gbk_ctx *c, int d, int dv, const double *x, long nx,
+                              const double *y, const double *w, long ny, double sigma, int dim,
+                              double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if (dim < 0 || dim >= d) return c->fail(GBK_ERR_ARG, "dimension index out of bounds");
+  if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  double *dout = io.out(out, (size_t)nx * dv, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  a.p0 = dim;
+  if (int rc = run_chunked(c, OP_GRADDIM, d, dv, a, dw, nullptr, dout, 1, nullptr)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_gradient_kdp(gbk_ctx *c, int d, int dv, const double *x, long nx,
+                              const double *y, const double *w, long ny, double sigma, int k,
+                              int dp, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if (k < 0 || k >= dv) return c->fail(GBK_ERR_ARG, "Invalid weight index");
+  if (dp < 0 || dp >= d) return c->fail(GBK_ERR_ARG, "Invalid derivative direction");
+  if (nx < ny)
+    return c->fail(GBK_ERR_ARG, "ConvolveGradient(X,k,dp) reads ny=%ld rows of X, which has %ld", ny, nx);
+  if (ny && (!x || !y || !w || !out)) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)ny * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  double *dout = io.out(out, (size_t)ny, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(ny, ny, sigma);  // the reference's target loop runs over ny rows
+  a.x = dx;
+  a.y = dy;
+  a.p0 = dp;
+  a.w = dw + k;
+  a.w_ld = dv;
+  a.out0 = dout;
+  a.out0_ld = 1;
+  if (int rc = c->launch(OP_GRADDIM, d, 1, a)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_hessian(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                         const double *w, long ny, double sigma, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  double *dout = io.out(out, (size_t)nx * dv * d * d, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  if (int rc = run_chunked(c, OP_HESSFULL, d, dv, a, dw, nullptr, dout, d * d, nullptr)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_hessian_rowcol(gbk_ctx *c, int d, int dv, const double *x, long nx,
+                                const double *y, const double *w, long ny, double sigma, int row,
+                                int col, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if (row < 0 || col < 0 || row >= d || col >= d) return c->fail(GBK_ERR_ARG, "Dimension index out of bounds");
+  if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  double *dout = io.out(out, (size_t)nx * dv, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  a.p0 = row;
+  a.p1 = col;
+  if (int rc = run_chunked(c, OP_HESSRC, d, dv, a, dw, nullptr, dout, 1, nullptr)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_hessian_kdpdq(gbk_ctx *c, int d, int dv, const double *x, long nx,
+                               const double *y, const double *w, long ny, double sigma, int k,
+                               int dp, int dq, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if (k < 0 || k >= dv) return c->fail(GBK_ERR_ARG, "Invalid weight index");
+  if (dp < 0 || dq < 0 || dp >= d || dq >= d) return c->fail(GBK_ERR_ARG, "Invalid derivative direction");
+  if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  double *dout = io.out(out, (size_t)nx, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(nx, ny, sigma);
+  a.x = dx;
+  a.y = dy;
+  a.p0 = dp;
+  a.p1 = dq;
+  a.w = dw + k;
+  a.w_ld = dv;
+  a.out0 = dout;
+  a.out0_ld = 1;
+  if (int rc = c->launch(OP_HESSRC, d, 1, a)) return rc;
+  return io.finish();
+}
+
+int gbk_convolve_special_hessian(gbk_ctx *c, int d, const double *y, const double *w, long n,
+                                 double sigma, const double *xi, double *out) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, d, n, n, sigma)) return rc;
+  if (n && (!y || !w || !xi || !out)) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dy = io.in(y, (size_t)n * d, "y");
+  const double *dw = io.in(w, (size_t)n * d, "w");
+  const double *dxi = io.in(xi, (size_t)n * d, "xi");
+  double *dout = io.out(out, (size_t)n * d, "out");
+  if (io.rc) return io.rc;
+  PairArgs a = base_args(n, n, sigma);
+  a.x = dy;
+  a.ta = dw;
+  a.ta_ld = d;
+  a.tb = dxi;
+  a.tb_ld = d;
+  a.y = dy;
+  a.w = dw;
+  a.w_ld = d;
+  a.sb = dxi;
+  a.sb_ld = d;
+  a.out0 = dout;
+  a.out0_ld = d;
+  if (int rc = c->launch(OP_SPECIAL, d, d, a)) return rc;
+  return io.finish();
+}
+
+int gbk_forward_adjoint(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                        const double *w, long ny, double sigma, const double *alpha, double *v,
+                        double *gx, double *gy, double *gw) {
+  GBK_GUARD(c);
+  if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
+  if ((nx && !x) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
+  if ((gx || gy || gw) && nx && !alpha) return c->fail(GBK_ERR_ARG, "alpha is required for the adjoint");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  const double *da = io.in(alpha, (size_t)nx * dv, "alpha");
+  double *dvv = io.out(v, (size_t)nx * dv, "v");
+  double *dgx = io.out(gx, (size_t)nx * d, "gx");
+  double *dgy = io.out(gy, (size_t)ny * d, "gy");
+  double *dgw = io.out(gw, (size_t)ny * dv, "gw");
+  if (io.rc) return io.rc;
+  // target side: v = K w and gx (alpha-weighted gradient), one pass
+  if (dvv || dgx) {
+    PairArgs a = base_args(nx, ny, sigma);
+    a.x = dx;
+    a.y = dy;
+    int op = (dvv && dgx) ? OP_CONV_GRADA : (dgx ? OP_GRADA : OP_CONV);
+    if (int rc = run_chunked(c, op, d, dv, a, dw, op == OP_CONV ? nullptr : da, dvv, 1, dgx)) return rc;
+  }
+  // source side: roles swapped (targets y with "alpha" w, sources x with weights alpha)
+  if (dgy || dgw) {
+    PairArgs a = base_args(ny, nx, sigma);
+    a.x = dy;
+    a.y = dx;
+    int op = (dgw && dgy) ? OP_CONV_GRADA : (dgy ? OP_GRADA : OP_CONV);
+    if (int rc = run_chunked(c, op, d, dv, a, da, op == OP_CONV ? nullptr : dw, dgw, 1, dgy)) return rc;
+  }
+  return io.finish();
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// Device-side building blocks shared by every Gaussian kernel-sum kernel.
+//
+// Precision model. The bulk arithmetic runs in FP32 on *pairs of targets* packed in float2 and
+// issued as Blackwell's packed FP32 instructions (FADD2/FMUL2/FFMA2 through the __fadd2_rn /
+// __fmul2_rn / __ffma2_rn builtins), so one instruction advances two kernel pairs. exp is
+// evaluated on the MUFU unit as 2^(r2 * c) with c = -log2(e)/sigma^2 (ex2.approx.ftz.f32): the
+// identity e^-a = 2^(-a log2 e). Each target accumulates a short run of sources in plain FP32 and
+// then folds the run into a (sum, compensation) pair with an error-free TwoSum, so the
+// compensation costs a few instructions per run rather than per pair. The FP64 mode uses the same
+// kernels with double lanes, libm-equivalent exp() and no compensation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbk {
+
+// ---------------------------------------------------------------------------------------------
+// Lane types: Lane<float> carries two targets (float2), Lane<double> one target.
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+struct Lane;
+
+template <>
+struct Lane<float> {
+  typedef float2 V;
+  static constexpr int kWidth = 2;
+  __device__ __forceinline__ static V add(V a, V b) { return __fadd2_rn(a, b); }
+  // a - b as one packed FMA with -1 (exact product, single rounding): there is no packed FSUB.
+  __device__ __forceinline__ static V sub(V a, V b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+  __device__ __forceinline__ static V mul(V a, V b) { return __fmul2_rn(a, b); }
+  __device__ __forceinline__ static V fma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
+  __device__ __forceinline__ static V zero() { return make_float2(0.f, 0.f); }
+  __device__ __forceinline__ static V splat(float s) { return make_float2(s, s); }
+  // 2^t per lane on the MUFU unit (t <= 0 here; results below 2^-126 flush to zero).
+  __device__ __forceinline__ static V exp2v(V t) {
+    float a, b;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(t.x));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(b) : "f"(t.y));
+    return make_float2(a, b);
+  }
+  __device__ __forceinline__ static float get(V v, int l) { return l == 0 ? v.x : v.y; }
+  __device__ __forceinline__ static V make(float a, float b) { return make_float2(a, b); }
+};
+
+template <>
+struct Lane<double> {
+  typedef double V;
+  static constexpr int kWidth = 1;
+  __device__ __forceinline__ static V add(V a, V b) { return __dadd_rn(a, b); }
+  __device__ __forceinline__ static V sub(V a, V b) { return __dsub_rn(a, b); }
+  __device__ __forceinline__ static V mul(V a, V b) { return __dmul_rn(a, b); }
+  __device__ __forceinline__ static V fma(V a, V b, V c) { return __fma_rn(a, b, c); }
+  __device__ __forceinline__ static V zero() { return 0.0; }
+  __device__ __forceinline__ static V splat(double s) { return s; }
+  // In FP64 mode the exponent argument is -r2/sigma^2 (natural base), evaluated with exp().
+  __device__ __forceinline__ static V exp2v(V t) { return exp(t); }
+  __device__ __forceinline__ static double get(V v, int) { return v; }
+};
+
+// Source values are stored in shared memory already broadcast to the lane type.
+template <typename T>
+struct SrcVal;
+template <>
+struct SrcVal<float> {
+  __device__ __forceinline__ static float2 make(double v) {
+    float f = (float)v;
+    return make_float2(f, f);
+  }
+};
+template <>
+struct SrcVal<double> {
+  __device__ __forceinline__ static double make(double v) { return v; }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Compensated accumulation: (sum, comp) += run, with Knuth's error-free TwoSum.
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+struct Comp {
+  typedef typename Lane<T>::V V;
+  __device__ __forceinline__ static void fold(V &sum, V &comp, V run) {
+    typedef Lane<T> L;
+    V s = L::add(sum, run);
+    V bb = L::sub(s, sum);
+    V err = L::add(L::sub(sum, L::sub(s, bb)), L::sub(run, bb));
+    comp = L::add(comp, err);
+    sum = s;
+  }
+};
+template <>
+struct Comp<double> {
+  __device__ __forceinline__ static void fold(double &sum, double &, double run) { sum += run; }
+};
+
+// Scale factor that turns r2 into the exp argument for the lane type.
+template <typename T>
+__host__ __device__ inline T exp_arg_scale(double sigma);
+template <>
+__host__ __device__ inline float exp_arg_scale<float>(double sigma) {
+  return (float)(-1.4426950408889634 / (sigma * sigma));  // -log2(e) / sigma^2
+}
+template <>
+__host__ __device__ inline double exp_arg_scale<double>(double sigma) {
+  return -1.0 / (sigma * sigma);
+}
+
+// Bounded-iteration helpers for any cross-block wait (none of the kernel-sum kernels wait).
+constexpr unsigned long long kSpinLimit = 1ull << 26;
+
+}  // namespace gbk

@@ -1,0 +1,62 @@
+// The context behind the opaque gbk_ctx handle of include/gbk.h.
+//
+// It replaces the legacy CUDA path's per-call cudaMalloc / cudaMemcpy / cudaFree
+// (lib/cuda_convolutions/GpuConv1D.cu:97-130): device buffers live as long as the context and
+// only grow, the stream is the caller's choice, and every CUDA status is checked.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <utility>
+
+#include "gbk_dispatch.h"
+
+struct gbk_ctx {
+  struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+  };
+  static constexpr int kStageSlots = 12;
+
+  int device = 0;
+  int num_sms = 1;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  int mode = 0;         // GBK_MODE_F32C / GBK_MODE_F64
+  int force_split = 0;  // 0 = automatic
+  long long launches = 0;
+  std::string err;
+
+  DevBuf partial;             // source-split partial sums
+  DevBuf stage[kStageSlots];  // host-argument staging
+  DevBuf reduce;              // FP64 reductions and small temporaries
+  DevBuf tmp;                 // op temporaries (e.g. K w for the kernel norm)
+
+  typedef std::tuple<int, int, int, int, int, int> TuneKey;  // op, mode, d, dv, log2 nx, log2 ny
+  std::map<TuneKey, std::pair<int, int>> tune;                // -> (variant, nsplit)
+  std::map<const void *, int> occ_cache;
+
+  int fail(int code, const char *fmt, ...);
+  int cuda(cudaError_t e, const char *what);
+  bool capturing() const;
+  int ensure(DevBuf &b, size_t bytes, const char *what);
+  TuneKey key(int op, int d, int dv, long nx, long ny) const;
+  int occupancy(const gbk::KernelEntry &e, int d);
+  int choose_split(const gbk::KernelEntry &e, int d, long nx, long ny);
+  int launch(int op, int d, int dv, gbk::PairArgs a);
+
+  void release() {
+    auto fr = [](DevBuf &b) {
+      if (b.p) cudaFree(b.p);
+      b.p = nullptr;
+      b.cap = 0;
+    };
+    fr(partial);
+    fr(reduce);
+    fr(tmp);
+    for (auto &b : stage) fr(b);
+  }
+};

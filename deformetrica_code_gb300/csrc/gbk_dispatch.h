@@ -1,0 +1,69 @@
+// Host-side table of compiled kernel-sum kernels: (operation, precision, d, dv, variant) ->
+// launcher. The instantiations live in gbk_k_conv.cu, gbk_k_grad.cu and gbk_k_hess.cu so that
+// the build compiles them in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gbk_pairs.cuh"
+
+namespace gbk {
+
+enum OpId {
+  OP_CONV = 0,       // Convolve
+  OP_CONV_GRADA = 1, // Convolve + ConvolveGradient(X, alpha), one pass
+  OP_GRADA = 2,      // ConvolveGradient(X, alpha)
+  OP_VARLIN = 3,     // ConvolveGradient(X)
+  OP_GRADDIM = 4,    // ConvolveGradient(X, dim)   (p0 = dim)
+  OP_HESSFULL = 5,   // ConvolveHessian(X)
+  OP_HESSRC = 6,     // ConvolveHessian(X, row, col) (p0 = row, p1 = col)
+  OP_SPECIAL = 7,    // ConvolveSpecialHessian(xi)
+  OP_COUNT = 8
+};
+
+enum Mode { MODE_F32C = 0, MODE_F64 = 1 };
+
+typedef cudaError_t (*LaunchFn)(PairArgs, int, cudaStream_t);
+
+struct KernelEntry {
+  LaunchFn fn;
+  const void *kernel;  // the pair kernel (for occupancy queries)
+  int block;  // threads per CTA
+  int r;      // targets per thread
+  int tj;     // sources per shared-memory tile
+  int no;     // accumulators per target (partial-buffer width)
+  int smem;   // dynamic shared memory bytes per CTA
+};
+
+// Accumulators per target of an op (the partial buffer holds nsplit * no * nx doubles).
+int op_outputs(int op, int d, int dv);
+
+// Fills *e and returns true when the combination is compiled. dv must be one of the compiled
+// column counts (see supported_dv); the host splits other counts into chunks.
+bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e);
+int num_variants(int op, int mode, int d, int dv);
+
+// Compiled weight-column counts for dimension d, largest first (used to chunk any dv).
+const int *supported_dv(int d, int *count);
+
+// Per-family lookups (one per instantiation file).
+bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e);
+bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e);
+bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry *e);
+
+}  // namespace gbk
+
+namespace gbk {
+// Helper for the instantiation files: records one compiled (op, T, D, BLOCK, R, TJ, MERGE).
+template <class OpT, typename T, int D, int BLOCK, int R, int TJ, int MERGE>
+inline bool set_entry(KernelEntry *e) {
+  e->fn = &launch_pairs<OpT, T, D, BLOCK, R, TJ, MERGE>;
+  e->kernel = (const void *)&pair_kernel<OpT, T, D, BLOCK, R, TJ, MERGE>;
+  e->block = BLOCK;
+  e->r = R;
+  e->tj = TJ;
+  e->no = OpT::NO;
+  e->smem = (int)(TJ * Rec<OpT, D>::NJP * sizeof(typename SrcLane<T>::SV));
+  return true;
+}
+}  // namespace gbk

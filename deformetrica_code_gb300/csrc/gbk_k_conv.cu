@@ -1,0 +1,61 @@
+// Instantiations: Convolve, fused Convolve + alpha-gradient, alpha-gradient.
+//
+// FP32-compensated variants (BLOCK threads, R targets per thread, TJ sources per tile, MERGE
+// sources per compensated run): the hot (d, dv) = (3, 3) and (2, 2) shapes carry several
+// variants for the autotuner; other shapes carry the default one. FP64 uses one target per
+// thread.
+#include "gbk_dispatch.h"
+
+namespace gbk {
+
+template <template <int, int> class OP, int D, int DV>
+static bool pick_conv_like(int mode, int variant, KernelEntry *e) {
+  typedef OP<D, DV> O;
+  if (mode == MODE_F64) return set_entry<O, double, D, 128, 1, 128, 128>(e);
+  constexpr bool hot = (D == 3 && DV == 3) || (D == 2 && DV == 2);
+  if constexpr (hot) {
+    switch (variant) {
+      case 1: return set_entry<O, float, D, 128, 4, 256, 64>(e);
+      case 2: return set_entry<O, float, D, 256, 2, 256, 64>(e);
+      case 3: return set_entry<O, float, D, 128, 8, 256, 64>(e);
+      default: break;
+    }
+  }
+  return set_entry<O, float, D, 256, 4, 256, 64>(e);
+}
+
+template <int D, int DV>
+using OpCG = OpConvGradAlpha<D, DV, true>;
+template <int D, int DV>
+using OpGA = OpConvGradAlpha<D, DV, false>;
+
+template <template <int, int> class OP>
+static bool by_shape(int mode, int d, int dv, int variant, KernelEntry *e) {
+  if (d == 2) {
+    switch (dv) {
+      case 1: return pick_conv_like<OP, 2, 1>(mode, variant, e);
+      case 2: return pick_conv_like<OP, 2, 2>(mode, variant, e);
+      case 3: return pick_conv_like<OP, 2, 3>(mode, variant, e);
+      case 4: return pick_conv_like<OP, 2, 4>(mode, variant, e);
+    }
+  } else if (d == 3) {
+    switch (dv) {
+      case 1: return pick_conv_like<OP, 3, 1>(mode, variant, e);
+      case 2: return pick_conv_like<OP, 3, 2>(mode, variant, e);
+      case 3: return pick_conv_like<OP, 3, 3>(mode, variant, e);
+      case 6: return pick_conv_like<OP, 3, 6>(mode, variant, e);
+    }
+  }
+  return false;
+}
+
+bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
+  switch (op) {
+    case OP_CONV: return by_shape<OpConv>(mode, d, dv, variant, e);
+    case OP_CONV_GRADA: return by_shape<OpCG>(mode, d, dv, variant, e);
+    case OP_GRADA: return by_shape<OpGA>(mode, d, dv, variant, e);
+  }
+  return false;
+}
+
+}  // namespace gbk

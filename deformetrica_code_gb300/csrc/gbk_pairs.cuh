@@ -1,0 +1,605 @@
+// Tiled N-body kernel template for every Gaussian kernel sum of the reference's ExactKernel
+// (src/support/kernels/ExactKernel.cxx) and AbstractKernel::ConvolveSpecialHessian
+// (src/support/kernels/AbstractKernel.cxx:22-88).
+//
+// Work decomposition. A CTA owns BLOCK*R targets (R per thread; in FP32 mode they are processed
+// two at a time in float2 lanes) and one contiguous range of sources (a "split"; grid.y splits
+// the source range when there are too few targets to fill 152 SMs). Sources stream through
+// shared memory in tiles of TJ records, each record already converted to the lane type and
+// broadcast, so the inner loop is: vector shared loads of one source record (warp-uniform
+// address: a broadcast) then, per target pair, d packed subtracts, the packed r^2, one packed
+// multiply for the exp argument, two MUFU ex2, and the operation's packed FMAs.
+//
+// Coordinates are centred per CTA: the midpoint of the CTA's target bounding box (in FP64) is
+// subtracted from targets and sources before rounding to FP32, so |x - y|^2 is formed from small
+// centred values (the differences themselves are never cancelled from large coordinates).
+//
+// Every op is linear in the source weights, so padded source slots carry zero weights and add
+// exactly +0. The kernels never wait on another CTA and never use atomics: with a split, each
+// split writes its own FP64 partial and a second kernel sums the splits in a fixed order, so the
+// results are bitwise reproducible run to run.
+#pragma once
+
+#include "gbk_common.cuh"
+
+namespace gbk {
+
+struct PairArgs {
+  // targets (row-major, D columns) and optional per-target extras
+  const double *x;
+  long nx;
+  const double *ta;  // extra A (alpha for the alpha-gradient, beta for the special Hessian)
+  int ta_ld;
+  const double *tb;  // extra B (xi for the special Hessian)
+  int tb_ld;
+  // sources (row-major, D columns), weights and optional per-source extras
+  const double *y;
+  long ny;
+  const double *w;  // weights, pointer already offset to the first column of this chunk
+  int w_ld;
+  const double *sb;  // source extra B (xi for the special Hessian)
+  int sb_ld;
+  double sigma;
+  int p0, p1, p2;  // op parameters: dim / (k, dp) / (row, col) / (k, dp, dq)
+  // outputs (pointer already offset to this chunk's first column)
+  double *out0;
+  int out0_ld;
+  double *out1;
+  int out1_ld;
+  int acc0, acc1;  // 1: add into out0 / out1 instead of overwriting (column chunks)
+  // source split
+  double *partial;  // [nsplit][NO][nx] FP64 partial sums when nsplit > 1
+  long j_chunk;     // sources per split (a multiple of TJ)
+  int nsplit;
+};
+
+template <typename T>
+struct Consts {
+  T cexp;  // exp argument scale: -log2(e)/sigma^2 (FP32) or -1/sigma^2 (FP64)
+};
+
+__device__ __forceinline__ void put(double *p, int acc, double v) {
+  if (acc)
+    *p += v;
+  else
+    *p = v;
+}
+
+// =============================================================================================
+// Operations. Each op declares:
+//   NT  : target extras (beyond x), NS : source extras (beyond y), NO : accumulators per target
+//   load_target / load_source : fetch extras (FP64) for one target / one source
+//   accum : per-pair update given dx = x_i - y_j, e = K_ij, target extras, source extras
+//   store : final scaling of the NO FP64 sums for target i and write to the outputs
+// =============================================================================================
+
+// ExactKernel::Convolve (ExactKernel.cxx:51-74): V_i = sum_j K_ij W_j.
+template <int D, int DV>
+struct OpConv {
+  static constexpr int NT = 0, NS = DV, NO = DV;
+  __device__ static void load_target(const PairArgs &, long, double *) {}
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) s[k] = a.w[j * a.w_ld + k];
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *, const SV *s, V *acc, int, int) {
+    typedef Lane<T> L;
+#pragma unroll
+    for (int k = 0; k < DV; ++k) acc[k] = L::fma(e, s[k], acc[k]);
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, v[k]);
+  }
+};
+
+// Fused forward + alpha-weighted gradient: V_i = sum_j K_ij W_j (when out0 != null) and
+// g_i = sum_j (alpha_i . W_j)(-2 K_ij / sigma^2)(x_i - y_j), which is
+// ExactKernel::ConvolveGradient(X, alpha) (ExactKernel.cxx:264-275) and the reference CUDA
+// GpuGrad1Conv1DOnDevice (lib/cuda_convolutions/GpuConv1D.cu:165-215). With CONV = false only
+// the gradient is accumulated.
+template <int D, int DV, bool CONV>
+struct OpConvGradAlpha {
+  static constexpr int NT = DV, NS = DV, NO = (CONV ? DV : 0) + D;
+  __device__ static void load_target(const PairArgs &a, long i, double *t) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) t[k] = a.ta[i * a.ta_ld + k];
+  }
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) s[k] = a.w[j * a.w_ld + k];
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *t, const SV *s, V *acc, int, int) {
+    typedef Lane<T> L;
+    constexpr int G0 = CONV ? DV : 0;
+    if (CONV) {
+#pragma unroll
+      for (int k = 0; k < DV; ++k) acc[k] = L::fma(e, s[k], acc[k]);
+    }
+    V ab = L::mul(t[0], s[0]);
+#pragma unroll
+    for (int k = 1; k < DV; ++k) ab = L::fma(t[k], s[k], ab);
+    V c = L::mul(e, ab);
+#pragma unroll
+    for (int l = 0; l < D; ++l) acc[G0 + l] = L::fma(c, dx[l], acc[G0 + l]);
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+    constexpr int G0 = CONV ? DV : 0;
+    if (CONV && a.out0) {
+#pragma unroll
+      for (int k = 0; k < DV; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, v[k]);
+    }
+    const double f = -2.0 / (a.sigma * a.sigma);
+#pragma unroll
+    for (int l = 0; l < D; ++l) put(a.out1 + i * a.out1_ld + l, a.acc1, v[G0 + l] * f);
+  }
+};
+
+// ExactKernel::ConvolveGradient(X) "varlin" (ExactKernel.cxx:166-202):
+// G_i(k, l) = sum_j W_jk (-2 K_ij / sigma^2)(x_i - y_j)_l, output [i][k][l].
+template <int D, int DV>
+struct OpVarlin {
+  static constexpr int NT = 0, NS = DV, NO = DV * D;
+  __device__ static void load_target(const PairArgs &, long, double *) {}
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) s[k] = a.w[j * a.w_ld + k];
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *, const SV *s, V *acc, int, int) {
+    typedef Lane<T> L;
+    V ed[D];
+#pragma unroll
+    for (int l = 0; l < D; ++l) ed[l] = L::mul(e, dx[l]);
+#pragma unroll
+    for (int k = 0; k < DV; ++k)
+#pragma unroll
+      for (int l = 0; l < D; ++l) acc[k * D + l] = L::fma(ed[l], s[k], acc[k * D + l]);
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+    const double f = -2.0 / (a.sigma * a.sigma);
+#pragma unroll
+    for (int o = 0; o < DV * D; ++o) put(a.out0 + i * a.out0_ld + o, a.acc0, v[o] * f);
+  }
+};
+
+// ExactKernel::ConvolveGradient(X, dim) (ExactKernel.cxx:294-323): sum_j dK/dx_dim W_j, with
+// dim = p0 chosen at run time (a uniform select; this op is not on the hot loop).
+template <typename V>
+__device__ __forceinline__ V pick(const V *v, int D, int k) {
+  return k == 0 ? v[0] : (k == 1 || D < 3 ? v[1] : v[2]);
+}
+
+template <int D, int DV>
+struct OpGradDim {
+  static constexpr int NT = 0, NS = DV, NO = DV;
+  __device__ static void load_target(const PairArgs &, long, double *) {}
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) s[k] = a.w[j * a.w_ld + k];
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *, const SV *s, V *acc, int p0, int) {
+    typedef Lane<T> L;
+    V g = L::mul(e, pick(dx, D, p0));
+#pragma unroll
+    for (int k = 0; k < DV; ++k) acc[k] = L::fma(g, s[k], acc[k]);
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+    const double f = -2.0 / (a.sigma * a.sigma);
+#pragma unroll
+    for (int k = 0; k < DV; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, v[k] * f);
+  }
+};
+
+// ExactKernel::ConvolveHessian(X) (ExactKernel.cxx:365-397) and its two single-entry forms
+// (:399-428, :430-470). Per pair H = K (4 (x-y)(x-y)^T / sigma^4 - 2 I / sigma^2); the op keeps
+// S_k(a,b) = sum_j K W_jk dx_a dx_b (a <= b) and C_k = sum_j K W_jk and forms
+// H_k(a,b) = 4/sigma^4 S_k(a,b) - 2/sigma^2 delta_ab C_k at the end.
+template <int D, int DV>
+struct OpHessFull {
+  static constexpr int NP = D * (D + 1) / 2;
+  static constexpr int NT = 0, NS = DV, NO = DV * (NP + 1);
+  __device__ static void load_target(const PairArgs &, long, double *) {}
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) s[k] = a.w[j * a.w_ld + k];
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *, const SV *s, V *acc, int, int) {
+    typedef Lane<T> L;
+    V q[NP];
+    int n = 0;
+#pragma unroll
+    for (int p = 0; p < D; ++p)
+#pragma unroll
+      for (int r = p; r < D; ++r) q[n++] = L::mul(dx[p], dx[r]);
+#pragma unroll
+    for (int k = 0; k < DV; ++k) {
+      V ew = L::mul(e, s[k]);
+      acc[k * (NP + 1)] = L::add(acc[k * (NP + 1)], ew);
+#pragma unroll
+      for (int m = 0; m < NP; ++m) acc[k * (NP + 1) + 1 + m] = L::fma(ew, q[m], acc[k * (NP + 1) + 1 + m]);
+    }
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+    const double s2 = a.sigma * a.sigma;
+    const double c4 = 4.0 / (s2 * s2), c2 = 2.0 / s2;
+#pragma unroll
+    for (int k = 0; k < DV; ++k) {
+      const double *vk = v + k * (NP + 1);
+      double *o = a.out0 + i * a.out0_ld + k * D * D;
+      int n = 0;
+#pragma unroll
+      for (int p = 0; p < D; ++p)
+#pragma unroll
+        for (int r = p; r < D; ++r) {
+          double h = c4 * vk[1 + n++] - (p == r ? c2 * vk[0] : 0.0);
+          put(o + p * D + r, a.acc0, h);
+          if (r != p) put(o + r * D + p, a.acc0, h);
+        }
+    }
+  }
+};
+
+// ExactKernel::ConvolveHessian(X, row, col) (ExactKernel.cxx:399-428) with row = p0, col = p1 at
+// run time; over one weight column it is also ConvolveHessian(X, k, dp, dq) (:430-470).
+// Keeps Q_k = sum_j K W_jk dx_row dx_col and C_k = sum_j K W_jk (C only matters on the diagonal).
+template <int D, int DV>
+struct OpHessRowCol {
+  static constexpr int NT = 0, NS = DV, NO = 2 * DV;
+  __device__ static void load_target(const PairArgs &, long, double *) {}
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < DV; ++k) s[k] = a.w[j * a.w_ld + k];
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *, const SV *s, V *acc, int p0, int p1) {
+    typedef Lane<T> L;
+    V q = L::mul(e, L::mul(pick(dx, D, p0), pick(dx, D, p1)));
+#pragma unroll
+    for (int k = 0; k < DV; ++k) {
+      acc[2 * k] = L::fma(q, s[k], acc[2 * k]);
+      acc[2 * k + 1] = L::fma(e, s[k], acc[2 * k + 1]);
+    }
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+    const double s2 = a.sigma * a.sigma;
+    const double c4 = 4.0 / (s2 * s2), c2 = 2.0 / s2;
+#pragma unroll
+    for (int k = 0; k < DV; ++k) {
+      double h = c4 * v[2 * k] - (a.p0 == a.p1 ? c2 * v[2 * k + 1] : 0.0);
+      put(a.out0 + i * a.out0_ld + k, a.acc0, h);
+    }
+  }
+};
+
+// Fused ConvolveSpecialHessian (AbstractKernel.cxx:22-88; reference CUDA GradDiff,
+// GpuConv1D.cu:552-607 scaled by -1/2 at CUDAExactKernel.cxx:223) over the sources themselves:
+// gamma_i = sum_j (beta_i . beta_j) H_ij (xi_j - xi_i)
+//         = sum_j (b.b) K [4/sigma^4 ((y_i - y_j).(xi_j - xi_i)) (y_i - y_j) - 2/sigma^2 (xi_j - xi_i)].
+// Targets carry (y_i, beta_i, xi_i), sources (y_j, beta_j, xi_j).
+template <int D>
+struct OpSpecialHessian {
+  static constexpr int NT = 2 * D, NS = 2 * D, NO = 2 * D;
+  __device__ static void load_target(const PairArgs &a, long i, double *t) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) t[k] = a.ta[i * a.ta_ld + k];
+#pragma unroll
+    for (int k = 0; k < D; ++k) t[D + k] = -a.tb[i * a.tb_ld + k];  // -xi_i
+  }
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) s[k] = a.w[j * a.w_ld + k];
+#pragma unroll
+    for (int k = 0; k < D; ++k) s[D + k] = a.sb[j * a.sb_ld + k];
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *t, const SV *s, V *acc, int, int) {
+    typedef Lane<T> L;
+    V bb = L::mul(t[0], s[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) bb = L::fma(t[k], s[k], bb);
+    V de[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) de[k] = L::add(s[D + k], t[D + k]);  // xi_j - xi_i
+    V q = L::mul(dx[0], de[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) q = L::fma(dx[k], de[k], q);
+    V c = L::mul(e, bb);
+    V cq = L::mul(c, q);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      acc[k] = L::fma(cq, dx[k], acc[k]);
+      acc[D + k] = L::fma(c, de[k], acc[D + k]);
+    }
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+    const double s2 = a.sigma * a.sigma;
+    const double c4 = 4.0 / (s2 * s2), c2 = 2.0 / s2;
+#pragma unroll
+    for (int k = 0; k < D; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, c4 * v[k] - c2 * v[D + k]);
+  }
+};
+
+// =============================================================================================
+// The kernel.
+// =============================================================================================
+template <typename T>
+struct SrcLane;
+template <>
+struct SrcLane<float> {
+  typedef float2 SV;
+};
+template <>
+struct SrcLane<double> {
+  typedef double SV;
+};
+
+// Packs the values of the W targets of one lane group (FP32: two targets, FP64: one).
+template <typename T>
+struct Pack;
+template <>
+struct Pack<float> {
+  __device__ __forceinline__ static float2 make(double a, double b) { return make_float2((float)a, (float)b); }
+};
+template <>
+struct Pack<double> {
+  __device__ __forceinline__ static double make(double a, double) { return a; }
+};
+
+template <class Op, int D>
+struct Rec {
+  static constexpr int NJ = D + Op::NS;
+  static constexpr int NJP = (NJ + 1) & ~1;  // even: records load as 16-byte vectors
+};
+
+// CENTER: subtract the CTA's target bounding-box midpoint (FP32 mode). FP64 mode forms x - y
+// directly, as the reference does.
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE>
+__global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
+  typedef Lane<T> L;
+  typedef typename L::V V;
+  typedef typename SrcLane<T>::SV SV;
+  constexpr int W = L::kWidth;
+  constexpr int G = R / W;  // lane groups per thread
+  constexpr int NJP = Rec<Op, D>::NJP;
+  constexpr int NO = Op::NO;
+  constexpr bool CENTER = (W == 2);
+  static_assert(R % W == 0, "R must be a multiple of the lane width");
+  static_assert(TJ % MERGE == 0, "TJ must be a multiple of MERGE");
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SV *tile = reinterpret_cast<SV *>(smem_raw);
+  __shared__ double s_red[2 * D][BLOCK / 32];
+  __shared__ double s_ctr[D];
+
+  const long i0 = (long)blockIdx.x * (BLOCK * R);
+  const long nx = a.nx;
+
+  // ---- centre of this CTA's target tile (bounding-box midpoint, FP64) ----
+  double ctr[D];
+  if (CENTER) {
+    double lo[D], hi[D];
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+      lo[l] = 1e300;
+      hi[l] = -1e300;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      long i = i0 + threadIdx.x + (long)r * BLOCK;
+      if (i < nx) {
+#pragma unroll
+        for (int l = 0; l < D; ++l) {
+          double v = a.x[i * D + l];
+          lo[l] = fmin(lo[l], v);
+          hi[l] = fmax(hi[l], v);
+        }
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lo[l] = fmin(lo[l], __shfl_xor_sync(0xffffffffu, lo[l], o));
+        hi[l] = fmax(hi[l], __shfl_xor_sync(0xffffffffu, hi[l], o));
+      }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+        s_red[l][threadIdx.x >> 5] = lo[l];
+        s_red[D + l][threadIdx.x >> 5] = hi[l];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < D) {
+      double mn = 1e300, mx = -1e300;
+      for (int w2 = 0; w2 < BLOCK / 32; ++w2) {
+        mn = fmin(mn, s_red[threadIdx.x][w2]);
+        mx = fmax(mx, s_red[D + threadIdx.x][w2]);
+      }
+      s_ctr[threadIdx.x] = (mn <= mx) ? 0.5 * (mn + mx) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < D; ++l) ctr[l] = s_ctr[l];
+  } else {
+#pragma unroll
+    for (int l = 0; l < D; ++l) ctr[l] = 0.0;
+  }
+
+  // ---- this thread's targets: centred coordinates and extras, in lanes ----
+  V xg[G][D];
+  V tg[G][Op::NT > 0 ? Op::NT : 1];
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    double xv[W][D], tv[W][Op::NT > 0 ? Op::NT : 1];
+#pragma unroll
+    for (int w2 = 0; w2 < W; ++w2) {
+      long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
+      long ic = i < nx ? i : (nx - 1);  // out-of-range lanes compute a copy, never stored
+#pragma unroll
+      for (int l = 0; l < D; ++l) xv[w2][l] = a.x[ic * D + l] - ctr[l];
+      Op::load_target(a, ic, tv[w2]);
+    }
+#pragma unroll
+    for (int l = 0; l < D; ++l) xg[g][l] = Pack<T>::make(xv[0][l], xv[W - 1][l]);
+#pragma unroll
+    for (int k = 0; k < Op::NT; ++k) tg[g][k] = Pack<T>::make(tv[0][k], tv[W - 1][k]);
+  }
+
+  V acc[G][NO], sum[G][NO], cmp[G][NO];
+#pragma unroll
+  for (int g = 0; g < G; ++g)
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+      acc[g][o] = L::zero();
+      sum[g][o] = L::zero();
+      cmp[g][o] = L::zero();
+    }
+
+  const T cexp = exp_arg_scale<T>(a.sigma);
+  const int p0 = a.p0, p1 = a.p1;
+  const V cx = L::splat(cexp);
+
+  const long jb = (long)blockIdx.y * a.j_chunk;
+  long je = jb + a.j_chunk;
+  if (je > a.ny) je = a.ny;
+
+  for (long jt = jb; jt < je; jt += TJ) {
+    const int cnt = (int)((je - jt) < TJ ? (je - jt) : TJ);
+    // ---- stage TJ source records: -(y - c) and extras, broadcast to the lane type ----
+    for (int r = threadIdx.x; r < TJ; r += BLOCK) {
+      double rec[NJP];
+      if (r < cnt) {
+        long j = jt + r;
+#pragma unroll
+        for (int l = 0; l < D; ++l) rec[l] = ctr[l] - a.y[j * D + l];
+        Op::load_source(a, j, rec + D);
+      } else {
+#pragma unroll
+        for (int q = 0; q < Rec<Op, D>::NJ; ++q) rec[q] = 0.0;  // zero weights: exact no-op
+      }
+#pragma unroll
+      for (int q = Rec<Op, D>::NJ; q < NJP; ++q) rec[q] = 0.0;
+#pragma unroll
+      for (int q = 0; q < NJP; ++q) tile[r * NJP + q] = SrcVal<T>::make(rec[q]);
+    }
+    __syncthreads();
+
+    const int nrun = (cnt + MERGE - 1) / MERGE;
+    for (int run = 0; run < nrun; ++run) {
+      const SV *rp = tile + run * MERGE * NJP;
+#pragma unroll 2
+      for (int jj = 0; jj < MERGE; ++jj) {
+        SV s[NJP];
+        const float4 *src = reinterpret_cast<const float4 *>(rp + jj * NJP);
+#pragma unroll
+        for (int q = 0; q < NJP / 2; ++q) {
+          float4 v4 = src[q];
+          *reinterpret_cast<float4 *>(&s[2 * q]) = v4;
+        }
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+          V dx[D];
+#pragma unroll
+          for (int l = 0; l < D; ++l) dx[l] = L::add(xg[g][l], s[l]);
+          V r2 = L::mul(dx[0], dx[0]);
+#pragma unroll
+          for (int l = 1; l < D; ++l) r2 = L::fma(dx[l], dx[l], r2);
+          V e = L::exp2v(L::mul(r2, cx));
+          Op::template accum<T>(dx, e, tg[g], s + D, acc[g], p0, p1);
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+#pragma unroll
+        for (int o = 0; o < NO; ++o) {
+          Comp<T>::fold(sum[g][o], cmp[g][o], acc[g][o]);
+          acc[g][o] = L::zero();
+        }
+    }
+    __syncthreads();
+  }
+
+  // ---- write: final sums in FP64 ----
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+#pragma unroll
+    for (int w2 = 0; w2 < W; ++w2) {
+      long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
+      if (i >= nx) continue;
+      double v[NO];
+#pragma unroll
+      for (int o = 0; o < NO; ++o) v[o] = (double)L::get(sum[g][o], w2) + (double)L::get(cmp[g][o], w2);
+      if (a.nsplit > 1) {
+        double *p = a.partial + (long)blockIdx.y * NO * nx;
+#pragma unroll
+        for (int o = 0; o < NO; ++o) p[(long)o * nx + i] = v[o];
+      } else {
+        Op::store(a, i, v);
+      }
+    }
+  }
+}
+
+// Sums the per-split FP64 partials in split order and applies the op's store.
+template <class Op>
+__global__ void split_reduce_kernel(const PairArgs a) {
+  constexpr int NO = Op::NO;
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nx) return;
+  double v[NO];
+#pragma unroll
+  for (int o = 0; o < NO; ++o) v[o] = 0.0;
+  for (int s = 0; s < a.nsplit; ++s) {
+    const double *p = a.partial + (long)s * NO * a.nx;
+#pragma unroll
+    for (int o = 0; o < NO; ++o) v[o] += p[(long)o * a.nx + i];
+  }
+  Op::store(a, i, v);
+}
+
+// Launch configuration of one pair kernel.
+struct LaunchCfg {
+  int variant;  // index into the op's compiled (BLOCK, R, TJ) table
+  int nsplit;   // source splits (grid.y); 1 = no partial buffer
+};
+
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE>
+cudaError_t launch_pairs(PairArgs a, int nsplit, cudaStream_t st) {
+  if (a.nx <= 0) return cudaSuccess;
+  constexpr int NJP = Rec<Op, D>::NJP;
+  typedef typename SrcLane<T>::SV SV;
+  const size_t smem = (size_t)TJ * NJP * sizeof(SV);
+  auto kern = pair_kernel<Op, T, D, BLOCK, R, TJ, MERGE>;
+  if (smem > 48 * 1024) {  // per current device; idempotent
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  if (nsplit < 1) nsplit = 1;
+  long per = (a.ny + nsplit - 1) / nsplit;
+  per = ((per + TJ - 1) / TJ) * TJ;
+  if (per < TJ) per = TJ;
+  nsplit = (int)((a.ny + per - 1) / per);
+  if (nsplit < 1) nsplit = 1;
+  a.j_chunk = per;
+  a.nsplit = nsplit;
+  if (a.ny == 0) {
+    a.j_chunk = TJ;
+    a.nsplit = 1;
+    nsplit = 1;
+  }
+  dim3 grid((unsigned)((a.nx + (long)BLOCK * R - 1) / ((long)BLOCK * R)), (unsigned)nsplit);
+  kern<<<grid, BLOCK, smem, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || nsplit == 1) return e;
+  split_reduce_kernel<Op><<<(unsigned)((a.nx + 255) / 256), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace gbk

@@ -1,0 +1,308 @@
+"""Python mirror of the reference's kernel-object interface over libgbkernel.so.
+
+``GB300ExactKernel`` has the method names, argument meanings and error behaviour of
+``AbstractKernel`` / ``ExactKernel`` (src/support/kernels/AbstractKernel.h:34-187,
+src/support/kernels/ExactKernel.cxx) so tests and scripts read like the reference's own kernel
+tests. Every method is one call into the CUDA library (include/gbk.h); there is no CPU path.
+
+Arrays may be numpy float64 arrays (host; results come back as numpy) or CUDA float64 torch
+tensors (device; the call is queued on torch's current stream and returns CUDA tensors).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GBKError, GBK_MODE_F32C, GBK_MODE_F64
+
+try:  # torch is only needed for device-resident arrays
+    import torch
+except Exception:  # pragma: no cover - torch is present in every supported setup
+    torch = None
+
+
+def _is_torch(a) -> bool:
+    return torch is not None and isinstance(a, torch.Tensor)
+
+
+def _check(a, name: str, cols: int | None = None):
+    if a is None:
+        return None
+    if _is_torch(a):
+        if a.dtype != torch.float64:
+            raise TypeError(f"{name}: expected float64, got {a.dtype}")
+        if not a.is_contiguous():
+            raise ValueError(f"{name}: must be contiguous (row-major)")
+    else:
+        if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise TypeError(f"{name}: expected a C-contiguous float64 numpy array")
+    if a.ndim != 2:
+        raise ValueError(f"{name}: expected a 2-D matrix, got shape {tuple(a.shape)}")
+    if cols is not None and a.shape[1] != cols:
+        raise ValueError(f"{name}: expected {cols} columns, got {a.shape[1]}")
+    return a
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_torch(a):
+        return ctypes.c_void_p(a.data_ptr()) if a.numel() else None
+    return ctypes.c_void_p(a.ctypes.data) if a.size else None
+
+
+class Context:
+    """Owns one gbk_ctx (device buffers, stream, precision mode, tuning table)."""
+
+    def __init__(self, device: int = 0, mode: int = GBK_MODE_F32C):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.gbk_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise GBKError(rc, self.lib.gbk_last_error(None).decode())
+        self.h = h
+        self.device = device
+        self.set_mode(mode)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbk_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc: int):
+        if rc != 0:
+            raise GBKError(rc, self.lib.gbk_last_error(self.h).decode())
+
+    def set_mode(self, mode: int):
+        self.check(self.lib.gbk_set_mode(self.h, mode))
+        self.mode = mode
+
+    def set_split(self, n: int):
+        self.check(self.lib.gbk_set_split(self.h, n))
+
+    def launch_count(self) -> int:
+        return int(self.lib.gbk_launch_count(self.h))
+
+    def bind_stream(self, *arrays):
+        """Queue on torch's current stream when any argument is a CUDA tensor."""
+        if any(_is_torch(a) and a.is_cuda for a in arrays if a is not None):
+            s = torch.cuda.current_stream(self.device).cuda_stream
+            self.check(self.lib.gbk_set_stream(self.h, ctypes.c_void_p(s)))
+        else:
+            self.check(self.lib.gbk_set_stream(self.h, None))
+
+    def synchronize(self):
+        self.check(self.lib.gbk_synchronize(self.h))
+
+    def autotune(self, op: str, d: int, dv: int, nx: int, ny: int, sigma: float):
+        self.check(self.lib.gbk_autotune(self.h, _lib.OPS[op], d, dv, nx, ny, sigma))
+
+    def tune_save(self, path: str):
+        self.check(self.lib.gbk_tune_save(self.h, path.encode()))
+
+    def tune_load(self, path: str):
+        self.check(self.lib.gbk_tune_load(self.h, path.encode()))
+
+
+def _empty_like(ref, shape):
+    if _is_torch(ref):
+        return torch.empty(shape, dtype=torch.float64, device=ref.device)
+    return np.empty(shape, dtype=np.float64)
+
+
+class GB300ExactKernel:
+    """Gaussian kernel K(x, y) = exp(-|x-y|^2 / sigma^2) evaluated by the GB300 library.
+
+    Mirrors ExactKernel<double, PointDim> (ExactKernel.h:34-194): SetKernelWidth clamps the
+    width at 1e-10 (AbstractKernel.h:87-89); sources/weights count mismatches raise like the
+    reference's std::runtime_error.
+    """
+
+    def __init__(self, point_dim: int, kernel_width: float = 1.0, context: Context | None = None,
+                 mode: int | None = None):
+        if point_dim not in (2, 3):
+            raise ValueError("PointDim must be 2 or 3")
+        self.d = point_dim
+        self.ctx = context or Context()
+        if mode is not None:
+            self.ctx.set_mode(mode)
+        self.m_Sources = None
+        self.m_Weights = None
+        self.SetKernelWidth(kernel_width)
+        self.m_Modified = False
+
+    # -- encapsulation (AbstractKernel.h:83-115) --
+    def GetKernelWidth(self) -> float:
+        return self.m_KernelWidth
+
+    def SetKernelWidth(self, h: float):
+        if h < 1e-10:
+            h = 1e-10
+        self.m_KernelWidth = float(h)
+        self.m_Modified = True
+
+    def GetSources(self):
+        return self.m_Sources
+
+    def SetSources(self, X):
+        self.m_Sources = _check(X, "sources", self.d)
+        self.m_Modified = True
+
+    def GetWeights(self):
+        return self.m_Weights
+
+    def SetWeights(self, W):
+        self.m_Weights = _check(W, "weights")
+        self.m_Modified = True
+
+    def Clone(self) -> "GB300ExactKernel":
+        k = GB300ExactKernel(self.d, self.m_KernelWidth, self.ctx)
+        k.m_Sources, k.m_Weights, k.m_Modified = self.m_Sources, self.m_Weights, self.m_Modified
+        return k
+
+    # -- helpers --
+    def _yw(self):
+        Y, W = self.m_Sources, self.m_Weights
+        if Y is None or W is None:
+            raise RuntimeError("sources and weights must be set")
+        if Y.shape[0] != W.shape[0]:
+            raise RuntimeError("Sources and weights count mismatch")
+        return Y, W
+
+    def _call(self, fn, *args):
+        self.ctx.check(fn(self.ctx.h, *args))
+
+    # -- convolutions --
+    def Convolve(self, X):
+        """ExactKernel::Convolve (ExactKernel.cxx:51-74)."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        out = _empty_like(X, (X.shape[0], W.shape[1]))
+        self.ctx.bind_stream(X, Y, W)
+        self._call(self.ctx.lib.gbk_convolve, self.d, W.shape[1], _ptr(X), X.shape[0], _ptr(Y),
+                   _ptr(W), Y.shape[0], self.m_KernelWidth, _ptr(out))
+        return out
+
+    def ConvolveGradient(self, X, *args):
+        """Overloads of ExactKernel::ConvolveGradient:
+        (X) varlin :166-202 -> (nx, dv, d); (X, alpha) :264-275 -> (nx, d);
+        (X, dim) :294-323 -> (nx, dv); (X, k, dp) :325-363 -> (ny,)."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        dv, lib = W.shape[1], self.ctx.lib
+        if len(args) == 0:
+            out = _empty_like(X, (X.shape[0], dv, self.d))
+            self.ctx.bind_stream(X, Y, W)
+            self._call(lib.gbk_convolve_gradient, self.d, dv, _ptr(X), X.shape[0], _ptr(Y), _ptr(W),
+                       Y.shape[0], self.m_KernelWidth, _ptr(out))
+            return out
+        if len(args) == 1 and not isinstance(args[0], (int, np.integer)):
+            alpha = _check(args[0], "alpha", dv)
+            if alpha.shape[0] != X.shape[0]:
+                raise RuntimeError("alpha must have one row per target")
+            out = _empty_like(X, (X.shape[0], self.d))
+            self.ctx.bind_stream(X, Y, W, alpha)
+            self._call(lib.gbk_convolve_gradient_alpha, self.d, dv, _ptr(X), X.shape[0], _ptr(Y),
+                       _ptr(W), Y.shape[0], self.m_KernelWidth, _ptr(alpha), _ptr(out))
+            return out
+        if len(args) == 1:
+            out = _empty_like(X, (X.shape[0], dv))
+            self.ctx.bind_stream(X, Y, W)
+            self._call(lib.gbk_convolve_gradient_dim, self.d, dv, _ptr(X), X.shape[0], _ptr(Y),
+                       _ptr(W), Y.shape[0], self.m_KernelWidth, int(args[0]), _ptr(out))
+            return out
+        if len(args) == 2:
+            out = _empty_like(X, (Y.shape[0],))
+            self.ctx.bind_stream(X, Y, W)
+            self._call(lib.gbk_convolve_gradient_kdp, self.d, dv, _ptr(X), X.shape[0], _ptr(Y),
+                       _ptr(W), Y.shape[0], self.m_KernelWidth, int(args[0]), int(args[1]), _ptr(out))
+            return out
+        raise TypeError("ConvolveGradient takes (X), (X, alpha), (X, dim) or (X, k, dp)")
+
+    def ConvolveAndGradient(self, X, alpha):
+        """Convolve(X) and ConvolveGradient(X, alpha) in one fused pass."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        alpha = _check(alpha, "alpha", W.shape[1])
+        v = _empty_like(X, (X.shape[0], W.shape[1]))
+        g = _empty_like(X, (X.shape[0], self.d))
+        self.ctx.bind_stream(X, Y, W, alpha)
+        self._call(self.ctx.lib.gbk_convolve_and_gradient_alpha, self.d, W.shape[1], _ptr(X),
+                   X.shape[0], _ptr(Y), _ptr(W), Y.shape[0], self.m_KernelWidth, _ptr(alpha),
+                   _ptr(v), _ptr(g))
+        return v, g
+
+    def ConvolveHessian(self, X, *args):
+        """Overloads of ExactKernel::ConvolveHessian:
+        (X) :365-397 -> (nx, dv, d, d); (X, row, col) :399-428 -> (nx, dv);
+        (X, k, dp, dq) :430-470 -> (nx,)."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        dv, lib = W.shape[1], self.ctx.lib
+        self.ctx.bind_stream(X, Y, W)
+        if len(args) == 0:
+            out = _empty_like(X, (X.shape[0], dv, self.d, self.d))
+            self._call(lib.gbk_convolve_hessian, self.d, dv, _ptr(X), X.shape[0], _ptr(Y), _ptr(W),
+                       Y.shape[0], self.m_KernelWidth, _ptr(out))
+            return out
+        if len(args) == 2:
+            out = _empty_like(X, (X.shape[0], dv))
+            self._call(lib.gbk_convolve_hessian_rowcol, self.d, dv, _ptr(X), X.shape[0], _ptr(Y),
+                       _ptr(W), Y.shape[0], self.m_KernelWidth, int(args[0]), int(args[1]), _ptr(out))
+            return out
+        if len(args) == 3:
+            out = _empty_like(X, (X.shape[0],))
+            self._call(lib.gbk_convolve_hessian_kdpdq, self.d, dv, _ptr(X), X.shape[0], _ptr(Y),
+                       _ptr(W), Y.shape[0], self.m_KernelWidth, int(args[0]), int(args[1]),
+                       int(args[2]), _ptr(out))
+            return out
+        raise TypeError("ConvolveHessian takes (X), (X, row, col) or (X, k, dp, dq)")
+
+    def ConvolveSpecialHessian(self, xi):
+        """AbstractKernel::ConvolveSpecialHessian (AbstractKernel.cxx:22-88)."""
+        Y, W = self._yw()
+        if W.shape[1] != self.d:
+            raise RuntimeError("ConvolveSpecialHessian needs weights with PointDim columns")
+        xi = _check(xi, "xi", self.d)
+        if xi.shape[0] != Y.shape[0]:
+            raise RuntimeError("Y and Xi count mismatch")
+        out = _empty_like(xi, (Y.shape[0], self.d))
+        self.ctx.bind_stream(Y, W, xi)
+        self._call(self.ctx.lib.gbk_convolve_special_hessian, self.d, _ptr(Y), _ptr(W), Y.shape[0],
+                   self.m_KernelWidth, _ptr(xi), _ptr(out))
+        return out
+
+    def ForwardAdjoint(self, X, alpha):
+        """Convolve plus the gradients of sum_i alpha_i . (K W)_i w.r.t. X, Y and W."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        alpha = _check(alpha, "alpha", W.shape[1])
+        v = _empty_like(X, (X.shape[0], W.shape[1]))
+        gx = _empty_like(X, (X.shape[0], self.d))
+        gy = _empty_like(X, (Y.shape[0], self.d))
+        gw = _empty_like(X, (Y.shape[0], W.shape[1]))
+        self.ctx.bind_stream(X, Y, W, alpha)
+        self._call(self.ctx.lib.gbk_forward_adjoint, self.d, W.shape[1], _ptr(X), X.shape[0],
+                   _ptr(Y), _ptr(W), Y.shape[0], self.m_KernelWidth, _ptr(alpha), _ptr(v), _ptr(gx),
+                   _ptr(gy), _ptr(gw))
+        return v, gx, gy, gw
+
+    def KernelNorm(self):
+        """<W, K W> over the sources, reduced in FP64 on the device."""
+        Y, W = self._yw()
+        out = np.zeros(1)
+        self.ctx.bind_stream(Y, W)
+        self._call(self.ctx.lib.gbk_kernel_norm, self.d, W.shape[1], _ptr(Y), _ptr(W), Y.shape[0],
+                   self.m_KernelWidth, ctypes.c_void_p(out.ctypes.data))
+        return float(out[0])
+
+
+__all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64"]

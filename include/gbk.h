@@ -1,0 +1,179 @@
+/*
+ * gbk.h -- C ABI of the GB300 Gaussian kernel-sum library (libgbkernel.so).
+ *
+ * This is the drop-in boundary for Deformetrica's Gaussian kernel sums. Each entry point
+ * replaces one method of the reference's kernel interface
+ *   src/support/kernels/AbstractKernel.h:34-187   (virtual Convolve / ConvolveGradient /
+ *                                                   ConvolveHessian / ConvolveSpecialHessian)
+ *   src/support/kernels/ExactKernel.cxx             (the FP64 CPU implementation)
+ *   src/support/kernels/CUDAExactKernel.cxx:41-320  (the legacy CUDA forwarding)
+ *   lib/cuda_convolutions/GpuConv1D.h               (GaussGpu*Conv1D host functions)
+ * and is what a new KernelFactory kernel type calls.
+ *
+ * Conventions (all entry points):
+ *  - Matrices are row-major double arrays: n rows x c columns, element (i, k) at p[i * c + k],
+ *    exactly the buffers the reference builds with vectorise_row_wise()
+ *    (src/support/linear_algebra/ArmadilloMatrixWrapper.h:241).
+ *    x: targets (nx x d); y: sources (ny x d); w: weights (ny x dv); sigma: kernel width.
+ *    K(x, y) = exp(-|x - y|^2 / sigma^2) (ExactKernel.h:78-86).
+ *  - Pointers may be device memory or host memory. Device pointers are used in place and the call
+ *    is asynchronous on the context's stream. When any pointer is host memory, the library copies
+ *    through context-owned device buffers and the call returns after the results are in host
+ *    memory (the synchronous behaviour of the reference's GaussGpu*Conv1D).
+ *  - Return value: GBK_OK (0) or a GBK_ERR_* code; gbk_last_error(ctx) describes the failure.
+ *    Shape errors are the ones the reference throws std::runtime_error for.
+ *  - d is 2 or 3. dv may be any positive count; the kernels are compiled for dv in {1,2,3,4} (d=2)
+ *    and {1,2,3,6} (d=3) and other counts run as column chunks.
+ *  - Precision (gbk_set_mode): GBK_MODE_F32C (default) evaluates pairs in FP32 with per-row
+ *    compensated accumulation and per-tile centred coordinates; GBK_MODE_F64 evaluates in FP64.
+ *  - A context is not thread-safe; use one context per host thread (the reference clones one
+ *    kernel object per subject thread, AbstractAtlas.cxx:218).
+ */
+#ifndef GBK_H
+#define GBK_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbk_ctx gbk_ctx;
+
+enum {
+  GBK_OK = 0,
+  GBK_ERR_ARG = 1,         /* bad shape / index / pointer (reference: std::runtime_error) */
+  GBK_ERR_UNSUPPORTED = 2, /* dimension or dv combination not supported */
+  GBK_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  GBK_ERR_ALLOC = 4,       /* device memory allocation failed */
+  GBK_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  GBK_ERR_STATE = 6        /* call not allowed in the current state (e.g. during capture) */
+};
+
+enum { GBK_MODE_F32C = 0, GBK_MODE_F64 = 1 };
+
+/* Operation identifiers (for gbk_autotune). */
+enum {
+  GBK_OP_CONVOLVE = 0,
+  GBK_OP_CONVOLVE_GRADIENT_ALPHA_FUSED = 1,
+  GBK_OP_GRADIENT_ALPHA = 2,
+  GBK_OP_GRADIENT_VARLIN = 3,
+  GBK_OP_GRADIENT_DIM = 4,
+  GBK_OP_HESSIAN = 5,
+  GBK_OP_HESSIAN_ROWCOL = 6,
+  GBK_OP_SPECIAL_HESSIAN = 7
+};
+
+/* ---- context --------------------------------------------------------------------------- */
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int gbk_version(void);
+
+/* Creates a context on CUDA device `device` with its own non-blocking stream. Replaces the
+ * per-call cudaMalloc/cudaFree of GpuConv1D.cu:97-130 with buffers that grow monotonically. */
+int gbk_create(int device, gbk_ctx **out);
+void gbk_destroy(gbk_ctx *ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char *gbk_last_error(const gbk_ctx *ctx);
+/* Uses `stream` (a cudaStream_t) for all later calls; NULL restores the context's own stream. */
+int gbk_set_stream(gbk_ctx *ctx, void *stream);
+void *gbk_get_stream(const gbk_ctx *ctx);
+int gbk_set_mode(gbk_ctx *ctx, int mode);
+int gbk_get_mode(const gbk_ctx *ctx);
+/* Waits for all work queued on the context's stream. */
+int gbk_synchronize(gbk_ctx *ctx);
+/* Number of the library's own kernels launched on this context so far. */
+long long gbk_launch_count(const gbk_ctx *ctx);
+
+/* ---- kernel sums (AbstractKernel surface) ------------------------------------------------ */
+
+/* ExactKernel::Convolve, ExactKernel.cxx:51-74; CUDAExactKernel::Convolve, CUDAExactKernel.cxx:41-90;
+ * GaussGpuEvalConv1D, GpuConv1D.cu:148-155.  out[i, k] = sum_j K(x_i, y_j) w[j, k]   (nx x dv) */
+int gbk_convolve(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                 const double *w, long ny, double sigma, double *out);
+
+/* ExactKernel::ConvolveGradient(X, alpha), ExactKernel.cxx:264-275; CUDAExactKernel.cxx:165-194;
+ * GaussGpuGrad1Conv1D, GpuConv1D.cu:282-288.
+ * out[i, :] = sum_j (alpha_i . w_j) (-2 K_ij / sigma^2)(x_i - y_j)   (nx x d; alpha is nx x dv) */
+int gbk_convolve_gradient_alpha(gbk_ctx *ctx, int d, int dv, const double *x, long nx,
+                                const double *y, const double *w, long ny, double sigma,
+                                const double *alpha, double *out);
+
+/* Convolve and ConvolveGradient(X, alpha) of the same (x, y, w) in ONE pass over the pairs
+ * (distance and exp evaluated once per pair). out_v: nx x dv, out_g: nx x d. */
+int gbk_convolve_and_gradient_alpha(gbk_ctx *ctx, int d, int dv, const double *x, long nx,
+                                    const double *y, const double *w, long ny, double sigma,
+                                    const double *alpha, double *out_v, double *out_g);
+
+/* ExactKernel::ConvolveGradient(X) ("varlin"), ExactKernel.cxx:166-202; CUDAExactKernel.cxx:261-320;
+ * GpuGradConv_varlin_1D, GpuConv1D.cu:475-521.
+ * out[i, k, l] = sum_j w[j, k] dK(x_i, y_j)/dx_l      (nx x dv x d; the reference's
+ * std::vector<MatrixType> of dv x d matrices, one per target) */
+int gbk_convolve_gradient(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                          const double *w, long ny, double sigma, double *out);
+
+/* ExactKernel::ConvolveGradient(X, dim), ExactKernel.cxx:294-323 (general sources; the legacy CUDA
+ * GpuGradConv1D, GpuConv1D.cu:350-392, assumed X == sources).
+ * out[i, k] = sum_j dK(x_i, y_j)/dx_dim w[j, k]       (nx x dv) */
+int gbk_convolve_gradient_dim(gbk_ctx *ctx, int d, int dv, const double *x, long nx,
+                              const double *y, const double *w, long ny, double sigma, int dim,
+                              double *out);
+
+/* ExactKernel::ConvolveGradient(X, k, dp), ExactKernel.cxx:325-363, including its quirk: the
+ * result has ny entries (one per SOURCE) and reads the first ny rows of x, so nx >= ny.
+ * out[i] = sum_j w[j, k] dK(x_i, y_j)/dx_dp, i < ny */
+int gbk_convolve_gradient_kdp(gbk_ctx *ctx, int d, int dv, const double *x, long nx,
+                              const double *y, const double *w, long ny, double sigma, int k,
+                              int dp, double *out);
+
+/* ExactKernel::ConvolveHessian(X), ExactKernel.cxx:365-397.
+ * out[i, k, a, b] = sum_j w[j, k] H_ab(x_i, y_j), H = K (4 (x-y)(x-y)^T / s^4 - 2 I / s^2)
+ * (nx x dv x d x d) */
+int gbk_convolve_hessian(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                         const double *w, long ny, double sigma, double *out);
+
+/* ExactKernel::ConvolveHessian(X, row, col), ExactKernel.cxx:399-428.  out: nx x dv */
+int gbk_convolve_hessian_rowcol(gbk_ctx *ctx, int d, int dv, const double *x, long nx,
+                                const double *y, const double *w, long ny, double sigma, int row,
+                                int col, double *out);
+
+/* ExactKernel::ConvolveHessian(X, k, dp, dq), ExactKernel.cxx:430-470.  out: nx */
+int gbk_convolve_hessian_kdpdq(gbk_ctx *ctx, int d, int dv, const double *x, long nx,
+                               const double *y, const double *w, long ny, double sigma, int k,
+                               int dp, int dq, double *out);
+
+/* AbstractKernel::ConvolveSpecialHessian(xi), AbstractKernel.cxx:22-88;
+ * CUDAExactKernel::ConvolveSpecialHessian, CUDAExactKernel.cxx:196-226 (GradDiff x -1/2).
+ * Sources y (n x d) with weights beta = w (n x d), xi (n x d):
+ * out[i, :] = sum_j (beta_i . beta_j) H(y_i, y_j) (xi_j - xi_i)   (n x d) */
+int gbk_convolve_special_hessian(gbk_ctx *ctx, int d, const double *y, const double *w, long n,
+                                 double sigma, const double *xi, double *out);
+
+/* Forward + adjoint of L = sum_i alpha_i . (K w)_i in two fused passes (distance and exp are
+ * recomputed, never stored): v = Convolve (nx x dv), gx = dL/dx (nx x d, equal to
+ * ConvolveGradient(X, alpha)), gy = dL/dy (ny x d), gw = dL/dw (ny x dv). Any output may be NULL.
+ * The source side has no single reference method; it equals ConvolveGradient(Y, w) and
+ * Convolve(Y) with sources X and weights alpha (K is symmetric). */
+int gbk_forward_adjoint(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                        const double *w, long ny, double sigma, const double *alpha, double *v,
+                        double *gx, double *gy, double *gw);
+
+/* <w, K w> = sum_ij w_i . K(y_i, y_j) w_j, summed in FP64 on the device (the RKHS regularity
+ * term, DeterministicAtlas.cxx:126-141). `out` is one double (host or device). */
+int gbk_kernel_norm(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
+                    double sigma, double *out);
+
+/* ---- tuning ------------------------------------------------------------------------------ */
+
+/* Times the compiled variants and source-split factors of `op` for this shape on synthetic data
+ * and keeps the fastest for calls whose (nx, ny) fall in the same size bucket. */
+int gbk_autotune(gbk_ctx *ctx, int op, int d, int dv, long nx, long ny, double sigma);
+/* Saves / loads the tuned table as JSON lines. */
+int gbk_tune_save(const gbk_ctx *ctx, const char *path);
+int gbk_tune_load(gbk_ctx *ctx, const char *path);
+/* Forces the number of source splits (0 = automatic) -- for tests and tuning. */
+int gbk_set_split(gbk_ctx *ctx, int nsplit);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBK_H */

@@ -1,0 +1,202 @@
+"""ctypes bindings to the FP64 oracle libraries (test infrastructure only).
+
+Every function takes and returns row-major float64 numpy arrays, mirroring the reference's
+``ExactKernel`` methods (file:line given per method in ``gauss_oracle.c``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PORT_SRC = os.path.join(_HERE, "gauss_oracle.c")
+_PORT_SO = os.path.join(_HERE, "_build", "liboracle_port.so")
+_REF_SO = os.path.join(_HERE, "_ref", "libref_exactkernel.so")
+_REF_SCRIPT = os.path.join(_HERE, "build_ref.sh")
+_lock = threading.Lock()
+
+
+def port_path() -> str:
+    return _PORT_SO
+
+
+def reference_path() -> str:
+    return _REF_SO
+
+
+def build_port(force: bool = False) -> str:
+    """Compile gauss_oracle.c with gcc (-O2 -fopenmp, the reference's RELEASE level)."""
+    with _lock:
+        if (not force and os.path.exists(_PORT_SO)
+                and os.path.getmtime(_PORT_SO) >= os.path.getmtime(_PORT_SRC)):
+            return _PORT_SO
+        os.makedirs(os.path.dirname(_PORT_SO), exist_ok=True)
+        tmp = _PORT_SO + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-std=c11",
+                               _PORT_SRC, "-o", tmp, "-lm"])
+        os.replace(tmp, _PORT_SO)
+        return _PORT_SO
+
+
+def build_reference(reference_root: str = "/root/reference") -> str | None:
+    """Build oracle/_ref from the reference sources when they are present; else return None."""
+    if not os.path.isdir(os.path.join(reference_root, "src", "support", "kernels")):
+        return None
+    with _lock:
+        if not os.path.exists(_REF_SO):
+            subprocess.check_call(["bash", _REF_SCRIPT, reference_root],
+                                  stdout=subprocess.DEVNULL)
+    return _REF_SO
+
+
+_D = ctypes.POINTER(ctypes.c_double)
+_L = ctypes.c_long
+_I = ctypes.c_int
+_F = ctypes.c_double
+
+_SIGS = {
+    "oracle_convolve": [_I, _I, _D, _L, _D, _D, _L, _F, _D],
+    "oracle_grad_alpha": [_I, _I, _D, _L, _D, _D, _L, _F, _D, _D],
+    "oracle_grad_varlin": [_I, _I, _D, _L, _D, _D, _L, _F, _D],
+    "oracle_grad_dim": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _D],
+    "oracle_grad_kdp": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _I, _D],
+    "oracle_hess_full": [_I, _I, _D, _L, _D, _D, _L, _F, _D],
+    "oracle_hess_rowcol": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _I, _D],
+    "oracle_hess_kdpdq": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _I, _I, _D],
+    "oracle_special_hessian": [_I, _I, _D, _D, _L, _F, _D, _D],
+}
+
+
+def _c(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class OracleLib:
+    """One loaded oracle library (``port`` or ``reference``) with numpy-level methods."""
+
+    def __init__(self, path: str, kind: str):
+        self.kind = kind
+        self.path = path
+        self._lib = ctypes.CDLL(path)
+        for name, argt in _SIGS.items():
+            fn = getattr(self._lib, name)
+            fn.argtypes = argt
+            fn.restype = ctypes.c_int
+        self._lib.oracle_last_error.restype = ctypes.c_char_p
+
+    def _check(self, rc: int):
+        if rc != 0:
+            msg = self._lib.oracle_last_error().decode() if rc == -1 else "bad dimension"
+            raise OracleError(msg)
+
+    @staticmethod
+    def _prep(x, y, w):
+        x, y, w = _f64(x), _f64(y), _f64(w)
+        if x.ndim != 2 or y.ndim != 2 or w.ndim != 2:
+            raise ValueError("x, y and w must be 2-D")
+        return x, y, w, x.shape[1], w.shape[1]
+
+    def convolve(self, x, y, w, sigma):
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((x.shape[0], dv))
+        self._check(self._lib.oracle_convolve(d, dv, _c(x), x.shape[0], _c(y), _c(w), y.shape[0],
+                                              sigma, _c(out)))
+        return out
+
+    def grad_alpha(self, x, y, w, sigma, alpha):
+        x, y, w, d, dv = self._prep(x, y, w)
+        alpha = _f64(alpha)
+        out = np.zeros((x.shape[0], d))
+        self._check(self._lib.oracle_grad_alpha(d, dv, _c(x), x.shape[0], _c(y), _c(w),
+                                                y.shape[0], sigma, _c(alpha), _c(out)))
+        return out
+
+    def grad_varlin(self, x, y, w, sigma):
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((x.shape[0], dv, d))
+        self._check(self._lib.oracle_grad_varlin(d, dv, _c(x), x.shape[0], _c(y), _c(w),
+                                                 y.shape[0], sigma, _c(out)))
+        return out
+
+    def grad_dim(self, x, y, w, sigma, dim):
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((x.shape[0], dv))
+        self._check(self._lib.oracle_grad_dim(d, dv, _c(x), x.shape[0], _c(y), _c(w),
+                                              y.shape[0], sigma, dim, _c(out)))
+        return out
+
+    def grad_kdp(self, x, y, w, sigma, k, dp):
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((y.shape[0],))
+        self._check(self._lib.oracle_grad_kdp(d, dv, _c(x), x.shape[0], _c(y), _c(w),
+                                              y.shape[0], sigma, k, dp, _c(out)))
+        return out
+
+    def hess_full(self, x, y, w, sigma):
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((x.shape[0], dv, d, d))
+        self._check(self._lib.oracle_hess_full(d, dv, _c(x), x.shape[0], _c(y), _c(w),
+                                               y.shape[0], sigma, _c(out)))
+        return out
+
+    def hess_rowcol(self, x, y, w, sigma, row, col):
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((x.shape[0], dv))
+        self._check(self._lib.oracle_hess_rowcol(d, dv, _c(x), x.shape[0], _c(y), _c(w),
+                                                 y.shape[0], sigma, row, col, _c(out)))
+        return out
+
+    def hess_kdpdq(self, x, y, w, sigma, k, dp, dq):
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((x.shape[0],))
+        self._check(self._lib.oracle_hess_kdpdq(d, dv, _c(x), x.shape[0], _c(y), _c(w),
+                                                y.shape[0], sigma, k, dp, dq, _c(out)))
+        return out
+
+    def special_hessian(self, y, w, sigma, xi):
+        y, w, xi = _f64(y), _f64(w), _f64(xi)
+        d, dv = y.shape[1], w.shape[1]
+        out = np.zeros((y.shape[0], d))
+        self._check(self._lib.oracle_special_hessian(d, dv, _c(y), _c(w), y.shape[0], sigma,
+                                                     _c(xi), _c(out)))
+        return out
+
+    # Source-side adjoint by symmetry of K (see oracle_fwd_adjoint in gauss_oracle.c).
+    def fwd_adjoint(self, x, y, w, sigma, alpha):
+        v = self.convolve(x, y, w, sigma)
+        gx = self.grad_alpha(x, y, w, sigma, alpha)
+        gw = self.convolve(y, x, alpha, sigma)
+        gy = self.grad_alpha(y, x, alpha, sigma, w)
+        return v, gx, gy, gw
+
+
+_cache: dict[str, OracleLib] = {}
+
+
+def load(kind: str = "port") -> OracleLib:
+    """Load the ``port`` (always buildable) or the ``reference`` library (may be absent)."""
+    if kind in _cache:
+        return _cache[kind]
+    if kind == "port":
+        lib = OracleLib(build_port(), "port")
+    elif kind == "reference":
+        path = _REF_SO if os.path.exists(_REF_SO) else build_reference()
+        if path is None or not os.path.exists(path):
+            raise FileNotFoundError("reference oracle library not built (reference tree absent)")
+        lib = OracleLib(path, "reference")
+    else:
+        raise ValueError(kind)
+    _cache[kind] = lib
+    return lib

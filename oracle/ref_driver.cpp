@@ -1,0 +1,203 @@
+// C entry points over the reference's own FP64 kernel layer (test infrastructure only).
+//
+// This file is compiled together with the unmodified reference sources
+// src/support/kernels/ExactKernel.cxx and src/support/kernels/AbstractKernel.cxx (plus the
+// Armadillo wrappers they use) into oracle/_ref/libref_exactkernel.so by oracle/build_ref.sh.
+// Each function builds ExactKernel<double, d> from row-major arrays, calls exactly one
+// reference method and writes the result back row-major. The same symbol names are exported by
+// the C restatement in oracle/gauss_oracle.c, so a test can run either library through one
+// ctypes binding and compare them.
+//
+// Return value: 0 on success, -1 when the reference threw (the message is kept for
+// oracle_last_error()), -2 for a dimension outside {2, 3}.
+
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ExactKernel.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+MatrixType from_rows(const double *p, long rows, long cols) {
+  MatrixType M((unsigned)rows, (unsigned)cols, 0.0);
+  for (long i = 0; i < rows; ++i)
+    for (long j = 0; j < cols; ++j) M((unsigned)i, (unsigned)j) = p[i * cols + j];
+  return M;
+}
+
+void to_rows(const MatrixType &M, double *out) {
+  const unsigned r = M.rows(), c = M.cols();
+  for (unsigned i = 0; i < r; ++i)
+    for (unsigned j = 0; j < c; ++j) out[(long)i * c + j] = M(i, j);
+}
+
+template <unsigned D>
+struct Setup {
+  ExactKernel<double, D> k;
+  Setup(const double *y, const double *w, long ny, int dv, double sigma) {
+    k.SetKernelWidth(sigma);
+    k.SetSources(from_rows(y, ny, D));
+    k.SetWeights(from_rows(w, ny, dv));
+  }
+};
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    f();
+    return 0;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return -1;
+  }
+}
+
+template <unsigned D>
+int convolve_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+               double sigma, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    to_rows(s.k.Convolve(from_rows(x, nx, D)), out);
+  });
+}
+
+template <unsigned D>
+int grad_alpha_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                 double sigma, const double *alpha, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    to_rows(s.k.ConvolveGradient(from_rows(x, nx, D), from_rows(alpha, nx, dv)), out);
+  });
+}
+
+template <unsigned D>
+int grad_varlin_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                  double sigma, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    std::vector<MatrixType> g = s.k.ConvolveGradient(from_rows(x, nx, D));
+    for (long i = 0; i < nx; ++i) to_rows(g[i], out + i * dv * D);
+  });
+}
+
+template <unsigned D>
+int grad_dim_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+               double sigma, int dim, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    to_rows(s.k.ConvolveGradient(from_rows(x, nx, D), (unsigned)dim), out);
+  });
+}
+
+template <unsigned D>
+int grad_kdp_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+               double sigma, int kk, int dp, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    VectorType v = s.k.ConvolveGradient(from_rows(x, nx, D), (unsigned)kk, (unsigned)dp);
+    for (unsigned i = 0; i < v.size(); ++i) out[i] = v(i);
+  });
+}
+
+template <unsigned D>
+int hess_full_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                double sigma, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    std::vector<std::vector<MatrixType> > h = s.k.ConvolveHessian(from_rows(x, nx, D));
+    for (long i = 0; i < nx; ++i)
+      for (int kk = 0; kk < dv; ++kk) to_rows(h[i][kk], out + ((i * dv) + kk) * D * D);
+  });
+}
+
+template <unsigned D>
+int hess_rowcol_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                  double sigma, int row, int col, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    to_rows(s.k.ConvolveHessian(from_rows(x, nx, D), (unsigned)row, (unsigned)col), out);
+  });
+}
+
+template <unsigned D>
+int hess_kdpdq_d(int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                 double sigma, int kk, int dp, int dq, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    VectorType v = s.k.ConvolveHessian(from_rows(x, nx, D), (unsigned)kk, (unsigned)dp, (unsigned)dq);
+    for (unsigned i = 0; i < v.size(); ++i) out[i] = v(i);
+  });
+}
+
+template <unsigned D>
+int special_hessian_d(int dv, const double *y, const double *w, long ny, double sigma,
+                      const double *xi, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    to_rows(s.k.ConvolveSpecialHessian(from_rows(xi, ny, D)), out);
+  });
+}
+
+}  // namespace
+
+#define DISPATCH(fn, ...)                         \
+  do {                                            \
+    if (d == 2) return fn##_d<2>(__VA_ARGS__);    \
+    if (d == 3) return fn##_d<3>(__VA_ARGS__);    \
+    return -2;                                    \
+  } while (0)
+
+extern "C" {
+
+const char *oracle_last_error(void) { return g_last_error.c_str(); }
+
+int oracle_convolve(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                    long ny, double sigma, double *out) {
+  DISPATCH(convolve, dv, x, nx, y, w, ny, sigma, out);
+}
+
+int oracle_grad_alpha(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                      long ny, double sigma, const double *alpha, double *out) {
+  DISPATCH(grad_alpha, dv, x, nx, y, w, ny, sigma, alpha, out);
+}
+
+int oracle_grad_varlin(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                       long ny, double sigma, double *out) {
+  DISPATCH(grad_varlin, dv, x, nx, y, w, ny, sigma, out);
+}
+
+int oracle_grad_dim(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                    long ny, double sigma, int dim, double *out) {
+  DISPATCH(grad_dim, dv, x, nx, y, w, ny, sigma, dim, out);
+}
+
+int oracle_grad_kdp(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                    long ny, double sigma, int k, int dp, double *out) {
+  DISPATCH(grad_kdp, dv, x, nx, y, w, ny, sigma, k, dp, out);
+}
+
+int oracle_hess_full(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                     long ny, double sigma, double *out) {
+  DISPATCH(hess_full, dv, x, nx, y, w, ny, sigma, out);
+}
+
+int oracle_hess_rowcol(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                       long ny, double sigma, int row, int col, double *out) {
+  DISPATCH(hess_rowcol, dv, x, nx, y, w, ny, sigma, row, col, out);
+}
+
+int oracle_hess_kdpdq(int d, int dv, const double *x, long nx, const double *y, const double *w,
+                      long ny, double sigma, int k, int dp, int dq, double *out) {
+  DISPATCH(hess_kdpdq, dv, x, nx, y, w, ny, sigma, k, dp, dq, out);
+}
+
+int oracle_special_hessian(int d, int dv, const double *y, const double *w, long ny, double sigma,
+                           const double *xi, double *out) {
+  DISPATCH(special_hessian, dv, y, w, ny, sigma, xi, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,124 @@
+"""Generates the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a checkout where the reference tree is available (default /root/reference):
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+It builds oracle/_ref (the reference's own ExactKernel / AbstractKernel compiled from its
+sources by oracle/build_ref.sh) and records its outputs:
+
+* ``kernel_precision.npz`` -- every ExactKernel method on the fixture of the reference's kernel
+  tests (tests/unit_tests/kernels/AbstractTestKernelPrecision.{h,cxx}: sigma = 1.88, X 501 rows,
+  Y 201 rows, entries exp(-U) with std::mt19937(1) re-seeded for every matrix), i.e. the
+  operations TestKernelPrecisionCUDA.cxx:17-203 compares, plus the remaining overloads.
+* ``kernel_random.npz`` -- the same methods on seeded, non-degenerate inputs (sigma 0.2 and 0.05,
+  uniform points, N(0,1) weights, ragged sizes).
+* ``parallel_transport.npz`` -- the inputs and ground truth of
+  tests/unit_tests/parallel-transport/TestParallelTransport.cxx:19-85 (read from the reference's
+  DLM text files), which pin the shooting oracle (oracle/deformation.py).
+
+The fixtures are small (tens to hundreds of KB) and are committed; the GPU machine never needs the
+reference tree.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import oracle  # noqa: E402
+from tests.golden.fixtures import precision_fixture, random_cases  # noqa: E402
+
+
+def read_dlm(path: str) -> np.ndarray:
+    """readMatrixDLM (src/io/MatrixDLM.cxx): whitespace-separated rows, one matrix."""
+    rows = [ln.split() for ln in open(path).read().strip().splitlines() if ln.strip()]
+    return np.array([[float(v) for v in r] for r in rows])
+
+
+def read_multiple_dlm(path: str) -> list[np.ndarray]:
+    """readMultipleMatrixDLM: a header 'count rows cols', then each matrix after a blank line."""
+    toks = open(path).read().split()
+    cnt, r, c = int(toks[0]), int(toks[1]), int(toks[2])
+    vals = np.array([float(t) for t in toks[3:]])
+    return [vals[k * r * c:(k + 1) * r * c].reshape(r, c) for k in range(cnt)]
+
+
+def all_ops(lib, X, Y, W, Z, sigma, W3):
+    """Every ExactKernel method of the reference on one input set (keys name the method)."""
+    d = X.shape[1]
+    out = {}
+    out["convolve"] = lib.convolve(X, Y, W, sigma)
+    out["grad_varlin"] = lib.grad_varlin(X, Y, W, sigma)
+    Za = Z[:, :W.shape[1]] if Z.shape[1] >= W.shape[1] else np.tile(Z, (1, 3))[:, :W.shape[1]]
+    out["grad_alpha_alpha"] = Za
+    out["grad_alpha"] = lib.grad_alpha(X, Y, W, sigma, Za)
+    for dim in range(d):
+        out[f"grad_dim_{dim}"] = lib.grad_dim(Y, Y, W, sigma, dim)  # TestKernelPrecisionCUDA uses Y
+        out[f"grad_dim_x_{dim}"] = lib.grad_dim(X, Y, W, sigma, dim)
+    if X.shape[0] >= Y.shape[0]:
+        out["grad_kdp"] = lib.grad_kdp(X, Y, W, sigma, W.shape[1] - 1, d - 1)
+    else:  # the reference's bounds-checked row access throws (ExactKernel.cxx:343-347)
+        try:
+            lib.grad_kdp(X, Y, W, sigma, W.shape[1] - 1, d - 1)
+            raise AssertionError("reference accepted ConvolveGradient(X,k,dp) with nx < ny")
+        except oracle.kernels.OracleError:
+            out["grad_kdp_raises"] = np.array(1)
+    out["hess_full"] = lib.hess_full(X, Y, W, sigma)
+    for r in range(d):
+        for c in range(d):
+            out[f"hess_rowcol_{r}{c}"] = lib.hess_rowcol(X, Y, W, sigma, r, c)
+    out["hess_kdpdq"] = lib.hess_kdpdq(X, Y, W, sigma, 0, 0, d - 1)
+    out["special_hessian"] = lib.special_hessian(Y, W3, sigma, W3)
+    return out
+
+
+def main(ref_root: str = "/root/reference"):
+    if oracle.build_reference(ref_root) is None:
+        raise SystemExit(f"reference tree not found at {ref_root}")
+    ref = oracle.load("reference")
+    port = oracle.load("port")
+
+    # 1. the reference's own kernel-test fixture
+    fx = precision_fixture()
+    res = {}
+    for d in (2, 3):
+        X, Y, Z = fx[f"X{d}D"], fx[f"Y{d}D"], fx[f"Z{d}D"]
+        W3 = fx[f"W{d}D"]
+        for wname in ([f"W{d}D", "W4D"] if d == 2 else [f"W{d}D", "W6D"]):
+            W = fx[wname]
+            for k, v in all_ops(ref, X, Y, W, Z, fx["kernel_width"], W3).items():
+                res[f"d{d}_{wname}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "kernel_precision.npz"), **res)
+
+    # 2. non-degenerate seeded cases
+    res = {}
+    for name, case in random_cases().items():
+        for k, v in all_ops(ref, case["X"], case["Y"], case["W"], case["Z"], case["sigma"],
+                            case["W3"]).items():
+            res[f"{name}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "kernel_random.npz"), **res)
+
+    del port
+
+    # 3. parallel-transport unit-test data (TestParallelTransport.cxx:19-85)
+    pt = os.path.join(ref_root, "tests", "unit_tests", "parallel-transport", "data")
+    np.savez_compressed(
+        os.path.join(HERE, "parallel_transport.npz"),
+        cp_regression=read_dlm(os.path.join(pt, "CPRegression.txt")),
+        mom_regression=read_dlm(os.path.join(pt, "MomRegression.txt")),
+        cp_transport=read_dlm(os.path.join(pt, "CPToTransport.txt")),
+        mom_transport=read_multiple_dlm(os.path.join(pt, "MomToTransport.txt"))[0],
+        ground_truth_mom=read_dlm(os.path.join(pt, "GroundTruthMom.txt")),
+        kernel_width=np.array(15.0),
+        number_of_time_points=np.array(30),
+    )
+    print("wrote", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main(*(sys.argv[1:2]))

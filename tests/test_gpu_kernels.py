@@ -1,0 +1,185 @@
+"""GPU parity: every kernel-sum entry point of libgbkernel.so against the FP64 oracle.
+
+Mirrors the reference's TestKernelPrecisionCUDA (tests/unit_tests/kernels/
+TestKernelPrecisionCUDA.cxx:17-203): same fixture, same element-wise criterion
+min(|x-y|/|x|, |x-y|) <= tol. Tolerances:
+  * FP64 mode: 1e-10 (the reference's eps_tol in double, AbstractTestKernelPrecision.h:76);
+  * compensated FP32 mode: 1e-6 on the reference fixture (the reference's float eps_tol,
+    AbstractTestKernelPrecision.h:79) and, on non-degenerate inputs whose sums cancel, a
+    normwise relative error <= 2e-6 (max_i |err_i| / max_i |ref_i|).
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import normwise_rel, reference_compare
+from tests.golden.fixtures import precision_fixture, random_cases
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-10
+F32_REF_TOL = 1e-6
+F32_NORM_TOL = 2e-6
+
+
+@pytest.fixture(scope="module")
+def gb():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import deformetrica_code_gb300 as g
+    return g
+
+
+@pytest.fixture(scope="module")
+def ctx(gb):
+    return gb.Context()
+
+
+def kern(gb, ctx, d, sigma, Y, W, mode):
+    ctx.set_mode(mode)
+    k = gb.GB300ExactKernel(d, sigma, context=ctx)
+    k.SetSources(np.ascontiguousarray(Y))
+    k.SetWeights(np.ascontiguousarray(W))
+    return k
+
+
+def run_all(k, X, Y, W, Za, W3):
+    d = X.shape[1]
+    out = {"convolve": k.Convolve(X), "grad_varlin": k.ConvolveGradient(X),
+           "grad_alpha": k.ConvolveGradient(X, np.ascontiguousarray(Za))}
+    for dim in range(d):
+        out[f"grad_dim_{dim}"] = k.ConvolveGradient(Y, dim)
+        out[f"grad_dim_x_{dim}"] = k.ConvolveGradient(X, dim)
+    if X.shape[0] >= Y.shape[0]:
+        out["grad_kdp"] = k.ConvolveGradient(X, W.shape[1] - 1, d - 1)
+    out["hess_full"] = k.ConvolveHessian(X)
+    for r in range(d):
+        for c in range(d):
+            out[f"hess_rowcol_{r}{c}"] = k.ConvolveHessian(X, r, c)
+    out["hess_kdpdq"] = k.ConvolveHessian(X, 0, 0, d - 1)
+    k.SetWeights(np.ascontiguousarray(W3))
+    out["special_hessian"] = k.ConvolveSpecialHessian(np.ascontiguousarray(W3))
+    k.SetWeights(np.ascontiguousarray(W))
+    return out
+
+
+@pytest.mark.parametrize("mode_name", ["f64", "f32c"])
+def test_reference_fixture_all_methods(gb, ctx, golden_precision, mode_name):
+    mode = gb.GBK_MODE_F64 if mode_name == "f64" else gb.GBK_MODE_F32C
+    tol = F64_TOL if mode_name == "f64" else F32_REF_TOL
+    fx = precision_fixture()
+    worst = {}
+    for d in (2, 3):
+        X, Y, Z, W3 = fx[f"X{d}D"], fx[f"Y{d}D"], fx[f"Z{d}D"], fx[f"W{d}D"]
+        for wname in ([f"W{d}D", "W4D"] if d == 2 else [f"W{d}D", "W6D"]):
+            W = fx[wname]
+            pre = f"d{d}_{wname}_"
+            k = kern(gb, ctx, d, fx["kernel_width"], Y, W, mode)
+            got = run_all(k, X, Y, W, golden_precision[pre + "grad_alpha_alpha"], W3)
+            for key, val in got.items():
+                worst[pre + key] = reference_compare(golden_precision[pre + key], val, np.inf)
+    bad = {k: v for k, v in worst.items() if v > tol}
+    assert not bad, f"above {tol}: {bad}"
+
+
+@pytest.mark.parametrize("mode_name", ["f64", "f32c"])
+def test_random_cases_all_methods(gb, ctx, golden_random, mode_name):
+    mode = gb.GBK_MODE_F64 if mode_name == "f64" else gb.GBK_MODE_F32C
+    bad = {}
+    for name, c in random_cases().items():
+        k = kern(gb, ctx, c["X"].shape[1], c["sigma"], c["Y"], c["W"], mode)
+        got = run_all(k, c["X"], c["Y"], c["W"], golden_random[name + "_grad_alpha_alpha"], c["W3"])
+        for key, val in got.items():
+            ref = golden_random[f"{name}_{key}"]
+            if mode_name == "f64":
+                err = reference_compare(ref, val, np.inf)
+                if err > F64_TOL:
+                    bad[f"{name}_{key}"] = err
+            else:
+                err = normwise_rel(val, ref)
+                if err > F32_NORM_TOL:
+                    bad[f"{name}_{key}"] = err
+    assert not bad, bad
+
+
+def test_grad_kdp_quirk_raises_like_reference(gb, ctx):
+    """ConvolveGradient(X,k,dp) reads ny rows of X (ExactKernel.cxx:343-347): nx < ny is an error."""
+    rng = np.random.default_rng(0)
+    k = kern(gb, ctx, 3, 0.3, rng.random((50, 3)), rng.standard_normal((50, 3)), gb.GBK_MODE_F32C)
+    with pytest.raises(gb.GBKError):
+        k.ConvolveGradient(rng.random((10, 3)), 0, 0)
+    with pytest.raises(gb.GBKError):
+        k.ConvolveGradient(rng.random((10, 3)), 3)  # dim out of range
+    k.SetWeights(rng.standard_normal((49, 3)))
+    with pytest.raises(RuntimeError):
+        k.Convolve(rng.random((10, 3)))  # sources and weights count mismatch
+
+
+@pytest.mark.parametrize("nx,ny", [(1, 1), (31, 193), (193, 31), (4097, 1000), (0, 10), (10, 0)])
+def test_ragged_sizes(gb, ctx, port, nx, ny):
+    rng = np.random.default_rng(nx * 7919 + ny)
+    X, Y = rng.random((nx, 3)), rng.random((ny, 3))
+    W, A = rng.standard_normal((ny, 3)), rng.standard_normal((nx, 3))
+    for mode, check in [(gb.GBK_MODE_F64, lambda a, b: reference_compare(b, a, 1) <= F64_TOL),
+                        (gb.GBK_MODE_F32C, lambda a, b: normwise_rel(a, b) <= F32_NORM_TOL)]:
+        k = kern(gb, ctx, 3, 0.2, Y, W, mode)
+        v, g = k.ConvolveAndGradient(X, A)
+        if nx:
+            assert check(v, port.convolve(X, Y, W, 0.2))
+            assert check(g, port.grad_alpha(X, Y, W, 0.2, A))
+        if ny == 0:
+            assert np.all(v == 0) and np.all(g == 0)
+
+
+def test_split_results_are_deterministic_and_consistent(gb, ctx, port):
+    """Source splits change only the summation grouping; repeated runs are bitwise equal."""
+    import torch
+    rng = np.random.default_rng(3)
+    X, Y = rng.random((1500, 3)), rng.random((20000, 3))
+    W, A = rng.standard_normal((20000, 3)), rng.standard_normal((1500, 3))
+    ref_v = port.convolve(X, Y, W, 0.1)
+    k = kern(gb, ctx, 3, 0.1, Y, W, gb.GBK_MODE_F32C)
+    outs = []
+    for ns in (1, 3, 7, 0):
+        ctx.set_split(ns)
+        v1 = k.Convolve(X)
+        v2 = k.Convolve(X)
+        assert np.array_equal(v1, v2), ns
+        assert normwise_rel(v1, ref_v) <= F32_NORM_TOL, ns
+        outs.append(v1)
+    ctx.set_split(0)
+    # device-pointer path gives the same bits as the host-pointer path
+    dev = lambda a: torch.from_numpy(a).cuda()
+    k2 = kern(gb, ctx, 3, 0.1, dev(Y), dev(W), gb.GBK_MODE_F32C)
+    vd = k2.Convolve(dev(X)).cpu().numpy()
+    torch.cuda.synchronize()
+    assert np.array_equal(vd, outs[-1])
+
+
+def test_forward_adjoint_matches_oracle(gb, ctx, port):
+    rng = np.random.default_rng(8)
+    X, Y = rng.random((700, 3)), rng.random((900, 3))
+    W, A = rng.standard_normal((900, 3)), rng.standard_normal((700, 3))
+    for mode, tol in [(gb.GBK_MODE_F64, 1e-12), (gb.GBK_MODE_F32C, F32_NORM_TOL)]:
+        k = kern(gb, ctx, 3, 0.15, Y, W, mode)
+        got = k.ForwardAdjoint(X, A)
+        ref = port.fwd_adjoint(X, Y, W, 0.15, A)
+        for g_, r_ in zip(got, ref):
+            assert normwise_rel(g_, r_) <= tol
+
+
+def test_kernel_norm_fp64(gb, ctx, port):
+    rng = np.random.default_rng(9)
+    Y, W = rng.random((800, 3)), rng.standard_normal((800, 3))
+    ref = float(np.sum(W * port.convolve(Y, Y, W, 0.2)))
+    for mode, tol in [(gb.GBK_MODE_F64, 1e-12), (gb.GBK_MODE_F32C, 2e-6)]:
+        k = kern(gb, ctx, 3, 0.2, Y, W, mode)
+        assert abs(k.KernelNorm() - ref) <= tol * abs(ref)
+
+
+def test_launch_count_increases(gb, ctx):
+    rng = np.random.default_rng(1)
+    k = kern(gb, ctx, 3, 0.2, rng.random((64, 3)), rng.standard_normal((64, 3)), gb.GBK_MODE_F32C)
+    n0 = ctx.launch_count()
+    k.Convolve(rng.random((64, 3)))
+    assert ctx.launch_count() > n0

@@ -32,11 +32,13 @@ struct Lane<float> {
   __device__ __forceinline__ static V fma(V a, V b, V c) { return __ffma2_rn(a, b, c); }
   __device__ __forceinline__ static V zero() { return make_float2(0.f, 0.f); }
   __device__ __forceinline__ static V splat(float s) { return make_float2(s, s); }
-  // 2^t per lane on the MUFU unit (t <= 0 here; results below 2^-126 flush to zero).
-  __device__ __forceinline__ static V exp2v(V t) {
+  // K = 2^(-r2') per lane on the MUFU unit. Coordinates are pre-scaled by sqrt(log2 e)/sigma,
+  // so r2' = |x' - y'|^2 = |x - y|^2 log2(e) / sigma^2 and 2^(-r2') = exp(-|x - y|^2 / sigma^2).
+  // Results below 2^-126 flush to zero.
+  __device__ __forceinline__ static V kexp(V r2, V) {
     float a, b;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(t.x));
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(b) : "f"(t.y));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(-r2.x));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(b) : "f"(-r2.y));
     return make_float2(a, b);
   }
   __device__ __forceinline__ static float get(V v, int l) { return l == 0 ? v.x : v.y; }
@@ -53,8 +55,8 @@ struct Lane<double> {
   __device__ __forceinline__ static V fma(V a, V b, V c) { return __fma_rn(a, b, c); }
   __device__ __forceinline__ static V zero() { return 0.0; }
   __device__ __forceinline__ static V splat(double s) { return s; }
-  // In FP64 mode the exponent argument is -r2/sigma^2 (natural base), evaluated with exp().
-  __device__ __forceinline__ static V exp2v(V t) { return exp(t); }
+  // FP64 mode: unscaled coordinates, K = exp(r2 * (-1/sigma^2)) with the CUDA math library.
+  __device__ __forceinline__ static V kexp(V r2, V cx) { return exp(r2 * cx); }
   __device__ __forceinline__ static double get(V v, int) { return v; }
 };
 
@@ -93,16 +95,22 @@ struct Comp<double> {
   __device__ __forceinline__ static void fold(double &sum, double &, double run) { sum += run; }
 };
 
-// Scale factor that turns r2 into the exp argument for the lane type.
+// Coordinate pre-scale of each lane type: FP32 works on x' = x sqrt(log2 e) / sigma (scaled in
+// FP64 before rounding, so x' keeps the relative precision of a rounded x); FP64 keeps x.
 template <typename T>
-__host__ __device__ inline T exp_arg_scale(double sigma);
+__host__ __device__ inline double coord_scale(double sigma);
 template <>
-__host__ __device__ inline float exp_arg_scale<float>(double sigma) {
-  return (float)(-1.4426950408889634 / (sigma * sigma));  // -log2(e) / sigma^2
+__host__ __device__ inline double coord_scale<float>(double sigma) {
+  return 1.2011224087864498 / sigma;  // sqrt(log2(e)) / sigma
 }
 template <>
-__host__ __device__ inline double exp_arg_scale<double>(double sigma) {
-  return -1.0 / (sigma * sigma);
+__host__ __device__ inline double coord_scale<double>(double) {
+  return 1.0;
+}
+// Scale of r2 inside kexp (FP64 only): -1/sigma^2.
+template <typename T>
+__host__ __device__ inline T exp_arg_scale(double sigma) {
+  return (T)(-1.0 / (sigma * sigma));
 }
 
 // Bounded-iteration helpers for any cross-block wait (none of the kernel-sum kernels wait).

@@ -54,11 +54,12 @@ bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry 
 }  // namespace gbk
 
 namespace gbk {
-// Helper for the instantiation files: records one compiled (op, T, D, BLOCK, R, TJ, MERGE).
-template <class OpT, typename T, int D, int BLOCK, int R, int TJ, int MERGE>
+// Helper for the instantiation files: records one compiled (op, T, D, BLOCK, R, TJ, MERGE) with
+// MINB resident CTAs per SM requested from the register allocator.
+template <class OpT, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB = 1>
 inline bool set_entry(KernelEntry *e) {
-  e->fn = &launch_pairs<OpT, T, D, BLOCK, R, TJ, MERGE>;
-  e->kernel = (const void *)&pair_kernel<OpT, T, D, BLOCK, R, TJ, MERGE>;
+  e->fn = &launch_pairs<OpT, T, D, BLOCK, R, TJ, MERGE, MINB>;
+  e->kernel = (const void *)&pair_kernel<OpT, T, D, BLOCK, R, TJ, MERGE, MINB>;
   e->block = BLOCK;
   e->r = R;
   e->tj = TJ;

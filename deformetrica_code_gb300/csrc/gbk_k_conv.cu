@@ -1,9 +1,10 @@
 // Instantiations: Convolve, fused Convolve + alpha-gradient, alpha-gradient.
 //
 // FP32-compensated variants (BLOCK threads, R targets per thread, TJ sources per tile, MERGE
-// sources per compensated run): the hot (d, dv) = (3, 3) and (2, 2) shapes carry several
-// variants for the autotuner; other shapes carry the default one. FP64 uses one target per
-// thread.
+// sources per compensated run, MINB CTAs per SM for the register allocator): the hot
+// (d, dv) = (3, 3) and (2, 2) shapes carry several variants for the autotuner; other shapes carry
+// the default one, which measured fastest on GB300 for the fused pass at N = M = 1e6 (578 ms vs
+// 603 ms for 4 targets per thread at 2 CTAs/SM). FP64 uses one target per thread.
 #include "gbk_dispatch.h"
 
 namespace gbk {
@@ -15,13 +16,14 @@ static bool pick_conv_like(int mode, int variant, KernelEntry *e) {
   constexpr bool hot = (D == 3 && DV == 3) || (D == 2 && DV == 2);
   if constexpr (hot) {
     switch (variant) {
-      case 1: return set_entry<O, float, D, 128, 4, 256, 64>(e);
-      case 2: return set_entry<O, float, D, 256, 2, 256, 64>(e);
-      case 3: return set_entry<O, float, D, 128, 8, 256, 64>(e);
+      case 1: return set_entry<O, float, D, 256, 4, 256, 64, 2>(e);
+      case 2: return set_entry<O, float, D, 128, 4, 256, 64, 4>(e);
+      case 3: return set_entry<O, float, D, 256, 2, 256, 64, 4>(e);
       default: break;
     }
   }
-  return set_entry<O, float, D, 256, 4, 256, 64>(e);
+  // default: 2 targets (one float2 lane pair) per thread, 3 CTAs of 256 threads per SM
+  return set_entry<O, float, D, 256, 2, 256, 64, 3>(e);
 }
 
 template <int D, int DV>

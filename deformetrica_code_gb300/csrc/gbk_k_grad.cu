@@ -7,7 +7,7 @@ template <template <int, int> class OP, int D, int DV>
 static bool pick_one(int mode, KernelEntry *e) {
   typedef OP<D, DV> O;
   if (mode == MODE_F64) return set_entry<O, double, D, 128, 1, 128, 128>(e);
-  return set_entry<O, float, D, 256, 2, 256, 64>(e);
+  return set_entry<O, float, D, 256, 2, 256, 64, 2>(e);
 }
 
 template <template <int, int> class OP>

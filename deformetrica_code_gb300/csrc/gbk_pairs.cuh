@@ -40,6 +40,7 @@ struct PairArgs {
   const double *sb;  // source extra B (xi for the special Hessian)
   int sb_ld;
   double sigma;
+  double xscale;  // coordinates are multiplied by this before the pair loop (set by launch_pairs)
   int p0, p1, p2;  // op parameters: dim / (k, dp) / (row, col) / (k, dp, dq)
   // outputs (pointer already offset to this chunk's first column)
   double *out0;
@@ -51,11 +52,6 @@ struct PairArgs {
   double *partial;  // [nsplit][NO][nx] FP64 partial sums when nsplit > 1
   long j_chunk;     // sources per split (a multiple of TJ)
   int nsplit;
-};
-
-template <typename T>
-struct Consts {
-  T cexp;  // exp argument scale: -log2(e)/sigma^2 (FP32) or -1/sigma^2 (FP64)
 };
 
 __device__ __forceinline__ void put(double *p, int acc, double v) {
@@ -131,7 +127,7 @@ struct OpConvGradAlpha {
 #pragma unroll
       for (int k = 0; k < DV; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, v[k]);
     }
-    const double f = -2.0 / (a.sigma * a.sigma);
+    const double f = -2.0 / (a.sigma * a.sigma * a.xscale);  // dx was accumulated pre-scaled
 #pragma unroll
     for (int l = 0; l < D; ++l) put(a.out1 + i * a.out1_ld + l, a.acc1, v[G0 + l] * f);
   }
@@ -159,7 +155,7 @@ struct OpVarlin {
       for (int l = 0; l < D; ++l) acc[k * D + l] = L::fma(ed[l], s[k], acc[k * D + l]);
   }
   __device__ static void store(const PairArgs &a, long i, const double *v) {
-    const double f = -2.0 / (a.sigma * a.sigma);
+    const double f = -2.0 / (a.sigma * a.sigma * a.xscale);
 #pragma unroll
     for (int o = 0; o < DV * D; ++o) put(a.out0 + i * a.out0_ld + o, a.acc0, v[o] * f);
   }
@@ -188,7 +184,7 @@ struct OpGradDim {
     for (int k = 0; k < DV; ++k) acc[k] = L::fma(g, s[k], acc[k]);
   }
   __device__ static void store(const PairArgs &a, long i, const double *v) {
-    const double f = -2.0 / (a.sigma * a.sigma);
+    const double f = -2.0 / (a.sigma * a.sigma * a.xscale);
 #pragma unroll
     for (int k = 0; k < DV; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, v[k] * f);
   }
@@ -226,7 +222,7 @@ struct OpHessFull {
   }
   __device__ static void store(const PairArgs &a, long i, const double *v) {
     const double s2 = a.sigma * a.sigma;
-    const double c4 = 4.0 / (s2 * s2), c2 = 2.0 / s2;
+    const double c4 = 4.0 / (s2 * s2 * a.xscale * a.xscale), c2 = 2.0 / s2;
 #pragma unroll
     for (int k = 0; k < DV; ++k) {
       const double *vk = v + k * (NP + 1);
@@ -267,7 +263,7 @@ struct OpHessRowCol {
   }
   __device__ static void store(const PairArgs &a, long i, const double *v) {
     const double s2 = a.sigma * a.sigma;
-    const double c4 = 4.0 / (s2 * s2), c2 = 2.0 / s2;
+    const double c4 = 4.0 / (s2 * s2 * a.xscale * a.xscale), c2 = 2.0 / s2;
 #pragma unroll
     for (int k = 0; k < DV; ++k) {
       double h = c4 * v[2 * k] - (a.p0 == a.p1 ? c2 * v[2 * k + 1] : 0.0);
@@ -318,7 +314,7 @@ struct OpSpecialHessian {
   }
   __device__ static void store(const PairArgs &a, long i, const double *v) {
     const double s2 = a.sigma * a.sigma;
-    const double c4 = 4.0 / (s2 * s2), c2 = 2.0 / s2;
+    const double c4 = 4.0 / (s2 * s2 * a.xscale * a.xscale), c2 = 2.0 / s2;
 #pragma unroll
     for (int k = 0; k < D; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, c4 * v[k] - c2 * v[D + k]);
   }
@@ -358,8 +354,8 @@ struct Rec {
 
 // CENTER: subtract the CTA's target bounding-box midpoint (FP32 mode). FP64 mode forms x - y
 // directly, as the reference does.
-template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE>
-__global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
   typedef Lane<T> L;
   typedef typename L::V V;
   typedef typename SrcLane<T>::SV SV;
@@ -432,7 +428,8 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
     for (int l = 0; l < D; ++l) ctr[l] = 0.0;
   }
 
-  // ---- this thread's targets: centred coordinates and extras, in lanes ----
+  const double xs = a.xscale;
+  // ---- this thread's targets: centred, pre-scaled coordinates and extras, in lanes ----
   V xg[G][D];
   V tg[G][Op::NT > 0 ? Op::NT : 1];
 #pragma unroll
@@ -443,7 +440,7 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
       long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
       long ic = i < nx ? i : (nx - 1);  // out-of-range lanes compute a copy, never stored
 #pragma unroll
-      for (int l = 0; l < D; ++l) xv[w2][l] = a.x[ic * D + l] - ctr[l];
+      for (int l = 0; l < D; ++l) xv[w2][l] = (a.x[ic * D + l] - ctr[l]) * xs;
       Op::load_target(a, ic, tv[w2]);
     }
 #pragma unroll
@@ -472,13 +469,13 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
 
   for (long jt = jb; jt < je; jt += TJ) {
     const int cnt = (int)((je - jt) < TJ ? (je - jt) : TJ);
-    // ---- stage TJ source records: -(y - c) and extras, broadcast to the lane type ----
+    // ---- stage TJ source records: -(y - c) * xscale and extras, broadcast to the lane type ----
     for (int r = threadIdx.x; r < TJ; r += BLOCK) {
       double rec[NJP];
       if (r < cnt) {
         long j = jt + r;
 #pragma unroll
-        for (int l = 0; l < D; ++l) rec[l] = ctr[l] - a.y[j * D + l];
+        for (int l = 0; l < D; ++l) rec[l] = (ctr[l] - a.y[j * D + l]) * xs;
         Op::load_source(a, j, rec + D);
       } else {
 #pragma unroll
@@ -511,7 +508,7 @@ __global__ void __launch_bounds__(BLOCK) pair_kernel(const PairArgs a) {
           V r2 = L::mul(dx[0], dx[0]);
 #pragma unroll
           for (int l = 1; l < D; ++l) r2 = L::fma(dx[l], dx[l], r2);
-          V e = L::exp2v(L::mul(r2, cx));
+          V e = L::kexp(r2, cx);
           Op::template accum<T>(dx, e, tg[g], s + D, acc[g], p0, p1);
         }
       }
@@ -570,13 +567,14 @@ struct LaunchCfg {
   int nsplit;   // source splits (grid.y); 1 = no partial buffer
 };
 
-template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE>
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB>
 cudaError_t launch_pairs(PairArgs a, int nsplit, cudaStream_t st) {
   if (a.nx <= 0) return cudaSuccess;
   constexpr int NJP = Rec<Op, D>::NJP;
   typedef typename SrcLane<T>::SV SV;
   const size_t smem = (size_t)TJ * NJP * sizeof(SV);
-  auto kern = pair_kernel<Op, T, D, BLOCK, R, TJ, MERGE>;
+  auto kern = pair_kernel<Op, T, D, BLOCK, R, TJ, MERGE, MINB>;
+  a.xscale = coord_scale<T>(a.sigma);
   if (smem > 48 * 1024) {  // per current device; idempotent
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

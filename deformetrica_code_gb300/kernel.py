@@ -94,10 +94,16 @@ class Context:
     def bind_stream(self, *arrays):
         """Queue on torch's current stream when any argument is a CUDA tensor."""
         if any(_is_torch(a) and a.is_cuda for a in arrays if a is not None):
-            s = torch.cuda.current_stream(self.device).cuda_stream
-            self.check(self.lib.gbk_set_stream(self.h, ctypes.c_void_p(s)))
+            self.use_torch_stream()
         else:
             self.check(self.lib.gbk_set_stream(self.h, None))
+
+    def use_torch_stream(self):
+        """Queue later calls on torch's current CUDA stream. torch reports the legacy default
+        stream as handle 0; the library reads NULL as "the context's own stream", so that case
+        is passed as cudaStreamLegacy (0x1)."""
+        s = torch.cuda.current_stream(self.device).cuda_stream or 1
+        self.check(self.lib.gbk_set_stream(self.h, ctypes.c_void_p(s)))
 
     def synchronize(self):
         self.check(self.lib.gbk_synchronize(self.h))

@@ -73,7 +73,8 @@ int gbk_create(int device, gbk_ctx **out);
 void gbk_destroy(gbk_ctx *ctx);
 /* Message of the last failed call on this context ("" if none). */
 const char *gbk_last_error(const gbk_ctx *ctx);
-/* Uses `stream` (a cudaStream_t) for all later calls; NULL restores the context's own stream. */
+/* Uses `stream` (a cudaStream_t) for all later calls; NULL restores the context's own stream
+ * (pass cudaStreamLegacy, i.e. (void *)0x1, to queue on the legacy default stream). */
 int gbk_set_stream(gbk_ctx *ctx, void *stream);
 void *gbk_get_stream(const gbk_ctx *ctx);
 int gbk_set_mode(gbk_ctx *ctx, int mode);

@@ -155,6 +155,90 @@ def accuracy(x, y, w, a, sigma, v, gx, gy, gw, sample: int = 2048, seed: int = 7
             "measure": "normwise max_i|err_i|/max_i|ref_i|"}
 
 
+def registration_workload():
+    """Shooting + adjoint registration: 1,000 control points on the cell-centred grid
+    {0.05, ..., 0.95}^3, momenta ~ N(0, 0.01) (std 0.1, seed 2), template = icosphere of radius
+    0.4 centred at (0.5, 0.5, 0.5) with 10,242 vertices / 20,480 faces, target = the same sphere
+    with vertices moved 0.05 sin(4 pi x) along the normals, deformation kernel width 0.15, 11
+    time points (10 Euler steps, Heun flow/adjoint), currents data term of width 0.1."""
+    from deformetrica_code_gb300 import meshes as M
+    g = np.arange(0.05, 1.0, 0.1)
+    cp = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    mom = 0.1 * np.random.default_rng(2).standard_normal(cp.shape)
+    tp, tf = M.icosphere(5, 0.4)
+    gp = M.sine_bump(tp, tf, 0.05, 4.0)
+    return cp, mom, tp, tf, gp, tf, dict(T=11, sigma_def=0.15, sigma_data=0.1, data_sigma2=0.01)
+
+
+def registration_bench(steps: int, cpu: bool = True):
+    """s/iter of one registration iteration (forward + gradient) on the GPU (graph replay) in the
+    compensated-FP32 and FP64 modes, the FP64 CPU oracle, and a central finite-difference check
+    of the gradient (eps = 1e-3, FP64 mode)."""
+    import deformetrica_code_gb300 as g
+    from deformetrica_code_gb300.deformation import Registration
+    cp, mom, tp, tf, gp, gf, kw = registration_workload()
+    res = {"workload": "1000 CP x 10242-vertex icosphere, T=11, sigma_def 0.15, currents sigma 0.1"}
+    for name, mode, nsteps in (("f32c", g.GBK_MODE_F32C, steps), ("f64", g.GBK_MODE_F64, max(2, steps // 4))):
+        ctx = g.Context(mode=mode)
+        reg = Registration(cp.shape[0], tp, tf, gp, gf, context=ctx, **kw)
+        for _ in range(3):  # eager, capture, first replay
+            ll, gcp, gm = reg.step(cp, mom)
+        ts = []
+        for _ in range(nsteps):
+            t0 = time.perf_counter()
+            ll, gcp, gm = reg.step(cp, mom)
+            ts.append(time.perf_counter() - t0)
+        res[name] = {"s_per_iter": statistics.mean(ts), "loglik": float(ll[0]),
+                     "kernels_per_iter": reg.graph_launches()}
+        if name == "f64":
+            v = np.random.default_rng(9).standard_normal(mom.shape)
+            eps = 1e-3
+            lp = reg.step(cp, mom + eps * v)[0][0]
+            lm_ = reg.step(cp, mom - eps * v)[0][0]
+            fd = (lp - lm_) / (2 * eps)
+            an = float(np.sum(gm * v))
+            res["fd_check"] = {"eps": eps, "fd": fd, "adjoint": an, "rel_diff": abs(fd - an) / abs(an)}
+        if name == "f32c":
+            g32 = gm
+        else:
+            res["f32c_vs_f64_grad_mom_normwise"] = float(np.linalg.norm(g32 - gm, axis=1).max()
+                                                         / np.linalg.norm(gm, axis=1).max())
+        reg.close()
+    if cpu:
+        import oracle
+        from oracle import deformation as D
+        K = oracle.load("port")
+        t0 = time.perf_counter()
+        D.registration(K, cp, mom, tp, tf, gp, gf, kw["T"], kw["sigma_def"], kw["sigma_data"],
+                       kw["data_sigma2"], kind="currents")
+        res["cpu_fp64_oracle"] = {"s_per_iter": time.perf_counter() - t0,
+                                  "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))}
+    return res
+
+
+def fp64_gpu_pairs(n: int, sigma: float):
+    """The same fused forward+adjoint step in the FP64 mode (plain FP64 kernel sums) at N = M = n."""
+    import torch
+    import deformetrica_code_gb300 as g
+    x, y, w, a = make_workload(n, n, seed=5)
+    ctx = g.Context(mode=g.GBK_MODE_F64)
+    ctx.use_torch_stream()
+    X, Y, W, A = (torch.from_numpy(t).cuda() for t in (x, y, w, a))
+    outs = [torch.empty_like(X) for _ in range(4)]
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    step = lambda: ctx.check(ctx.lib.gbk_forward_adjoint(ctx.h, 3, 3, p(X), n, p(Y), p(W), n, sigma, p(A),
+                                                         *[p(o) for o in outs]))
+    step()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    step()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e)
+    return {"value": n * n / (ms / 1e3), "unit": UNIT, "N": n, "ms_per_step": ms}
+
+
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return 0
@@ -202,6 +286,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--fp64-n", type=int, default=200_000)
+    ap.add_argument("--no-registration", action="store_true")
+    ap.add_argument("--reg-steps", type=int, default=10)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -338,6 +426,10 @@ def main():
                                         GY.cpu().numpy(), GW.cpu().numpy())
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(args.cpu_sample)
+        if not args.no_fp64:
+            line["fp64_gpu"] = fp64_gpu_pairs(args.fp64_n, args.sigma)
+        if not args.no_registration:
+            line["shooting_adjoint"] = registration_bench(args.reg_steps, cpu=not args.no_cpu_baseline)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

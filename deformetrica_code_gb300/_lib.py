@@ -66,6 +66,20 @@ SIGNATURES = {
     "gbk_tune_save": (_I, [_P, ctypes.c_char_p]),
     "gbk_tune_load": (_I, [_P, ctypes.c_char_p]),
     "gbk_set_split": (_I, [_P, _I]),
+    "gbk_shoot": (_I, [_P, _I, _L, _P, _P, _I, _D, _P, _P]),
+    "gbk_flow_landmarks": (_I, [_P, _I, _L, _P, _P, _I, _D, _L, _P, _I, _P]),
+    "gbk_adjoint_landmarks": (_I, [_P, _I, _L, _P, _P, _I, _D, _L, _P, _P, _I, _P]),
+    "gbk_compute_update_at": (_I, [_P, _I, _L, _P, _P, _P, _P, _L, _P, _P, _D, _P, _P]),
+    "gbk_adjoint_diffeo": (_I, [_P, _I, _L, _P, _P, _I, _D, _L, _P, _P, _I, _P, _P]),
+    "gbk_currents_match": (_I, [_P, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
+    "gbk_varifold_match": (_I, [_P, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
+    "gbk_registration_create": (_I, [_P, _I, _L, _L, _P, _L, _P, _L, _P, _L, _P, _I, _D, _D, _D, _I, _I,
+                                     ctypes.POINTER(_P)]),
+    "gbk_registration_step": (_I, [_P, _P, _P, _P, _P, _P]),
+    "gbk_registration_set_graph": (_I, [_P, _I]),
+    "gbk_registration_trajectories": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "gbk_registration_graph_launches": (ctypes.c_longlong, [_P]),
+    "gbk_registration_destroy": (None, [_P]),
 }
 
 _lib = None

@@ -16,6 +16,7 @@
 #include "../../include/gbk.h"
 #include "gbk_ctx.h"
 #include "gbk_dispatch.h"
+#include "gbk_hostio.h"
 
 using namespace gbk;
 
@@ -34,6 +35,7 @@ int op_outputs(int op, int d, int dv) {
     case OP_HESSFULL: return dv * (d * (d + 1) / 2 + 1);
     case OP_HESSRC: return 2 * dv;
     case OP_SPECIAL: return 2 * d;
+    case OP_ADJCP: return 5 * d;
   }
   return 0;
 }
@@ -48,6 +50,7 @@ bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
     case OP_HESSFULL:
     case OP_HESSRC:
     case OP_SPECIAL: return find_kernel_hess(op, mode, d, dv, variant, e);
+    case OP_ADJCP: return find_kernel_deform(op, mode, d, dv, variant, e);
   }
   return false;
 }
@@ -123,70 +126,6 @@ int gbk_ctx::ensure(DevBuf &b, size_t bytes, const char *what) {
   return GBK_OK;
 }
 
-static bool is_device_pointer(const void *p) {
-  if (!p) return true;
-  cudaPointerAttributes at;
-  cudaError_t e = cudaPointerGetAttributes(&at, p);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
-// Stages host arguments through the context's device buffers.
-struct HostIO {
-  gbk_ctx *c;
-  int slot = 0;
-  int rc = GBK_OK;
-  bool any_host = false;
-  struct Out {
-    double *host;
-    double *dev;
-    size_t n;
-  };
-  std::vector<Out> outs;
-  explicit HostIO(gbk_ctx *ctx) : c(ctx) {}
-
-  const double *in(const double *p, size_t n, const char *name) {
-    if (rc || !p || n == 0 || is_device_pointer(p)) return p;
-    any_host = true;
-    if (slot >= gbk_ctx::kStageSlots) {
-      rc = c->fail(GBK_ERR_ARG, "too many host arguments");
-      return nullptr;
-    }
-    gbk_ctx::DevBuf &b = c->stage[slot++];
-    rc = c->ensure(b, n * sizeof(double), name);
-    if (rc) return nullptr;
-    rc = c->cuda(cudaMemcpyAsync(b.p, p, n * sizeof(double), cudaMemcpyHostToDevice, c->stream),
-                 "cudaMemcpyAsync H2D");
-    return rc ? nullptr : (const double *)b.p;
-  }
-  double *out(double *p, size_t n, const char *name) {
-    if (rc || !p || n == 0 || is_device_pointer(p)) return p;
-    any_host = true;
-    if (slot >= gbk_ctx::kStageSlots) {
-      rc = c->fail(GBK_ERR_ARG, "too many host arguments");
-      return nullptr;
-    }
-    gbk_ctx::DevBuf &b = c->stage[slot++];
-    rc = c->ensure(b, n * sizeof(double), name);
-    if (rc) return nullptr;
-    outs.push_back({p, (double *)b.p, n});
-    return (double *)b.p;
-  }
-  int finish() {
-    if (rc) return rc;
-    for (auto &o : outs) {
-      rc = c->cuda(cudaMemcpyAsync(o.host, o.dev, o.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
-                   "cudaMemcpyAsync D2H");
-      if (rc) return rc;
-    }
-    if (any_host) rc = c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
-    return rc;
-  }
-};
-
 // Tuning-table key: operation, precision, shape and size buckets (powers of two).
 static int bucket(long n) {
   int b = 0;
@@ -246,6 +185,18 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
   if (it != tune.end()) {
     variant = it->second.first;
     ns = it->second.second;
+  } else {
+    // Too little work for the default shape to fill the GPU (e.g. control points x control
+    // points): use the small shape (fewer targets per CTA, shorter source tiles, more splits).
+    KernelEntry e0;
+    if (find_kernel(op, mode, d, dv, 0, &e0)) {
+      long per_cta = (long)e0.block * e0.r;
+      long itiles = (a.nx + per_cta - 1) / per_cta;
+      long max_split = std::max(1L, a.ny / (2L * e0.tj));
+      KernelEntry es;
+      if (itiles * max_split < 2L * num_sms && find_kernel(op, mode, d, dv, VARIANT_SMALL, &es))
+        variant = VARIANT_SMALL;
+    }
   }
   KernelEntry e;
   if (!find_kernel(op, mode, d, dv, variant, &e) && !find_kernel(op, mode, d, dv, 0, &e))

@@ -1,0 +1,33 @@
+// Device-pointer loop bodies of the deformation engine (gbk_deform.cu), shared with the
+// registration and atlas objects.
+#pragma once
+
+#include "gbk_ctx.h"
+
+namespace gbk {
+
+struct DeformScratch {
+  int *flag;  // "momenta below 1e-20" flag (device int)
+  double *va;  // max(ncp, nlm) x d temporaries
+  double *vb;
+  double *vc;
+  double *vd;
+};
+
+int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *mom0, int T,
+                 double sigma, double *pos, double *mom, const DeformScratch &s);
+int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
+                double sigma, long nlm, const double *lm0, int heun, double *lm,
+                const DeformScratch &s);
+int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
+                             int T, double sigma, long nlm, const double *lm,
+                             const double *theta_final, int heun, double *theta,
+                             const DeformScratch &s);
+int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
+                     const double *xp, const double *xm, long nlm, const double *lm,
+                     const double *theta, double sigma, double *dpos, double *dmom);
+int adjoint_diffeo_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
+                          double sigma, long nlm, const double *lm, const double *theta, int heun,
+                          double *xp, double *xm, const DeformScratch &s);
+
+}  // namespace gbk

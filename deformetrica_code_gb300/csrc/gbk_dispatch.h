@@ -18,8 +18,12 @@ enum OpId {
   OP_HESSFULL = 5,   // ConvolveHessian(X)
   OP_HESSRC = 6,     // ConvolveHessian(X, row, col) (p0 = row, p1 = col)
   OP_SPECIAL = 7,    // ConvolveSpecialHessian(xi)
-  OP_COUNT = 8
+  OP_ADJCP = 8,      // control-point part of ComputeUpdateAt (fused)
+  OP_COUNT = 9
 };
+
+// Launch-shape index for problems too small to fill the GPU with the default shape.
+constexpr int VARIANT_SMALL = 8;
 
 enum Mode { MODE_F32C = 0, MODE_F64 = 1 };
 
@@ -50,6 +54,7 @@ const int *supported_dv(int d, int *count);
 bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry *e);
+bool find_kernel_deform(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 
 }  // namespace gbk
 

@@ -12,7 +12,11 @@ namespace gbk {
 template <template <int, int> class OP, int D, int DV>
 static bool pick_conv_like(int mode, int variant, KernelEntry *e) {
   typedef OP<D, DV> O;
-  if (mode == MODE_F64) return set_entry<O, double, D, 128, 1, 128, 128>(e);
+  if (mode == MODE_F64) {
+    if (variant == VARIANT_SMALL) return set_entry<O, double, D, 64, 1, 32, 32, 8>(e);
+    return set_entry<O, double, D, 128, 1, 128, 128>(e);
+  }
+  if (variant == VARIANT_SMALL) return set_entry<O, float, D, 64, 2, 32, 32, 8>(e);
   constexpr bool hot = (D == 3 && DV == 3) || (D == 2 && DV == 2);
   if constexpr (hot) {
     switch (variant) {

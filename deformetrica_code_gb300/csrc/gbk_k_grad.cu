@@ -4,36 +4,40 @@
 namespace gbk {
 
 template <template <int, int> class OP, int D, int DV>
-static bool pick_one(int mode, KernelEntry *e) {
+static bool pick_one(int mode, int variant, KernelEntry *e) {
   typedef OP<D, DV> O;
+  if (variant == VARIANT_SMALL) {
+    if (mode == MODE_F64) return set_entry<O, double, D, 64, 1, 32, 32, 8>(e);
+    return set_entry<O, float, D, 64, 2, 32, 32, 8>(e);
+  }
   if (mode == MODE_F64) return set_entry<O, double, D, 128, 1, 128, 128>(e);
   return set_entry<O, float, D, 256, 2, 256, 64, 2>(e);
 }
 
 template <template <int, int> class OP>
-static bool by_shape(int mode, int d, int dv, KernelEntry *e) {
+static bool by_shape(int mode, int d, int dv, int variant, KernelEntry *e) {
   if (d == 2) {
     switch (dv) {
-      case 1: return pick_one<OP, 2, 1>(mode, e);
-      case 2: return pick_one<OP, 2, 2>(mode, e);
-      case 3: return pick_one<OP, 2, 3>(mode, e);
-      case 4: return pick_one<OP, 2, 4>(mode, e);
+      case 1: return pick_one<OP, 2, 1>(mode, variant, e);
+      case 2: return pick_one<OP, 2, 2>(mode, variant, e);
+      case 3: return pick_one<OP, 2, 3>(mode, variant, e);
+      case 4: return pick_one<OP, 2, 4>(mode, variant, e);
     }
   } else if (d == 3) {
     switch (dv) {
-      case 1: return pick_one<OP, 3, 1>(mode, e);
-      case 2: return pick_one<OP, 3, 2>(mode, e);
-      case 3: return pick_one<OP, 3, 3>(mode, e);
-      case 6: return pick_one<OP, 3, 6>(mode, e);
+      case 1: return pick_one<OP, 3, 1>(mode, variant, e);
+      case 2: return pick_one<OP, 3, 2>(mode, variant, e);
+      case 3: return pick_one<OP, 3, 3>(mode, variant, e);
+      case 6: return pick_one<OP, 3, 6>(mode, variant, e);
     }
   }
   return false;
 }
 
-bool find_kernel_grad(int op, int mode, int d, int dv, int, KernelEntry *e) {
+bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
   switch (op) {
-    case OP_VARLIN: return by_shape<OpVarlin>(mode, d, dv, e);
-    case OP_GRADDIM: return by_shape<OpGradDim>(mode, d, dv, e);
+    case OP_VARLIN: return by_shape<OpVarlin>(mode, d, dv, variant, e);
+    case OP_GRADDIM: return by_shape<OpGradDim>(mode, d, dv, variant, e);
   }
   return false;
 }

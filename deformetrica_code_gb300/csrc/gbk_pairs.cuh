@@ -320,6 +320,77 @@ struct OpSpecialHessian {
   }
 };
 
+// The control-point part of AdjointEquationsIntegrator::ComputeUpdateAt
+// (AdjointEquationsIntegrator.cxx:476-570) in ONE pass over the CP x CP pairs. The reference
+// makes five kernel calls for it (Convolve and varlin ConvolveGradient of [p | xi_pos], d calls of
+// ConvolveGradient(X, dim) with weights xi_mom[:, dim] p, and ConvolveSpecialHessian(xi_mom));
+// with dx = x_i - x_j, dK = -2 K dx / sigma^2, dxi = xi_mom_j - xi_mom_i they sum to
+//   dXi3_i = sum_j (xi_pos_i . p_j + p_i . xi_pos_j) dK
+//   dXi4_i = sum_j (p_i . p_j) K [4/sigma^4 (dx . dxi) dx - 2/sigma^2 dxi]
+//   dXi5_i = sum_j K xi_pos_j
+//   dXi6_i = sum_j (dK . dxi) p_j
+// and the op writes dPos = dXi3 + dXi4 (out0) and dMom = dXi5 + dXi6 (out1).
+// Target and source extras are (p, xi_pos, xi_mom): ta -> p, tb -> xi_pos, a.sb -> xi_mom, all
+// with leading dimension D.
+template <int D>
+struct OpAdjointCP {
+  static constexpr int NT = 3 * D, NS = 3 * D, NO = 5 * D;
+  __device__ static void load_target(const PairArgs &a, long i, double *t) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      t[k] = a.ta[i * D + k];
+      t[D + k] = a.tb[i * D + k];
+      t[2 * D + k] = -a.sb[i * D + k];  // -xi_mom_i
+    }
+  }
+  __device__ static void load_source(const PairArgs &a, long j, double *s) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      s[k] = a.w[j * D + k];
+      s[D + k] = a.tb[j * D + k];
+      s[2 * D + k] = a.sb[j * D + k];
+    }
+  }
+  template <typename T, typename V, typename SV>
+  __device__ __forceinline__ static void accum(const V *dx, V e, const V *t, const SV *s, V *acc, int, int) {
+    typedef Lane<T> L;
+    // t: p_i, xp_i, -xm_i ; s: p_j, xp_j, xm_j
+    V a1 = L::mul(t[D], s[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) a1 = L::fma(t[D + k], s[k], a1);
+#pragma unroll
+    for (int k = 0; k < D; ++k) a1 = L::fma(t[k], s[D + k], a1);
+    V bb = L::mul(t[0], s[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) bb = L::fma(t[k], s[k], bb);
+    V dxi[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) dxi[k] = L::add(s[2 * D + k], t[2 * D + k]);
+    V q = L::mul(dx[0], dxi[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) q = L::fma(dx[k], dxi[k], q);
+    V ka = L::mul(e, a1), kb = L::mul(e, bb);
+    V kbq = L::mul(kb, q), kq = L::mul(e, q);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      acc[k] = L::fma(ka, dx[k], acc[k]);                  // A
+      acc[D + k] = L::fma(kbq, dx[k], acc[D + k]);         // B
+      acc[2 * D + k] = L::fma(kb, dxi[k], acc[2 * D + k]); // C
+      acc[3 * D + k] = L::fma(e, s[D + k], acc[3 * D + k]);  // E
+      acc[4 * D + k] = L::fma(kq, s[k], acc[4 * D + k]);   // F
+    }
+  }
+  __device__ static void store(const PairArgs &a, long i, const double *v) {
+    const double s2 = a.sigma * a.sigma, xs = a.xscale;
+    const double cg = -2.0 / (s2 * xs), c4 = 4.0 / (s2 * s2 * xs * xs), c2 = -2.0 / s2;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      put(a.out0 + i * a.out0_ld + k, a.acc0, cg * v[k] + c4 * v[D + k] + c2 * v[2 * D + k]);
+      put(a.out1 + i * a.out1_ld + k, a.acc1, v[3 * D + k] + cg * v[4 * D + k]);
+    }
+  }
+};
+
 // =============================================================================================
 // The kernel.
 // =============================================================================================

@@ -241,7 +241,7 @@ int gbk_tune_load(gbk_ctx *c, const char *path) {
     int op, mode, d, dv, bx, by, v, ns;
     if (sscanf(line, "{\"op\": %d, \"mode\": %d, \"d\": %d, \"dv\": %d, \"bx\": %d, \"by\": %d, \"variant\": %d, \"nsplit\": %d}",
                &op, &mode, &d, &dv, &bx, &by, &v, &ns) == 8) {
-      if (v < 0 || v >= num_variants(op, mode, d, dv) || ns < 0) continue;  // nsplit 0 = automatic
+      if (v < 0 || (v >= num_variants(op, mode, d, dv) && v != VARIANT_SMALL) || ns < 0) continue;  // nsplit 0 = automatic
       c->tune[gbk_ctx::TuneKey{op, mode, d, dv, bx, by}] = {v, ns};
     }
   }

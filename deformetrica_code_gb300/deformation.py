@@ -1,0 +1,163 @@
+"""Python interface to the device-resident deformation engine, data terms and registration step.
+
+Mirrors the reference's Diffeos (Diffeos.cxx:589-712), AdjointEquationsIntegrator
+(AdjointEquationsIntegrator.cxx:33-570), the surface data terms (OrientedSurfaceMesh.cxx,
+NonOrientedSurfaceMesh.cxx) and one DeterministicAtlas subject iteration
+(DeterministicAtlas.cxx:99-280, AbstractAtlas.cxx:559-613). Inputs are float64 numpy arrays
+(host) or CUDA float64 torch tensors; every computation runs in libgbkernel.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from .kernel import Context, _empty_like, _is_torch, _ptr
+
+
+def _f64(a):
+    if _is_torch(a):
+        return a.contiguous()
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    if _is_torch(a):
+        import torch
+        return a.to(torch.int32).contiguous()
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Deformation:
+    """Landmark diffeomorphism: Gaussian kernel of width sigma, T time points on [0, 1]."""
+
+    def __init__(self, d: int, sigma: float, T: int, heun: bool = True, context: Context | None = None):
+        self.d, self.sigma, self.T, self.heun = d, float(sigma), int(T), bool(heun)
+        self.ctx = context or Context()
+
+    def _call(self, name, *args, arrays=()):
+        self.ctx.bind_stream(*arrays)
+        self.ctx.check(getattr(self.ctx.lib, name)(self.ctx.h, *args))
+
+    def shoot(self, cp0, mom0):
+        cp0, mom0 = _f64(cp0), _f64(mom0)
+        n = cp0.shape[0]
+        pos = _empty_like(cp0, (self.T, n, self.d))
+        mom = _empty_like(cp0, (self.T, n, self.d))
+        self._call("gbk_shoot", self.d, n, _ptr(cp0), _ptr(mom0), self.T, self.sigma, _ptr(pos),
+                   _ptr(mom), arrays=(cp0, mom0))
+        return pos, mom
+
+    def flow(self, pos, mom, lm0):
+        pos, mom, lm0 = _f64(pos), _f64(mom), _f64(lm0)
+        lm = _empty_like(lm0, (self.T, lm0.shape[0], self.d))
+        self._call("gbk_flow_landmarks", self.d, pos.shape[1], _ptr(pos), _ptr(mom), self.T, self.sigma,
+                   lm0.shape[0], _ptr(lm0), int(self.heun), _ptr(lm), arrays=(pos, mom, lm0))
+        return lm
+
+    def adjoint_landmarks(self, pos, mom, lm, theta_final):
+        pos, mom, lm, th = _f64(pos), _f64(mom), _f64(lm), _f64(theta_final)
+        theta = _empty_like(th, (self.T, lm.shape[1], self.d))
+        self._call("gbk_adjoint_landmarks", self.d, pos.shape[1], _ptr(pos), _ptr(mom), self.T, self.sigma,
+                   lm.shape[1], _ptr(lm), _ptr(th), int(self.heun), _ptr(theta), arrays=(pos, mom, lm, th))
+        return theta
+
+    def compute_update_at(self, pos, mom, xi_pos, xi_mom, lm=None, theta=None):
+        pos, mom, xp, xm = (_f64(a) for a in (pos, mom, xi_pos, xi_mom))
+        nlm = 0 if lm is None else lm.shape[0]
+        lm = None if lm is None else _f64(lm)
+        theta = None if theta is None else _f64(theta)
+        dpos = _empty_like(pos, pos.shape)
+        dmom = _empty_like(pos, pos.shape)
+        self._call("gbk_compute_update_at", self.d, pos.shape[0], _ptr(pos), _ptr(mom), _ptr(xp), _ptr(xm),
+                   nlm, _ptr(lm), _ptr(theta), self.sigma, _ptr(dpos), _ptr(dmom), arrays=(pos, mom, xp, xm))
+        return dpos, dmom
+
+    def adjoint_diffeo(self, pos, mom, lm=None, theta=None):
+        pos, mom = _f64(pos), _f64(mom)
+        nlm = 0 if lm is None else lm.shape[1]
+        lm = None if lm is None else _f64(lm)
+        theta = None if theta is None else _f64(theta)
+        xp = _empty_like(pos, pos.shape)
+        xm = _empty_like(pos, pos.shape)
+        self._call("gbk_adjoint_diffeo", self.d, pos.shape[1], _ptr(pos), _ptr(mom), self.T, self.sigma, nlm,
+                   _ptr(lm), _ptr(theta), int(self.heun), _ptr(xp), _ptr(xm), arrays=(pos, mom))
+        return xp, xm
+
+
+def _surface(name, ctx, pts, tris, pts_t, tris_t, sigma, grad=True):
+    ctx = ctx or Context()
+    pts, pts_t = _f64(pts), _f64(pts_t)
+    tris, tris_t = _i32(tris), _i32(tris_t)
+    match = np.zeros(1)
+    g = np.zeros(pts.shape) if grad else None
+    ctx.bind_stream()
+    ctx.check(getattr(ctx.lib, name)(ctx.h, pts.shape[0], _ptr(pts), tris.shape[0], _ptr(tris),
+                                     pts_t.shape[0], _ptr(pts_t), tris_t.shape[0], _ptr(tris_t),
+                                     float(sigma), ctypes.c_void_p(match.ctypes.data), _ptr(g)))
+    return float(match[0]), g
+
+
+def currents_match(pts, tris, pts_t, tris_t, sigma, grad=True, context: Context | None = None):
+    """Currents distance |S - T|^2 and its gradient w.r.t. pts (OrientedSurfaceMesh.cxx:124-241)."""
+    return _surface("gbk_currents_match", context, pts, tris, pts_t, tris_t, sigma, grad)
+
+
+def varifold_match(pts, tris, pts_t, tris_t, sigma, grad=True, context: Context | None = None):
+    """Varifold distance and its gradient w.r.t. pts (NonOrientedSurfaceMesh.cxx:124-265)."""
+    return _surface("gbk_varifold_match", context, pts, tris, pts_t, tris_t, sigma, grad)
+
+
+class Registration:
+    """One subject of DeterministicAtlas with a frozen template, replayed from a CUDA graph."""
+
+    KINDS = {"currents": 0, "varifold": 1}
+
+    def __init__(self, ncp: int, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T: int, sigma_def: float,
+                 sigma_data: float, data_sigma2: float, kind: str = "currents", heun: bool = True,
+                 context: Context | None = None):
+        self.ctx = context or Context()
+        self.ncp, self.T = int(ncp), int(T)
+        tp, tt = _f64(tmpl_pts), _i32(tmpl_tris)
+        gp, gt = _f64(tgt_pts), _i32(tgt_tris)
+        self.nv = tp.shape[0]
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbk_registration_create(
+            self.ctx.h, 3, self.ncp, tp.shape[0], _ptr(tp), tt.shape[0], _ptr(tt), gp.shape[0], _ptr(gp),
+            gt.shape[0], _ptr(gt), self.T, float(sigma_def), float(sigma_data), float(data_sigma2),
+            self.KINDS[kind], int(heun), ctypes.byref(h)))
+        self.h = h
+
+    def set_graph(self, enable: bool):
+        self.ctx.check(self.ctx.lib.gbk_registration_set_graph(self.h, int(enable)))
+
+    def step(self, cp, mom):
+        """Returns (loglik[5] = L, L_data, L_reg, match, <Kp,p>), dL/dcp, dL/dp."""
+        cp, mom = _f64(cp), _f64(mom)
+        ll = np.zeros(5)
+        gcp = _empty_like(cp, cp.shape)
+        gmom = _empty_like(cp, cp.shape)
+        self.ctx.check(self.ctx.lib.gbk_registration_step(self.h, _ptr(cp), _ptr(mom),
+                                                          ctypes.c_void_p(ll.ctypes.data), _ptr(gcp), _ptr(gmom)))
+        return ll, gcp, gmom
+
+    def graph_launches(self) -> int:
+        return int(self.ctx.lib.gbk_registration_graph_launches(self.h))
+
+    def trajectories(self):
+        shp_c = (self.T, self.ncp, 3)
+        shp_v = (self.T, self.nv, 3)
+        out = [np.zeros(shp_c), np.zeros(shp_c), np.zeros(shp_v), np.zeros(shp_v), np.zeros(shp_c), np.zeros(shp_c)]
+        self.ctx.check(self.ctx.lib.gbk_registration_trajectories(self.h, *[ctypes.c_void_p(a.ctypes.data) for a in out]))
+        return dict(zip(("pos", "mom", "lm", "theta", "xi_pos", "xi_mom"), out))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbk_registration_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

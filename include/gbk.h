@@ -162,6 +162,83 @@ int gbk_forward_adjoint(gbk_ctx *ctx, int d, int dv, const double *x, long nx, c
 int gbk_kernel_norm(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
                     double sigma, double *out);
 
+/* ---- deformation (trajectories are T x n x d row-major blocks; dt = 1 / (T - 1)) --------- */
+
+/* Diffeos::Shoot, Diffeos.cxx:589-660: explicit Euler on x' = K(x,x) p, p' = -G(x)^T p, one
+ * fused Convolve + alpha-gradient pass per step. Nearly zero momenta (|p0|_F < 1e-20) give the
+ * reference's constant trajectory (:611-613). */
+int gbk_shoot(gbk_ctx *ctx, int d, long ncp, const double *cp0, const double *mom0, int T,
+              double sigma, double *pos_traj, double *mom_traj);
+
+/* Diffeos::FlowLandmarkPointsTrajectory, Diffeos.cxx:661-712: y' = K(y, x_t) p_t with Heun's
+ * scheme when heun != 0 (the reference's ImprovedEuler default, Diffeos.cxx:27). */
+int gbk_flow_landmarks(gbk_ctx *ctx, int d, long ncp, const double *pos_traj,
+                       const double *mom_traj, int T, double sigma, long nlm, const double *lm0,
+                       int heun, double *lm_traj);
+
+/* AdjointEquationsIntegrator::IntegrateAdjointOfLandmarkPointsEquations,
+ * AdjointEquationsIntegrator.cxx:59-136 (no jumps): theta backward from theta_final. */
+int gbk_adjoint_landmarks(gbk_ctx *ctx, int d, long ncp, const double *pos_traj,
+                          const double *mom_traj, int T, double sigma, long nlm,
+                          const double *lm_traj, const double *theta_final, int heun,
+                          double *theta_traj);
+
+/* AdjointEquationsIntegrator::ComputeUpdateAt, AdjointEquationsIntegrator.cxx:476-570 (landmark
+ * points): dpos = dXi1 + dXi3 + dXi4, dmom = dXi2 + dXi5 + dXi6, in one fused CP x CP pass and
+ * one fused CP x landmark pass (nlm may be 0). */
+int gbk_compute_update_at(gbk_ctx *ctx, int d, long ncp, const double *pos, const double *mom,
+                          const double *xi_pos, const double *xi_mom, long nlm, const double *lm,
+                          const double *theta, double sigma, double *dpos, double *dmom);
+
+/* AdjointEquationsIntegrator::IntegrateAdjointOfDiffeoParametersEquations, :414-470. */
+int gbk_adjoint_diffeo(gbk_ctx *ctx, int d, long ncp, const double *pos_traj,
+                       const double *mom_traj, int T, double sigma, long nlm,
+                       const double *lm_traj, const double *theta_traj, int heun,
+                       double *xipos_traj, double *ximom_traj);
+
+/* ---- surface data terms (d = 3; triangles are int triplets, host or device) -------------- */
+
+/* OrientedSurfaceMesh::ComputeMatch / ComputeMatchGradient, OrientedSurfaceMesh.cxx:124-241
+ * (currents): *match = |T|^2 + |S|^2 - 2 <S,T>; grad (nv x 3, may be NULL) = d match / d pts.
+ * Reductions are FP64; `match` is one double. */
+int gbk_currents_match(gbk_ctx *ctx, long nv, const double *pts, long nf, const int *tris,
+                       long nv_t, const double *pts_t, long nf_t, const int *tris_t, double sigma,
+                       double *match, double *grad);
+
+/* NonOrientedSurfaceMesh::ComputeMatch / ComputeMatchGradient, NonOrientedSurfaceMesh.cxx:124-265
+ * (varifolds). */
+int gbk_varifold_match(gbk_ctx *ctx, long nv, const double *pts, long nf, const int *tris,
+                       long nv_t, const double *pts_t, long nf_t, const int *tris_t, double sigma,
+                       double *match, double *grad);
+
+/* ---- registration iteration (shooting + flow + data term + adjoint), CUDA-graph replay ---- */
+
+typedef struct gbk_registration gbk_registration;
+
+/* One subject of DeterministicAtlas with a frozen template (DeterministicAtlas.cxx:99-154,
+ * AbstractAtlas.cxx:559-613): template mesh (nv, nf) deformed by ncp control points over T time
+ * points, matched to the target mesh with data_kind 0 = currents, 1 = varifold. All device
+ * memory is allocated here. */
+int gbk_registration_create(gbk_ctx *ctx, int d, long ncp, long nv, const double *tmpl_pts,
+                            long nf, const int *tmpl_tris, long nv_t, const double *tgt_pts,
+                            long nf_t, const int *tgt_tris, int T, double sigma_def,
+                            double sigma_data, double data_sigma2, int data_kind, int heun,
+                            gbk_registration **out);
+/* Log-likelihood and gradient at (cp, mom): loglik[5] = {L, L_data, L_reg, match, <K p, p>},
+ * grad_cp / grad_mom = dL/dcp, dL/dp (ncp x d). Any output may be NULL. Returns when the outputs
+ * are written. The first call runs the kernels directly, the second captures them into a CUDA
+ * graph, later calls replay it. */
+int gbk_registration_step(gbk_registration *reg, const double *cp, const double *mom,
+                          double *loglik, double *grad_cp, double *grad_mom);
+/* 0 disables graph capture (every step launches the kernels directly). */
+int gbk_registration_set_graph(gbk_registration *reg, int enable);
+/* Copies of the last step's trajectories (T x ncp x d or T x nv x d); any pointer may be NULL. */
+int gbk_registration_trajectories(gbk_registration *reg, double *pos, double *mom, double *lm,
+                                  double *theta, double *xi_pos, double *xi_mom);
+/* Kernels in one captured iteration (0 before the capture). */
+long long gbk_registration_graph_launches(const gbk_registration *reg);
+void gbk_registration_destroy(gbk_registration *reg);
+
 /* ---- tuning ------------------------------------------------------------------------------ */
 
 /* Times the compiled variants and source-split factors of `op` for this shape on synthetic data

@@ -1,0 +1,111 @@
+"""FP64 restatement of the reference's surface data terms (TEST INFRASTRUCTURE ONLY).
+
+Currents: OrientedSurfaceMesh.cxx:124-352. Varifolds: NonOrientedSurfaceMesh.cxx:124-378.
+Every kernel sum goes through the kernel oracle, as the reference goes through its kernel object.
+Meshes are (points nv x 3, triangles nf x 3 int) arrays; the reference reads them from VTK.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .kernels import OracleLib
+
+
+def centers_normals(pts, tris):
+    """OrientedSurfaceMesh::UpdateCentersNormals, :298-328: c = mean of the vertices,
+    n = (p2 - p0) x (p1 - p0) / 2."""
+    p0, p1, p2 = pts[tris[:, 0]], pts[tris[:, 1]], pts[tris[:, 2]]
+    return (p0 + p1 + p2) / 3.0, np.cross(p2 - p0, p1 - p0) / 2
+
+
+def currents_norm(K: OracleLib, sigma, c, n):
+    """UpdateSelfNorm, :330-352: sum_f n_f . (K n)_f."""
+    return float(np.sum(K.convolve(c, c, n, sigma) * n))
+
+
+def currents_match(K: OracleLib, sigma, pts_s, tris_s, pts_t, tris_t):
+    """ComputeMatch, :124-163: |T|^2 + |S|^2 - 2 <S, T>."""
+    cs, ns = centers_normals(pts_s, tris_s)
+    ct, nt = centers_normals(pts_t, tris_t)
+    m = currents_norm(K, sigma, ct, nt) + currents_norm(K, sigma, cs, ns)
+    sdt = K.convolve(ct, cs, ns, sigma)
+    return m - 2.0 * float(np.sum(sdt * nt))
+
+
+def currents_match_gradient(K: OracleLib, sigma, pts_s, tris_s, pts_t, tris_t):
+    """ComputeMatchGradient, :165-241: gradient with respect to the vertices of S."""
+    cs, ns = centers_normals(pts_s, tris_s)
+    ct, nt = centers_normals(pts_t, tris_t)
+    ktau_s = K.convolve(cs, cs, ns, sigma)
+    gk_s = K.grad_alpha(cs, cs, ns, sigma, ns)
+    ktau_t = K.convolve(cs, ct, nt, sigma)
+    gk_t = K.grad_alpha(cs, ct, nt, sigma, ns)
+    gktau = (gk_s - gk_t) * 2.0 / 3.0
+    grad = np.zeros_like(pts_s)
+    p = pts_s
+    i0, i1, i2 = tris_s[:, 0], tris_s[:, 1], tris_s[:, 2]
+    e0, e1, e2 = p[i2] - p[i1], p[i0] - p[i2], p[i1] - p[i0]
+    kt = ktau_s - ktau_t
+    for idx, e in ((i0, e0), (i1, e1), (i2, e2)):
+        np.add.at(grad, idx, np.cross(e, kt) + gktau)
+    return grad
+
+
+def varifold_normals(pts, tris):
+    """NonOrientedSurfaceMesh::UpdateCentersNormals, :269-310: n / sqrt(|n| + 1e-20) and the
+    upper-triangle products n_p n_q (p <= q)."""
+    c, n = centers_normals(pts, tris)
+    n = n / np.sqrt(np.linalg.norm(n, axis=1) + 1e-20)[:, None]
+    iu = np.triu_indices(3)
+    mn = (n[:, :, None] * n[:, None, :])[:, iu[0], iu[1]]
+    return c, n, mn
+
+
+def special_product(M, X):
+    """NonOrientedSurfaceMesh::special_product, :364-378: symmetric 3x3 from 6 entries times X."""
+    iu = np.triu_indices(3)
+    S = np.zeros(M.shape[:-1] + (3, 3))
+    S[..., iu[0], iu[1]] = M
+    S[..., iu[1], iu[0]] = M
+    return np.einsum("...pq,...q->...p", S, X)
+
+
+def varifold_norm(K: OracleLib, sigma, c, n, mn):
+    kw = K.convolve(c, c, mn, sigma)
+    return float(np.sum(n * special_product(kw, n)))
+
+
+def varifold_match(K: OracleLib, sigma, pts_s, tris_s, pts_t, tris_t):
+    """NonOrientedSurfaceMesh::ComputeMatch, :124-165."""
+    cs, ns, ms = varifold_normals(pts_s, tris_s)
+    ct, nt, mt = varifold_normals(pts_t, tris_t)
+    m = varifold_norm(K, sigma, ct, nt, mt) + varifold_norm(K, sigma, cs, ns, ms)
+    sdt = K.convolve(ct, cs, ms, sigma)
+    return m - 2.0 * float(np.sum(nt * special_product(sdt, nt)))
+
+
+def varifold_match_gradient(K: OracleLib, sigma, pts_s, tris_s, pts_t, tris_t):
+    """NonOrientedSurfaceMesh::ComputeMatchGradient, :169-265."""
+    cs, ns, ms = varifold_normals(pts_s, tris_s)
+    ct, nt, mt = varifold_normals(pts_t, tris_t)
+    ktau_s = K.convolve(cs, cs, ms, sigma)
+    gk_s = K.grad_varlin(cs, cs, ms, sigma)        # (nf, 6, 3)
+    ktau_t = K.convolve(cs, ct, mt, sigma)
+    gk_t = K.grad_varlin(cs, ct, mt, sigma)
+    p = pts_s
+    grad = np.zeros_like(p)
+    i0, i1, i2 = tris_s[:, 0], tris_s[:, 1], tris_s[:, 2]
+    e0, e1, e2 = p[i2] - p[i1], p[i0] - p[i2], p[i1] - p[i0]
+    mag2 = np.sum(ns * ns, axis=1)
+    ok = mag2 > 1e-20
+    kt = 2.0 * special_product(ktau_s - ktau_t, ns)
+    aux = special_product(ms, kt)
+    kt = (kt - aux / (2 * mag2[:, None])) / np.sqrt(mag2)[:, None]
+    delta = gk_s - gk_t
+    gk = np.stack([np.sum(special_product(delta[:, :, pdir], ns) * ns, axis=1) for pdir in range(3)],
+                  axis=1) * (2.0 / 3.0)
+    kt[~ok] = 0.0
+    gk[~ok] = 0.0
+    for idx, e in ((i0, e0), (i1, e1), (i2, e2)):
+        np.add.at(grad, idx, np.cross(e, kt) + gk)
+    return grad

@@ -46,8 +46,9 @@ def ctx(gb):
 def kern(gb, ctx, d, sigma, Y, W, mode):
     ctx.set_mode(mode)
     k = gb.GB300ExactKernel(d, sigma, context=ctx)
-    k.SetSources(np.ascontiguousarray(Y))
-    k.SetWeights(np.ascontiguousarray(W))
+    c = (lambda a: a) if not isinstance(Y, np.ndarray) else np.ascontiguousarray
+    k.SetSources(c(Y))
+    k.SetWeights(c(W))
     return k
 
 

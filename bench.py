@@ -29,7 +29,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "kernel pairs/s fwd+adjoint"
 UNIT = "pairs/s"
-FLOPS_PER_PAIR_PASS = 27  # FP32 flops of one fused pass per pair (FMA = 2), see the design doc
+FLOPS_PER_PAIR_PASS = 26  # FP32 flops per pair of one fused Convolve + alpha-gradient pass (FMA = 2)
 SMS = 152
 FP32_LANES = 128
 

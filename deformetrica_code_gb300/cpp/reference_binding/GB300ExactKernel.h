@@ -1,0 +1,183 @@
+// GB300ExactKernel.h -- the kernel type a Deformetrica build adds to use the GB300 library.
+//
+// Drop-in beside src/support/kernels/CUDAExactKernel.h: it derives from ExactKernel because the
+// factory's base type is ExactKernel (KernelFactory.h:44), and overrides every convolution method
+// of AbstractKernel (AbstractKernel.h:120-160), so no call falls back to the CPU loops. Each method
+// builds the row-major buffers the legacy CUDA path builds (vectorise_row_wise,
+// CUDAExactKernel.cxx:46-48) and makes one call into the C ABI of include/gbk.h; failures throw
+// std::runtime_error with the library's message, as the reference does for shape errors. One
+// library context per host thread (kernel objects are created per subject thread,
+// AbstractAtlas.cxx:218), lazily created on first use.
+//
+// Selecting it takes an enum value GB300Exact in KernelType.h:20-28 and one case in each
+// KernelFactory::CreateKernelObject overload (KernelFactory.cxx:100-117, 128-144, 155-171); see
+// INTEGRATION.md for the full patch.
+#pragma once
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ExactKernel.h"
+#include "gbk.h"
+
+namespace gb300_binding {
+
+inline gbk_ctx *thread_context() {
+  struct Holder {
+    gbk_ctx *c = nullptr;
+    ~Holder() {
+      if (c) gbk_destroy(c);
+    }
+  };
+  static thread_local Holder h;
+  if (!h.c) {
+    if (gbk_create(0, &h.c) != GBK_OK) throw std::runtime_error(std::string("gbk_create: ") + gbk_last_error(nullptr));
+  }
+  return h.c;
+}
+
+inline void check(int rc) {
+  if (rc != GBK_OK) throw std::runtime_error(gbk_last_error(thread_context()));
+}
+
+}  // namespace gb300_binding
+
+template <class ScalarType, unsigned int PointDim>
+class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
+ public:
+  typedef ExactKernel<ScalarType, PointDim> Superclass;
+
+  GB300ExactKernel() : Superclass() {}
+  GB300ExactKernel(const GB300ExactKernel &o) : Superclass(o) {}
+  GB300ExactKernel(const MatrixType &X, double h) : Superclass(X, h) {}
+  GB300ExactKernel(const MatrixType &X, const MatrixType &W, double h) : Superclass(X, W, h) {}
+  virtual GB300ExactKernel *Clone() const { return new GB300ExactKernel(*this); }
+  virtual ~GB300ExactKernel() {}
+
+  virtual MatrixType Convolve(const MatrixType &X) {
+    Buffers b(this, X);
+    std::vector<double> out((size_t)X.rows() * b.dv);
+    gb300_binding::check(gbk_convolve(gb300_binding::thread_context(), PointDim, b.dv, b.x.memptr(), X.rows(),
+                                      b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(), out.data()));
+    return from_rows(out, X.rows(), b.dv);
+  }
+
+  virtual std::vector<MatrixType> ConvolveGradient(const MatrixType &X) {
+    Buffers b(this, X);
+    std::vector<double> out((size_t)X.rows() * b.dv * PointDim);
+    gb300_binding::check(gbk_convolve_gradient(gb300_binding::thread_context(), PointDim, b.dv, b.x.memptr(),
+                                               X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                               this->GetKernelWidth(), out.data()));
+    std::vector<MatrixType> g;
+    for (unsigned i = 0; i < X.rows(); ++i) {
+      MatrixType Gi(b.dv, PointDim, 0.0);
+      for (unsigned k = 0; k < b.dv; ++k)
+        for (unsigned l = 0; l < PointDim; ++l) Gi(k, l) = out[((size_t)i * b.dv + k) * PointDim + l];
+      g.push_back(Gi);
+    }
+    return g;
+  }
+
+  virtual MatrixType ConvolveGradient(const MatrixType &X, const MatrixType &alpha) {
+    Buffers b(this, X);
+    VectorType a = alpha.vectorise_row_wise();
+    std::vector<double> out((size_t)X.rows() * PointDim);
+    gb300_binding::check(gbk_convolve_gradient_alpha(gb300_binding::thread_context(), PointDim, b.dv,
+                                                     b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                     this->GetKernelWidth(), a.memptr(), out.data()));
+    return from_rows(out, X.rows(), PointDim);
+  }
+
+  virtual VectorType ConvolveGradient(const MatrixType &X, unsigned int k, unsigned int dp) {
+    Buffers b(this, X);
+    std::vector<double> out(b.ny);
+    gb300_binding::check(gbk_convolve_gradient_kdp(gb300_binding::thread_context(), PointDim, b.dv,
+                                                   b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                   this->GetKernelWidth(), (int)k, (int)dp, out.data()));
+    return VectorType(out);
+  }
+
+  virtual MatrixType ConvolveGradient(const MatrixType &X, unsigned int dim) {
+    Buffers b(this, X);
+    std::vector<double> out((size_t)X.rows() * b.dv);
+    gb300_binding::check(gbk_convolve_gradient_dim(gb300_binding::thread_context(), PointDim, b.dv,
+                                                   b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                   this->GetKernelWidth(), (int)dim, out.data()));
+    return from_rows(out, X.rows(), b.dv);
+  }
+
+  virtual std::vector<std::vector<MatrixType> > ConvolveHessian(const MatrixType &X) {
+    Buffers b(this, X);
+    const unsigned D = PointDim;
+    std::vector<double> out((size_t)X.rows() * b.dv * D * D);
+    gb300_binding::check(gbk_convolve_hessian(gb300_binding::thread_context(), D, b.dv, b.x.memptr(), X.rows(),
+                                              b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(),
+                                              out.data()));
+    std::vector<std::vector<MatrixType> > h;
+    for (unsigned i = 0; i < X.rows(); ++i) {
+      std::vector<MatrixType> Hi;
+      for (unsigned k = 0; k < b.dv; ++k) {
+        MatrixType H(D, D, 0.0);
+        for (unsigned a = 0; a < D; ++a)
+          for (unsigned c = 0; c < D; ++c) H(a, c) = out[(((size_t)i * b.dv + k) * D + a) * D + c];
+        Hi.push_back(H);
+      }
+      h.push_back(Hi);
+    }
+    return h;
+  }
+
+  virtual VectorType ConvolveHessian(const MatrixType &X, unsigned int k, unsigned int dp, unsigned int dq) {
+    Buffers b(this, X);
+    std::vector<double> out(X.rows());
+    gb300_binding::check(gbk_convolve_hessian_kdpdq(gb300_binding::thread_context(), PointDim, b.dv,
+                                                    b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                    this->GetKernelWidth(), (int)k, (int)dp, (int)dq, out.data()));
+    return VectorType(out);
+  }
+
+  virtual MatrixType ConvolveHessian(const MatrixType &X, unsigned int row, unsigned int col) {
+    Buffers b(this, X);
+    std::vector<double> out((size_t)X.rows() * b.dv);
+    gb300_binding::check(gbk_convolve_hessian_rowcol(gb300_binding::thread_context(), PointDim, b.dv,
+                                                     b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                     this->GetKernelWidth(), (int)row, (int)col, out.data()));
+    return from_rows(out, X.rows(), b.dv);
+  }
+
+  virtual MatrixType ConvolveSpecialHessian(const MatrixType &xi) {
+    Buffers b(this, this->GetSources());
+    if (xi.rows() != b.ny) throw std::runtime_error("Y and Xi count mismatch");
+    VectorType x = xi.vectorise_row_wise();
+    std::vector<double> out((size_t)b.ny * PointDim);
+    gb300_binding::check(gbk_convolve_special_hessian(gb300_binding::thread_context(), PointDim, b.y.memptr(),
+                                                      b.w.memptr(), b.ny, this->GetKernelWidth(), x.memptr(),
+                                                      out.data()));
+    return from_rows(out, b.ny, PointDim);
+  }
+
+ private:
+  struct Buffers {
+    VectorType x, y, w;
+    unsigned ny, dv;
+    Buffers(GB300ExactKernel *k, const MatrixType &X) {
+      MatrixType &Y = k->GetSources();
+      MatrixType &W = k->GetWeights();
+      if (Y.rows() != W.rows()) throw std::runtime_error("Sources and weights count mismatch");
+      x = X.vectorise_row_wise();
+      y = Y.vectorise_row_wise();
+      w = W.vectorise_row_wise();
+      ny = Y.rows();
+      dv = W.columns();
+    }
+  };
+
+  static MatrixType from_rows(const std::vector<double> &v, unsigned rows, unsigned cols) {
+    MatrixType M(rows, cols, 0.0);
+    for (unsigned i = 0; i < rows; ++i)
+      for (unsigned j = 0; j < cols; ++j) M(i, j) = v[(size_t)i * cols + j];
+    return M;
+  }
+};

@@ -30,6 +30,7 @@ sys.path.insert(0, ROOT)
 METRIC = "kernel pairs/s fwd+adjoint"
 UNIT = "pairs/s"
 FLOPS_PER_PAIR_PASS = 26  # FP32 flops per pair of one fused Convolve + alpha-gradient pass (FMA = 2)
+LANE_OPS_PER_PAIR_PASS = 16  # FP32 lane instructions per pair of that pass (FMA = 1)
 SMS = 152
 FP32_LANES = 128
 
@@ -418,7 +419,9 @@ def main():
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
                          "frac": achieved / peak_tflops, "traffic": None,
-                         "kernel": "pair_kernel<OpConvGradAlpha<3,3,true>, float> (one fused pass)",
+                         "kernel": "pair_kernel<OpConvGradAlpha<3,3,true>, float2 lanes> (one fused pass)",
+                         "fp32_lane_frac": LANE_OPS_PER_PAIR_PASS * pairs / (kernel_ms / 1e3)
+                         / (SMS * FP32_LANES * sm_mhz * 1e6),
                          "kernel_ms": kernel_ms,
                          "peak_source": f"nominal FP32 {SMS} SMs x {FP32_LANES} lanes x 2 flops x median sampled SM clock {sm_mhz:.0f} MHz"},
             "clocks": clocks,

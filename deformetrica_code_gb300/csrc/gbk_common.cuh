@@ -16,8 +16,13 @@
 namespace gbk {
 
 // ---------------------------------------------------------------------------------------------
-// Lane types: Lane<float> carries two targets (float2), Lane<double> one target.
+// Lane types: Lane<float> carries two targets (float2, packed FFMA2), Lane<f32s> one target in
+// scalar FP32, Lane<double> one target in FP64. Packed FFMA2 halves issue slots, but with three
+// distinct register operands per instruction it measured ~68% of the FP32 lane peak on GB300
+// (operand bandwidth) against ~78% for scalar FFMA, so both FP32 forms are kept.
 // ---------------------------------------------------------------------------------------------
+struct f32s {};  // tag: scalar FP32 lanes
+
 template <typename T>
 struct Lane;
 
@@ -46,6 +51,24 @@ struct Lane<float> {
 };
 
 template <>
+struct Lane<f32s> {
+  typedef float V;
+  static constexpr int kWidth = 1;
+  __device__ __forceinline__ static V add(V a, V b) { return __fadd_rn(a, b); }
+  __device__ __forceinline__ static V sub(V a, V b) { return __fsub_rn(a, b); }
+  __device__ __forceinline__ static V mul(V a, V b) { return __fmul_rn(a, b); }
+  __device__ __forceinline__ static V fma(V a, V b, V c) { return __fmaf_rn(a, b, c); }
+  __device__ __forceinline__ static V zero() { return 0.f; }
+  __device__ __forceinline__ static V splat(float s) { return s; }
+  __device__ __forceinline__ static V kexp(V r2, V) {
+    float a;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(-r2));
+    return a;
+  }
+  __device__ __forceinline__ static float get(V v, int) { return v; }
+};
+
+template <>
 struct Lane<double> {
   typedef double V;
   static constexpr int kWidth = 1;
@@ -71,6 +94,10 @@ struct SrcVal<float> {
   }
 };
 template <>
+struct SrcVal<f32s> {
+  __device__ __forceinline__ static float make(double v) { return (float)v; }
+};
+template <>
 struct SrcVal<double> {
   __device__ __forceinline__ static double make(double v) { return v; }
 };
@@ -91,6 +118,16 @@ struct Comp {
   }
 };
 template <>
+struct Comp<f32s> {
+  __device__ __forceinline__ static void fold(float &sum, float &comp, float run) {
+    float s = __fadd_rn(sum, run);
+    float bb = __fsub_rn(s, sum);
+    float err = __fadd_rn(__fsub_rn(sum, __fsub_rn(s, bb)), __fsub_rn(run, bb));
+    comp = __fadd_rn(comp, err);
+    sum = s;
+  }
+};
+template <>
 struct Comp<double> {
   __device__ __forceinline__ static void fold(double &sum, double &, double run) { sum += run; }
 };
@@ -104,13 +141,21 @@ __host__ __device__ inline double coord_scale<float>(double sigma) {
   return 1.2011224087864498 / sigma;  // sqrt(log2(e)) / sigma
 }
 template <>
+__host__ __device__ inline double coord_scale<f32s>(double sigma) {
+  return 1.2011224087864498 / sigma;
+}
+template <>
 __host__ __device__ inline double coord_scale<double>(double) {
   return 1.0;
 }
 // Scale of r2 inside kexp (FP64 only): -1/sigma^2.
 template <typename T>
-__host__ __device__ inline T exp_arg_scale(double sigma) {
-  return (T)(-1.0 / (sigma * sigma));
+__host__ __device__ inline typename Lane<T>::V exp_arg_scale(double sigma) {
+  return (typename Lane<T>::V)(-1.0 / (sigma * sigma));
+}
+template <>
+__host__ __device__ inline float2 exp_arg_scale<float>(double sigma) {
+  return float2{0.f, 0.f};  // unused: FP32 lanes work on pre-scaled coordinates
 }
 
 // Bounded-iteration helpers for any cross-block wait (none of the kernel-sum kernels wait).

@@ -60,16 +60,18 @@ bool find_kernel_deform(int op, int mode, int d, int dv, int variant, KernelEntr
 
 namespace gbk {
 // Helper for the instantiation files: records one compiled (op, T, D, BLOCK, R, TJ, MERGE) with
-// MINB resident CTAs per SM requested from the register allocator.
-template <class OpT, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB = 1>
+// MINB resident CTAs per SM requested from the register allocator, the per-source loop unrolled
+// UNR times and the compensation terms in registers (CSM = 0) or shared memory (CSM = 1, 2).
+template <class OpT, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB = 1, int UNR = 2,
+          int CSM = 0>
 inline bool set_entry(KernelEntry *e) {
-  e->fn = &launch_pairs<OpT, T, D, BLOCK, R, TJ, MERGE, MINB>;
-  e->kernel = (const void *)&pair_kernel<OpT, T, D, BLOCK, R, TJ, MERGE, MINB>;
+  e->fn = &launch_pairs<OpT, T, D, BLOCK, R, TJ, MERGE, MINB, UNR, CSM>;
+  e->kernel = (const void *)&pair_kernel<OpT, T, D, BLOCK, R, TJ, MERGE, MINB, UNR, CSM>;
   e->block = BLOCK;
   e->r = R;
   e->tj = TJ;
   e->no = OpT::NO;
-  e->smem = (int)(TJ * Rec<OpT, D>::NJP * sizeof(typename SrcLane<T>::SV));
+  e->smem = (int)pair_smem_bytes<OpT, T, D, BLOCK, R, TJ, CSM>();
   return true;
 }
 }  // namespace gbk

@@ -1,10 +1,11 @@
 // Instantiations: Convolve, fused Convolve + alpha-gradient, alpha-gradient.
 //
 // FP32-compensated variants (BLOCK threads, R targets per thread, TJ sources per tile, MERGE
-// sources per compensated run, MINB CTAs per SM for the register allocator): the hot
-// (d, dv) = (3, 3) and (2, 2) shapes carry several variants for the autotuner; other shapes carry
-// the default one, which measured fastest on GB300 for the fused pass at N = M = 1e6 (578 ms vs
-// 603 ms for 4 targets per thread at 2 CTAs/SM). FP64 uses one target per thread.
+// sources per compensated run, MINB CTAs per SM for the register allocator, UNR unroll of the
+// source loop): the hot (d, dv) = (3, 3) and (2, 2) shapes carry several variants for the
+// autotuner; other shapes carry the default one. Fused pass at N = M = 1e6 on GB300: default
+// 564 ms; 2-way unroll 578 ms; 4 targets per thread at 2 CTAs/SM 603 ms; scalar FP32 lanes 568 ms;
+// compensation terms in shared memory 605-636 ms (removed). FP64 uses one target per thread.
 #include "gbk_dispatch.h"
 
 namespace gbk {
@@ -20,14 +21,14 @@ static bool pick_conv_like(int mode, int variant, KernelEntry *e) {
   constexpr bool hot = (D == 3 && DV == 3) || (D == 2 && DV == 2);
   if constexpr (hot) {
     switch (variant) {
-      case 1: return set_entry<O, float, D, 256, 4, 256, 64, 2>(e);
-      case 2: return set_entry<O, float, D, 128, 4, 256, 64, 4>(e);
-      case 3: return set_entry<O, float, D, 256, 2, 256, 64, 4>(e);
+      case 1: return set_entry<O, float, D, 256, 2, 256, 64, 3, 2>(e);   // 2-way unroll
+      case 2: return set_entry<O, float, D, 256, 4, 256, 64, 2, 2>(e);   // 4 targets / thread
+      case 3: return set_entry<O, f32s, D, 256, 2, 256, 64, 3, 4>(e);    // scalar FP32 lanes
       default: break;
     }
   }
-  // default: 2 targets (one float2 lane pair) per thread, 3 CTAs of 256 threads per SM
-  return set_entry<O, float, D, 256, 2, 256, 64, 3>(e);
+  // default: one float2 lane pair per thread, 4-way unrolled source loop, 3 CTAs of 256 per SM
+  return set_entry<O, float, D, 256, 2, 256, 64, 3, 4>(e);
 }
 
 template <int D, int DV>

@@ -11,7 +11,7 @@ static bool pick_one(int mode, int variant, KernelEntry *e) {
     return set_entry<O, float, D, 64, 2, 32, 32, 8>(e);
   }
   if (mode == MODE_F64) return set_entry<O, double, D, 128, 1, 128, 128>(e);
-  return set_entry<O, float, D, 256, 2, 256, 64, 2>(e);
+  return set_entry<O, float, D, 256, 2, 256, 64, 2, 4>(e);
 }
 
 template <template <int, int> class OP>

@@ -20,6 +20,8 @@
 // results are bitwise reproducible run to run.
 #pragma once
 
+#include <type_traits>
+
 #include "gbk_common.cuh"
 
 namespace gbk {
@@ -401,6 +403,10 @@ struct SrcLane<float> {
   typedef float2 SV;
 };
 template <>
+struct SrcLane<f32s> {
+  typedef float SV;
+};
+template <>
 struct SrcLane<double> {
   typedef double SV;
 };
@@ -413,28 +419,42 @@ struct Pack<float> {
   __device__ __forceinline__ static float2 make(double a, double b) { return make_float2((float)a, (float)b); }
 };
 template <>
+struct Pack<f32s> {
+  __device__ __forceinline__ static float make(double a, double) { return (float)a; }
+};
+template <>
 struct Pack<double> {
   __device__ __forceinline__ static double make(double a, double) { return a; }
 };
 
-template <class Op, int D>
+// Source record length, padded so that a record is a whole number of 16-byte vectors.
+template <class Op, int D, typename T>
 struct Rec {
   static constexpr int NJ = D + Op::NS;
-  static constexpr int NJP = (NJ + 1) & ~1;  // even: records load as 16-byte vectors
+  static constexpr int PER16 = 16 / (int)sizeof(typename SrcLane<T>::SV);
+  static constexpr int NJP = (NJ + PER16 - 1) / PER16 * PER16;
 };
 
-// CENTER: subtract the CTA's target bounding-box midpoint (FP32 mode). FP64 mode forms x - y
-// directly, as the reference does.
-template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB>
+// Dynamic shared memory of one CTA: the source tile, then (CSM > 0) the per-thread compensation
+// terms (CSM = 1) or running sums and compensation terms (CSM = 2) of the G lane groups.
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int CSM>
+constexpr size_t pair_smem_bytes() {
+  return (size_t)TJ * Rec<Op, D, T>::NJP * sizeof(typename SrcLane<T>::SV) +
+         (size_t)CSM * (R / Lane<T>::kWidth) * Op::NO * BLOCK * sizeof(typename Lane<T>::V);
+}
+
+// FP32 mode subtracts the CTA's target bounding-box midpoint (centring); FP64 mode forms x - y
+// directly, as the reference does. UNR: unroll of the per-source loop. CSM: see pair_smem_bytes.
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
   typedef Lane<T> L;
   typedef typename L::V V;
   typedef typename SrcLane<T>::SV SV;
   constexpr int W = L::kWidth;
   constexpr int G = R / W;  // lane groups per thread
-  constexpr int NJP = Rec<Op, D>::NJP;
+  constexpr int NJP = Rec<Op, D, T>::NJP;
   constexpr int NO = Op::NO;
-  constexpr bool CENTER = (W == 2);
+  constexpr bool CENTER = !std::is_same<T, double>::value;
   static_assert(R % W == 0, "R must be a multiple of the lane width");
   static_assert(TJ % MERGE == 0, "TJ must be a multiple of MERGE");
 
@@ -520,6 +540,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
     for (int k = 0; k < Op::NT; ++k) tg[g][k] = Pack<T>::make(tv[0][k], tv[W - 1][k]);
   }
 
+  // running sums / compensation: registers, or shared memory after the tile (CSM)
+  V *csm = reinterpret_cast<V *>(smem_raw + (size_t)TJ * NJP * sizeof(SV));
   V acc[G][NO], sum[G][NO], cmp[G][NO];
 #pragma unroll
   for (int g = 0; g < G; ++g)
@@ -528,11 +550,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
       acc[g][o] = L::zero();
       sum[g][o] = L::zero();
       cmp[g][o] = L::zero();
+      if (CSM >= 1) csm[(g * NO + o) * BLOCK + threadIdx.x] = L::zero();
+      if (CSM >= 2) csm[((G + g) * NO + o) * BLOCK + threadIdx.x] = L::zero();
     }
 
-  const T cexp = exp_arg_scale<T>(a.sigma);
+  const V cx = exp_arg_scale<T>(a.sigma);
   const int p0 = a.p0, p1 = a.p1;
-  const V cx = L::splat(cexp);
 
   const long jb = (long)blockIdx.y * a.j_chunk;
   long je = jb + a.j_chunk;
@@ -550,10 +573,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
         Op::load_source(a, j, rec + D);
       } else {
 #pragma unroll
-        for (int q = 0; q < Rec<Op, D>::NJ; ++q) rec[q] = 0.0;  // zero weights: exact no-op
+        for (int q = 0; q < Rec<Op, D, T>::NJ; ++q) rec[q] = 0.0;  // zero weights: exact no-op
       }
 #pragma unroll
-      for (int q = Rec<Op, D>::NJ; q < NJP; ++q) rec[q] = 0.0;
+      for (int q = Rec<Op, D, T>::NJ; q < NJP; ++q) rec[q] = 0.0;
 #pragma unroll
       for (int q = 0; q < NJP; ++q) tile[r * NJP + q] = SrcVal<T>::make(rec[q]);
     }
@@ -562,14 +585,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
     const int nrun = (cnt + MERGE - 1) / MERGE;
     for (int run = 0; run < nrun; ++run) {
       const SV *rp = tile + run * MERGE * NJP;
-#pragma unroll 2
+#pragma unroll UNR
       for (int jj = 0; jj < MERGE; ++jj) {
         SV s[NJP];
         const float4 *src = reinterpret_cast<const float4 *>(rp + jj * NJP);
 #pragma unroll
-        for (int q = 0; q < NJP / 2; ++q) {
+        for (int q = 0; q < (int)(NJP * sizeof(SV) / 16); ++q) {
           float4 v4 = src[q];
-          *reinterpret_cast<float4 *>(&s[2 * q]) = v4;
+          *reinterpret_cast<float4 *>(reinterpret_cast<char *>(s) + 16 * q) = v4;
         }
 #pragma unroll
         for (int g = 0; g < G; ++g) {
@@ -587,7 +610,21 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
       for (int g = 0; g < G; ++g)
 #pragma unroll
         for (int o = 0; o < NO; ++o) {
-          Comp<T>::fold(sum[g][o], cmp[g][o], acc[g][o]);
+          if (CSM == 0) {
+            Comp<T>::fold(sum[g][o], cmp[g][o], acc[g][o]);
+          } else {
+            V &cm = csm[(g * NO + o) * BLOCK + threadIdx.x];
+            V c = cm;
+            if (CSM == 1) {
+              Comp<T>::fold(sum[g][o], c, acc[g][o]);
+            } else {
+              V &sm = csm[((G + g) * NO + o) * BLOCK + threadIdx.x];
+              V s2 = sm;
+              Comp<T>::fold(s2, c, acc[g][o]);
+              sm = s2;
+            }
+            cm = c;
+          }
           acc[g][o] = L::zero();
         }
     }
@@ -603,7 +640,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
       if (i >= nx) continue;
       double v[NO];
 #pragma unroll
-      for (int o = 0; o < NO; ++o) v[o] = (double)L::get(sum[g][o], w2) + (double)L::get(cmp[g][o], w2);
+      for (int o = 0; o < NO; ++o) {
+        V sv = CSM >= 2 ? csm[((G + g) * NO + o) * BLOCK + threadIdx.x] : sum[g][o];
+        V cv = CSM >= 1 ? csm[(g * NO + o) * BLOCK + threadIdx.x] : cmp[g][o];
+        v[o] = (double)L::get(sv, w2) + (double)L::get(cv, w2);
+      }
       if (a.nsplit > 1) {
         double *p = a.partial + (long)blockIdx.y * NO * nx;
 #pragma unroll
@@ -638,13 +679,11 @@ struct LaunchCfg {
   int nsplit;   // source splits (grid.y); 1 = no partial buffer
 };
 
-template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB>
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 cudaError_t launch_pairs(PairArgs a, int nsplit, cudaStream_t st) {
   if (a.nx <= 0) return cudaSuccess;
-  constexpr int NJP = Rec<Op, D>::NJP;
-  typedef typename SrcLane<T>::SV SV;
-  const size_t smem = (size_t)TJ * NJP * sizeof(SV);
-  auto kern = pair_kernel<Op, T, D, BLOCK, R, TJ, MERGE, MINB>;
+  const size_t smem = pair_smem_bytes<Op, T, D, BLOCK, R, TJ, CSM>();
+  auto kern = pair_kernel<Op, T, D, BLOCK, R, TJ, MERGE, MINB, UNR, CSM>;
   a.xscale = coord_scale<T>(a.sigma);
   if (smem > 48 * 1024) {  // per current device; idempotent
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

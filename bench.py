@@ -31,6 +31,9 @@ METRIC = "kernel pairs/s fwd+adjoint"
 UNIT = "pairs/s"
 FLOPS_PER_PAIR_PASS = 26  # FP32 flops per pair of one fused Convolve + alpha-gradient pass (FMA = 2)
 LANE_OPS_PER_PAIR_PASS = 16  # FP32 lane instructions per pair of that pass (FMA = 1)
+# DRAM bytes (read + write) of one fused pass at N = M = 1e6 from one ncu capture of this kernel
+# (profiles/pair_kernel_fused_N1e6_traffic.md); None for other sizes.
+TRAFFIC_1E6 = 378095616 + 299555840
 SMS = 152
 FP32_LANES = 128
 
@@ -418,7 +421,8 @@ def main():
             "e2e": {"value": pairs * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
-                         "frac": achieved / peak_tflops, "traffic": None,
+                         "frac": achieved / peak_tflops,
+                         "traffic": TRAFFIC_1E6 if n == 1_000_000 else None,
                          "kernel": "pair_kernel<OpConvGradAlpha<3,3,true>, float2 lanes> (one fused pass)",
                          "fp32_lane_frac": LANE_OPS_PER_PAIR_PASS * pairs / (kernel_ms / 1e3)
                          / (SMS * FP32_LANES * sm_mhz * 1e6),

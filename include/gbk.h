@@ -239,6 +239,18 @@ int gbk_registration_trajectories(gbk_registration *reg, double *pos, double *mo
 long long gbk_registration_graph_launches(const gbk_registration *reg);
 void gbk_registration_destroy(gbk_registration *reg);
 
+/* The same <w, K w> for callers that cannot allocate device memory when they need it (a loop
+ * running inside a memory budget fixed at start-up, a pre-sized pool, a stream whose operations
+ * must all be known in advance). No counterpart in the reference. Allocates nothing: its scratch
+ * (the K w intermediate and source-split partials) is a 16 MiB __device__ array in the library,
+ * held by every GPU that loads it until the process exits. y, w and `out` (one double) must be
+ * device pointers; n * dv above 2^21 (2,097,152) returns GBK_ERR_ARG before any launch. Errors are
+ * reported by the return code only (gbk_last_error is not updated). The first call on a device
+ * looks up the array's address: make it before any stream capture. All calls share the array, so
+ * calls that overlap on the GPU race: serialise them. Queued on the context's stream. */
+int gbk_kernel_norm_noalloc(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
+                            double sigma, double *out);
+
 /* ---- tuning ------------------------------------------------------------------------------ */
 
 /* Times the compiled variants and source-split factors of `op` for this shape on synthetic data

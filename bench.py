@@ -222,6 +222,59 @@ def registration_bench(steps: int, cpu: bool = True):
     return res
 
 
+def atlas_workload(nsub: int = 64, seed: int = 4):
+    """Batched atlas: 64 subjects, each a perturbed sphere (Fibonacci points, radial noise 0.02,
+    convex-hull triangulation) with a vertex count drawn log-uniform in [5,000, 50,000]; shared
+    10,242-vertex icosphere template; 2,000 control points = a seed-fixed random subset of the 13^3
+    grid on [0,1]^3; momenta ~ N(0, 0.01) (standard deviation 0.01) per subject; 11 time points;
+    deformation width 0.15, currents width 0.1 (the registration workload's)."""
+    from deformetrica_code_gb300 import meshes as M
+    rng = np.random.default_rng(seed)
+    g = np.linspace(0.0, 1.0, 13)
+    grid = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    cp = grid[np.sort(rng.choice(grid.shape[0], 2000, replace=False))]
+    nvs = np.round(np.exp(rng.uniform(np.log(5000), np.log(50000), nsub))).astype(int)
+    targets = [M.perturbed_sphere(int(n), noise=0.02, seed=1000 + i) for i, n in enumerate(nvs)]
+    mom = 0.01 * rng.standard_normal((nsub, cp.shape[0], 3))
+    tp, tf = M.icosphere(5, 0.4)
+    return cp, mom, tp, tf, targets, dict(T=11, sigma_def=0.15, sigma_data=0.1, data_sigma2=0.01)
+
+
+def atlas_bench(steps: int, cpu: bool = True):
+    """s/iter of one batched atlas iteration (all subjects, forward + gradient, graph replay)."""
+    import deformetrica_code_gb300 as g
+    from deformetrica_code_gb300.deformation import Atlas
+    cp, mom, tp, tf, targets, kw = atlas_workload()
+    ctx = g.Context()
+    atlas = Atlas(cp, tp, tf, targets, context=ctx, **kw)
+    for _ in range(3):
+        ll, gm, gc, gt = atlas.step(mom)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ll, gm, gc, gt = atlas.step(mom)
+        ts.append(time.perf_counter() - t0)
+    nfs = [t[1].shape[0] for t in targets]
+    res = {"workload": f"{len(targets)} subjects, target faces {min(nfs)}..{max(nfs)}, 10242-vertex template, "
+                       f"2000 CP, T=11, currents", "f32c": {"s_per_iter": statistics.mean(ts),
+                                                            "loglik": float(ll[0]),
+                                                            "kernels_per_iter": atlas.graph_launches()}}
+    atlas.close()
+    if cpu:
+        import oracle
+        from oracle import deformation as D
+        K = oracle.load("port")
+        k = int(np.argsort(nfs)[len(nfs) // 2])  # the median-size subject
+        t0 = time.perf_counter()
+        D.registration(K, cp, mom[k], tp, tf, targets[k][0], targets[k][1], kw["T"], kw["sigma_def"],
+                       kw["sigma_data"], kw["data_sigma2"])
+        one = time.perf_counter() - t0
+        res["cpu_fp64_oracle"] = {"s_per_subject_median": one, "s_per_iter_extrapolated": one * len(targets),
+                                  "note": "one median-size subject timed, x64 extrapolated",
+                                  "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))}
+    return res
+
+
 def fp64_gpu_pairs(n: int, sigma: float):
     """The same fused forward+adjoint step in the FP64 mode (plain FP64 kernel sums) at N = M = n."""
     import torch
@@ -296,6 +349,8 @@ def main():
     ap.add_argument("--fp64-n", type=int, default=200_000)
     ap.add_argument("--no-registration", action="store_true")
     ap.add_argument("--reg-steps", type=int, default=10)
+    ap.add_argument("--no-atlas", action="store_true")
+    ap.add_argument("--atlas-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -439,6 +494,8 @@ def main():
             line["fp64_gpu"] = fp64_gpu_pairs(args.fp64_n, args.sigma)
         if not args.no_registration:
             line["shooting_adjoint"] = registration_bench(args.reg_steps, cpu=not args.no_cpu_baseline)
+        if not args.no_atlas:
+            line["atlas"] = atlas_bench(args.atlas_steps, cpu=not args.no_cpu_baseline)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -81,6 +81,12 @@ SIGNATURES = {
     "gbk_registration_trajectories": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "gbk_registration_graph_launches": (ctypes.c_longlong, [_P]),
     "gbk_registration_destroy": (None, [_P]),
+    "gbk_atlas_create": (_I, [_P, _L, _P, _L, _P, _L, _P, _I, _P, _P, _P, _P, _I, _D, _D, _D, _I, _I,
+                              ctypes.POINTER(_P)]),
+    "gbk_atlas_step": (_I, [_P, _P, _P, _P, _P, _P]),
+    "gbk_atlas_set_graph": (_I, [_P, _I]),
+    "gbk_atlas_graph_launches": (ctypes.c_longlong, [_P]),
+    "gbk_atlas_destroy": (None, [_P]),
 }
 
 _lib = None

@@ -28,9 +28,12 @@ constexpr int VARIANT_SMALL = 8;
 enum Mode { MODE_F32C = 0, MODE_F64 = 1 };
 
 typedef cudaError_t (*LaunchFn)(PairArgs, int, cudaStream_t);
+// batched: (args, items, nitems, reduce items, nreduce items, stream)
+typedef cudaError_t (*LaunchBatchedFn)(const PairArgs *, const int4 *, int, const int2 *, int, cudaStream_t);
 
 struct KernelEntry {
   LaunchFn fn;
+  LaunchBatchedFn fnb;
   const void *kernel;  // the pair kernel (for occupancy queries)
   int block;  // threads per CTA
   int r;      // targets per thread
@@ -66,6 +69,7 @@ template <class OpT, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int
           int CSM = 0>
 inline bool set_entry(KernelEntry *e) {
   e->fn = &launch_pairs<OpT, T, D, BLOCK, R, TJ, MERGE, MINB, UNR, CSM>;
+  e->fnb = &launch_pairs_batched<OpT, T, D, BLOCK, R, TJ, MERGE, MINB, UNR, CSM>;
   e->kernel = (const void *)&pair_kernel<OpT, T, D, BLOCK, R, TJ, MERGE, MINB, UNR, CSM>;
   e->block = BLOCK;
   e->r = R;

@@ -445,8 +445,8 @@ constexpr size_t pair_smem_bytes() {
 
 // FP32 mode subtracts the CTA's target bounding-box midpoint (centring); FP64 mode forms x - y
 // directly, as the reference does. UNR: unroll of the per-source loop. CSM: see pair_smem_bytes.
-template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
-__global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int UNR, int CSM>
+__device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_idx, const int split) {
   typedef Lane<T> L;
   typedef typename L::V V;
   typedef typename SrcLane<T>::SV SV;
@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
   __shared__ double s_red[2 * D][BLOCK / 32];
   __shared__ double s_ctr[D];
 
-  const long i0 = (long)blockIdx.x * (BLOCK * R);
+  const long i0 = tile_idx * (BLOCK * R);
   const long nx = a.nx;
 
   // ---- centre of this CTA's target tile (bounding-box midpoint, FP64) ----
@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
   const V cx = exp_arg_scale<T>(a.sigma);
   const int p0 = a.p0, p1 = a.p1;
 
-  const long jb = (long)blockIdx.y * a.j_chunk;
+  const long jb = (long)split * a.j_chunk;
   long je = jb + a.j_chunk;
   if (je > a.ny) je = a.ny;
 
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
         v[o] = (double)L::get(sv, w2) + (double)L::get(cv, w2);
       }
       if (a.nsplit > 1) {
-        double *p = a.partial + (long)blockIdx.y * NO * nx;
+        double *p = a.partial + (long)split * NO * nx;
 #pragma unroll
         for (int o = 0; o < NO; ++o) p[(long)o * nx + i] = v[o];
       } else {
@@ -654,6 +654,21 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
       }
     }
   }
+}
+
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
+__global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
+  pair_block<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM>(a, (long)blockIdx.x, (int)blockIdx.y);
+}
+
+// Batched form: CTA b works on item items[b] = (problem, target tile, source split) of the
+// problem's arguments args[problem]. One launch covers every problem of a batch (the subjects of
+// an atlas), whatever their sizes; items are ordered by the host (largest first).
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
+__global__ void __launch_bounds__(BLOCK, MINB) pair_kernel_batched(const PairArgs *args, const int4 *items) {
+  const int4 it = items[blockIdx.x];
+  const PairArgs a = args[it.x];
+  pair_block<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM>(a, (long)it.y, it.z);
 }
 
 // Sums the per-split FP64 partials in split order and applies the op's store.
@@ -678,6 +693,42 @@ struct LaunchCfg {
   int variant;  // index into the op's compiled (BLOCK, R, TJ) table
   int nsplit;   // source splits (grid.y); 1 = no partial buffer
 };
+
+// Batched split reduction: thread over (problem, target) items ritems[b] = (problem, first target).
+template <class Op>
+__global__ void split_reduce_batched_kernel(const PairArgs *args, const int2 *ritems) {
+  constexpr int NO = Op::NO;
+  const int2 it = ritems[blockIdx.x];
+  const PairArgs &a = args[it.x];
+  const long i = (long)it.y + threadIdx.x;
+  if (i >= a.nx || a.nsplit <= 1) return;
+  double v[NO];
+#pragma unroll
+  for (int o = 0; o < NO; ++o) v[o] = 0.0;
+  for (int s = 0; s < a.nsplit; ++s) {
+    const double *p = a.partial + (long)s * NO * a.nx;
+#pragma unroll
+    for (int o = 0; o < NO; ++o) v[o] += p[(long)o * a.nx + i];
+  }
+  Op::store(a, i, v);
+}
+
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
+cudaError_t launch_pairs_batched(const PairArgs *args, const int4 *items, int nitems, const int2 *ritems,
+                                 int nritems, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  const size_t smem = pair_smem_bytes<Op, T, D, BLOCK, R, TJ, CSM>();
+  auto kern = pair_kernel_batched<Op, T, D, BLOCK, R, TJ, MERGE, MINB, UNR, CSM>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<(unsigned)nitems, BLOCK, smem, st>>>(args, items);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || nritems <= 0) return e;
+  split_reduce_batched_kernel<Op><<<(unsigned)nritems, 256, 0, st>>>(args, ritems);
+  return cudaGetLastError();
+}
 
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 cudaError_t launch_pairs(PairArgs a, int nsplit, cudaStream_t st) {

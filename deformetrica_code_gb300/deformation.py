@@ -161,3 +161,56 @@ class Registration:
             self.close()
         except Exception:
             pass
+
+
+class Atlas:
+    """DeterministicAtlas iteration over many subjects, every stage one launch for all subjects
+    (uneven target meshes balanced by source chunks), replayed from a CUDA graph."""
+
+    KINDS = {"currents": 0, "varifold": 1}
+
+    def __init__(self, cp, tmpl_pts, tmpl_tris, targets, T: int, sigma_def: float, sigma_data: float,
+                 data_sigma2: float, kind: str = "currents", heun: bool = True, context: Context | None = None):
+        self.ctx = context or Context()
+        cp = np.ascontiguousarray(cp, dtype=np.float64)
+        tp, tt = np.ascontiguousarray(tmpl_pts, np.float64), np.ascontiguousarray(tmpl_tris, np.int32)
+        self.S, self.ncp, self.nv = len(targets), cp.shape[0], tp.shape[0]
+        nv_t = np.array([t[0].shape[0] for t in targets], dtype=np.int64)
+        nf_t = np.array([t[1].shape[0] for t in targets], dtype=np.int64)
+        pts = np.ascontiguousarray(np.concatenate([t[0] for t in targets]), np.float64)
+        tris = np.ascontiguousarray(np.concatenate([t[1] for t in targets]), np.int32)
+        h = ctypes.c_void_p()
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_atlas_create(
+            self.ctx.h, self.ncp, c(cp), self.nv, c(tp), tt.shape[0], c(tt), self.S, c(nv_t), c(pts), c(nf_t),
+            c(tris), int(T), float(sigma_def), float(sigma_data), float(data_sigma2), self.KINDS[kind], int(heun),
+            ctypes.byref(h)))
+        self.h = h
+
+    def set_graph(self, enable: bool):
+        self.ctx.check(self.ctx.lib.gbk_atlas_set_graph(self.h, int(enable)))
+
+    def step(self, mom):
+        """mom: S x ncp x 3. Returns loglik (3 + S), dL/dp (S x ncp x 3), dL/dcp, template gradient."""
+        mom = np.ascontiguousarray(mom, dtype=np.float64)
+        ll = np.zeros(3 + self.S)
+        gm = np.zeros((self.S, self.ncp, 3))
+        gc = np.zeros((self.ncp, 3))
+        gt = np.zeros((self.nv, 3))
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_atlas_step(self.h, c(mom), c(ll), c(gm), c(gc), c(gt)))
+        return ll, gm, gc, gt
+
+    def graph_launches(self) -> int:
+        return int(self.ctx.lib.gbk_atlas_graph_launches(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbk_atlas_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -251,6 +251,31 @@ void gbk_registration_destroy(gbk_registration *reg);
 int gbk_kernel_norm_noalloc(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
                             double sigma, double *out);
 
+/* ---- batched atlas iteration (all subjects per launch), CUDA-graph replay ---------------- */
+
+typedef struct gbk_atlas gbk_atlas;
+
+/* A DeterministicAtlas iteration with a shared template mesh (nv vertices, nf faces) and shared
+ * control points cp (ncp x 3), nsub subjects each matched to its own target mesh
+ * (DeterministicAtlas.cxx:99-280, AbstractAtlas.cxx:138-613). Target meshes are concatenated:
+ * tgt_pts holds sum(nv_t) x 3 points, tgt_tris sum(nf_t) x 3 vertex indices local to each subject.
+ * data_kind 0 = currents, 1 = varifold. Every stage runs as one launch over all subjects; all
+ * device memory is allocated here. */
+int gbk_atlas_create(gbk_ctx *ctx, long ncp, const double *cp, long nv, const double *tmpl_pts,
+                     long nf, const int *tmpl_tris, int nsub, const long *nv_t,
+                     const double *tgt_pts, const long *nf_t, const int *tgt_tris, int T,
+                     double sigma_def, double sigma_data, double data_sigma2, int data_kind,
+                     int heun, gbk_atlas **out);
+/* mom: nsub x ncp x 3. loglik[3 + nsub] = {L, L_data, L_reg, L_0 .. L_{nsub-1}};
+ * grad_mom (nsub x ncp x 3) = dL/dp_s; grad_cp (ncp x 3) = sum_s dL_s/dcp; grad_tmpl (nv x 3) =
+ * sum_s -theta_s(0), the template vertex gradient. Any output may be NULL. Graph replay from the
+ * third call, as gbk_registration_step. */
+int gbk_atlas_step(gbk_atlas *atlas, const double *mom, double *loglik, double *grad_mom,
+                   double *grad_cp, double *grad_tmpl);
+int gbk_atlas_set_graph(gbk_atlas *atlas, int enable);
+long long gbk_atlas_graph_launches(const gbk_atlas *atlas);
+void gbk_atlas_destroy(gbk_atlas *atlas);
+
 /* ---- tuning ------------------------------------------------------------------------------ */
 
 /* Times the compiled variants and source-split factors of `op` for this shape on synthetic data

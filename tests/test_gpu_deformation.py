@@ -195,3 +195,45 @@ def test_registration_step_matches_oracle_and_graph_replay(gb, ctx, K, kind):
         assert normwise_rel(gm, gmom_r) <= tol
         assert normwise_rel(gc, gcp_r) <= tol
         reg.close()
+
+
+@pytest.mark.parametrize("kind", ["currents", "varifold"])
+def test_batched_atlas_matches_per_subject_oracle(gb, ctx, K, kind):
+    """One batched atlas iteration over subjects with uneven target meshes equals the sum of the
+    per-subject oracle registrations (DeterministicAtlas / AbstractAtlas restated), and graph replay
+    reproduces the eager iteration bitwise."""
+    from oracle import deformation as D
+    from deformetrica_code_gb300 import meshes as M
+    from deformetrica_code_gb300.deformation import Atlas
+    tp, tf = M.icosphere(2, 0.35)
+    targets = [M.perturbed_sphere(n, noise=0.02, seed=40 + i, radius=0.36) for i, n in enumerate((150, 420, 260))]
+    cp = grid_cp(3, 0.25, 0.75)
+    rng = np.random.default_rng(4)
+    mom = 0.01 * rng.standard_normal((len(targets), cp.shape[0], 3))
+    kw = dict(T=5, sigma_def=0.25, sigma_data=0.15, data_sigma2=0.01)
+    Ls, gcp, gt = [], np.zeros_like(cp), np.zeros_like(tp)
+    gms = []
+    for s, (p_t, f_t) in enumerate(targets):
+        L, gc, gm, info = D.registration(K, cp, mom[s], tp, tf, p_t, f_t, kw["T"], kw["sigma_def"],
+                                         kw["sigma_data"], kw["data_sigma2"], kind=kind)
+        Ls.append(L)
+        gcp += gc
+        gms.append(gm)
+        gt -= info["theta"][0]
+    for mode, tol in modes(gb):
+        ctx.set_mode(mode)
+        atlas = Atlas(cp, tp, tf, targets, kind=kind, context=ctx, **kw)
+        outs = [atlas.step(mom) for _ in range(3)]  # eager, capture + replay, replay
+        assert atlas.graph_launches() > 10
+        for o in outs[1:]:
+            for a_, b_ in zip(o, outs[0]):
+                assert np.array_equal(a_, b_)
+        ll, gm, gc, gtt = outs[0]
+        ltol = 1e-9 if mode == gb.GBK_MODE_F64 else 1e-5
+        assert abs(ll[0] - sum(Ls)) <= ltol * abs(sum(Ls))
+        for s in range(len(targets)):
+            assert abs(ll[3 + s] - Ls[s]) <= ltol * abs(Ls[s])
+            assert normwise_rel(gm[s], gms[s]) <= tol
+        assert normwise_rel(gc, gcp) <= tol
+        assert normwise_rel(gtt, gt) <= tol
+        atlas.close()

@@ -308,6 +308,8 @@ struct gbk_atlas {
       a.j_chunk = jc;
       a.nsplit = nsplit;
       a.partial = nullptr;  // patched in upload()
+      // coordinate pre-scale of the lane type (the single-problem launcher sets it itself)
+      a.xscale = c->mode == MODE_F64 ? coord_scale<double>(a.sigma) : coord_scale<float>(a.sigma);
       if (nsplit > 1) partial_per_subject = std::max(partial_per_subject, (size_t)nsplit * L.e.no * a.nx);
       for (long t = 0; t < itiles; ++t)
         for (int sp = 0; sp < nsplit; ++sp) items.push_back({s, (int)t, sp, std::min(jc, a.ny - (long)sp * jc)});
@@ -732,15 +734,17 @@ int gbk_atlas_create(gbk_ctx *c, long ncp, const double *cp, long nv, const doub
     if (!rc) rc = c->cuda(cudaMemcpyAsync(a->tw, tw.data(), tw.size() * sizeof(double), cudaMemcpyHostToDevice, st), "copy");
     if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
   }
-  // |T_s|^2 once per subject: one Convolve of the target faces, FP64 dot
+  // |T_s|^2 once per subject: one Convolve of the target faces, FP64 dot. Temporaries sized by the
+  // largest target, released after creation.
+  long max_ft = 0;
+  for (int s = 0; s < nsub; ++s) max_ft = std::max(max_ft, nf_t[s]);
+  double *kw = nullptr, *wdev = nullptr;
+  if (!rc) rc = c->cuda(cudaMalloc(&kw, (size_t)max_ft * a->dw * sizeof(double)), "cudaMalloc (target norms)");
+  if (!rc) rc = c->cuda(cudaMalloc(&wdev, (size_t)max_ft * 6 * sizeof(double)), "cudaMalloc (target norms)");
+  std::vector<double> wd;
   for (int s = 0; !rc && s < nsub; ++s) {
     const double *ws_t = a->tw + a->toff[s] * a->dw;
     const long fs = nf_t[s];
-    double *kw = a->ktt;  // temporary (n_t x dw fits: ktt holds S x nf x 6)
-    if ((size_t)fs * a->dw > S * nf * 6) {
-      rc = c->fail(GBK_ERR_ARG, "target %d too large for the scratch", s);
-      break;
-    }
     PairArgs q = pair_args(fs, fs, sigma_data);
     q.x = a->ct + a->toff[s] * 3;
     q.y = q.x;
@@ -753,23 +757,20 @@ int gbk_atlas_create(gbk_ctx *c, long ncp, const double *cp, long nv, const doub
     if (data_kind == 0) {
       rc = c->cuda(dot_f64(a->stream, ws_t, kw, fs * 3, a->norm_t + s, 0), "dot");
     } else {
-      // |T|^2 = sum_f w(n~_f) . (K MN)_f with w the dual weights of MN: w = MN with off-diagonals doubled
-      std::vector<double> wd((size_t)fs * 6);
+      // |T|^2 = sum_f w(n~_f) . (K MN)_f, w = MN with the off-diagonal entries doubled
+      wd.resize((size_t)fs * 6);
       for (long f = 0; f < fs; ++f)
         for (int q6 = 0; q6 < 6; ++q6) {
           const double v = tw[(size_t)(a->toff[s] + f) * 6 + q6];
           wd[(size_t)f * 6 + q6] = (q6 == 1 || q6 == 2 || q6 == 4) ? 2.0 * v : v;
         }
-      double *wdev = a->kt;  // temporary, S x nf x 3 doubles
-      if ((size_t)fs * 6 > S * nf * 3) {
-        rc = c->fail(GBK_ERR_ARG, "target %d too large for the scratch", s);
-        break;
-      }
       rc = c->cuda(cudaMemcpyAsync(wdev, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice, a->stream), "copy");
       if (!rc) rc = c->cuda(dot_f64(a->stream, wdev, kw, fs * 6, a->norm_t + s, 0), "dot");
-      if (!rc) rc = c->cuda(cudaStreamSynchronize(a->stream), "sync");
     }
+    if (!rc) rc = c->cuda(cudaStreamSynchronize(a->stream), "sync");
   }
+  if (kw) cudaFree(kw);
+  if (wdev) cudaFree(wdev);
   if (!rc) rc = c->cuda(cudaStreamSynchronize(a->stream), "sync");
   if (!rc) rc = a->build_launches();
   if (!rc) rc = a->upload();

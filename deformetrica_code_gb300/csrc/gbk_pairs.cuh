@@ -663,7 +663,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
 
 // Batched form: CTA b works on item items[b] = (problem, target tile, source split) of the
 // problem's arguments args[problem]. One launch covers every problem of a batch (the subjects of
-// an atlas), whatever their sizes; items are ordered by the host (largest first).
+// an atlas), whatever their sizes; items are ordered by the host (largest first). The host fills
+// every field of args, including j_chunk, nsplit, partial and xscale (coord_scale of the lane type).
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel_batched(const PairArgs *args, const int4 *items) {
   const int4 it = items[blockIdx.x];

@@ -4,10 +4,12 @@ The compute path is libgbkernel.so (include/gbk.h). Importing this package loads
 if it has not been built: there is no CPU or PyTorch fallback.
 """
 from . import _lib
-from ._lib import GBKError, GBK_MODE_F32C, GBK_MODE_F64
+from ._lib import (GBKError, GBK_MODE_F32C, GBK_MODE_F64, GBK_ORDER_AUTO, GBK_ORDER_OFF, GBK_ORDER_SPATIAL,
+                   GBK_ORDER_SPATIAL_NOPRUNE)
 
 _lib.load()
 
 from .kernel import Context, GB300ExactKernel  # noqa: E402
 
-__all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64"]
+__all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64", "GBK_ORDER_AUTO",
+           "GBK_ORDER_OFF", "GBK_ORDER_SPATIAL", "GBK_ORDER_SPATIAL_NOPRUNE"]

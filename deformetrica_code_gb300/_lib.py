@@ -21,6 +21,10 @@ GBK_ERR_STATE = 6
 
 GBK_MODE_F32C = 0
 GBK_MODE_F64 = 1
+GBK_ORDER_AUTO = 0
+GBK_ORDER_OFF = 1
+GBK_ORDER_SPATIAL = 2
+GBK_ORDER_SPATIAL_NOPRUNE = 3
 
 OPS = {
     "convolve": 0,
@@ -48,6 +52,9 @@ SIGNATURES = {
     "gbk_get_stream": (_P, [_P]),
     "gbk_set_mode": (_I, [_P, _I]),
     "gbk_get_mode": (_I, [_P]),
+    "gbk_evaluated_pairs": (ctypes.c_longlong, [_P]),
+    "gbk_set_order": (_I, [_P, _I]),
+    "gbk_get_order": (_I, [_P]),
     "gbk_synchronize": (_I, [_P]),
     "gbk_launch_count": (ctypes.c_longlong, [_P]),
     "gbk_convolve": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P]),

@@ -801,6 +801,7 @@ int gbk_atlas_step(gbk_atlas *a, const double *mom, double *loglik, double *grad
   int rc = c->cuda(cudaMemcpyAsync(a->mom, mom, nb_mom, cudaMemcpyDefault, a->stream), "copy momenta");
   cudaStream_t saved = c->stream;
   c->stream = a->stream;
+  gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
   if (!rc) {
     if (!a->use_graph || a->steps == 0) {
       rc = a->body();

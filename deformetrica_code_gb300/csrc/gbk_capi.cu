@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -17,6 +18,7 @@
 #include "gbk_ctx.h"
 #include "gbk_dispatch.h"
 #include "gbk_hostio.h"
+#include "gbk_order.h"
 
 using namespace gbk;
 
@@ -203,6 +205,50 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     return fail(GBK_ERR_UNSUPPORTED, "no kernel for op %d, d=%d, dv=%d", op, d, dv);
   if (force_split > 0) ns = force_split;
   if (ns <= 0) ns = choose_split(e, d, a.nx, a.ny);
+  // spatial order of targets and sources (see GBK_ORDER_* in gbk.h)
+  bool spatial = false, prune = false;
+  if (!a.xperm && !a.xtiles && a.nx > 0 && a.ny > 0 && a.nx < INT_MAX && a.ny < INT_MAX) {
+    switch (order) {
+      case GBK_ORDER_SPATIAL: spatial = prune = true; break;
+      case GBK_ORDER_SPATIAL_NOPRUNE: spatial = true; break;
+      case GBK_ORDER_AUTO:
+        spatial = prune = a.nx >= 4096 && a.ny >= 4096 && (double)a.nx * (double)a.ny >= (double)(1L << 27);
+        break;
+      default: break;
+    }
+  }
+  if (spatial) {
+    OrderView tv, sv;
+    if (int rc = order_targets(this, d, a.x, a.nx, e.block * e.r, a.sigma, &tv)) return rc;
+    if (int rc = order_sources(this, d, a.y, a.ny, e.tj, &sv)) return rc;
+    a.xperm = tv.perm;
+    a.xtiles = tv.tiles;
+    a.nxtiles = tv.ntiles;
+    a.xtile_bound = tv.tile_bound;
+    a.ybox = prune ? sv.boxes : nullptr;
+    launches += kOrderTargetLaunches + kOrderSourceLaunches;
+    if (op == OP_ADJCP) {
+      a.yperm = sv.perm;  // its source extras share arrays with the targets: gather while staging
+    } else {
+      // sorted copies of the source rows the op reads: y, the weight columns, the special
+      // Hessian's xi
+      const double *src[3] = {a.y, a.w, a.sb};
+      const int ld[3] = {d, a.w_ld, a.sb_ld};
+      const int cols[3] = {d, op == OP_SPECIAL ? d : dv, d};
+      double *dst[3];
+      const int na = op == OP_SPECIAL ? 3 : 2;
+      if (int rc = gather_sources(this, sv.perm, a.ny, src, ld, cols, na, dst)) return rc;
+      a.y = dst[0];
+      a.w = dst[1];
+      a.w_ld = cols[1];
+      if (op == OP_SPECIAL) {
+        a.sb = dst[2];
+        a.sb_ld = d;
+      }
+      launches += na;
+    }
+  }
+  a.pair_count = pair_counter;
   if (ns > 1) {
     // launch_pairs rounds the split count; size the buffer for the requested count
     int rc = ensure(partial, (size_t)ns * e.no * std::max(a.nx, 1L) * sizeof(double), "split partials");
@@ -322,6 +368,15 @@ int gbk_create(int device, gbk_ctx **out) {
     return GBK_ERR_CUDA;
   }
   c->stream = c->own_stream;
+  if (cudaMalloc(&c->pair_counter, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(c->pair_counter, 0, sizeof(unsigned long long)) != cudaSuccess) {
+    cudaGetLastError();
+    c->release();
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    g_create_err = "device allocation of the pair counter failed";
+    return GBK_ERR_ALLOC;
+  }
   *out = c;
   return GBK_OK;
 }
@@ -355,12 +410,37 @@ int gbk_set_mode(gbk_ctx *c, int mode) {
 
 int gbk_get_mode(const gbk_ctx *c) { return c ? c->mode : -1; }
 
+int gbk_set_order(gbk_ctx *c, int order) {
+  if (!c) return GBK_ERR_ARG;
+  if (order < GBK_ORDER_AUTO || order > GBK_ORDER_SPATIAL_NOPRUNE)
+    return c->fail(GBK_ERR_ARG, "unknown order %d", order);
+  c->order = order;
+  return GBK_OK;
+}
+
+int gbk_get_order(const gbk_ctx *c) { return c ? c->order : -1; }
+
 int gbk_synchronize(gbk_ctx *c) {
   GBK_GUARD(c);
   return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
 }
 
 long long gbk_launch_count(const gbk_ctx *c) { return c ? c->launches : 0; }
+
+long long gbk_evaluated_pairs(gbk_ctx *c) {
+  if (!c || !c->pair_counter) return -1;
+  if (cudaSetDevice(c->device) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  unsigned long long v = 0;
+  if (cudaMemcpyAsync(&v, c->pair_counter, sizeof v, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return (long long)v;
+}
 
 int gbk_set_split(gbk_ctx *c, int nsplit) {
   if (!c || nsplit < 0) return GBK_ERR_ARG;

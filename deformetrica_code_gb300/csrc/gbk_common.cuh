@@ -158,6 +158,21 @@ __host__ __device__ inline float2 exp_arg_scale<float>(double sigma) {
   return float2{0.f, 0.f};  // unused: FP32 lanes work on pre-scaled coordinates
 }
 
+// Squared distance (input units) beyond which the lane type's kernel value is exactly zero, with
+// margin. FP32 lanes evaluate ex2.approx.ftz(-r2) on coordinates scaled by coord_scale: for
+// r2 >= 127 the result is subnormal and flushed to +0, and 130 leaves room for the FP32 rounding
+// of r2. FP64 lanes evaluate exp(-|dx|^2 / sigma^2), which is below half the smallest subnormal
+// (exp(-745.13)) and rounds to zero for arguments under -800.
+template <typename T>
+inline double prune_dist2(double sigma) {
+  const double s = coord_scale<T>(sigma);
+  return 130.0 / (s * s);
+}
+template <>
+inline double prune_dist2<double>(double sigma) {
+  return 800.0 * sigma * sigma;
+}
+
 // Bounded-iteration helpers for any cross-block wait (none of the kernel-sum kernels wait).
 constexpr unsigned long long kSpinLimit = 1ull << 26;
 

@@ -34,6 +34,12 @@ struct gbk_ctx {
   DevBuf stage[kStageSlots];  // host-argument staging
   DevBuf reduce;              // FP64 reductions and small temporaries
   DevBuf tmp;                 // op temporaries (e.g. K w for the kernel norm)
+  int order = 0;              // GBK_ORDER_* (0 = automatic)
+  DevBuf order_keep[2];       // spatial order of the targets / sources of the last launch
+  DevBuf order_tmp;           // Morton keys and bounding boxes
+  DevBuf order_cub;           // radix-sort scratch
+  DevBuf order_src;           // source rows in sorted order
+  unsigned long long *pair_counter = nullptr;  // device: pairs evaluated by launch()
 
   typedef std::tuple<int, int, int, int, int, int> TuneKey;  // op, mode, d, dv, log2 nx, log2 ny
   std::map<TuneKey, std::pair<int, int>> tune;                // -> (variant, nsplit)
@@ -48,6 +54,14 @@ struct gbk_ctx {
   int choose_split(const gbk::KernelEntry &e, int d, long nx, long ny);
   int launch(int op, int d, int dv, gbk::PairArgs a);
 
+  // Holds the order policy at `o` for a scope (the registration and atlas steps use OFF).
+  struct OrderScope {
+    gbk_ctx *c;
+    int saved;
+    OrderScope(gbk_ctx *ctx, int o) : c(ctx), saved(ctx->order) { c->order = o; }
+    ~OrderScope() { c->order = saved; }
+  };
+
   void release() {
     auto fr = [](DevBuf &b) {
       if (b.p) cudaFree(b.p);
@@ -57,6 +71,13 @@ struct gbk_ctx {
     fr(partial);
     fr(reduce);
     fr(tmp);
+    fr(order_keep[0]);
+    fr(order_keep[1]);
+    fr(order_tmp);
+    fr(order_cub);
+    fr(order_src);
+    if (pair_counter) cudaFree(pair_counter);
+    pair_counter = nullptr;
     for (auto &b : stage) fr(b);
   }
 };

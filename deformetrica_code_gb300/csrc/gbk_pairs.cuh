@@ -54,6 +54,16 @@ struct PairArgs {
   double *partial;  // [nsplit][NO][nx] FP64 partial sums when nsplit > 1
   long j_chunk;     // sources per split (a multiple of TJ)
   int nsplit;
+  // spatial order (all null: rows in caller order, fixed target tiles, every source chunk visited)
+  const int *xperm;    // sorted target position -> target row
+  const int2 *xtiles;  // per CTA: [begin, end) of sorted target positions
+  const int *nxtiles;  // number of valid xtiles entries (grid.x is the host bound xtile_bound)
+  long xtile_bound;
+  const int *yperm;    // sorted source position -> source row
+  const double *ybox;  // per TJ chunk of sorted sources: lo[D], hi[D]; null = no pruning
+  double prune_d2;     // a source chunk whose box is farther than this (squared) from the CTA's
+                       // target box contributes exact zeros only (set by launch_pairs)
+  unsigned long long *pair_count;  // if set, += (target, source) pairs this launch evaluated
 };
 
 __device__ __forceinline__ void put(double *p, int acc, double v) {
@@ -443,8 +453,15 @@ constexpr size_t pair_smem_bytes() {
          (size_t)CSM * (R / Lane<T>::kWidth) * Op::NO * BLOCK * sizeof(typename Lane<T>::V);
 }
 
+// Source chunks per visit mask (pruning): 512 bytes of shared memory.
+constexpr int kPruneWindow = 4096;
+
 // FP32 mode subtracts the CTA's target bounding-box midpoint (centring); FP64 mode forms x - y
 // directly, as the reference does. UNR: unroll of the per-source loop. CSM: see pair_smem_bytes.
+// With a spatial order (a.xtiles), the CTA's targets are the sorted positions of its tile, rows
+// a.xperm[...]; sources are visited in sorted order (a.yperm) and a source chunk whose box is
+// farther than a.prune_d2 from the CTA's target box is skipped: every pair term in it is exactly
+// zero, so the sums are the same as when it is visited.
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int UNR, int CSM>
 __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_idx, const int split) {
   typedef Lane<T> L;
@@ -457,18 +474,33 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
   constexpr bool CENTER = !std::is_same<T, double>::value;
   static_assert(R % W == 0, "R must be a multiple of the lane width");
   static_assert(TJ % MERGE == 0, "TJ must be a multiple of MERGE");
+  static_assert(BLOCK % 32 == 0 && kPruneWindow % BLOCK == 0, "visit-mask rounds need whole warps");
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SV *tile = reinterpret_cast<SV *>(smem_raw);
   __shared__ double s_red[2 * D][BLOCK / 32];
   __shared__ double s_ctr[D];
+  __shared__ double s_box[2 * D];
+  __shared__ unsigned s_visit[kPruneWindow / 32];
 
-  const long i0 = tile_idx * (BLOCK * R);
-  const long nx = a.nx;
+  // ---- this CTA's targets: sorted positions [i0, iend) (caller order when unsorted) ----
+  long i0, iend;
+  if (a.xtiles) {
+    if (tile_idx >= (long)*a.nxtiles) return;  // beyond the tiles of this order: whole CTA
+    const int2 tl = a.xtiles[tile_idx];
+    i0 = tl.x;
+    iend = tl.y;
+  } else {
+    i0 = tile_idx * (BLOCK * R);
+    iend = i0 + BLOCK * R < a.nx ? i0 + BLOCK * R : a.nx;
+  }
+  const int *const xperm = a.xperm;
+  const int *const yperm = a.yperm;
+  const bool prune = a.ybox != nullptr;
 
-  // ---- centre of this CTA's target tile (bounding-box midpoint, FP64) ----
+  // ---- bounding box of the CTA's targets (FP64): centre for FP32 lanes, box for pruning ----
   double ctr[D];
-  if (CENTER) {
+  if (CENTER || prune) {
     double lo[D], hi[D];
 #pragma unroll
     for (int l = 0; l < D; ++l) {
@@ -478,10 +510,11 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       long i = i0 + threadIdx.x + (long)r * BLOCK;
-      if (i < nx) {
+      if (i < iend) {
+        const long row = xperm ? (long)xperm[i] : i;
 #pragma unroll
         for (int l = 0; l < D; ++l) {
-          double v = a.x[i * D + l];
+          double v = a.x[row * D + l];
           lo[l] = fmin(lo[l], v);
           hi[l] = fmax(hi[l], v);
         }
@@ -509,7 +542,9 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
         mn = fmin(mn, s_red[threadIdx.x][w2]);
         mx = fmax(mx, s_red[D + threadIdx.x][w2]);
       }
-      s_ctr[threadIdx.x] = (mn <= mx) ? 0.5 * (mn + mx) : 0.0;
+      s_ctr[threadIdx.x] = (CENTER && mn <= mx) ? 0.5 * (mn + mx) : 0.0;
+      s_box[threadIdx.x] = mn;
+      s_box[D + threadIdx.x] = mx;
     }
     __syncthreads();
 #pragma unroll
@@ -529,7 +564,8 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
 #pragma unroll
     for (int w2 = 0; w2 < W; ++w2) {
       long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
-      long ic = i < nx ? i : (nx - 1);  // out-of-range lanes compute a copy, never stored
+      long ic = i < iend ? i : (iend - 1);  // out-of-range lanes compute a copy, never stored
+      if (xperm) ic = xperm[ic];
 #pragma unroll
       for (int l = 0; l < D; ++l) xv[w2][l] = (a.x[ic * D + l] - ctr[l]) * xs;
       Op::load_target(a, ic, tv[w2]);
@@ -560,14 +596,45 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
   const long jb = (long)split * a.j_chunk;
   long je = jb + a.j_chunk;
   if (je > a.ny) je = a.ny;
+  long visited = 0;  // sources of the visited chunks
 
   for (long jt = jb; jt < je; jt += TJ) {
+    if (prune) {
+      // Visit mask of the next kPruneWindow source chunks, one distance test per chunk for the
+      // whole CTA (FP64, spread over the threads), then one shared-memory bit per chunk.
+      const long q = (jt - jb) / TJ;
+      const int wq = (int)(q % kPruneWindow);
+      if (wq == 0) {
+        __syncthreads();  // every thread is done with the previous window's mask
+#pragma unroll 4
+        for (int r = 0; r < kPruneWindow / BLOCK; ++r) {
+          const long jc = jt + (long)(r * BLOCK + threadIdx.x) * TJ;  // first source of the chunk
+          bool visit = false;
+          if (jc < je) {
+            const double *cb = a.ybox + (jc / TJ) * (2 * D);
+            double d2 = 0.0;
+#pragma unroll
+            for (int l = 0; l < D; ++l) {
+              const double gap = fmax(0.0, fmax(cb[l] - s_box[D + l], s_box[l] - cb[D + l]));
+              d2 += gap * gap;
+            }
+            visit = !(d2 > a.prune_d2);
+          }
+          const unsigned bits = __ballot_sync(0xffffffffu, visit);
+          if ((threadIdx.x & 31) == 0) s_visit[(r * BLOCK + threadIdx.x) >> 5] = bits;
+        }
+        __syncthreads();
+      }
+      if (!((s_visit[wq >> 5] >> (wq & 31)) & 1u)) continue;  // same decision in every thread
+    }
     const int cnt = (int)((je - jt) < TJ ? (je - jt) : TJ);
+    visited += cnt;
     // ---- stage TJ source records: -(y - c) * xscale and extras, broadcast to the lane type ----
     for (int r = threadIdx.x; r < TJ; r += BLOCK) {
       double rec[NJP];
       if (r < cnt) {
         long j = jt + r;
+        if (yperm) j = yperm[j];
 #pragma unroll
         for (int l = 0; l < D; ++l) rec[l] = (ctr[l] - a.y[j * D + l]) * xs;
         Op::load_source(a, j, rec + D);
@@ -631,13 +698,16 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
     __syncthreads();
   }
 
+  if (a.pair_count && threadIdx.x == 0 && visited > 0)
+    atomicAdd(a.pair_count, (unsigned long long)(iend - i0) * (unsigned long long)visited);
+
   // ---- write: final sums in FP64 ----
 #pragma unroll
   for (int g = 0; g < G; ++g) {
 #pragma unroll
     for (int w2 = 0; w2 < W; ++w2) {
       long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
-      if (i >= nx) continue;
+      if (i >= iend) continue;
       double v[NO];
 #pragma unroll
       for (int o = 0; o < NO; ++o) {
@@ -645,12 +715,12 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
         V cv = CSM >= 1 ? csm[(g * NO + o) * BLOCK + threadIdx.x] : cmp[g][o];
         v[o] = (double)L::get(sv, w2) + (double)L::get(cv, w2);
       }
-      if (a.nsplit > 1) {
-        double *p = a.partial + (long)split * NO * nx;
+      if (a.nsplit > 1) {  // partials by sorted position; the reduction maps to rows
+        double *p = a.partial + (long)split * NO * a.nx;
 #pragma unroll
-        for (int o = 0; o < NO; ++o) p[(long)o * nx + i] = v[o];
+        for (int o = 0; o < NO; ++o) p[(long)o * a.nx + i] = v[o];
       } else {
-        Op::store(a, i, v);
+        Op::store(a, xperm ? (long)xperm[i] : i, v);
       }
     }
   }
@@ -686,7 +756,7 @@ __global__ void split_reduce_kernel(const PairArgs a) {
 #pragma unroll
     for (int o = 0; o < NO; ++o) v[o] += p[(long)o * a.nx + i];
   }
-  Op::store(a, i, v);
+  Op::store(a, a.xperm ? (long)a.xperm[i] : i, v);
 }
 
 // Launch configuration of one pair kernel.
@@ -711,7 +781,7 @@ __global__ void split_reduce_batched_kernel(const PairArgs *args, const int2 *ri
 #pragma unroll
     for (int o = 0; o < NO; ++o) v[o] += p[(long)o * a.nx + i];
   }
-  Op::store(a, i, v);
+  Op::store(a, a.xperm ? (long)a.xperm[i] : i, v);
 }
 
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
@@ -754,7 +824,9 @@ cudaError_t launch_pairs(PairArgs a, int nsplit, cudaStream_t st) {
     a.nsplit = 1;
     nsplit = 1;
   }
-  dim3 grid((unsigned)((a.nx + (long)BLOCK * R - 1) / ((long)BLOCK * R)), (unsigned)nsplit);
+  a.prune_d2 = prune_dist2<T>(a.sigma);
+  const long tiles = a.xtiles ? a.xtile_bound : (a.nx + (long)BLOCK * R - 1) / ((long)BLOCK * R);
+  dim3 grid((unsigned)tiles, (unsigned)nsplit);
   kern<<<grid, BLOCK, smem, st>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || nsplit == 1) return e;

@@ -213,7 +213,10 @@ int gbk_registration_step(gbk_registration *r, const double *cp, const double *m
   const size_t nb = (size_t)r->ncp * r->d * sizeof(double);
   int rc = c->cuda(cudaMemcpyAsync(r->cp, cp, nb, cudaMemcpyDefault, r->stream), "copy cp");
   if (!rc) rc = c->cuda(cudaMemcpyAsync(r->mom, mom, nb, cudaMemcpyDefault, r->stream), "copy mom");
-  if (!rc) rc = r->run();
+  if (!rc) {
+    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    rc = r->run();
+  }
   if (!rc && loglik) rc = c->cuda(cudaMemcpyAsync(loglik, r->out, 5 * sizeof(double), cudaMemcpyDefault, r->stream), "copy L");
   if (!rc && grad_cp) rc = c->cuda(cudaMemcpyAsync(grad_cp, r->gcp, nb, cudaMemcpyDefault, r->stream), "copy grad");
   if (!rc && grad_mom) rc = c->cuda(cudaMemcpyAsync(grad_mom, r->gmom, nb, cudaMemcpyDefault, r->stream), "copy grad");

@@ -85,11 +85,25 @@ class Context:
         self.check(self.lib.gbk_set_mode(self.h, mode))
         self.mode = mode
 
+    def set_order(self, order: int):
+        """GBK_ORDER_AUTO / OFF / SPATIAL / SPATIAL_NOPRUNE (include/gbk.h)."""
+        self.check(self.lib.gbk_set_order(self.h, order))
+
+    def get_order(self) -> int:
+        return int(self.lib.gbk_get_order(self.h))
+
     def set_split(self, n: int):
         self.check(self.lib.gbk_set_split(self.h, n))
 
     def launch_count(self) -> int:
         return int(self.lib.gbk_launch_count(self.h))
+
+    def evaluated_pairs(self) -> int:
+        """(target, source) pairs evaluated so far (pruned source chunks excluded); waits."""
+        v = int(self.lib.gbk_evaluated_pairs(self.h))
+        if v < 0:
+            raise GBKError(3, "gbk_evaluated_pairs failed")
+        return v
 
     def bind_stream(self, *arrays):
         """Queue on torch's current stream when any argument is a CUDA tensor."""

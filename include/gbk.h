@@ -50,6 +50,17 @@ enum {
 
 enum { GBK_MODE_F32C = 0, GBK_MODE_F64 = 1 };
 
+/* Order in which the kernel sums visit targets and sources (gbk_set_order).
+ *  AUTO: SPATIAL for calls with nx, ny >= 4096 and nx * ny >= 2^27, OFF below.
+ *  OFF: rows in caller order, every (target, source) pair evaluated.
+ *  SPATIAL: targets and sources sorted along a Morton curve on the device before the sum; each CTA
+ *    takes a compact tile of targets (smaller FP32 coordinate rounding after centring) and skips
+ *    source chunks too far away to contribute anything but exact zeros in the precision mode.
+ *    Outputs are still written in caller row order.
+ *  SPATIAL_NOPRUNE: the same order with every pair evaluated (gives the same bits as SPATIAL).
+ * The reference has no counterpart: ExactKernel always visits every pair in row order. */
+enum { GBK_ORDER_AUTO = 0, GBK_ORDER_OFF = 1, GBK_ORDER_SPATIAL = 2, GBK_ORDER_SPATIAL_NOPRUNE = 3 };
+
 /* Operation identifiers (for gbk_autotune). */
 enum {
   GBK_OP_CONVOLVE = 0,
@@ -79,10 +90,18 @@ int gbk_set_stream(gbk_ctx *ctx, void *stream);
 void *gbk_get_stream(const gbk_ctx *ctx);
 int gbk_set_mode(gbk_ctx *ctx, int mode);
 int gbk_get_mode(const gbk_ctx *ctx);
+/* Sets the GBK_ORDER_* policy of later kernel-sum calls (default GBK_ORDER_AUTO). The
+ * registration and atlas steps always use GBK_ORDER_OFF. No counterpart in the reference. */
+int gbk_set_order(gbk_ctx *ctx, int order);
+int gbk_get_order(const gbk_ctx *ctx);
 /* Waits for all work queued on the context's stream. */
 int gbk_synchronize(gbk_ctx *ctx);
 /* Number of the library's own kernels launched on this context so far. */
 long long gbk_launch_count(const gbk_ctx *ctx);
+/* (target, source) pairs the kernel sums of this context have evaluated so far (pairs in source
+ * chunks skipped by GBK_ORDER_SPATIAL are not counted; the registration and atlas steps are not
+ * counted). Waits for the context's stream; -1 on error. No counterpart in the reference. */
+long long gbk_evaluated_pairs(gbk_ctx *ctx);
 
 /* ---- kernel sums (AbstractKernel surface) ------------------------------------------------ */
 

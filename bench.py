@@ -5,10 +5,14 @@ Workload (default): forward + full adjoint of a Gaussian kernel sum at N = M = 1
 means ~ U[0.15, 0.85]^3, clipped to [0,1]), weights and adjoint seeds ~ N(0,1), sigma = 0.1,
 seed 3. One step = gbk_forward_adjoint: the target-side pass (Convolve + alpha-gradient, fused)
 and the source-side pass (dL/dy, dL/dw, fused), every pair's distance and exp recomputed.
-Metric: kernel pairs per second, pairs = N * M per step (each evaluated in both passes).
+Metric: kernel pairs per second, pairs = N * M per step (each evaluated in both passes). The
+library's default order sorts both point sets spatially and skips source chunks whose kernel
+values are exactly zero; the line reports how many pairs were evaluated, and the roofline counts
+evaluated pairs only.
 
 Prints ONE JSON line (rank 0). `--impl reference` times the reference's CPU algorithm instead
-(the FP64 oracle restating ExactKernel; oracle/_ref when it was built on this host).
+(the FP64 oracle restating ExactKernel; oracle/_ref when it was built on this host). `--sweep`
+runs the N x d x sigma sweep of the same step instead, one JSON line per case.
 """
 from __future__ import annotations
 
@@ -275,6 +279,55 @@ def atlas_bench(steps: int, cpu: bool = True):
     return res
 
 
+def data_term_bench(steps: int, cpu: bool = True, nu: int = 500, nv: int = 200, sigma: float = 0.05):
+    """Currents and varifold distance + vertex gradient between two noisy tori (R 0.5, r 0.2,
+    noise 0.01, seeds 5 and 6, nu x nv grid -> 2 nu nv triangles each), sigma 0.05, FP32C with
+    FP64 reductions. pairs per call = 3 F^2 (template x template, template x target, target x
+    target). The CPU figure is the FP64 oracle on a 100 x 40 grid (8,000 triangles)."""
+    import torch
+    import deformetrica_code_gb300 as g
+    from deformetrica_code_gb300.deformation import currents_match, varifold_match
+    from deformetrica_code_gb300.meshes import torus
+    ps, fs = torus(nu, nv, seed=5)
+    pt, ft = torus(nu, nv, seed=6)
+    F = fs.shape[0]
+    pairs = 3.0 * F * F
+    ctx = g.Context()
+    res = {"workload": f"two noisy tori, {F} triangles each, sigma {sigma}: distance + gradient w.r.t. all"
+                       f" {ps.shape[0]} template vertices", "pairs_per_call": pairs}
+    for kind, fn in (("currents", currents_match), ("varifold", varifold_match)):
+        fn(ps, fs, pt, ft, sigma, context=ctx)  # warm-up (buffers, order scratch)
+        torch.cuda.synchronize()
+        ts = []
+        ev0 = ctx.evaluated_pairs()
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            m, _ = fn(ps, fs, pt, ft, sigma, context=ctx)  # host arrays in and out, synchronous
+            ts.append(time.perf_counter() - t0)
+        ev = (ctx.evaluated_pairs() - ev0) / steps
+        sec = statistics.median(ts)
+        res[kind] = {"s_per_call": sec, "pairs_per_s": pairs / sec, "evaluated_pairs_per_call": ev,
+                     "match": m, "includes": "host->device copy of both meshes, device->host gradient"}
+    if cpu:
+        import oracle
+        from oracle import geometry as G
+        K = oracle.load("port")
+        cs, cfs = torus(100, 40, seed=5)
+        ct, cft = torus(100, 40, seed=6)
+        Fc = cfs.shape[0]
+        for kind in ("currents", "varifold"):
+            om = G.currents_match if kind == "currents" else G.varifold_match
+            og = G.currents_match_gradient if kind == "currents" else G.varifold_match_gradient
+            t0 = time.perf_counter()
+            om(K, sigma, cs, cfs, ct, cft)
+            og(K, sigma, cs, cfs, ct, cft)
+            dt = time.perf_counter() - t0
+            res[kind]["cpu_oracle"] = {"s_per_call": dt, "pairs_per_s": 3.0 * Fc * Fc / dt, "triangles": Fc,
+                                       "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+                                       "kind": "port (FP64)"}
+    return res
+
+
 def fp64_gpu_pairs(n: int, sigma: float):
     """The same fused forward+adjoint step in the FP64 mode (plain FP64 kernel sums) at N = M = n."""
     import torch
@@ -296,6 +349,83 @@ def fp64_gpu_pairs(n: int, sigma: float):
     torch.cuda.synchronize()
     ms = s.elapsed_time(e)
     return {"value": n * n / (ms / 1e3), "unit": UNIT, "N": n, "ms_per_step": ms}
+
+
+def sweep_mixture(ns, ds, sigmas, fp64_max_n: int = 100_000, sample: int = 4096):
+    """The large kernel-sum + adjoint sweep: fwd+adjoint at N = M for every (N, d, sigma) on the
+    8-Gaussian mixture (seed 3), FP32C in the default order; FP64 mode timed too for N <= fp64_max_n.
+    Errors per output against the FP64 oracle on `sample` rows against all partners. Prints one
+    JSON line per case."""
+    import torch
+    import deformetrica_code_gb300 as g
+    import oracle
+    port = oracle.load("port")
+    ctx = g.Context()
+    ctx.use_torch_stream()
+    c64 = g.Context(mode=g.GBK_MODE_F64)
+    c64.use_torch_stream()
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    stream = torch.cuda.current_stream()
+
+    def timed(c, d, n, X, Y, W, A, outs, sigma):
+        step = lambda: c.check(c.lib.gbk_forward_adjoint(c.h, d, d, p(X), n, p(Y), p(W), n, sigma, p(A),
+                                                         *[p(o) for o in outs]))
+        step()
+        torch.cuda.synchronize()
+        ev0, ms, k = c.evaluated_pairs(), [], 0
+        while k < 3 or (sum(ms) < 300.0 and k < 50):
+            s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s_.record(stream)
+            step()
+            e_.record(stream)
+            torch.cuda.synchronize()
+            ms.append(s_.elapsed_time(e_))
+            k += 1
+        return statistics.median(ms), (c.evaluated_pairs() - ev0) / k
+
+    for d in ds:
+        for n in ns:
+            x, y, w, a = make_workload(n, n, d=d, seed=3)
+            X, Y, W, A = (torch.from_numpy(t).cuda() for t in (x, y, w, a))
+            outs = [torch.empty_like(X) for _ in range(4)]
+            rng = np.random.default_rng(7)
+            it = np.sort(rng.choice(n, size=min(sample, n), replace=False))
+            jt = np.sort(rng.choice(n, size=min(sample, n), replace=False))
+            xs, ys = np.ascontiguousarray(x[it]), np.ascontiguousarray(y[jt])
+            for sigma in sigmas:
+                ms, ev = timed(ctx, d, n, X, Y, W, A, outs, sigma)
+                got = [o.cpu().numpy() for o in outs]
+                ref = {"v": port.convolve(xs, y, w, sigma), "gx": port.grad_alpha(xs, y, w, sigma, np.ascontiguousarray(a[it])),
+                       "gy": port.grad_alpha(ys, x, a, sigma, np.ascontiguousarray(w[jt])), "gw": port.convolve(ys, x, a, sigma)}
+                mag = {"v": port.convolve(xs, y, np.abs(w), sigma), "gw": port.convolve(ys, x, np.abs(a), sigma)}
+                rows = {"v": it, "gx": it, "gy": jt, "gw": jt}
+                errs = {}
+                for q, (key, r) in enumerate(ref.items()):
+                    gq = got[q][rows[key]]
+                    e = gq - r
+                    errs[key] = {"normwise": float(np.linalg.norm(e, axis=1).max() / np.linalg.norm(r, axis=1).max()),
+                                 "max_abs": float(np.abs(e).max())}
+                    if key in mag:
+                        errs[key]["condition_aware"] = float((np.abs(e) / np.maximum(mag[key], 1e-300)).max())
+                line = {"sweep": "mixture fwd+adjoint", "N": n, "d": d, "sigma": sigma, "ms": ms,
+                        "pairs_per_s": float(n) * n / (ms / 1e3), "evaluated_fraction": ev / (2.0 * n * n),
+                        "errors": errs, "error_sample": f"{len(it)} rows vs all {n} partners, FP64 oracle"}
+                if float(n) * n < 2.0 ** 30:  # below the default order's threshold: the spatial order too
+                    ctx.set_order(g.GBK_ORDER_SPATIAL)
+                    ms_s, ev_s = timed(ctx, d, n, X, Y, W, A, outs, sigma)
+                    ctx.set_order(g.GBK_ORDER_AUTO)
+                    got_s = [o.cpu().numpy() for o in outs]
+                    line["spatial_order"] = {
+                        "ms": ms_s, "pairs_per_s": float(n) * n / (ms_s / 1e3), "evaluated_fraction": ev_s / (2.0 * n * n),
+                        "normwise": {key: float(np.linalg.norm(got_s[q][rows[key]] - r, axis=1).max()
+                                                / np.linalg.norm(r, axis=1).max()) for q, (key, r) in enumerate(ref.items())}}
+                if n <= fp64_max_n:
+                    ms64, _ = timed(c64, d, n, X, Y, W, A, [torch.empty_like(X) for _ in range(4)], sigma)
+                    line["fp64_gpu"] = {"ms": ms64, "pairs_per_s": float(n) * n / (ms64 / 1e3)}
+                print(json.dumps(line), flush=True)
+            del X, Y, W, A, outs
+            torch.cuda.empty_cache()
+    return 0
 
 
 def run_reference_arm(args, rank, world):
@@ -351,6 +481,13 @@ def main():
     ap.add_argument("--reg-steps", type=int, default=10)
     ap.add_argument("--no-atlas", action="store_true")
     ap.add_argument("--atlas-steps", type=int, default=3)
+    ap.add_argument("--sweep", action="store_true",
+                    help="run the N x d x sigma sweep instead (one JSON line per case)")
+    ap.add_argument("--sweep-n", default="1e4,3e4,1e5,3e5,1e6")
+    ap.add_argument("--sweep-d", default="2,3")
+    ap.add_argument("--sweep-sigma", default="0.02,0.1,0.5")
+    ap.add_argument("--no-data-terms", action="store_true")
+    ap.add_argument("--data-term-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -360,6 +497,12 @@ def main():
 
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
+    if args.sweep:
+        import torch
+        torch.cuda.set_device(local_rank)
+        ns = [int(float(v)) for v in args.sweep_n.split(",")]
+        return sweep_mixture(ns, [int(v) for v in args.sweep_d.split(",")],
+                             [float(v) for v in args.sweep_sigma.split(",")])
 
     import torch
     import deformetrica_code_gb300 as g
@@ -397,6 +540,7 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    ev0 = ctx.evaluated_pairs()
 
     # ---- timed region: K steps, L2 flushed between steps (outside the events) ----
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -412,6 +556,7 @@ def main():
             evs[i][1].record(stream)
         torch.cuda.synchronize()
         launches = ctx.launch_count() - l0
+        ev1 = ctx.evaluated_pairs()
         step_ms = [s.elapsed_time(e) for s, e in evs]
         # dominant kernel: one fused pass, averaged over launches
         kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
@@ -421,6 +566,8 @@ def main():
             one_side()
             e.record(stream)
         torch.cuda.synchronize()
+    ev_pass = (ctx.evaluated_pairs() - ev1) / len(kev)  # pairs one fused pass evaluated
+    ev_step = (ev1 - ev0) / args.steps  # both passes of a step
     kernel_ms = statistics.mean(s.elapsed_time(e) for s, e in kev)
     ms = sum(step_ms) / len(step_ms)
     if dist:
@@ -460,7 +607,7 @@ def main():
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 2070.0
     peak_tflops = SMS * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
-    achieved = FLOPS_PER_PAIR_PASS * pairs / (kernel_ms / 1e3) / 1e12
+    achieved = FLOPS_PER_PAIR_PASS * ev_pass / (kernel_ms / 1e3) / 1e12  # evaluated pairs only
 
     if rank == 0:
         line = {
@@ -471,6 +618,9 @@ def main():
                                    " (8-Gaussian mixture, std 0.05, seed 3)",
                        "N": n, "M": m, "d": d, "dv": dv, "sigma": args.sigma,
                        "pairs_per_step": pairs, "l2": "flushed between steps (256 MiB write)",
+                       "order": "GBK_ORDER_AUTO: Morton-sorted targets and sources, source chunks whose"
+                                " kernel values are exactly zero skipped",
+                       "evaluated_pairs_per_step": ev_step, "evaluated_fraction": ev_step / (2.0 * pairs),
                        "parallelism": f"replicas{world}"},
             "gpu_launches": launches,
             "e2e": {"value": pairs * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -479,8 +629,9 @@ def main():
                          "frac": achieved / peak_tflops,
                          "traffic": TRAFFIC_1E6 if n == 1_000_000 else None,
                          "kernel": "pair_kernel<OpConvGradAlpha<3,3,true>, float2 lanes> (one fused pass)",
-                         "fp32_lane_frac": LANE_OPS_PER_PAIR_PASS * pairs / (kernel_ms / 1e3)
+                         "fp32_lane_frac": LANE_OPS_PER_PAIR_PASS * ev_pass / (kernel_ms / 1e3)
                          / (SMS * FP32_LANES * sm_mhz * 1e6),
+                         "evaluated_pairs_per_pass": ev_pass,
                          "kernel_ms": kernel_ms,
                          "peak_source": f"nominal FP32 {SMS} SMs x {FP32_LANES} lanes x 2 flops x median sampled SM clock {sm_mhz:.0f} MHz"},
             "clocks": clocks,
@@ -496,6 +647,8 @@ def main():
             line["shooting_adjoint"] = registration_bench(args.reg_steps, cpu=not args.no_cpu_baseline)
         if not args.no_atlas:
             line["atlas"] = atlas_bench(args.atlas_steps, cpu=not args.no_cpu_baseline)
+        if not args.no_data_terms:
+            line["data_terms"] = data_term_bench(args.data_term_steps, cpu=not args.no_cpu_baseline)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -212,40 +212,49 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
       case GBK_ORDER_SPATIAL: spatial = prune = true; break;
       case GBK_ORDER_SPATIAL_NOPRUNE: spatial = true; break;
       case GBK_ORDER_AUTO:
-        spatial = prune = a.nx >= 4096 && a.ny >= 4096 && (double)a.nx * (double)a.ny >= (double)(1L << 27);
+        spatial = prune = a.nx >= 4096 && a.ny >= 4096 && (double)a.nx * (double)a.ny >= (double)(1L << 30);
         break;
       default: break;
     }
   }
   if (spatial) {
+    // sorted copies of the source rows the op reads (y, the weight columns, the special Hessian's
+    // xi); OpAdjointCP's source extras share arrays with its targets, so it gathers while staging
+    SourceCopies want;
+    if (op != OP_ADJCP) {
+      want.na = op == OP_SPECIAL ? 3 : 2;
+      want.src[0] = a.y;
+      want.ld[0] = want.cols[0] = d;
+      want.src[1] = a.w;
+      want.ld[1] = a.w_ld;
+      want.cols[1] = op == OP_SPECIAL ? d : dv;
+      want.src[2] = a.sb;
+      want.ld[2] = a.sb_ld;
+      want.cols[2] = d;
+    }
+    SortedSet xs, ys;
     OrderView tv, sv;
-    if (int rc = order_targets(this, d, a.x, a.nx, e.block * e.r, a.sigma, &tv)) return rc;
-    if (int rc = order_sources(this, d, a.y, a.ny, e.tj, &sv)) return rc;
+    if (int rc = order_sort(this, d, a.x, a.nx, &xs)) return rc;
+    if (int rc = order_sort(this, d, a.y, a.ny, &ys)) return rc;
+    if (int rc = order_targets(this, d, xs, e.block * e.r, a.sigma, &tv)) return rc;
+    if (int rc = order_sources(this, d, a.y, ys, e.tj, want, &sv)) return rc;
+    launches += xs.launches + ys.launches;
     a.xperm = tv.perm;
     a.xtiles = tv.tiles;
     a.nxtiles = tv.ntiles;
-    a.xtile_bound = tv.tile_bound;
+    a.xtile_bound = tv.grid;
     a.ybox = prune ? sv.boxes : nullptr;
-    launches += kOrderTargetLaunches + kOrderSourceLaunches;
+    launches += tv.launches + sv.launches;
     if (op == OP_ADJCP) {
-      a.yperm = sv.perm;  // its source extras share arrays with the targets: gather while staging
+      a.yperm = sv.perm;
     } else {
-      // sorted copies of the source rows the op reads: y, the weight columns, the special
-      // Hessian's xi
-      const double *src[3] = {a.y, a.w, a.sb};
-      const int ld[3] = {d, a.w_ld, a.sb_ld};
-      const int cols[3] = {d, op == OP_SPECIAL ? d : dv, d};
-      double *dst[3];
-      const int na = op == OP_SPECIAL ? 3 : 2;
-      if (int rc = gather_sources(this, sv.perm, a.ny, src, ld, cols, na, dst)) return rc;
-      a.y = dst[0];
-      a.w = dst[1];
-      a.w_ld = cols[1];
+      a.y = sv.copies[0];
+      a.w = sv.copies[1];
+      a.w_ld = want.cols[1];
       if (op == OP_SPECIAL) {
-        a.sb = dst[2];
+        a.sb = sv.copies[2];
         a.sb_ld = d;
       }
-      launches += na;
     }
   }
   a.pair_count = pair_counter;
@@ -285,6 +294,7 @@ static double clamp_sigma(double s) { return s < 1e-10 ? 1e-10 : s; }  // Abstra
   do {                                                                     \
     if (!(ctx)) return GBK_ERR_ARG;                                        \
     (ctx)->err.clear();                                                    \
+    ++(ctx)->call_epoch;                                                   \
     if (cudaSetDevice((ctx)->device) != cudaSuccess) {                     \
       cudaGetLastError();                                                  \
       return (ctx)->fail(GBK_ERR_CUDA, "cudaSetDevice(%d)", (ctx)->device); \
@@ -314,6 +324,7 @@ static PairArgs base_args(long nx, long ny, double sigma) {
 // column in one output row) and row stride dv*ocol; out1 (gradient) accumulates over chunks.
 static int run_chunked(gbk_ctx *c, int op, int d, int dv, PairArgs a, const double *w,
                        const double *alpha, double *out0, int ocol, double *out1) {
+  gbk_ctx::OrderCacheScope cache(c);  // the chunks share x and y
   auto ch = column_chunks(d, dv);
   for (size_t q = 0; q < ch.size(); ++q) {
     int c0 = ch[q].first, cw = ch[q].second;
@@ -368,8 +379,9 @@ int gbk_create(int device, gbk_ctx **out) {
     return GBK_ERR_CUDA;
   }
   c->stream = c->own_stream;
-  if (cudaMalloc(&c->pair_counter, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMemset(c->pair_counter, 0, sizeof(unsigned long long)) != cudaSuccess) {
+  // pair counter and the spatial order's self-resetting ticket
+  if (cudaMalloc(&c->pair_counter, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(c->pair_counter, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     c->release();
     cudaStreamDestroy(c->own_stream);
@@ -377,6 +389,7 @@ int gbk_create(int device, gbk_ctx **out) {
     g_create_err = "device allocation of the pair counter failed";
     return GBK_ERR_ALLOC;
   }
+  c->order_ticket = reinterpret_cast<unsigned *>(c->pair_counter + 1);
   *out = c;
   return GBK_OK;
 }
@@ -687,6 +700,7 @@ int gbk_forward_adjoint(gbk_ctx *c, int d, int dv, const double *x, long nx, con
   double *dgy = io.out(gy, (size_t)ny * d, "gy");
   double *dgw = io.out(gw, (size_t)ny * dv, "gw");
   if (io.rc) return io.rc;
+  gbk_ctx::OrderCacheScope cache(c);  // both passes sort x and y: once each
   // target side: v = K w and gx (alpha-weighted gradient), one pass
   if (dvv || dgx) {
     PairArgs a = base_args(nx, ny, sigma);

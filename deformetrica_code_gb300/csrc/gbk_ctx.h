@@ -35,11 +35,25 @@ struct gbk_ctx {
   DevBuf reduce;              // FP64 reductions and small temporaries
   DevBuf tmp;                 // op temporaries (e.g. K w for the kernel norm)
   int order = 0;              // GBK_ORDER_* (0 = automatic)
-  DevBuf order_keep[2];       // spatial order of the targets / sources of the last launch
-  DevBuf order_tmp;           // Morton keys and bounding boxes
+  struct SortSlot {           // a point set in spatial order: perm, sorted keys, box
+    DevBuf buf;
+    const double *ptr = nullptr;
+    long n = 0;
+    int d = 0;
+    int key_bits = 0;
+    long long epoch = -1;     // call_epoch of the sort
+    long long last_use = 0;
+  };
+  SortSlot sort_slot[2];
+  long long sort_clock = 0;
+  long long call_epoch = 0;   // advanced by every API entry
+  bool order_cache = false;   // reuse sorts within the current API call (inputs unchanged)
+  DevBuf order_keep[2];       // target tiles / source chunk boxes of the last launch
+  DevBuf order_tmp;           // Morton keys and block boxes
   DevBuf order_cub;           // radix-sort scratch
   DevBuf order_src;           // source rows in sorted order
-  unsigned long long *pair_counter = nullptr;  // device: pairs evaluated by launch()
+  unsigned long long *pair_counter = nullptr;  // device: pairs evaluated by launch(), then a ticket
+  unsigned *order_ticket = nullptr;            // device: in the pair counter's allocation
 
   typedef std::tuple<int, int, int, int, int, int> TuneKey;  // op, mode, d, dv, log2 nx, log2 ny
   std::map<TuneKey, std::pair<int, int>> tune;                // -> (variant, nsplit)
@@ -53,6 +67,14 @@ struct gbk_ctx {
   int occupancy(const gbk::KernelEntry &e, int d);
   int choose_split(const gbk::KernelEntry &e, int d, long nx, long ny);
   int launch(int op, int d, int dv, gbk::PairArgs a);
+
+  // Lets launches of one API call reuse spatial sorts of the same (unchanged) rows.
+  struct OrderCacheScope {
+    gbk_ctx *c;
+    bool saved;
+    OrderCacheScope(gbk_ctx *ctx) : c(ctx), saved(ctx->order_cache) { c->order_cache = true; }
+    ~OrderCacheScope() { c->order_cache = saved; }
+  };
 
   // Holds the order policy at `o` for a scope (the registration and atlas steps use OFF).
   struct OrderScope {
@@ -73,11 +95,17 @@ struct gbk_ctx {
     fr(tmp);
     fr(order_keep[0]);
     fr(order_keep[1]);
+    for (auto &ss : sort_slot) {
+      fr(ss.buf);
+      ss.ptr = nullptr;
+      ss.epoch = -1;
+    }
     fr(order_tmp);
     fr(order_cub);
     fr(order_src);
     if (pair_counter) cudaFree(pair_counter);
     pair_counter = nullptr;
+    order_ticket = nullptr;
     for (auto &b : stage) fr(b);
   }
 };

@@ -14,30 +14,49 @@ struct gbk_ctx;
 
 namespace gbk {
 
+// Source arrays to copy into sorted order: src[0] must be the coordinates (d columns); row p of
+// copy k is row perm[p] of src[k] (its first cols[k] of ld[k] columns), rows cols[k] wide.
+struct SourceCopies {
+  int na = 0;
+  const double *src[3] = {nullptr, nullptr, nullptr};
+  int ld[3] = {0, 0, 0};
+  int cols[3] = {0, 0, 0};
+  double *dst[3] = {nullptr, nullptr, nullptr};  // filled by order_sources
+};
+
+// A point set in spatial order (device memory of the context, valid until the slot is reused).
+struct SortedSet {
+  const int *perm = nullptr;       // sorted position -> row
+  const unsigned *keys = nullptr;  // sorted keys, key_bits wide (Morton keys or their top bits)
+  const double *box = nullptr;     // lo[d], hi[d] of the set
+  long n = 0;
+  int key_bits = 0;
+  int launches = 0;  // own kernels launched by the sort (0 when an earlier sort was reused)
+};
+
 struct OrderView {
   const int *perm = nullptr;    // sorted position -> row
   const int2 *tiles = nullptr;  // targets: [begin, end) sorted positions per CTA
   const int *ntiles = nullptr;  // targets: number of tiles (device)
-  long tile_bound = 0;          // targets: upper bound on the number of tiles (grid size)
+  long tile_bound = 0;          // targets: upper bound on the number of tiles
+  long grid = 0;                // targets: CTAs to launch (they loop over the tiles)
   const double *boxes = nullptr;  // sources: lo[d], hi[d] per chunk of `chunk` sorted sources
+  double *copies[3] = {nullptr, nullptr, nullptr};  // sources: the sorted copies requested
+  int launches = 0;             // own kernels launched to build it
 };
 
-// Target order for CTAs of `tile` targets; `sigma` sets the coarse cell width (in units of the
-// FP32 coordinate scale) that no tile crosses. Kept in the context's target-order buffer until the
-// next order_targets call on its stream.
-int order_targets(gbk_ctx *c, int d, const double *x, long n, int tile, double sigma, OrderView *out);
+// Sorts n points (steps 1-3) into one of the context's two sort slots, or, inside an order-cache
+// scope of the context, returns the sort of the same rows made earlier in the same API call.
+int order_sort(gbk_ctx *c, int d, const double *x, long n, SortedSet *out);
 
-// Source order with one bounding box per `chunk` consecutive sorted sources (the source-order
-// buffer of the context).
-int order_sources(gbk_ctx *c, int d, const double *y, long n, int chunk, OrderView *out);
+// Target tiles of `tile` sorted targets for CTAs; `sigma` sets the coarse cell width (in units of
+// the FP32 coordinate scale) that no tile crosses. Kept in the context's tile buffer until the next
+// call on its stream.
+int order_targets(gbk_ctx *c, int d, const SortedSet &s, int tile, double sigma, OrderView *out);
 
-// Copies narrays source arrays (row p of dst[k] = row perm[p] of src[k], cols[k] of its ld[k]
-// columns) into the context's sorted-source buffer, one launch per array.
-int gather_sources(gbk_ctx *c, const int *perm, long n, const double *const *src, const int *ld, const int *cols,
-                   int narrays, double **dst);
-
-// Own kernels launched by one order_targets / order_sources call (the radix sort is extra).
-constexpr int kOrderTargetLaunches = 4;
-constexpr int kOrderSourceLaunches = 4;
+// One bounding box per `chunk` (a multiple of 32) consecutive sorted sources and the sorted copies
+// `copies` asks for (the context's source-box and sorted-source buffers).
+int order_sources(gbk_ctx *c, int d, const double *y, const SortedSet &s, int chunk, const SourceCopies &copies,
+                  OrderView *out);
 
 }  // namespace gbk

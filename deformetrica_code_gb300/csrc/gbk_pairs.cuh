@@ -57,8 +57,8 @@ struct PairArgs {
   // spatial order (all null: rows in caller order, fixed target tiles, every source chunk visited)
   const int *xperm;    // sorted target position -> target row
   const int2 *xtiles;  // per CTA: [begin, end) of sorted target positions
-  const int *nxtiles;  // number of valid xtiles entries (grid.x is the host bound xtile_bound)
-  long xtile_bound;
+  const int *nxtiles;  // number of valid xtiles entries
+  long xtile_bound;    // grid.x for a spatial order (CTAs loop over the tiles)
   const int *yperm;    // sorted source position -> source row
   const double *ybox;  // per TJ chunk of sorted sources: lo[D], hi[D]; null = no pruning
   double prune_d2;     // a source chunk whose box is farther than this (squared) from the CTA's
@@ -726,9 +726,15 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
   }
 }
 
+// Caller order: CTA x takes target tile x. Spatial order: the CTAs loop over the tiles the order
+// built (their count is known on the device only; the grid is sized for the usual count).
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
-  pair_block<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM>(a, (long)blockIdx.x, (int)blockIdx.y);
+  const long nt = a.xtiles ? (long)*a.nxtiles : (long)gridDim.x;
+  for (long t = blockIdx.x; t < nt; t += gridDim.x) {
+    if (t != (long)blockIdx.x) __syncthreads();  // the previous tile is done with shared memory
+    pair_block<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM>(a, t, (int)blockIdx.y);
+  }
 }
 
 // Batched form: CTA b works on item items[b] = (problem, target tile, source split) of the

@@ -51,7 +51,8 @@ enum {
 enum { GBK_MODE_F32C = 0, GBK_MODE_F64 = 1 };
 
 /* Order in which the kernel sums visit targets and sources (gbk_set_order).
- *  AUTO: SPATIAL for calls with nx, ny >= 4096 and nx * ny >= 2^27, OFF below.
+ *  AUTO: SPATIAL for calls with nx, ny >= 4096 and nx * ny >= 2^30, OFF below (where sorting
+ *    costs more than a few percent of the sum).
  *  OFF: rows in caller order, every (target, source) pair evaluated.
  *  SPATIAL: targets and sources sorted along a Morton curve on the device before the sum; each CTA
  *    takes a compact tile of targets (smaller FP32 coordinate rounding after centring) and skips

@@ -212,10 +212,22 @@ def test_auto_orders_large_calls_only(gb, ctx):
         k.Convolve(x)
         return ctx.launch_count() - n0
 
-    # the order adds 4 kernels per point set (box, box, keys, tiles or chunk boxes) and one gather
-    # per sorted source array (coordinates, weights)
-    assert launches(gb.GBK_ORDER_AUTO, 1000) == launches(gb.GBK_ORDER_OFF, 1000)
-    assert launches(gb.GBK_ORDER_AUTO, 12000) == launches(gb.GBK_ORDER_OFF, 12000) + 10
-    assert launches(gb.GBK_ORDER_SPATIAL, 1000) == launches(gb.GBK_ORDER_OFF, 1000) + 10
+    # the order adds, per point set, a box and a keys kernel and (up to 16384 points) a one-CTA sort
+    # (the device radix sort above that is counted as the library's), then one tiles kernel for the
+    # targets and one kernel for the source boxes and copies
+    assert launches(gb.GBK_ORDER_AUTO, 12000) == launches(gb.GBK_ORDER_OFF, 12000)
+    assert launches(gb.GBK_ORDER_AUTO, 40000) == launches(gb.GBK_ORDER_OFF, 40000) + 6
+    assert launches(gb.GBK_ORDER_SPATIAL, 1000) == launches(gb.GBK_ORDER_OFF, 1000) + 8
+    assert launches(gb.GBK_ORDER_SPATIAL, 20000) == launches(gb.GBK_ORDER_OFF, 20000) + 6
+
+    # forward + adjoint: x and y are sorted once each for both passes
+    def fa_launches(order, n):
+        k = kern(gb, ctx, 3, 0.1, rng.random((n, 3)), rng.standard_normal((n, 3)), gb.GBK_MODE_F32C, order)
+        x, al = rng.random((n, 3)), rng.standard_normal((n, 3))
+        n0 = ctx.launch_count()
+        k.ForwardAdjoint(x, al)
+        return ctx.launch_count() - n0
+
+    assert fa_launches(gb.GBK_ORDER_SPATIAL, 1000) == fa_launches(gb.GBK_ORDER_OFF, 1000) + 10
     with pytest.raises(gb.GBKError):
         ctx.set_order(7)

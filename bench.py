@@ -328,6 +328,48 @@ def data_term_bench(steps: int, cpu: bool = True, nu: int = 500, nv: int = 200, 
     return res
 
 
+def small_kernel_bench(n: int = 4096, sigma: float = 0.2, reps: int = 50, cpu: bool = True):
+    """Convolve and ConvolveGradient(X, alpha = X) at x, y = 4096 points uniform in [0,1]^3,
+    weights N(0,1), sigma 0.2 (the reference's CPU-runnable kernel case): per call through the
+    Python kernel object, device arrays (kernel) and host arrays (end to end), FP32C; the FP64
+    oracle on the CPU beside it."""
+    import torch
+    import deformetrica_code_gb300 as g
+    rng = np.random.default_rng(1)
+    x, y, w = rng.random((n, 3)), rng.random((n, 3)), rng.standard_normal((n, 3))
+    ctx = g.Context()
+    res = {"workload": f"x, y: {n} points uniform in [0,1]^3, w ~ N(0,1), sigma {sigma}; alpha = x for the gradient",
+           "pairs_per_call": float(n) * n}
+    dev = lambda a: torch.from_numpy(a).cuda()
+    for where, args in (("device", (dev(x), dev(y), dev(w))), ("host", (x, y, w))):
+        k = g.GB300ExactKernel(3, sigma, context=ctx)
+        X, Y, W = args
+        k.SetSources(Y)
+        k.SetWeights(W)
+        for name, fn in (("convolve", lambda: k.Convolve(X)), ("gradient_alpha", lambda: k.ConvolveGradient(X, X))):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / reps
+            res.setdefault(name, {})[where] = {"s_per_call": dt, "pairs_per_s": float(n) * n / dt}
+    if cpu:
+        import oracle
+        port = oracle.load("port")
+        for name, fn in (("convolve", lambda: port.convolve(x, y, w, sigma)),
+                         ("gradient_alpha", lambda: port.grad_alpha(x, y, w, sigma, x))):
+            t0 = time.perf_counter()
+            for _ in range(5):
+                fn()
+            dt = (time.perf_counter() - t0) / 5
+            res[name]["cpu_oracle"] = {"s_per_call": dt, "pairs_per_s": float(n) * n / dt, "kind": "port (FP64)",
+                                       "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))}
+    return res
+
+
 def fp64_gpu_pairs(n: int, sigma: float):
     """The same fused forward+adjoint step in the FP64 mode (plain FP64 kernel sums) at N = M = n."""
     import torch
@@ -487,6 +529,7 @@ def main():
     ap.add_argument("--sweep-d", default="2,3")
     ap.add_argument("--sweep-sigma", default="0.02,0.1,0.5")
     ap.add_argument("--no-data-terms", action="store_true")
+    ap.add_argument("--no-small", action="store_true", help="skip the 4096-point kernel-sum case")
     ap.add_argument("--data-term-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
@@ -571,9 +614,8 @@ def main():
     kernel_ms = statistics.mean(s.elapsed_time(e) for s, e in kev)
     ms = sum(step_ms) / len(step_ms)
     if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+        from deformetrica_code_gb300.distributed import max_over_ranks
+        ms = max_over_ranks(ms)
         dist.barrier()
 
     pairs = float(n) * m
@@ -649,6 +691,8 @@ def main():
             line["atlas"] = atlas_bench(args.atlas_steps, cpu=not args.no_cpu_baseline)
         if not args.no_data_terms:
             line["data_terms"] = data_term_bench(args.data_term_steps, cpu=not args.no_cpu_baseline)
+        if not args.no_small:
+            line["small_kernel_sum"] = small_kernel_bench(cpu=not args.no_cpu_baseline)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -5,7 +5,10 @@
 // source loop): the hot (d, dv) = (3, 3) and (2, 2) shapes carry several variants for the
 // autotuner; other shapes carry the default one. Fused pass at N = M = 1e6 on GB300: default
 // 564 ms; 2-way unroll 578 ms; 4 targets per thread at 2 CTAs/SM 603 ms; scalar FP32 lanes 568 ms;
-// compensation terms in shared memory 605-636 ms (removed). FP64 uses one target per thread.
+// compensation terms in shared memory 605-636 ms (removed). Longer plain-FP32 runs before each
+// compensated fold are faster but less accurate (spatial order, 1e6: MERGE 64 534 ms, normwise
+// 1.9e-7; 128: 524 ms, 2.7e-7; 256: 519 ms, 4.0e-7), so every variant keeps runs of 64 and the
+// autotuner only trades speed for speed. FP64 uses one target per thread.
 #include "gbk_dispatch.h"
 
 namespace gbk {

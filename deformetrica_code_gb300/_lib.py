@@ -87,6 +87,7 @@ SIGNATURES = {
     "gbk_registration_set_graph": (_I, [_P, _I]),
     "gbk_registration_trajectories": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "gbk_registration_graph_launches": (ctypes.c_longlong, [_P]),
+    "gbk_registration_optimize": (_I, [_P, _P, _P, _I, _I, _D, _I, _D, _D, _D, _I, _P, _P, _P, _P, _P, _P, _P]),
     "gbk_registration_destroy": (None, [_P]),
     "gbk_atlas_create": (_I, [_P, _L, _P, _L, _P, _L, _P, _I, _P, _P, _P, _P, _I, _D, _D, _D, _I, _I,
                               ctypes.POINTER(_P)]),

@@ -144,6 +144,31 @@ class Registration:
     def graph_launches(self) -> int:
         return int(self.ctx.lib.gbk_registration_graph_launches(self.h))
 
+    STOP = {0: "max_iterations", 1: "line_search", 2: "tolerance"}
+
+    def optimize(self, cp, mom, max_iterations: int, initial_step: float = 1e-3, optimize_cp: bool = True,
+                 max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2, tolerance: float = 1e-4,
+                 nb_iter_freeze: int = 3):
+        """The reference's FastGradientAscent over control points and momenta, on the device
+        (gbk_registration_optimize). Returns a dict: cp, mom (final fixed effects), aux_cp, aux_mom,
+        grad_cp, grad_mom (extrapolated point and gradient there), history ([data, regularity] per
+        iteration), step, tau, freeze_counter, grad_sq_norms, evaluations, stopped."""
+        cp = np.array(cp, dtype=np.float64)
+        mom = np.array(mom, dtype=np.float64)
+        hist = np.zeros((max_iterations + 1, 2))
+        info = np.zeros(8)
+        aux_cp, aux_mom, g_cp, g_mom = (np.zeros_like(cp) for _ in range(4))
+        iters = ctypes.c_int(0)
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_registration_optimize(
+            self.h, c(cp), c(mom), int(optimize_cp), int(max_iterations), float(initial_step), int(max_line_search),
+            float(shrink), float(expand), float(tolerance), int(nb_iter_freeze), c(hist), ctypes.byref(iters), c(info),
+            c(aux_cp), c(aux_mom), c(g_cp), c(g_mom)))
+        return {"cp": cp, "mom": mom, "aux_cp": aux_cp, "aux_mom": aux_mom, "grad_cp": g_cp, "grad_mom": g_mom,
+                "history": hist[:iters.value], "step": info[:2] if optimize_cp else info[1:2], "tau": float(info[2]),
+                "freeze_counter": int(info[3]), "grad_sq_norms": info[4:6] if optimize_cp else info[5:6],
+                "evaluations": int(info[6]), "stopped": self.STOP[int(info[7])]}
+
     def trajectories(self):
         shp_c = (self.T, self.ncp, 3)
         shp_v = (self.T, self.nv, 3)

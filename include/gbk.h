@@ -257,6 +257,23 @@ int gbk_registration_trajectories(gbk_registration *reg, double *pos, double *mo
                                   double *theta, double *xi_pos, double *xi_mom);
 /* Kernels in one captured iteration (0 before the capture). */
 long long gbk_registration_graph_launches(const gbk_registration *reg);
+/* FastGradientAscent::Update (FastGradientAscent.cxx:48-300) of this registration: Nesterov-
+ * accelerated gradient ascent with one step size per parameter group (control points when
+ * optimize_cp, then momenta), multivariate line search, step expansion after nb_iter_freeze
+ * accepted first trials, stop on |dL| < tolerance |L_0 - L| (reference defaults: 10 line-search
+ * iterations, shrink 0.5, expand 1.2, tolerance 1e-4, nb_iter_freeze 3). Parameters, trials and
+ * gradients stay on the device; every evaluation replays the iteration graph. cp and mom (ncp x 3,
+ * host or device) are the start point and receive the final fixed effects; history receives one
+ * [data, regularity] row per accepted iteration (at most max_iterations + 1 rows, *iterations of
+ * them); info (8 doubles, optional): final step sizes (control points, momenta), tau, the freeze
+ * counter, the two squared gradient norms, the number of evaluations and the stop reason (0 max
+ * iterations, 1 line search exhausted, 2 tolerance). aux_cp / aux_mom / grad_cp / grad_mom
+ * (optional) receive the extrapolated point and the gradient there, as the reference's state. */
+int gbk_registration_optimize(gbk_registration *reg, double *cp, double *mom, int optimize_cp, int max_iterations,
+                              double initial_step, int max_line_search, double shrink, double expand,
+                              double tolerance, int nb_iter_freeze, double *history, int *iterations,
+                              double *info, double *aux_cp, double *aux_mom, double *grad_cp,
+                              double *grad_mom);
 void gbk_registration_destroy(gbk_registration *reg);
 
 /* The same <w, K w> for callers that cannot allocate device memory when they need it (a loop

@@ -1,0 +1,141 @@
+"""Restatement of the reference's FastGradientAscent estimator (test infrastructure only: the
+oracle for the library's device-resident registration optimiser).
+
+Follows src/core/estimators/FastGradientAscent.cxx:48-300 (Update: Nesterov-accelerated gradient
+ascent with a per-parameter-group step size, multivariate line search, step expansion after
+m_NbIterFreeze accepted first trials, stop on the relative log-likelihood change) and :306-335
+(GradientAscentStep). Defaults are the reference's: FastGradientAscent.cxx:22 (NbIterFreeze 3,
+multivariate line search on) and SparseDiffeoParameters.cxx:75-82 (10 line-search iterations,
+expand 1.2, shrink 0.5, tolerance 1e-4).
+
+`evaluate(params, need_grad)` returns (terms, grads, grad_sq_norms): terms = [data, regularity]
+log-likelihood terms at `params` (a list of arrays, one per parameter group, in the reference's
+order: population effects alphabetically, then individual ones), and, when need_grad, the
+gradient of each group and the squared norm the reference weights the step with
+(DeterministicAtlas.cxx:230-234).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: int,
+                         max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2,
+                         tolerance: float = 1e-4, nb_iter_freeze: int = 3, multivariate: bool = True):
+    fixed = [np.array(p, dtype=np.float64) for p in params]
+    aux = [p.copy() for p in fixed]
+    history = [None] * (max_iterations + 1)
+    terms0, grads, sq = evaluate(aux, True)
+    history[0] = np.asarray(terms0, dtype=np.float64)
+    lsq_ref = float(np.sum(history[0]))
+    n = len(fixed)
+    step = np.full(n, float(initial_step))
+    tau = 1.0
+    freeze = 1
+    evaluations = 1
+    it = 1
+    stopped = "max_iterations"
+
+    def ascent(local_step):  # GradientAscentStep, :306-335
+        return [aux[k] + grads[k] * local_step[k] for k in range(n)]
+
+    while it < max_iterations + 1:
+        found = False
+        new = None
+        new_terms = None
+        for li in range(max_line_search):
+            cand = ascent(step)
+            t, _, _ = evaluate(cand, False)
+            evaluations += 1
+            q = float(np.sum(t)) - lsq_ref - float(np.dot(sq, step)) * shrink
+            if q >= 0:
+                found, new, new_terms = True, cand, np.asarray(t, dtype=np.float64)
+                if li == 0:
+                    freeze += 1
+                break
+            elif n > 1 and multivariate:
+                freeze = 1
+                step = step * shrink
+                props, qs, ts = [], np.empty(n), []
+                for k in range(n):
+                    local = step.copy()
+                    local[k] /= shrink
+                    ck = ascent(local)
+                    tk, _, _ = evaluate(ck, False)
+                    evaluations += 1
+                    props.append(ck)
+                    ts.append(np.asarray(tk, dtype=np.float64))
+                    qs[k] = float(np.sum(tk)) - lsq_ref - float(np.dot(sq, local)) * shrink
+                idx = int(np.argmax(qs))
+                if qs[idx] >= 0:
+                    new, new_terms = props[idx], ts[idx]
+                    step[idx] /= shrink
+                    found = True
+                    break
+            else:
+                freeze = 1
+                step = step * shrink
+        if not found:
+            stopped = "line_search"
+            break
+        history[it] = new_terms
+        tau_next = (1.0 + math.sqrt(1.0 + 4.0 * tau * tau)) / 2.0
+        if freeze > nb_iter_freeze:
+            step = step * expand
+            tau_next = (1.0 + math.sqrt(1.0 + 4.0 * tau * tau / expand)) / 2.0
+        tau_scale = (tau - 1.0) / tau_next
+        aux = [new[k] + (new[k] - fixed[k]) * tau_scale for k in range(n)]
+        fixed = new
+        tau = tau_next
+        t_aux, grads, sq = evaluate(aux, True)
+        evaluations += 1
+        lsq_ref = float(np.sum(t_aux))
+        d_cur = float(np.sum(history[it - 1]) - np.sum(history[it]))
+        d_ref = float(np.sum(history[0]) - np.sum(history[it]))
+        if abs(d_cur) < tolerance * abs(d_ref):
+            stopped = "tolerance"
+            it += 1
+            break
+        it += 1
+    done = [h for h in history if h is not None]
+    return {"params": fixed, "aux": aux, "grads": grads, "grad_sq_norms": np.asarray(sq, dtype=np.float64),
+            "step": step, "tau": tau, "freeze_counter": freeze, "iter": it, "history": np.stack(done),
+            "evaluations": evaluations, "stopped": stopped}
+
+
+def registration_evaluator(K, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T: int, sigma_def: float,
+                           sigma_data: float, data_sigma2: float, kind: str = "currents", heun: bool = True):
+    """evaluate() of one landmark registration with control points and momenta optimised (the
+    reference's DeterministicAtlas with one subject and a frozen template): parameter groups
+    [ControlPoints, Momenta]."""
+    from .deformation import registration
+
+    def evaluate(params, need_grad):
+        cp, mom = params
+        L, g_cp, g_mom, info = registration(K, cp, mom, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T, sigma_def,
+                                            sigma_data, data_sigma2, kind=kind, heun=heun)
+        data = -0.5 * info["match"] / data_sigma2
+        terms = [data, L - data]
+        if not need_grad:
+            return terms, None, None
+        return terms, [g_cp, g_mom], np.array([float(np.sum(g_cp * g_cp)), float(np.sum(g_mom * g_mom))])
+
+    return evaluate
+
+
+def initial_control_points(points, spacing: float):
+    """Regular grid over a bounding box (AbstractAtlas.cxx:240-330 without the image criterion):
+    per axis, spacing apart, centred so the leftover extent is split evenly; x outermost."""
+    lo, hi = np.min(points, axis=0), np.max(points, axis=0)
+    axes = []
+    for d in range(points.shape[1]):
+        off = 0.5 * (hi[d] - lo[d] - spacing * math.floor((hi[d] - lo[d]) / spacing))
+        v, x = [], lo[d] + off
+        while x <= hi[d]:
+            v.append(x)
+            x += spacing
+        axes.append(v)
+    mesh = np.meshgrid(*axes, indexing="ij")
+    return np.stack([m.ravel() for m in mesh], axis=1)

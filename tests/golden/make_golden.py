@@ -16,6 +16,11 @@ sources by oracle/build_ref.sh) and records its outputs:
 * ``parallel_transport.npz`` -- the inputs and ground truth of
   tests/unit_tests/parallel-transport/TestParallelTransport.cxx:19-85 (read from the reference's
   DLM text files), which pin the shooting oracle (oracle/deformation.py).
+* ``amygdala_registration.npz`` -- functional test 6 of the reference
+  (tests/functional_tests/configure.ini [Test6], registration/landmark/3d/amygdalas): the two
+  meshes as the reference reads them (VTK float points, triangles re-oriented by its normals
+  filter), the initial control points, and the final FastGradientAscent state the reference
+  stored in deformetrica-state.bin (decoded by deformetrica_code_gb300.formats).
 
 The fixtures are small (tens to hundreds of KB) and are committed; the GPU machine never needs the
 reference tree.
@@ -117,7 +122,33 @@ def main(ref_root: str = "/root/reference"):
         kernel_width=np.array(15.0),
         number_of_time_points=np.array(30),
     )
+    # 4. functional test 6: landmark registration of two amygdala meshes
+    amygdala_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
+
+
+def amygdala_fixture(ref_root: str = "/root/reference"):
+    """Inputs and expected final state of the reference's amygdala registration (model.xml:
+    OrientedSurfaceMesh, data-sigma 0.1, object and deformation kernel width 10, 10 time points;
+    optimization_parameters.xml: FastGradientAscent, initial step 1e-7, 10 iterations)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "formats", os.path.join(os.path.dirname(os.path.dirname(HERE)), "deformetrica_code_gb300", "formats.py"))
+    F = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(F)
+    from oracle.optimize import initial_control_points
+    d = os.path.join(ref_root, "tests", "functional_tests", "registration", "landmark", "3d", "amygdalas")
+    tp, tf_raw = F.read_vtk_polydata(os.path.join(d, "data", "decimatedAmygdala1.vtk"))
+    gp, gf_raw = F.read_vtk_polydata(os.path.join(d, "data", "decimatedAmygdala2.vtk"))
+    tf, gf = F.reorient_like_reader(tp, tf_raw), F.reorient_like_reader(gp, gf_raw)
+    st = F.read_deformation_state(os.path.join(d, "deformetrica-state.bin"))
+    cp0 = initial_control_points(tp[tf].mean(axis=1), 10.0)  # the template's triangle centres' box
+    np.savez_compressed(
+        os.path.join(HERE, "amygdala_registration.npz"),
+        tmpl_pts=tp, tmpl_tris_raw=tf_raw, tmpl_tris=tf, tgt_pts=gp, tgt_tris_raw=gf_raw, tgt_tris=gf, cp0=cp0,
+        kernel_width=np.array(10.0), data_kernel_width=np.array(10.0), data_sigma2=np.array(0.01),
+        number_of_time_points=np.array(10), initial_step=np.array(1e-7), max_iterations=np.array(10),
+        **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
 if __name__ == "__main__":

@@ -1,0 +1,96 @@
+"""End-to-end parity with the reference's functional test 6 (tests/functional_tests/configure.ini
+[Test6]: registration/landmark/3d/amygdalas -- an OrientedSurfaceMesh registration, exact Gaussian
+kernels of width 10, data-sigma 0.1, 10 time points, FastGradientAscent from step 1e-7 for 10
+iterations), CPU part: the on-disk formats and the FP64 oracle of the whole estimation.
+
+The expected values are the final optimiser state the reference stored in
+deformetrica-state.bin, decoded into tests/golden/amygdala_registration.npz by
+tests/golden/make_golden.py. The reference compares states with an absolute tolerance of 1e-8
+(Tolerance.hpp), which at log-likelihoods of 5e5 only its own summation order meets; the
+restatements here are held to relative bounds instead.
+
+The reference run used the standard (not improved) Euler scheme for the landmark flow and its
+adjoint: estimate_atlas.cxx:247 switches to it unless SparseDiffeoParameters::m_UseImprovedEuler
+is set, a member the parameter constructor never initialises and the test's XML never sets. The
+oracle reproduces the stored state with the standard scheme only (with Heun the log-likelihood
+history is off by 0.3 %).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN
+
+
+@pytest.fixture(scope="module")
+def fx():
+    return dict(np.load(os.path.join(GOLDEN, "amygdala_registration.npz")))
+
+
+def test_reorientation_is_consistent_and_inward(fx):
+    from deformetrica_code_gb300.formats import reorient_like_reader
+    for pts, raw, tris in ((fx["tmpl_pts"], fx["tmpl_tris_raw"], fx["tmpl_tris"]),
+                           (fx["tgt_pts"], fx["tgt_tris_raw"], fx["tgt_tris"])):
+        got = reorient_like_reader(pts, raw)
+        np.testing.assert_array_equal(got, tris)
+        # every triangle keeps its vertex set
+        np.testing.assert_array_equal(np.sort(got, axis=1), np.sort(raw, axis=1))
+        # consistent: every interior edge is run in opposite directions by its two triangles
+        directed = {}
+        for t in got:
+            for j in range(3):
+                e = (int(t[j]), int(t[(j + 1) % 3]))
+                assert e not in directed
+                directed[e] = True
+        # flipped outward orientation: n = (p1 - p0) x (p2 - p0) points inward, so the signed
+        # volume is negative for these closed surfaces
+        p0, p1, p2 = pts[got[:, 0]], pts[got[:, 1]], pts[got[:, 2]]
+        vol = np.sum(np.einsum("ij,ij->i", p0, np.cross(p1, p2))) / 6.0
+        assert vol < 0
+
+
+def test_readers_match_fixture_when_reference_present(fx):
+    d = "/root/reference/tests/functional_tests/registration/landmark/3d/amygdalas"
+    if not os.path.isdir(d):
+        pytest.skip("reference tree not present")
+    from deformetrica_code_gb300.formats import read_deformation_state, read_vtk_polydata
+    p, f = read_vtk_polydata(os.path.join(d, "data", "decimatedAmygdala1.vtk"))
+    np.testing.assert_array_equal(p, fx["tmpl_pts"])
+    np.testing.assert_array_equal(f, fx["tmpl_tris_raw"])
+    st = read_deformation_state(os.path.join(d, "deformetrica-state.bin"))
+    np.testing.assert_array_equal(st["history"], fx["state_history"])
+    np.testing.assert_array_equal(st["momenta"], fx["state_momenta"])
+    # the stored template is the read one
+    np.testing.assert_array_equal(st["template"], fx["tmpl_pts"])
+
+
+def test_initial_control_points_are_the_reference_grid(fx):
+    from oracle.optimize import initial_control_points
+    cp0 = initial_control_points(fx["tmpl_pts"][fx["tmpl_tris"]].mean(axis=1), 10.0)
+    np.testing.assert_array_equal(cp0, fx["cp0"])
+    assert cp0.shape == (8, 3)
+    # the final control points moved less than 1e-2 from the grid (steps of ~1e-7 x 1e3)
+    assert np.abs(fx["state_control_points"] - cp0).max() < 1e-2
+
+
+def test_oracle_reproduces_reference_state(fx):
+    import oracle
+    from oracle.optimize import fast_gradient_ascent, registration_evaluator
+    K = oracle.load("port")
+    ev = registration_evaluator(K, fx["tmpl_pts"], fx["tmpl_tris"], fx["tgt_pts"], fx["tgt_tris"], 10, 10.0, 10.0,
+                                0.01, "currents", heun=False)
+    cp0 = fx["cp0"]
+    r = fast_gradient_ascent(ev, [cp0, np.zeros_like(cp0)], 1e-7, 10)
+    h, href = r["history"], fx["state_history"]
+    assert h.shape == href.shape
+    assert np.all(np.abs(h - href) <= 1e-12 * np.abs(href).max() + 1e-7 * np.abs(href))
+    assert r["iter"] == int(fx["state_iter"]) and r["freeze_counter"] == int(fx["state_freeze_counter"])
+    assert abs(r["tau"] - float(fx["state_tau"])) <= 1e-14
+    np.testing.assert_allclose(r["step"], fx["state_step"], rtol=1e-14)
+    np.testing.assert_allclose(r["grad_sq_norms"], fx["state_grad_sq_norms"], rtol=1e-10)
+    for got, key in ((r["params"][0], "control_points"), (r["params"][1], "momenta"), (r["aux"][0], "aux_control_points"),
+                     (r["aux"][1], "aux_momenta"), (r["grads"][0], "grad_control_points"),
+                     (r["grads"][1], "grad_momenta")):
+        ref = fx["state_" + key]
+        assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max(), key

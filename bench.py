@@ -328,6 +328,60 @@ def data_term_bench(steps: int, cpu: bool = True, nu: int = 500, nv: int = 200, 
     return res
 
 
+def optimizer_bench(cpu: bool = True, reg_iters: int = 10):
+    """The device-resident FastGradientAscent (gbk_registration_optimize): (1) the reference's
+    functional test 6, amygdala landmark registration (8 control points, 75/79-vertex meshes, 10
+    iterations from step 1e-7, fixture tests/golden/amygdala_registration.npz) in FP64 and FP32C
+    against the FP64 oracle of the same estimation on the CPU; (2) `reg_iters` iterations on the
+    1000-control-point, 10,242-vertex registration workload (FP32C), per iteration and per
+    evaluation."""
+    import deformetrica_code_gb300 as g
+    from deformetrica_code_gb300.deformation import Registration
+    fx = dict(np.load(os.path.join(ROOT, "tests", "golden", "amygdala_registration.npz")))
+    res = {"amygdala": {"workload": "reference functional test 6: 8 CP, 75/79-vertex currents registration, "
+                                    "sigma 10, data-sigma 0.1, T = 10, 10 FastGradientAscent iterations"}}
+    for name, mode in (("f64", g.GBK_MODE_F64), ("f32c", g.GBK_MODE_F32C)):
+        ctx = g.Context(mode=mode)
+        reg = Registration(8, fx["tmpl_pts"], fx["tmpl_tris"], fx["tgt_pts"], fx["tgt_tris"], T=10, sigma_def=10.0,
+                           sigma_data=10.0, data_sigma2=0.01, kind="currents", heun=False, context=ctx)
+        reg.optimize(fx["cp0"], np.zeros_like(fx["cp0"]), 10, 1e-7)  # warm-up (graph capture)
+        t0 = time.perf_counter()
+        r = reg.optimize(fx["cp0"], np.zeros_like(fx["cp0"]), 10, 1e-7)
+        dt = time.perf_counter() - t0
+        href = fx["state_history"]
+        res["amygdala"][name] = {"s_total": dt, "evaluations": r["evaluations"],
+                                 "history_max_rel_err_vs_reference_state": float(
+                                     np.abs(r["history"] - href).max() / np.abs(href).max()),
+                                 "momenta_max_rel_err_vs_reference_state": float(
+                                     np.abs(r["mom"] - fx["state_momenta"]).max() / np.abs(fx["state_momenta"]).max())}
+        reg.close()
+    if cpu:
+        import oracle
+        from oracle.optimize import fast_gradient_ascent, registration_evaluator
+        K = oracle.load("port")
+        ev = registration_evaluator(K, fx["tmpl_pts"], fx["tmpl_tris"], fx["tgt_pts"], fx["tgt_tris"], 10, 10.0, 10.0,
+                                    0.01, "currents", heun=False)
+        t0 = time.perf_counter()
+        r = fast_gradient_ascent(ev, [fx["cp0"], np.zeros_like(fx["cp0"])], 1e-7, 10)
+        res["amygdala"]["cpu_oracle"] = {"s_total": time.perf_counter() - t0, "evaluations": r["evaluations"],
+                                         "kind": "port (FP64)"}
+    cp, mom, tp, tf, gp, gf, kw = registration_workload()
+    ctx = g.Context()
+    reg = Registration(cp.shape[0], tp, tf, gp, gf, kind="currents", context=ctx, **kw)
+    reg.optimize(cp, mom, 2, 1e-4)  # warm-up
+    t0 = time.perf_counter()
+    r = reg.optimize(cp, mom, reg_iters, 1e-4)
+    dt = time.perf_counter() - t0
+    reg.close()
+    res["registration_1000cp"] = {"workload": "1000 CP x 10242-vertex icosphere, T=11, sigma_def 0.15, currents "
+                                              f"sigma 0.1, {reg_iters} FastGradientAscent iterations from step 1e-4, FP32C",
+                                  "s_total": dt, "s_per_iteration": dt / max(1, len(r["history"]) - 1),
+                                  "evaluations": r["evaluations"], "s_per_evaluation": dt / max(1, r["evaluations"]),
+                                  "loglik_first_last": [float(r["history"][0].sum()), float(r["history"][-1].sum())],
+                                  "stopped": r["stopped"]}
+    return res
+
+
 def small_kernel_bench(n: int = 4096, sigma: float = 0.2, reps: int = 50, cpu: bool = True):
     """Convolve and ConvolveGradient(X, alpha = X) at x, y = 4096 points uniform in [0,1]^3,
     weights N(0,1), sigma 0.2 (the reference's CPU-runnable kernel case): per call through the
@@ -530,6 +584,7 @@ def main():
     ap.add_argument("--sweep-sigma", default="0.02,0.1,0.5")
     ap.add_argument("--no-data-terms", action="store_true")
     ap.add_argument("--no-small", action="store_true", help="skip the 4096-point kernel-sum case")
+    ap.add_argument("--no-optimizer", action="store_true", help="skip the registration optimiser runs")
     ap.add_argument("--data-term-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
@@ -693,6 +748,8 @@ def main():
             line["data_terms"] = data_term_bench(args.data_term_steps, cpu=not args.no_cpu_baseline)
         if not args.no_small:
             line["small_kernel_sum"] = small_kernel_bench(cpu=not args.no_cpu_baseline)
+        if not args.no_optimizer:
+            line["optimizer"] = optimizer_bench(cpu=not args.no_cpu_baseline)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

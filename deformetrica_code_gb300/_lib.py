@@ -81,6 +81,8 @@ SIGNATURES = {
     "gbk_adjoint_diffeo": (_I, [_P, _I, _L, _P, _P, _I, _D, _L, _P, _P, _I, _P, _P]),
     "gbk_currents_match": (_I, [_P, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
     "gbk_varifold_match": (_I, [_P, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
+    "gbk_curve_currents_match": (_I, [_P, _I, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
+    "gbk_curve_varifold_match": (_I, [_P, _I, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
     "gbk_registration_create": (_I, [_P, _I, _L, _L, _P, _L, _P, _L, _P, _L, _P, _I, _D, _D, _D, _I, _I,
                                      ctypes.POINTER(_P)]),
     "gbk_registration_step": (_I, [_P, _P, _P, _P, _P, _P]),

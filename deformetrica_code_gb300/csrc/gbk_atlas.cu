@@ -700,7 +700,7 @@ int gbk_atlas_create(gbk_ctx *c, long ncp, const double *cp, long nv, const doub
     foff += nf_t[s];
   }
   std::vector<int> ptr, fc;
-  if (!rc) build_csr(nv, nf, th.data(), ptr, fc);
+  if (!rc) build_csr(nv, nf, 3, th.data(), ptr, fc);
   const long n = ncp * 3, m = nv * 3, rows3 = a->rows * 3;
   const size_t S = nsub, TT = T;
   struct {

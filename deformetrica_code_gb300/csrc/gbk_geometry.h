@@ -10,8 +10,10 @@
 namespace gbk {
 
 struct SurfaceTerm {
-  int kind = 0;  // 0 currents (OrientedSurfaceMesh), 1 varifold (NonOrientedSurfaceMesh)
-  int dw = 3;    // face weight columns: 3 (normals) or 6 (normal tensors)
+  int kind = 0;  // 0 currents (OrientedSurfaceMesh / OrientedPolyLine), 1 varifold (NonOriented...)
+  int d = 3;     // dimension
+  int cell = 3;  // vertices per cell: 3 triangles (d = 3), 2 segments (d = 2 or 3)
+  int dw = 3;    // cell weight columns: d (normals, tangents) or d(d+1)/2 (their tensors)
   double sigma = 1.0;
   long nv = 0, nf = 0, nv_t = 0, nf_t = 0;
   int *tris = nullptr, *tris_t = nullptr, *csr_ptr = nullptr, *csr_fc = nullptr;
@@ -23,14 +25,14 @@ struct SurfaceTerm {
   double *scal = nullptr;  // [0] |T|^2, [1] |S|^2, [2] <S,T>
   std::vector<void *> owned;
 
-  int init(gbk_ctx *c, int kind, double sigma, long nv, long nf, const int *tris_host, long nv_t,
-           long nf_t, const int *tris_t_host);
+  int init(gbk_ctx *c, int kind, int d, int cell, double sigma, long nv, long nf, const int *cells_host,
+           long nv_t, long nf_t, const int *cells_t_host);
   int set_target(gbk_ctx *c, const double *pts_t);
   int evaluate(gbk_ctx *c, const double *pts_s, double *match_dev, double *grad_dev, double scale,
                int accumulate);
   void release();
 };
 
-void build_csr(long nv, long nf, const int *tris, std::vector<int> &ptr, std::vector<int> &fc);
+void build_csr(long nv, long nf, int cell, const int *cells, std::vector<int> &ptr, std::vector<int> &fc);
 
 }  // namespace gbk

@@ -1,5 +1,5 @@
-// One registration iteration of a subject of DeterministicAtlas with a frozen template, on the
-// device, replayed from a CUDA graph.
+// One registration iteration of a subject of DeterministicAtlas with a frozen template (a triangle
+// mesh in 3-D or a polyline in 2-D / 3-D), on the device, replayed from a CUDA graph.
 //
 // Log-likelihood (DeterministicAtlas.cxx:99-154) L = -0.5 match / data_sigma2 - 0.5 <K p, p>
 // and its gradient (AbstractAtlas.cxx:559-613, DeterministicAtlas.cxx:246-280):
@@ -143,10 +143,13 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   *out = nullptr;
   c->err.clear();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
-  if (d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "surface registration needs d = 3");
+  if (data_kind < 0 || data_kind > 3)
+    return c->fail(GBK_ERR_ARG, "data_kind must be 0/1 (surface currents/varifold) or 2/3 (curve currents/varifold)");
+  const int cell = data_kind < 2 ? 3 : 2;
+  if (cell == 3 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "surface registration needs d = 3");
+  if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d not supported", d);
   if (ncp <= 0 || nv <= 0 || nf <= 0 || nv_t <= 0 || nf_t <= 0 || T < 2)
     return c->fail(GBK_ERR_ARG, "bad sizes");
-  if (data_kind != 0 && data_kind != 1) return c->fail(GBK_ERR_ARG, "data_kind must be 0 (currents) or 1 (varifold)");
   if (!(data_sigma2 > 0)) return c->fail(GBK_ERR_ARG, "data_sigma2 must be positive");
   if (!tmpl_pts || !tmpl_tris || !tgt_pts || !tgt_tris) return c->fail(GBK_ERR_ARG, "null pointer");
   gbk_registration *r = new gbk_registration();
@@ -160,7 +163,7 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   r->sigma_data = sigma_data;
   r->data_sigma2 = data_sigma2;
   int rc = c->cuda(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "stream");
-  std::vector<int> th((size_t)nf * 3), tth((size_t)nf_t * 3);
+  std::vector<int> th((size_t)nf * cell), tth((size_t)nf_t * cell);
   if (!rc) {
     cudaMemcpy(th.data(), tmpl_tris, th.size() * sizeof(int), cudaMemcpyDefault);
     cudaMemcpy(tth.data(), tgt_tris, tth.size() * sizeof(int), cudaMemcpyDefault);
@@ -168,7 +171,7 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   }
   cudaStream_t saved = c->stream;
   c->stream = r->stream;
-  if (!rc) rc = r->surf.init(c, data_kind, sigma_data, nv, nf, th.data(), nv_t, nf_t, tth.data());
+  if (!rc) rc = r->surf.init(c, data_kind & 1, d, cell, sigma_data, nv, nf, th.data(), nv_t, nf_t, tth.data());
   const long n = ncp * d, m = nv * d, rows = std::max(ncp, nv);
   struct {
     double **p;
@@ -183,8 +186,8 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
     if (!rc) rc = r->alloc((void **)b.p, b.count * sizeof(double));
   if (!rc) rc = r->alloc((void **)&r->s.flag, 16);
   double *tgt_dev = nullptr;
-  if (!rc) rc = r->alloc((void **)&tgt_dev, (size_t)nv_t * 3 * sizeof(double));
-  if (!rc) rc = c->cuda(cudaMemcpyAsync(tgt_dev, tgt_pts, (size_t)nv_t * 3 * sizeof(double), cudaMemcpyDefault, r->stream), "copy target");
+  if (!rc) rc = r->alloc((void **)&tgt_dev, (size_t)nv_t * d * sizeof(double));
+  if (!rc) rc = c->cuda(cudaMemcpyAsync(tgt_dev, tgt_pts, (size_t)nv_t * d * sizeof(double), cudaMemcpyDefault, r->stream), "copy target");
   if (!rc) rc = c->cuda(cudaMemcpyAsync(r->lm0, tmpl_pts, (size_t)m * sizeof(double), cudaMemcpyDefault, r->stream), "copy template");
   if (!rc) rc = r->surf.set_target(c, tgt_dev);
   if (!rc) rc = c->cuda(cudaStreamSynchronize(r->stream), "sync");

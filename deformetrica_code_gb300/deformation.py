@@ -85,14 +85,15 @@ class Deformation:
         return xp, xm
 
 
-def _surface(name, ctx, pts, tris, pts_t, tris_t, sigma, grad=True):
+def _surface(name, ctx, pts, tris, pts_t, tris_t, sigma, grad=True, with_dim=False):
     ctx = ctx or Context()
     pts, pts_t = _f64(pts), _f64(pts_t)
     tris, tris_t = _i32(tris), _i32(tris_t)
     match = np.zeros(1)
     g = np.zeros(pts.shape) if grad else None
     ctx.bind_stream()
-    ctx.check(getattr(ctx.lib, name)(ctx.h, pts.shape[0], _ptr(pts), tris.shape[0], _ptr(tris),
+    dim = (pts.shape[1],) if with_dim else ()
+    ctx.check(getattr(ctx.lib, name)(ctx.h, *dim, pts.shape[0], _ptr(pts), tris.shape[0], _ptr(tris),
                                      pts_t.shape[0], _ptr(pts_t), tris_t.shape[0], _ptr(tris_t),
                                      float(sigma), ctypes.c_void_p(match.ctypes.data), _ptr(g)))
     return float(match[0]), g
@@ -108,10 +109,24 @@ def varifold_match(pts, tris, pts_t, tris_t, sigma, grad=True, context: Context 
     return _surface("gbk_varifold_match", context, pts, tris, pts_t, tris_t, sigma, grad)
 
 
-class Registration:
-    """One subject of DeterministicAtlas with a frozen template, replayed from a CUDA graph."""
+def curve_currents_match(pts, segs, pts_t, segs_t, sigma, grad=True, context: Context | None = None):
+    """Currents distance between polylines of 2-point segments (d = 2 or 3) and its gradient w.r.t.
+    pts (OrientedPolyLine::ComputeMatch, ComputeMatchGradient)."""
+    return _surface("gbk_curve_currents_match", context, pts, segs, pts_t, segs_t, sigma, grad, True)
 
-    KINDS = {"currents": 0, "varifold": 1}
+
+def curve_varifold_match(pts, segs, pts_t, segs_t, sigma, grad=True, context: Context | None = None):
+    """Varifold distance between polylines and its gradient w.r.t. pts
+    (NonOrientedPolyLine.cxx:125-256)."""
+    return _surface("gbk_curve_varifold_match", context, pts, segs, pts_t, segs_t, sigma, grad, True)
+
+
+class Registration:
+    """One subject of DeterministicAtlas with a frozen template, replayed from a CUDA graph: a
+    triangle mesh in 3-D (kind "currents" / "varifold") or a polyline of 2-point segments in 2-D or
+    3-D ("curve_currents" / "curve_varifold"); the dimension is the template's."""
+
+    KINDS = {"currents": 0, "varifold": 1, "curve_currents": 2, "curve_varifold": 3}
 
     def __init__(self, ncp: int, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T: int, sigma_def: float,
                  sigma_data: float, data_sigma2: float, kind: str = "currents", heun: bool = True,
@@ -120,10 +135,10 @@ class Registration:
         self.ncp, self.T = int(ncp), int(T)
         tp, tt = _f64(tmpl_pts), _i32(tmpl_tris)
         gp, gt = _f64(tgt_pts), _i32(tgt_tris)
-        self.nv = tp.shape[0]
+        self.nv, self.d = tp.shape[0], tp.shape[1]
         h = ctypes.c_void_p()
         self.ctx.check(self.ctx.lib.gbk_registration_create(
-            self.ctx.h, 3, self.ncp, tp.shape[0], _ptr(tp), tt.shape[0], _ptr(tt), gp.shape[0], _ptr(gp),
+            self.ctx.h, self.d, self.ncp, tp.shape[0], _ptr(tp), tt.shape[0], _ptr(tt), gp.shape[0], _ptr(gp),
             gt.shape[0], _ptr(gt), self.T, float(sigma_def), float(sigma_data), float(data_sigma2),
             self.KINDS[kind], int(heun), ctypes.byref(h)))
         self.h = h
@@ -170,8 +185,8 @@ class Registration:
                 "evaluations": int(info[6]), "stopped": self.STOP[int(info[7])]}
 
     def trajectories(self):
-        shp_c = (self.T, self.ncp, 3)
-        shp_v = (self.T, self.nv, 3)
+        shp_c = (self.T, self.ncp, self.d)
+        shp_v = (self.T, self.nv, self.d)
         out = [np.zeros(shp_c), np.zeros(shp_c), np.zeros(shp_v), np.zeros(shp_v), np.zeros(shp_c), np.zeros(shp_c)]
         self.ctx.check(self.ctx.lib.gbk_registration_trajectories(self.h, *[ctypes.c_void_p(a.ctypes.data) for a in out]))
         return dict(zip(("pos", "mom", "lm", "theta", "xi_pos", "xi_mom"), out))

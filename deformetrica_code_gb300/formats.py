@@ -132,7 +132,9 @@ def _archive_items(text: str):
     blob = []
     for line in text.split("\n"):
         s = line.strip()
-        if s and _B64.fullmatch(s) and not s.isdigit() and (len(s) >= 16 or s.endswith("=")):
+        # a blob starts on a base64 line of 16+ characters or a padded one, and runs on over the
+        # following base64 lines (its last line can be short)
+        if s and _B64.fullmatch(s) and not s.isdigit() and (blob or len(s) >= 16 or s.endswith("=")):
             blob.append(s)
             continue
         if blob:

@@ -230,15 +230,26 @@ int gbk_currents_match(gbk_ctx *ctx, long nv, const double *pts, long nf, const 
 int gbk_varifold_match(gbk_ctx *ctx, long nv, const double *pts, long nf, const int *tris,
                        long nv_t, const double *pts_t, long nf_t, const int *tris_t, double sigma,
                        double *match, double *grad);
+/* OrientedPolyLine::ComputeMatch / ComputeMatchGradient (curve currents: segment centres and
+ * tangents p1 - p0) between two polylines of nseg 2-point segments in d = 2 or 3 dimensions. */
+int gbk_curve_currents_match(gbk_ctx *ctx, int d, long nv, const double *pts, long nseg, const int *segs,
+                             long nv_t, const double *pts_t, long nseg_t, const int *segs_t, double sigma,
+                             double *match, double *grad);
+/* NonOrientedPolyLine::ComputeMatch / ComputeMatchGradient (NonOrientedPolyLine.cxx:125-256:
+ * curve varifold, tangents t / sqrt(|t|) and their tensors). */
+int gbk_curve_varifold_match(gbk_ctx *ctx, int d, long nv, const double *pts, long nseg, const int *segs,
+                             long nv_t, const double *pts_t, long nseg_t, const int *segs_t, double sigma,
+                             double *match, double *grad);
 
 /* ---- registration iteration (shooting + flow + data term + adjoint), CUDA-graph replay ---- */
 
 typedef struct gbk_registration gbk_registration;
 
 /* One subject of DeterministicAtlas with a frozen template (DeterministicAtlas.cxx:99-154,
- * AbstractAtlas.cxx:559-613): template mesh (nv, nf) deformed by ncp control points over T time
- * points, matched to the target mesh with data_kind 0 = currents, 1 = varifold. All device
- * memory is allocated here. */
+ * AbstractAtlas.cxx:559-613): template (nv points, nf cells) deformed by ncp control points over T
+ * time points, matched to the target with data_kind 0 = surface currents, 1 = surface varifold
+ * (triangles, d = 3), 2 = curve currents, 3 = curve varifold (2-point segments, d = 2 or 3). All
+ * device memory is allocated here. */
 int gbk_registration_create(gbk_ctx *ctx, int d, long ncp, long nv, const double *tmpl_pts,
                             long nf, const int *tmpl_tris, long nv_t, const double *tgt_pts,
                             long nf_t, const int *tgt_tris, int T, double sigma_def,

@@ -204,8 +204,7 @@ def registration(K: OracleLib, cp, mom, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, 
     DeterministicAtlas::AddGradientRegularityTerm, :246-280).
     """
     from . import geometry as G
-    match_f = G.currents_match if kind == "currents" else G.varifold_match
-    grad_f = G.currents_match_gradient if kind == "currents" else G.varifold_match_gradient
+    match_f, grad_f = G.KINDS[kind]
     pos, mo = shoot(K, sigma_def, cp, mom, T)
     lm = flow_landmarks(K, sigma_def, pos, mo, tmpl_pts, heun)
     match = match_f(K, sigma_data, lm[-1], tmpl_tris, tgt_pts, tgt_tris)

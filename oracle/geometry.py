@@ -1,8 +1,10 @@
-"""FP64 restatement of the reference's surface data terms (TEST INFRASTRUCTURE ONLY).
+"""FP64 restatement of the reference's surface and curve data terms (TEST INFRASTRUCTURE ONLY).
 
-Currents: OrientedSurfaceMesh.cxx:124-352. Varifolds: NonOrientedSurfaceMesh.cxx:124-378.
+Surface currents: OrientedSurfaceMesh.cxx:124-352. Surface varifolds: NonOrientedSurfaceMesh.cxx:
+124-378. Curve currents: OrientedPolyLine.cxx (ComputeMatch, ComputeMatchGradient,
+UpdateCentersTangents, UpdateSelfNorm). Curve varifolds: NonOrientedPolyLine.cxx:125-300, 364-378.
 Every kernel sum goes through the kernel oracle, as the reference goes through its kernel object.
-Meshes are (points nv x 3, triangles nf x 3 int) arrays; the reference reads them from VTK.
+Meshes are (points nv x d, cells nf x 3 or nf x 2 int) arrays; the reference reads them from VTK.
 """
 from __future__ import annotations
 
@@ -62,9 +64,11 @@ def varifold_normals(pts, tris):
 
 
 def special_product(M, X):
-    """NonOrientedSurfaceMesh::special_product, :364-378: symmetric 3x3 from 6 entries times X."""
-    iu = np.triu_indices(3)
-    S = np.zeros(M.shape[:-1] + (3, 3))
+    """NonOrientedSurfaceMesh::special_product, :364-378 (NonOrientedPolyLine::special_product for
+    any d): the symmetric d x d matrix of the d(d+1)/2 upper-triangle entries M times X."""
+    d = X.shape[-1]
+    iu = np.triu_indices(d)
+    S = np.zeros(M.shape[:-1] + (d, d))
     S[..., iu[0], iu[1]] = M
     S[..., iu[1], iu[0]] = M
     return np.einsum("...pq,...q->...p", S, X)
@@ -109,3 +113,83 @@ def varifold_match_gradient(K: OracleLib, sigma, pts_s, tris_s, pts_t, tris_t):
     for idx, e in ((i0, e0), (i1, e1), (i2, e2)):
         np.add.at(grad, idx, np.cross(e, kt) + gk)
     return grad
+
+
+# ---- curves (polylines of 2-point segments), d = 2 or 3 ----
+
+def centers_tangents(pts, segs):
+    """OrientedPolyLine::UpdateCentersTangents: c = (p0 + p1) / 2, t = p1 - p0."""
+    p0, p1 = pts[segs[:, 0]], pts[segs[:, 1]]
+    return (p0 + p1) / 2.0, p1 - p0
+
+
+def curve_currents_match(K: OracleLib, sigma, pts_s, segs_s, pts_t, segs_t):
+    """OrientedPolyLine::ComputeMatch: |T|^2 + |S|^2 - 2 <S, T> with tangent weights."""
+    cs, ts = centers_tangents(pts_s, segs_s)
+    ct, tt = centers_tangents(pts_t, segs_t)
+    m = currents_norm(K, sigma, ct, tt) + currents_norm(K, sigma, cs, ts)
+    return m - 2.0 * float(np.sum(K.convolve(ct, cs, ts, sigma) * tt))
+
+
+def curve_currents_match_gradient(K: OracleLib, sigma, pts_s, segs_s, pts_t, segs_t):
+    """OrientedPolyLine::ComputeMatchGradient: per segment Ktau = 2 (K_S t_S - K_T t_T)(c) goes
+    with - / + to the two ends, and the alpha-gradient difference to both ends."""
+    cs, ts = centers_tangents(pts_s, segs_s)
+    ct, tt = centers_tangents(pts_t, segs_t)
+    ktau = 2.0 * (K.convolve(cs, cs, ts, sigma) - K.convolve(cs, ct, tt, sigma))
+    gk = K.grad_alpha(cs, cs, ts, sigma, ts) - K.grad_alpha(cs, ct, tt, sigma, ts)
+    grad = np.zeros_like(pts_s)
+    np.add.at(grad, segs_s[:, 0], -ktau + gk)
+    np.add.at(grad, segs_s[:, 1], ktau + gk)
+    return grad
+
+
+def curve_varifold_tangents(pts, segs):
+    """NonOrientedPolyLine::UpdateCentersTangents, :266-300: t / sqrt(|t| + 1e-20) and the
+    upper-triangle products t_p t_q (p <= q)."""
+    c, t = centers_tangents(pts, segs)
+    t = t / np.sqrt(np.linalg.norm(t, axis=1) + 1e-20)[:, None]
+    d = t.shape[1]
+    iu = np.triu_indices(d)
+    return c, t, (t[:, :, None] * t[:, None, :])[:, iu[0], iu[1]]
+
+
+def curve_varifold_match(K: OracleLib, sigma, pts_s, segs_s, pts_t, segs_t):
+    """NonOrientedPolyLine::ComputeMatch, :125-170."""
+    cs, ts, ms = curve_varifold_tangents(pts_s, segs_s)
+    ct, tt, mt = curve_varifold_tangents(pts_t, segs_t)
+    m = varifold_norm(K, sigma, ct, tt, mt) + varifold_norm(K, sigma, cs, ts, ms)
+    sdt = K.convolve(ct, cs, ms, sigma)
+    return m - 2.0 * float(np.sum(tt * special_product(sdt, tt)))
+
+
+def curve_varifold_match_gradient(K: OracleLib, sigma, pts_s, segs_s, pts_t, segs_t):
+    """NonOrientedPolyLine::ComputeMatchGradient, :174-256."""
+    cs, ts, ms = curve_varifold_tangents(pts_s, segs_s)
+    ct, tt, mt = curve_varifold_tangents(pts_t, segs_t)
+    d = ts.shape[1]
+    ktau_s = K.convolve(cs, cs, ms, sigma)
+    gk_s = K.grad_varlin(cs, cs, ms, sigma)  # (nf, d(d+1)/2, d)
+    ktau_t = K.convolve(cs, ct, mt, sigma)
+    gk_t = K.grad_varlin(cs, ct, mt, sigma)
+    mag2 = np.sum(ts * ts, axis=1)
+    ok = mag2 > 1e-20
+    kt = 4.0 * special_product(ktau_s - ktau_t, ts)
+    aux = special_product(ms, kt)
+    kt = (kt - aux / (2 * mag2[:, None])) / np.sqrt(mag2)[:, None]
+    delta = gk_s - gk_t
+    gk = np.stack([np.sum(special_product(delta[:, :, q], ts) * ts, axis=1) for q in range(d)], axis=1)
+    kt[~ok] = 0.0
+    gk[~ok] = 0.0
+    grad = np.zeros_like(pts_s)
+    np.add.at(grad, segs_s[:, 0], -kt + gk)
+    np.add.at(grad, segs_s[:, 1], kt + gk)
+    return grad
+
+
+KINDS = {
+    "currents": (currents_match, currents_match_gradient),
+    "varifold": (varifold_match, varifold_match_gradient),
+    "curve_currents": (curve_currents_match, curve_currents_match_gradient),
+    "curve_varifold": (curve_varifold_match, curve_varifold_match_gradient),
+}

@@ -16,6 +16,9 @@ sources by oracle/build_ref.sh) and records its outputs:
 * ``parallel_transport.npz`` -- the inputs and ground truth of
   tests/unit_tests/parallel-transport/TestParallelTransport.cxx:19-85 (read from the reference's
   DLM text files), which pin the shooting oracle (oracle/deformation.py).
+* ``skull_registration.npz`` -- functional test 5 (registration/landmark/2d/skulls: a 2-D
+  NonOrientedPolyline registration): the two polylines (x, y of the VTK points, 2-point LINES
+  cells), the initial control points and the final FastGradientAscent state.
 * ``amygdala_registration.npz`` -- functional test 6 of the reference
   (tests/functional_tests/configure.ini [Test6], registration/landmark/3d/amygdalas): the two
   meshes as the reference reads them (VTK float points, triangles re-oriented by its normals
@@ -122,20 +125,47 @@ def main(ref_root: str = "/root/reference"):
         kernel_width=np.array(15.0),
         number_of_time_points=np.array(30),
     )
-    # 4. functional test 6: landmark registration of two amygdala meshes
+    # 4. functional tests 5 and 6: landmark registrations of two skull curves, two amygdala meshes
+    skull_fixture(ref_root)
     amygdala_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
+
+
+def _formats():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "formats", os.path.join(os.path.dirname(os.path.dirname(HERE)), "deformetrica_code_gb300", "formats.py"))
+    F = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(F)
+    return F
+
+
+def skull_fixture(ref_root: str = "/root/reference"):
+    """Inputs and expected final state of the reference's skull registration (model.xml:
+    NonOrientedPolyline, data-sigma 1, object kernel width 40, deformation kernel width 60, 6 time
+    points; optimization_parameters.xml: FastGradientAscent, 10 iterations, default initial step
+    1e-3 (SparseDiffeoParameters.cxx:82))."""
+    F = _formats()
+    from oracle.optimize import initial_control_points
+    d = os.path.join(ref_root, "tests", "functional_tests", "registration", "landmark", "2d", "skulls")
+    tp, tf = F.read_vtk_polydata(os.path.join(d, "data", "template.vtk"))
+    gp, gf = F.read_vtk_polydata(os.path.join(d, "data", "skull_sapiens.vtk"))
+    tp, gp = np.ascontiguousarray(tp[:, :2]), np.ascontiguousarray(gp[:, :2])  # a 2-D object
+    st = F.read_deformation_state(os.path.join(d, "deformetrica-state.bin"))
+    cp0 = initial_control_points(tp[tf].mean(axis=1), 60.0)  # the segment centres' box
+    np.savez_compressed(
+        os.path.join(HERE, "skull_registration.npz"),
+        tmpl_pts=tp, tmpl_segs=tf, tgt_pts=gp, tgt_segs=gf, cp0=cp0,
+        kernel_width=np.array(60.0), data_kernel_width=np.array(40.0), data_sigma2=np.array(1.0),
+        number_of_time_points=np.array(6), initial_step=np.array(1e-3), max_iterations=np.array(10),
+        **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
 def amygdala_fixture(ref_root: str = "/root/reference"):
     """Inputs and expected final state of the reference's amygdala registration (model.xml:
     OrientedSurfaceMesh, data-sigma 0.1, object and deformation kernel width 10, 10 time points;
     optimization_parameters.xml: FastGradientAscent, initial step 1e-7, 10 iterations)."""
-    import importlib.util
-    spec = importlib.util.spec_from_file_location(
-        "formats", os.path.join(os.path.dirname(os.path.dirname(HERE)), "deformetrica_code_gb300", "formats.py"))
-    F = importlib.util.module_from_spec(spec)
-    spec.loader.exec_module(F)
+    F = _formats()
     from oracle.optimize import initial_control_points
     d = os.path.join(ref_root, "tests", "functional_tests", "registration", "landmark", "3d", "amygdalas")
     tp, tf_raw = F.read_vtk_polydata(os.path.join(d, "data", "decimatedAmygdala1.vtk"))

@@ -1,7 +1,10 @@
-"""End-to-end parity with the reference's functional test 6 (tests/functional_tests/configure.ini
+"""End-to-end parity with the reference's functional tests 6 (tests/functional_tests/configure.ini
 [Test6]: registration/landmark/3d/amygdalas -- an OrientedSurfaceMesh registration, exact Gaussian
 kernels of width 10, data-sigma 0.1, 10 time points, FastGradientAscent from step 1e-7 for 10
-iterations), CPU part: the on-disk formats and the FP64 oracle of the whole estimation.
+iterations) and 5 ([Test5]: registration/landmark/2d/skulls -- a 2-D NonOrientedPolyline
+registration, data kernel 40, deformation kernel 60, data-sigma 1, 6 time points, 10 iterations
+from the default step 1e-3), CPU part: the on-disk formats and the FP64 oracle of the whole
+estimations.
 
 The expected values are the final optimiser state the reference stored in
 deformetrica-state.bin, decoded into tests/golden/amygdala_registration.npz by
@@ -26,6 +29,26 @@ from tests.conftest import GOLDEN
 @pytest.fixture(scope="module")
 def fx():
     return dict(np.load(os.path.join(GOLDEN, "amygdala_registration.npz")))
+
+
+@pytest.fixture(scope="module")
+def skull():
+    return dict(np.load(os.path.join(GOLDEN, "skull_registration.npz")))
+
+
+def check_state(r, fx, hist_rel=1e-7, rel=1e-10):
+    h, href = r["history"], fx["state_history"]
+    assert h.shape == href.shape
+    assert np.all(np.abs(h - href) <= 1e-12 * np.abs(href).max() + hist_rel * np.abs(href))
+    assert r["iter"] == int(fx["state_iter"]) and r["freeze_counter"] == int(fx["state_freeze_counter"])
+    assert abs(r["tau"] - float(fx["state_tau"])) <= 1e-14
+    np.testing.assert_allclose(r["step"], fx["state_step"], rtol=1e-14)
+    np.testing.assert_allclose(r["grad_sq_norms"], fx["state_grad_sq_norms"], rtol=rel)
+    for got, key in ((r["params"][0], "control_points"), (r["params"][1], "momenta"), (r["aux"][0], "aux_control_points"),
+                     (r["aux"][1], "aux_momenta"), (r["grads"][0], "grad_control_points"),
+                     (r["grads"][1], "grad_momenta")):
+        ref = fx["state_" + key]
+        assert np.abs(got - ref).max() <= rel * np.abs(ref).max(), key
 
 
 def test_reorientation_is_consistent_and_inward(fx):
@@ -81,16 +104,36 @@ def test_oracle_reproduces_reference_state(fx):
     ev = registration_evaluator(K, fx["tmpl_pts"], fx["tmpl_tris"], fx["tgt_pts"], fx["tgt_tris"], 10, 10.0, 10.0,
                                 0.01, "currents", heun=False)
     cp0 = fx["cp0"]
-    r = fast_gradient_ascent(ev, [cp0, np.zeros_like(cp0)], 1e-7, 10)
-    h, href = r["history"], fx["state_history"]
-    assert h.shape == href.shape
-    assert np.all(np.abs(h - href) <= 1e-12 * np.abs(href).max() + 1e-7 * np.abs(href))
-    assert r["iter"] == int(fx["state_iter"]) and r["freeze_counter"] == int(fx["state_freeze_counter"])
-    assert abs(r["tau"] - float(fx["state_tau"])) <= 1e-14
-    np.testing.assert_allclose(r["step"], fx["state_step"], rtol=1e-14)
-    np.testing.assert_allclose(r["grad_sq_norms"], fx["state_grad_sq_norms"], rtol=1e-10)
-    for got, key in ((r["params"][0], "control_points"), (r["params"][1], "momenta"), (r["aux"][0], "aux_control_points"),
-                     (r["aux"][1], "aux_momenta"), (r["grads"][0], "grad_control_points"),
-                     (r["grads"][1], "grad_momenta")):
-        ref = fx["state_" + key]
-        assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max(), key
+    check_state(fast_gradient_ascent(ev, [cp0, np.zeros_like(cp0)], 1e-7, 10), fx)
+
+
+def test_skull_oracle_reproduces_reference_state(skull):
+    import oracle
+    from oracle.optimize import fast_gradient_ascent, initial_control_points, registration_evaluator
+    K = oracle.load("port")
+    cp0 = initial_control_points(skull["tmpl_pts"][skull["tmpl_segs"]].mean(axis=1), 60.0)
+    np.testing.assert_array_equal(cp0, skull["cp0"])
+    ev = registration_evaluator(K, skull["tmpl_pts"], skull["tmpl_segs"], skull["tgt_pts"], skull["tgt_segs"], 6,
+                                60.0, 40.0, 1.0, "curve_varifold", heun=False)
+    check_state(fast_gradient_ascent(ev, [cp0, np.zeros_like(cp0)], 1e-3, 10), skull)
+
+
+@pytest.mark.parametrize("kind", ["curve_currents", "curve_varifold"])
+@pytest.mark.parametrize("d", [2, 3])
+def test_curve_gradients_match_finite_differences(skull, kind, d):
+    import oracle
+    from oracle import geometry as G
+    K = oracle.load("port")
+    rng = np.random.default_rng(d)
+    lift = lambda p: p if d == 2 else np.concatenate([p, rng.normal(0, 5, (p.shape[0], 1))], axis=1)
+    ps, pt = lift(skull["tmpl_pts"]), lift(skull["tgt_pts"])
+    fm, fg = G.KINDS[kind]
+    g = fg(K, 40.0, ps, skull["tmpl_segs"], pt, skull["tgt_segs"])
+    for i in (3, 70, 149):
+        for k in range(d):
+            a, b = ps.copy(), ps.copy()
+            a[i, k] += 1e-4
+            b[i, k] -= 1e-4
+            num = (fm(K, 40.0, a, skull["tmpl_segs"], pt, skull["tgt_segs"])
+                   - fm(K, 40.0, b, skull["tmpl_segs"], pt, skull["tgt_segs"])) / 2e-4
+            assert abs(num - g[i, k]) <= 1e-5 * max(1.0, np.abs(g).max()), (i, k, num, g[i, k])

@@ -1,6 +1,7 @@
 """GPU: the device-resident registration optimiser (gbk_registration_optimize, the reference's
-FastGradientAscent.cxx:48-300) on the reference's functional test 6 (amygdala landmark
-registration; see tests/test_functional_registration.py for the fixture and the oracle).
+FastGradientAscent.cxx:48-300) on the reference's functional tests 6 (amygdala surface
+registration, 3-D currents) and 5 (skull curve registration, 2-D varifold); see
+tests/test_functional_registration.py for the fixtures and the oracle.
 
 FP64 mode reproduces the final state the reference stored (log-likelihood history, control
 points, momenta, the extrapolated point and its gradient, step sizes, tau, counters) to 1e-9
@@ -25,26 +26,33 @@ def gb():
     return g
 
 
-@pytest.fixture(scope="module")
-def fx():
-    return dict(np.load(os.path.join(GOLDEN, "amygdala_registration.npz")))
+CASES = {
+    "amygdala": dict(file="amygdala_registration.npz", cells="tmpl_tris", tcells="tgt_tris", kind="currents"),
+    "skull": dict(file="skull_registration.npz", cells="tmpl_segs", tcells="tgt_segs", kind="curve_varifold"),
+}
 
 
-def run(gb, fx, mode):
+def run(gb, case, mode):
     from deformetrica_code_gb300.deformation import Registration
+    c = CASES[case]
+    fx = dict(np.load(os.path.join(GOLDEN, c["file"])))
     ctx = gb.Context(mode=mode)
-    reg = Registration(8, fx["tmpl_pts"], fx["tmpl_tris"], fx["tgt_pts"], fx["tgt_tris"], T=10, sigma_def=10.0,
-                       sigma_data=10.0, data_sigma2=0.01, kind="currents", heun=False, context=ctx)
     cp0 = fx["cp0"]
-    r = reg.optimize(cp0, np.zeros_like(cp0), max_iterations=10, initial_step=1e-7)
+    reg = Registration(cp0.shape[0], fx["tmpl_pts"], fx[c["cells"]], fx["tgt_pts"], fx[c["tcells"]],
+                       T=int(fx["number_of_time_points"]), sigma_def=float(fx["kernel_width"]),
+                       sigma_data=float(fx["data_kernel_width"]), data_sigma2=float(fx["data_sigma2"]),
+                       kind=c["kind"], heun=False, context=ctx)
+    r = reg.optimize(cp0, np.zeros_like(cp0), max_iterations=int(fx["max_iterations"]),
+                     initial_step=float(fx["initial_step"]))
     reg.close()
-    return r
+    return r, fx
 
 
+@pytest.mark.parametrize("case", ["amygdala", "skull"])
 @pytest.mark.parametrize("mode_name,tol", [("f64", 1e-9), ("f32c", 1e-5)])
-def test_optimizer_reproduces_reference_state(gb, fx, mode_name, tol):
+def test_optimizer_reproduces_reference_state(gb, case, mode_name, tol):
     mode = gb.GBK_MODE_F64 if mode_name == "f64" else gb.GBK_MODE_F32C
-    r = run(gb, fx, mode)
+    r, fx = run(gb, case, mode)
     h, href = r["history"], fx["state_history"]
     assert h.shape == href.shape, (h.shape, href.shape)
     assert np.all(np.abs(h - href) <= tol * np.abs(href).max() + 1e-6 * np.abs(href)), np.abs(h - href).max()

@@ -382,6 +382,27 @@ def optimizer_bench(cpu: bool = True, reg_iters: int = 10):
     return res
 
 
+def atlas_optimizer_bench(iters: int = 3):
+    """FastGradientAscent of the 64-subject atlas workload on the device (control points,
+    template with gradient smoothing of width 0.15, momenta), FP32C: seconds per iteration."""
+    import deformetrica_code_gb300 as g
+    from deformetrica_code_gb300.deformation import Atlas
+    cp, mom, tp, tf, targets, kw = atlas_workload()
+    ctx = g.Context()
+    atlas = Atlas(cp, tp, tf, targets, kind="currents", context=ctx, **kw)
+    atlas.set_template_smoothing(kw["sigma_def"])
+    atlas.optimize(cp, tp, mom, 1, 1e-4)  # warm-up: eager iteration, graph capture
+    t0 = time.perf_counter()
+    r = atlas.optimize(cp, tp, mom, iters, 1e-4)
+    dt = time.perf_counter() - t0
+    atlas.close()
+    return {"workload": f"64-subject atlas, {iters} FastGradientAscent iterations over control points, template "
+                        "(smoothed gradient) and momenta, FP32C", "s_total": dt,
+            "s_per_iteration": dt / max(1, len(r["history"]) - 1), "evaluations": r["evaluations"],
+            "s_per_evaluation": dt / max(1, r["evaluations"]),
+            "loglik_first_last": [float(r["history"][0].sum()), float(r["history"][-1].sum())]}
+
+
 def small_kernel_bench(n: int = 4096, sigma: float = 0.2, reps: int = 50, cpu: bool = True):
     """Convolve and ConvolveGradient(X, alpha = X) at x, y = 4096 points uniform in [0,1]^3,
     weights N(0,1), sigma 0.2 (the reference's CPU-runnable kernel case): per call through the
@@ -750,6 +771,8 @@ def main():
             line["small_kernel_sum"] = small_kernel_bench(cpu=not args.no_cpu_baseline)
         if not args.no_optimizer:
             line["optimizer"] = optimizer_bench(cpu=not args.no_cpu_baseline)
+            if not args.no_atlas:
+                line["optimizer"]["atlas_64_subjects"] = atlas_optimizer_bench()
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

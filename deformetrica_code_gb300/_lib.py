@@ -96,6 +96,8 @@ SIGNATURES = {
     "gbk_atlas_step": (_I, [_P, _P, _P, _P, _P, _P]),
     "gbk_atlas_set_graph": (_I, [_P, _I]),
     "gbk_atlas_graph_launches": (ctypes.c_longlong, [_P]),
+    "gbk_atlas_set_template_smoothing": (_I, [_P, _D]),
+    "gbk_atlas_optimize": (_I, [_P, _P, _P, _P, _I, _I, _I, _D, _I, _D, _D, _D, _I, _P, _P, _P]),
     "gbk_atlas_destroy": (None, [_P]),
 }
 

@@ -28,6 +28,7 @@
 #include "gbk_dispatch.h"
 #include "gbk_geometry.h"
 #include "gbk_ops.h"
+#include "gbk_optimize.h"
 
 using namespace gbk;
 
@@ -239,6 +240,7 @@ struct gbk_atlas {
   int S = 0, T = 2, heun = 1, kind = 0, dw = 3, use_graph = 1, steps = 0;
   long ncp = 0, nv = 0, nf = 0;
   double sigma_def = 1, sigma_data = 1, data_sigma2 = 1;
+  double smoothing = 0.0;  // template-gradient smoothing width (0: the L2 gradient)
   std::vector<long> nft;  // target faces per subject
   cudaStream_t stream = nullptr;
   std::vector<void *> owned;
@@ -251,7 +253,7 @@ struct gbk_atlas {
   double *pos = nullptr, *momt = nullptr, *xp = nullptr, *xm = nullptr;  // S x T x ncp x 3
   double *lm0 = nullptr, *lm = nullptr, *theta = nullptr;       // nv x 3, S x T x nv x 3
   double *va = nullptr, *vb = nullptr, *vc = nullptr, *vd = nullptr;  // S x max(ncp, nv) x 3
-  double *kp = nullptr, *greg = nullptr, *gmom = nullptr, *gcp = nullptr, *gtmpl = nullptr;
+  double *kp = nullptr, *greg = nullptr, *gmom = nullptr, *gcp = nullptr, *gtmpl = nullptr, *gtmpl_l2 = nullptr;
   double *thT = nullptr;                                        // S x nv x 3
   int *flag = nullptr, *tris = nullptr, *csr_ptr = nullptr, *csr_fc = nullptr;
   double *cs = nullptr, *ns = nullptr, *mns = nullptr, *ws = nullptr;   // S x nf x {3,6}
@@ -357,6 +359,45 @@ struct gbk_atlas {
   // launch order is fixed at build time; body() replays it with the element-wise kernels between
   int body();
   int build_launches();
+  // one iteration on `stream`: eager at first, captured the second time, replayed afterwards
+  int run() {
+    cudaStream_t saved = c->stream;
+    c->stream = stream;
+    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    int rc = GBK_OK;
+    if (!use_graph || steps == 0) {
+      rc = body();
+    } else {
+      if (!exec) {
+        long long l0 = c->launches;
+        rc = c->cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        if (!rc) {
+          rc = body();
+          cudaGraph_t g = nullptr;
+          cudaError_t e = cudaStreamEndCapture(stream, &g);
+          if (!rc && e != cudaSuccess) rc = c->cuda(e, "end capture");
+          if (!rc) rc = c->cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate");
+          graph = g;
+          graph_kernels = c->launches - l0;
+          c->launches = l0;
+        }
+      }
+      if (!rc) {
+        rc = c->cuda(cudaGraphLaunch(exec, stream), "graph launch");
+        c->launches += graph_kernels;
+      }
+    }
+    c->stream = saved;
+    if (!rc) ++steps;
+    return rc;
+  }
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    steps = 0;
+  }
   void release() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -606,10 +647,22 @@ int gbk_atlas::body() {
   lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, gmom, n, nullptr, 0, -1.0, xm, sT_n, -1.0, kp, sr,
                                                            nullptr, nullptr, 0);
   sum_subjects_kernel<<<nb(n), 256, 0, st>>>(S, n, gcp, xp, sT_n, -1.0, greg, sr, -1.0);
-  sum_subjects_kernel<<<nb(m), 256, 0, st>>>(S, m, gtmpl, theta, sT_m, -1.0, nullptr, 0, 0.0);
+  sum_subjects_kernel<<<nb(m), 256, 0, st>>>(S, m, smoothing > 0 ? gtmpl_l2 : gtmpl, theta, sT_m, -1.0, nullptr, 0,
+                                              0.0);
   c->launches += 3;
   if (L != launches.size()) return c->fail(GBK_ERR_STATE, "atlas: launch order mismatch");
-  return ok(cudaGetLastError(), "atlas gradients");
+  if ((rc = ok(cudaGetLastError(), "atlas gradients"))) return rc;
+  if (smoothing > 0) {  // Sobolev template gradient: K_smooth(template, template) L2 (ConvolveGradTemplate)
+    PairArgs q = pa(nv, nv, smoothing);
+    q.x = lm0;
+    q.y = lm0;
+    q.w = gtmpl_l2;
+    q.w_ld = 3;
+    q.out0 = gtmpl;
+    q.out0_ld = 3;
+    if ((rc = c->launch(OP_CONV, 3, 3, q))) return rc;
+  }
+  return GBK_OK;
 }
 
 extern "C" {
@@ -710,7 +763,8 @@ int gbk_atlas_create(gbk_ctx *c, long ncp, const double *cp, long nv, const doub
               {&a->xp, S * TT * n}, {&a->xm, S * TT * n}, {&a->lm0, (size_t)m}, {&a->lm, S * TT * m},
               {&a->theta, S * TT * m}, {&a->va, S * rows3}, {&a->vb, S * rows3}, {&a->vc, S * rows3},
               {&a->vd, S * rows3}, {&a->kp, S * rows3}, {&a->greg, S * rows3}, {&a->gmom, S * n},
-              {&a->gcp, (size_t)n}, {&a->gtmpl, (size_t)m}, {&a->cs, S * nf * 3}, {&a->ns, S * nf * 3},
+              {&a->gcp, (size_t)n}, {&a->gtmpl, (size_t)m}, {&a->gtmpl_l2, (size_t)m},
+              {&a->cs, S * nf * 3}, {&a->ns, S * nf * 3},
               {&a->mns, S * nf * 6}, {&a->ws, S * nf * 6}, {&a->kts, S * nf * 6}, {&a->ktt, S * nf * 6},
               {&a->gs, S * nf * 3}, {&a->gt, S * nf * 3}, {&a->kt, S * nf * 3}, {&a->gk, S * nf * 3},
               {&a->ct, (size_t)tot_f * 3}, {&a->tw, (size_t)tot_f * a->dw}, {&a->norm_t, S}, {&a->dot_ss, S},
@@ -799,35 +853,7 @@ int gbk_atlas_step(gbk_atlas *a, const double *mom, double *loglik, double *grad
   if (!mom) return c->fail(GBK_ERR_ARG, "null momenta");
   const size_t nb_mom = (size_t)a->S * a->ncp * 3 * sizeof(double);
   int rc = c->cuda(cudaMemcpyAsync(a->mom, mom, nb_mom, cudaMemcpyDefault, a->stream), "copy momenta");
-  cudaStream_t saved = c->stream;
-  c->stream = a->stream;
-  gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
-  if (!rc) {
-    if (!a->use_graph || a->steps == 0) {
-      rc = a->body();
-    } else {
-      if (!a->exec) {
-        long long l0 = c->launches;
-        rc = c->cuda(cudaStreamBeginCapture(a->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        if (!rc) {
-          rc = a->body();
-          cudaGraph_t g = nullptr;
-          cudaError_t e = cudaStreamEndCapture(a->stream, &g);
-          if (!rc && e != cudaSuccess) rc = c->cuda(e, "end capture");
-          if (!rc) rc = c->cuda(cudaGraphInstantiate(&a->exec, g, 0), "graph instantiate");
-          a->graph = g;
-          a->graph_kernels = c->launches - l0;
-          c->launches = l0;
-        }
-      }
-      if (!rc) {
-        rc = c->cuda(cudaGraphLaunch(a->exec, a->stream), "graph launch");
-        c->launches += a->graph_kernels;
-      }
-    }
-  }
-  c->stream = saved;
-  if (!rc) ++a->steps;
+  if (!rc) rc = a->run();
   const size_t n = (size_t)a->ncp * 3 * sizeof(double);
   if (!rc && loglik) rc = c->cuda(cudaMemcpyAsync(loglik, a->out, (a->S + 3) * sizeof(double), cudaMemcpyDefault, a->stream), "copy");
   if (!rc && grad_mom) rc = c->cuda(cudaMemcpyAsync(grad_mom, a->gmom, a->S * n, cudaMemcpyDefault, a->stream), "copy");
@@ -839,6 +865,108 @@ int gbk_atlas_step(gbk_atlas *a, const double *mom, double *loglik, double *grad
 }
 
 long long gbk_atlas_graph_launches(const gbk_atlas *a) { return a ? a->graph_kernels : 0; }
+
+int gbk_atlas_set_template_smoothing(gbk_atlas *a, double width) {
+  if (!a) return GBK_ERR_ARG;
+  if (!(width >= 0)) return a->c->fail(GBK_ERR_ARG, "smoothing width must be >= 0");
+  a->smoothing = width < 1e-20 ? 0.0 : width;  // AbstractAtlas.cxx:729: below 1e-20, no smoothing
+  a->drop_graph();                            // the iteration changes: capture it again
+  return GBK_OK;
+}
+
+// FastGradientAscent (gbk_optimize.cu) of the atlas log-likelihood over the groups, in the
+// reference's order, ControlPoints, TemplateData (each when optimised) and Momenta (all subjects);
+// the template step uses the smoothed template gradient and its squared norm is <L2, smoothed>
+// (DeterministicAtlas.cxx:212-234).
+int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int optimize_cp, int optimize_template,
+                       int max_iterations, double initial_step, int max_line_search, double shrink, double expand,
+                       double tolerance, int nb_iter_freeze, double *history, int *iterations, double *info) {
+  if (!a) return GBK_ERR_ARG;
+  gbk_ctx *c = a->c;
+  c->err.clear();
+  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
+  if (!cp || !tmpl || !mom || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
+  const long n = a->ncp * 3, m = a->nv * 3, nm = (long)a->S * n;
+  cudaStream_t st = a->stream;
+  double *sq_dev = nullptr;
+  int rc = c->cuda(cudaMalloc(&sq_dev, 4 * sizeof(double)), "cudaMalloc (optimiser)");
+  if (!rc && !optimize_cp) rc = c->cuda(cudaMemcpyAsync(a->cp, cp, n * sizeof(double), cudaMemcpyDefault, st), "copy");
+  if (!rc && !optimize_template)
+    rc = c->cuda(cudaMemcpyAsync(a->lm0, tmpl, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+  int ng = 0, gcp = -1, gt = -1;
+  long sizes[3];
+  double *params[3];
+  if (optimize_cp) {
+    gcp = ng;
+    sizes[ng] = n;
+    params[ng++] = cp;
+  }
+  if (optimize_template) {
+    gt = ng;
+    sizes[ng] = m;
+    params[ng++] = tmpl;
+  }
+  const int gm = ng;
+  sizes[ng] = nm;
+  params[ng++] = mom;
+  FgaEvaluate ev = [&](double *const *p, bool need_grad, double *terms, double *const *g, double *sq) -> int {
+    int e = GBK_OK;
+    if (gcp >= 0) e = c->cuda(cudaMemcpyAsync(a->cp, p[gcp], n * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+    if (!e && gt >= 0) e = c->cuda(cudaMemcpyAsync(a->lm0, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+    if (!e) e = c->cuda(cudaMemcpyAsync(a->mom, p[gm], nm * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+    if (!e) e = a->run();
+    double out[3];
+    if (!e) e = c->cuda(cudaMemcpyAsync(out, a->out, sizeof out, cudaMemcpyDeviceToHost, st), "read L");
+    double h[3] = {0, 0, 0};
+    if (!e && need_grad) {
+      if (gcp >= 0) e = c->cuda(cudaMemcpyAsync(g[gcp], a->gcp, n * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+      if (!e && gt >= 0)
+        e = c->cuda(cudaMemcpyAsync(g[gt], a->gtmpl, m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+      if (!e) e = c->cuda(cudaMemcpyAsync(g[gm], a->gmom, nm * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+      if (!e) e = c->cuda(dot_f64(st, a->gcp, a->gcp, n, sq_dev, 0), "norm");
+      if (!e) e = c->cuda(dot_f64(st, a->smoothing > 0 ? a->gtmpl_l2 : a->gtmpl, a->gtmpl, m, sq_dev + 1, 0), "norm");
+      if (!e) e = c->cuda(dot_f64(st, a->gmom, a->gmom, nm, sq_dev + 2, 0), "norm");
+      if (!e) e = c->cuda(cudaMemcpyAsync(h, sq_dev, sizeof h, cudaMemcpyDeviceToHost, st), "read norms");
+    }
+    if (!e) e = c->cuda(cudaStreamSynchronize(st), "sync");
+    if (!e) {
+      terms[0] = out[1];
+      terms[1] = out[2];
+      if (need_grad) {
+        if (gcp >= 0) sq[gcp] = h[0];
+        if (gt >= 0) sq[gt] = h[1];
+        sq[gm] = h[2];
+      }
+    }
+    return e;
+  };
+  FgaOptions o;
+  o.max_iterations = max_iterations;
+  o.max_line_search = max_line_search;
+  o.nb_iter_freeze = nb_iter_freeze;
+  o.initial_step = initial_step;
+  o.shrink = shrink;
+  o.expand = expand;
+  o.tolerance = tolerance;
+  FgaResult res;
+  if (!rc) rc = fast_gradient_ascent(c, st, ng, sizes, params, o, ev, &res, nullptr, nullptr);
+  if (sq_dev) cudaFree(sq_dev);
+  if (rc) return rc;
+  std::copy(res.history.begin(), res.history.end(), history);
+  *iterations = res.rows;
+  if (info) {  // steps and squared norms per group (cp, template, momenta; 0 when frozen)
+    for (int k = 0; k < 10; ++k) info[k] = 0.0;
+    if (gcp >= 0) info[0] = res.step[gcp], info[5] = res.sq[gcp];
+    if (gt >= 0) info[1] = res.step[gt], info[6] = res.sq[gt];
+    info[2] = res.step[gm];
+    info[7] = res.sq[gm];
+    info[3] = res.tau;
+    info[4] = res.freeze;
+    info[8] = (double)res.evaluations;
+    info[9] = res.stop;
+  }
+  return GBK_OK;
+}
 
 void gbk_atlas_destroy(gbk_atlas *a) {
   if (!a) return;

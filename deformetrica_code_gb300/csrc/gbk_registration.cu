@@ -26,6 +26,7 @@
 #include "gbk_geometry.h"
 #include "gbk_hostio.h"
 #include "gbk_ops.h"
+#include "gbk_optimize.h"
 
 using namespace gbk;
 
@@ -250,10 +251,10 @@ int gbk_registration_trajectories(gbk_registration *r, double *pos, double *mom,
 long long gbk_registration_graph_launches(const gbk_registration *r) { return r ? r->graph_launches : 0; }
 
 // Nesterov-accelerated gradient ascent of the registration log-likelihood over the control points
-// and momenta (FastGradientAscent.cxx:48-300, GradientAscentStep :306-335): every parameter, trial
-// point and gradient stays on the device; each evaluation is one replay of the iteration graph and
-// one 40-byte read of the log-likelihood terms (plus the two squared gradient norms after an
-// accepted step) for the line-search decisions, which the host takes.
+// and momenta (FastGradientAscent.cxx:48-300, gbk_optimize.cu): every parameter, trial point and
+// gradient stays on the device; each evaluation is one replay of the iteration graph and one
+// 40-byte read of the log-likelihood terms (plus the squared gradient norms after an accepted
+// step) for the line-search decisions, which the host takes.
 int gbk_registration_optimize(gbk_registration *r, double *cp, double *mom, int optimize_cp, int max_iterations,
                               double initial_step, int max_line_search, double shrink, double expand,
                               double tolerance, int nb_iter_freeze, double *history, int *iterations,
@@ -264,198 +265,70 @@ int gbk_registration_optimize(gbk_registration *r, double *cp, double *mom, int 
   c->err.clear();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !mom || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
-  if (max_iterations < 0 || max_line_search < 1 || !(shrink > 0 && shrink < 1) || !(expand >= 1) ||
-      !(initial_step > 0) || nb_iter_freeze < 0)
-    return c->fail(GBK_ERR_ARG, "bad optimiser parameters");
   const long n = r->ncp * r->d;
   const size_t nb = (size_t)n * sizeof(double);
-  const int ng = optimize_cp ? 2 : 1;  // parameter groups: [ControlPoints,] Momenta
   gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
   cudaStream_t st = r->stream;
-  // device state: fixed, aux, new, two multivariate proposals, gradients (cp, mom each)
-  std::vector<double *> buf(12, nullptr);
   double *sq_dev = nullptr;
-  int rc = GBK_OK;
-  for (auto &b : buf)
-    if (!rc) rc = c->cuda(cudaMalloc(&b, nb), "cudaMalloc (optimiser)");
-  if (!rc) rc = c->cuda(cudaMalloc(&sq_dev, 4 * sizeof(double)), "cudaMalloc (optimiser)");
-  auto cleanup = [&]() {
-    cudaStreamSynchronize(st);
-    for (auto b : buf)
-      if (b) cudaFree(b);
-    if (sq_dev) cudaFree(sq_dev);
-  };
-  if (rc) {
-    cleanup();
-    return rc;
-  }
-  double *fixed[2] = {buf[0], buf[1]}, *aux[2] = {buf[2], buf[3]}, *nw[2] = {buf[4], buf[5]};
-  double *prop[2][2] = {{buf[6], buf[7]}, {buf[8], buf[9]}}, *grad[2] = {buf[10], buf[11]};
-  double sq[2] = {0, 0};
-  long evaluations = 0;
-  // evaluate at (pcp, pmom): the two log-likelihood terms; with need_grad the gradients go to grad[]
-  auto evaluate = [&](const double *pcp, const double *pmom, bool need_grad, double terms[2]) -> int {
-    int e = c->cuda(cudaMemcpyAsync(r->cp, pcp, nb, cudaMemcpyDeviceToDevice, st), "copy cp");
-    if (!e) e = c->cuda(cudaMemcpyAsync(r->mom, pmom, nb, cudaMemcpyDeviceToDevice, st), "copy mom");
+  int rc = c->cuda(cudaMalloc(&sq_dev, 4 * sizeof(double)), "cudaMalloc (optimiser)");
+  if (!rc && !optimize_cp) rc = c->cuda(cudaMemcpyAsync(r->cp, cp, nb, cudaMemcpyDefault, st), "copy cp");
+  // groups: [control points,] momenta
+  const int ng = optimize_cp ? 2 : 1;
+  const long sizes[2] = {n, n};
+  double *params[2] = {optimize_cp ? cp : mom, mom};
+  double *aux_out[2] = {optimize_cp ? aux_cp : aux_mom, aux_mom};
+  double *grad_out[2] = {optimize_cp ? grad_cp : grad_mom, grad_mom};
+  FgaEvaluate ev = [&](double *const *p, bool need_grad, double *terms, double *const *g, double *sq) -> int {
+    int e = GBK_OK;
+    if (optimize_cp) e = c->cuda(cudaMemcpyAsync(r->cp, p[0], nb, cudaMemcpyDeviceToDevice, st), "copy cp");
+    if (!e) e = c->cuda(cudaMemcpyAsync(r->mom, p[ng - 1], nb, cudaMemcpyDeviceToDevice, st), "copy mom");
     if (!e) e = r->run();
     double out[5];
     if (!e) e = c->cuda(cudaMemcpyAsync(out, r->out, sizeof out, cudaMemcpyDeviceToHost, st), "read L");
+    double h[2] = {0, 0};
     if (!e && need_grad) {
-      e = c->cuda(cudaMemcpyAsync(grad[0], r->gcp, nb, cudaMemcpyDeviceToDevice, st), "copy grad");
-      if (!e) e = c->cuda(cudaMemcpyAsync(grad[1], r->gmom, nb, cudaMemcpyDeviceToDevice, st), "copy grad");
+      if (optimize_cp) e = c->cuda(cudaMemcpyAsync(g[0], r->gcp, nb, cudaMemcpyDeviceToDevice, st), "copy grad");
+      if (!e) e = c->cuda(cudaMemcpyAsync(g[ng - 1], r->gmom, nb, cudaMemcpyDeviceToDevice, st), "copy grad");
       if (!e) e = c->cuda(dot_f64(st, r->gcp, r->gcp, n, sq_dev, 0), "grad norm");
       if (!e) e = c->cuda(dot_f64(st, r->gmom, r->gmom, n, sq_dev + 1, 0), "grad norm");
-      double h[2];
       if (!e) e = c->cuda(cudaMemcpyAsync(h, sq_dev, sizeof h, cudaMemcpyDeviceToHost, st), "read norms");
-      if (!e) e = c->cuda(cudaStreamSynchronize(st), "sync");
-      if (!e) {
-        sq[0] = optimize_cp ? h[0] : h[1];
-        sq[1] = h[1];
-      }
-    } else if (!e) {
-      e = c->cuda(cudaStreamSynchronize(st), "sync");
     }
+    if (!e) e = c->cuda(cudaStreamSynchronize(st), "sync");
     if (!e) {
       terms[0] = out[1];
       terms[1] = out[2];
-    }
-    ++evaluations;
-    return e;
-  };
-  // groups: g = 0 .. ng-1 map to (cp, mom) or (mom)
-  auto gparam = [&](double *const *pair, int g) { return optimize_cp ? pair[g] : pair[1]; };
-  // new = aux + grad * step (GradientAscentStep); cp is carried unchanged when not optimised
-  auto ascent = [&](double *const *dst, const double *step) -> int {
-    int e = GBK_OK;
-    if (optimize_cp) {
-      e = c->cuda(lincomb(st, dst[0], aux[0], step[0], grad[0], 0.0, nullptr, n), "ascent");
-      if (!e) e = c->cuda(lincomb(st, dst[1], aux[1], step[1], grad[1], 0.0, nullptr, n), "ascent");
-    } else {
-      e = c->cuda(cudaMemcpyAsync(dst[0], aux[0], nb, cudaMemcpyDeviceToDevice, st), "copy cp");
-      if (!e) e = c->cuda(lincomb(st, dst[1], aux[1], step[0], grad[1], 0.0, nullptr, n), "ascent");
-    }
-    return e;
-  };
-  (void)gparam;
-  rc = c->cuda(cudaMemcpyAsync(fixed[0], cp, nb, cudaMemcpyDefault, st), "copy cp");
-  if (!rc) rc = c->cuda(cudaMemcpyAsync(fixed[1], mom, nb, cudaMemcpyDefault, st), "copy mom");
-  if (!rc) rc = c->cuda(cudaMemcpyAsync(aux[0], fixed[0], nb, cudaMemcpyDeviceToDevice, st), "copy");
-  if (!rc) rc = c->cuda(cudaMemcpyAsync(aux[1], fixed[1], nb, cudaMemcpyDeviceToDevice, st), "copy");
-  std::vector<double> hist((size_t)(max_iterations + 1) * 2, 0.0);
-  double t0[2];
-  if (!rc) rc = evaluate(aux[0], aux[1], true, t0);
-  if (rc) {
-    cleanup();
-    return rc;
-  }
-  hist[0] = t0[0];
-  hist[1] = t0[1];
-  double lsq_ref = t0[0] + t0[1];
-  double step[2] = {initial_step, initial_step};
-  double tau = 1.0;
-  int freeze = 1, it = 1, stop = 0;  // stop: 0 max iterations, 1 line search failed, 2 tolerance
-  auto dotsq = [&](const double *s) { return sq[0] * s[0] + (ng == 2 ? sq[1] * s[1] : 0.0); };
-  while (it < max_iterations + 1 && !rc) {
-    bool found = false;
-    double new_terms[2] = {0, 0};
-    for (int li = 0; li < max_line_search && !rc; ++li) {
-      double t[2];
-      if ((rc = ascent(nw, step))) break;
-      if ((rc = evaluate(nw[0], nw[1], false, t))) break;
-      const double q = t[0] + t[1] - lsq_ref - dotsq(step) * shrink;
-      if (q >= 0) {
-        found = true;
-        new_terms[0] = t[0];
-        new_terms[1] = t[1];
-        if (li == 0) ++freeze;
-        break;
-      } else if (ng > 1) {  // multivariate line search: every group but one shrunk
-        freeze = 1;
-        for (int g = 0; g < ng; ++g) step[g] *= shrink;
-        double qs[2], ts[2][2];
-        for (int k = 0; k < ng && !rc; ++k) {
-          double local[2] = {step[0], step[1]};
-          local[k] /= shrink;
-          if ((rc = ascent(prop[k], local))) break;
-          if ((rc = evaluate(prop[k][0], prop[k][1], false, ts[k]))) break;
-          qs[k] = ts[k][0] + ts[k][1] - lsq_ref - dotsq(local) * shrink;
-        }
-        if (rc) break;
-        int idx = 0;
-        for (int k = 1; k < ng; ++k)
-          if (qs[k] > qs[idx]) idx = k;
-        if (qs[idx] >= 0) {
-          std::swap(nw[0], prop[idx][0]);
-          std::swap(nw[1], prop[idx][1]);
-          new_terms[0] = ts[idx][0];
-          new_terms[1] = ts[idx][1];
-          step[idx] /= shrink;
-          found = true;
-          break;
-        }
-      } else {
-        freeze = 1;
-        for (int g = 0; g < ng; ++g) step[g] *= shrink;
+      if (need_grad) {
+        if (optimize_cp) sq[0] = h[0];
+        sq[ng - 1] = h[1];
       }
     }
-    if (rc) break;
-    if (!found) {
-      stop = 1;
-      break;
-    }
-    hist[(size_t)it * 2] = new_terms[0];
-    hist[(size_t)it * 2 + 1] = new_terms[1];
-    double tau_next = (1.0 + std::sqrt(1.0 + 4.0 * tau * tau)) / 2.0;
-    if (freeze > nb_iter_freeze) {
-      for (int g = 0; g < ng; ++g) step[g] *= expand;
-      tau_next = (1.0 + std::sqrt(1.0 + 4.0 * tau * tau / expand)) / 2.0;
-    }
-    const double ts_ = (tau - 1.0) / tau_next;
-    // aux = new + (new - fixed) * tau_scale; fixed = new
-    for (int g = 0; g < 2 && !rc; ++g)
-      rc = c->cuda(lincomb(st, aux[g], nw[g], ts_, nw[g], -ts_, fixed[g], n), "extrapolate");
-    if (rc) break;
-    std::swap(fixed[0], nw[0]);
-    std::swap(fixed[1], nw[1]);
-    tau = tau_next;
-    double ta[2];
-    if ((rc = evaluate(aux[0], aux[1], true, ta))) break;
-    lsq_ref = ta[0] + ta[1];
-    const double cur = (hist[(size_t)(it - 1) * 2] + hist[(size_t)(it - 1) * 2 + 1]) -
-                       (hist[(size_t)it * 2] + hist[(size_t)it * 2 + 1]);
-    const double ref = (hist[0] + hist[1]) - (hist[(size_t)it * 2] + hist[(size_t)it * 2 + 1]);
-    ++it;
-    if (std::fabs(cur) < tolerance * std::fabs(ref)) {
-      stop = 2;
-      break;
-    }
+    return e;
+  };
+  FgaOptions o;
+  o.max_iterations = max_iterations;
+  o.max_line_search = max_line_search;
+  o.nb_iter_freeze = nb_iter_freeze;
+  o.initial_step = initial_step;
+  o.shrink = shrink;
+  o.expand = expand;
+  o.tolerance = tolerance;
+  FgaResult res;
+  if (!rc) rc = fast_gradient_ascent(c, st, ng, sizes, params, o, ev, &res, aux_out, grad_out);
+  if (sq_dev) cudaFree(sq_dev);
+  if (rc) return rc;
+  std::copy(res.history.begin(), res.history.end(), history);
+  *iterations = res.rows;
+  if (info) {
+    info[0] = res.step[0];
+    info[1] = res.step[ng - 1];
+    info[2] = res.tau;
+    info[3] = res.freeze;
+    info[4] = res.sq[0];
+    info[5] = res.sq[ng - 1];
+    info[6] = (double)res.evaluations;
+    info[7] = res.stop;
   }
-  if (!rc) {
-    rc = c->cuda(cudaMemcpyAsync(cp, fixed[0], nb, cudaMemcpyDefault, st), "copy cp");
-    if (!rc) rc = c->cuda(cudaMemcpyAsync(mom, fixed[1], nb, cudaMemcpyDefault, st), "copy mom");
-    if (!rc && aux_cp) rc = c->cuda(cudaMemcpyAsync(aux_cp, aux[0], nb, cudaMemcpyDefault, st), "copy");
-    if (!rc && aux_mom) rc = c->cuda(cudaMemcpyAsync(aux_mom, aux[1], nb, cudaMemcpyDefault, st), "copy");
-    if (!rc && grad_cp) rc = c->cuda(cudaMemcpyAsync(grad_cp, grad[0], nb, cudaMemcpyDefault, st), "copy");
-    if (!rc && grad_mom) rc = c->cuda(cudaMemcpyAsync(grad_mom, grad[1], nb, cudaMemcpyDefault, st), "copy");
-    if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
-  }
-  if (!rc) {
-    const int rows = stop == 1 ? it : std::min(it, max_iterations + 1);
-    std::copy(hist.begin(), hist.begin() + (size_t)rows * 2, history);
-    *iterations = rows;
-    if (info) {
-      info[0] = step[0];
-      info[1] = ng == 2 ? step[1] : step[0];
-      info[2] = tau;
-      info[3] = freeze;
-      info[4] = sq[0];
-      info[5] = sq[1];
-      info[6] = (double)evaluations;
-      info[7] = stop;
-    }
-  }
-  cleanup();
-  return rc;
+  return GBK_OK;
 }
 
 void gbk_registration_destroy(gbk_registration *r) {

@@ -244,6 +244,31 @@ class Atlas:
     def graph_launches(self) -> int:
         return int(self.ctx.lib.gbk_atlas_graph_launches(self.h))
 
+    def set_template_smoothing(self, width: float):
+        """Template-gradient smoothing width (ConvolveGradTemplate); 0 = the L2 gradient."""
+        self.ctx.check(self.ctx.lib.gbk_atlas_set_template_smoothing(self.h, float(width)))
+
+    def optimize(self, cp, tmpl, mom, max_iterations: int, initial_step: float = 1e-3, optimize_cp: bool = True,
+                 optimize_template: bool = True, max_line_search: int = 10, shrink: float = 0.5,
+                 expand: float = 1.2, tolerance: float = 1e-4, nb_iter_freeze: int = 3):
+        """The reference's FastGradientAscent over control points, template points and momenta, on
+        the device (gbk_atlas_optimize). Returns a dict: cp, tmpl, mom (final), history, step and
+        grad_sq_norms per optimised group, tau, freeze_counter, evaluations, stopped."""
+        cp, tmpl, mom = (np.array(v, dtype=np.float64) for v in (cp, tmpl, mom))
+        hist = np.zeros((max_iterations + 1, 2))
+        info = np.zeros(10)
+        iters = ctypes.c_int(0)
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_atlas_optimize(
+            self.h, c(cp), c(tmpl), c(mom), int(optimize_cp), int(optimize_template), int(max_iterations),
+            float(initial_step), int(max_line_search), float(shrink), float(expand), float(tolerance),
+            int(nb_iter_freeze), c(hist), ctypes.byref(iters), c(info)))
+        groups = [g for g, on in ((0, optimize_cp), (1, optimize_template), (2, True)) if on]
+        return {"cp": cp, "tmpl": tmpl, "mom": mom, "history": hist[:iters.value], "step": info[groups],
+                "grad_sq_norms": info[[5 + g for g in groups]], "tau": float(info[3]),
+                "freeze_counter": int(info[4]), "evaluations": int(info[8]),
+                "stopped": Registration.STOP[int(info[9])]}
+
     def close(self):
         if getattr(self, "h", None):
             self.ctx.lib.gbk_atlas_destroy(self.h)

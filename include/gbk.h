@@ -322,6 +322,22 @@ int gbk_atlas_step(gbk_atlas *atlas, const double *mom, double *loglik, double *
                    double *grad_cp, double *grad_tmpl);
 int gbk_atlas_set_graph(gbk_atlas *atlas, int enable);
 long long gbk_atlas_graph_launches(const gbk_atlas *atlas);
+/* Smooths the template gradient by a Gaussian of this width over the template points
+ * (AbstractAtlas::ConvolveGradTemplate, AbstractAtlas.cxx:724-748; the reference uses
+ * smoothing-kernel-width-ratio x deformation kernel width, estimate_atlas.cxx:457); 0 (default)
+ * returns the L2 gradient. */
+int gbk_atlas_set_template_smoothing(gbk_atlas *atlas, double width);
+/* FastGradientAscent (FastGradientAscent.cxx:48-300) of the atlas over its control points
+ * (optimize_cp), template points (optimize_template) and all subjects' momenta, on the device.
+ * cp (ncp x 3), tmpl (nv x 3), mom (nsub x ncp x 3): start point in, final fixed effects out (host or
+ * device). history: one [data, regularity] row per iteration (at most max_iterations + 1,
+ * *iterations of them). info (10 doubles, optional): final steps (cp, template, momenta), tau,
+ * freeze counter, squared gradient norms (cp, template as <L2, smoothed>, momenta), evaluations,
+ * stop reason (0 max iterations, 1 line search, 2 tolerance). */
+int gbk_atlas_optimize(gbk_atlas *atlas, double *cp, double *tmpl, double *mom, int optimize_cp,
+                       int optimize_template, int max_iterations, double initial_step, int max_line_search,
+                       double shrink, double expand, double tolerance, int nb_iter_freeze, double *history,
+                       int *iterations, double *info);
 void gbk_atlas_destroy(gbk_atlas *atlas);
 
 /* ---- tuning ------------------------------------------------------------------------------ */

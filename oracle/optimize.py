@@ -125,6 +125,57 @@ def registration_evaluator(K, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T: int, si
     return evaluate
 
 
+def atlas_evaluator(K, tmpl_cells, targets, T: int, sigma_def: float, sigma_data: float, data_sigma2: float,
+                    kind: str = "currents", heun: bool = True, smoothing_width: float = 0.0,
+                    optimize_cp: bool = True, optimize_template: bool = True, cp=None, tmpl=None):
+    """evaluate() of a DeterministicAtlas over the subjects `targets` ([(points, cells)]): parameter
+    groups in the reference's order [ControlPoints] [TemplateData] Momenta (one ncp x d block per
+    subject, stacked). The template gradient is the sum over subjects of -theta_s(0)
+    (AbstractAtlas.cxx:559-613) smoothed by a Gaussian of width smoothing_width over the template
+    points (ConvolveGradTemplate, :724-748; no smoothing at width 0), and its squared norm is
+    <L2, smoothed> (DeterministicAtlas.cxx:232). Frozen groups take their values from `cp` /
+    `tmpl`."""
+    from .deformation import registration
+    cp_frozen, tmpl_frozen = cp, tmpl
+
+    def evaluate(params, need_grad):
+        k = 0
+        cp = params[k] if optimize_cp else cp_frozen
+        k += int(optimize_cp)
+        tmpl = params[k] if optimize_template else tmpl_frozen
+        k += int(optimize_template)
+        mom = params[k]
+        data = reg = 0.0
+        g_cp = np.zeros_like(cp)
+        g_t = np.zeros_like(tmpl)
+        g_mom = np.zeros_like(mom)
+        for s, (pts, cells) in enumerate(targets):
+            L, gc, gm, info = registration(K, cp, mom[s], tmpl, tmpl_cells, pts, cells, T, sigma_def, sigma_data,
+                                           data_sigma2, kind=kind, heun=heun)
+            d_s = -0.5 * info["match"] / data_sigma2
+            data += d_s
+            reg += L - d_s
+            g_cp += gc
+            g_mom[s] = gm
+            g_t -= info["theta"][0]
+        terms = [data, reg]
+        if not need_grad:
+            return terms, None, None
+        grads, sq = [], []
+        if optimize_cp:
+            grads.append(g_cp)
+            sq.append(float(np.sum(g_cp * g_cp)))
+        if optimize_template:
+            sob = K.convolve(tmpl, tmpl, g_t, smoothing_width) if smoothing_width >= 1e-20 else g_t
+            grads.append(sob)
+            sq.append(float(np.sum(g_t * sob)))
+        grads.append(g_mom)
+        sq.append(float(np.sum(g_mom * g_mom)))
+        return terms, grads, np.array(sq)
+
+    return evaluate
+
+
 def initial_control_points(points, spacing: float):
     """Regular grid over a bounding box (AbstractAtlas.cxx:240-330 without the image criterion):
     per axis, spacing apart, centred so the leftover extent is split evenly; x outermost."""

@@ -37,7 +37,7 @@ FLOPS_PER_PAIR_PASS = 26  # FP32 flops per pair of one fused Convolve + alpha-gr
 LANE_OPS_PER_PAIR_PASS = 16  # FP32 lane instructions per pair of that pass (FMA = 1)
 # DRAM bytes (read + write) of one fused pass at N = M = 1e6 from one ncu capture of this kernel
 # (profiles/pair_kernel_fused_N1e6_traffic.md); None for other sizes.
-TRAFFIC_1E6 = 378095616 + 299555840
+TRAFFIC_1E6 = 384661248 + 313689600
 SMS = 152
 FP32_LANES = 128
 

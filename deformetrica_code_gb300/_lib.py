@@ -25,6 +25,8 @@ GBK_ORDER_AUTO = 0
 GBK_ORDER_OFF = 1
 GBK_ORDER_SPATIAL = 2
 GBK_ORDER_SPATIAL_NOPRUNE = 3
+GBK_GRADIENT_REFERENCE = 0
+GBK_GRADIENT_EXACT = 1
 
 OPS = {
     "convolve": 0,
@@ -55,6 +57,8 @@ SIGNATURES = {
     "gbk_evaluated_pairs": (ctypes.c_longlong, [_P]),
     "gbk_set_order": (_I, [_P, _I]),
     "gbk_get_order": (_I, [_P]),
+    "gbk_set_gradient_mode": (_I, [_P, _I]),
+    "gbk_get_gradient_mode": (_I, [_P]),
     "gbk_synchronize": (_I, [_P]),
     "gbk_launch_count": (ctypes.c_longlong, [_P]),
     "gbk_convolve": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P]),
@@ -83,6 +87,10 @@ SIGNATURES = {
     "gbk_varifold_match": (_I, [_P, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
     "gbk_curve_currents_match": (_I, [_P, _I, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
     "gbk_curve_varifold_match": (_I, [_P, _I, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
+    "gbk_pointcloud_match": (_I, [_P, _I, _L, _P, _P, _L, _P, _P, _D, _P, _P]),
+    "gbk_volume_match": (_I, [_P, _I, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
+    "gbk_landmark_match": (_I, [_P, _I, _L, _P, _P, _P, _P]),
+    "gbk_registration_set_point_weights": (_I, [_P, _P, _P]),
     "gbk_registration_create": (_I, [_P, _I, _L, _L, _P, _L, _P, _L, _P, _L, _P, _I, _D, _D, _D, _I, _I,
                                      ctypes.POINTER(_P)]),
     "gbk_registration_step": (_I, [_P, _P, _P, _P, _P, _P]),

@@ -433,6 +433,16 @@ int gbk_set_order(gbk_ctx *c, int order) {
 
 int gbk_get_order(const gbk_ctx *c) { return c ? c->order : -1; }
 
+int gbk_set_gradient_mode(gbk_ctx *c, int mode) {
+  if (!c) return GBK_ERR_ARG;
+  if (mode != GBK_GRADIENT_REFERENCE && mode != GBK_GRADIENT_EXACT)
+    return c->fail(GBK_ERR_ARG, "unknown gradient mode %d", mode);
+  c->gradient_mode = mode;
+  return GBK_OK;
+}
+
+int gbk_get_gradient_mode(const gbk_ctx *c) { return c ? c->gradient_mode : -1; }
+
 int gbk_synchronize(gbk_ctx *c) {
   GBK_GUARD(c);
   return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");

@@ -35,6 +35,7 @@ struct gbk_ctx {
   DevBuf reduce;              // FP64 reductions and small temporaries
   DevBuf tmp;                 // op temporaries (e.g. K w for the kernel norm)
   int order = 0;              // GBK_ORDER_* (0 = automatic)
+  int gradient_mode = 0;      // GBK_GRADIENT_* of the point-cloud and volume data terms
   struct SortSlot {           // a point set in spatial order: perm, sorted keys, box
     DevBuf buf;
     const double *ptr = nullptr;

@@ -144,15 +144,22 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   *out = nullptr;
   c->err.clear();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
-  if (data_kind < 0 || data_kind > 3)
-    return c->fail(GBK_ERR_ARG, "data_kind must be 0/1 (surface currents/varifold) or 2/3 (curve currents/varifold)");
-  const int cell = data_kind < 2 ? 3 : 2;
-  if (cell == 3 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "surface registration needs d = 3");
+  if (data_kind < 0 || data_kind > 6)
+    return c->fail(GBK_ERR_ARG, "data_kind must be 0/1 (surface currents/varifold), 2/3 (curve currents/varifold), "
+                                "4 (point cloud), 5 (volume mesh) or 6 (landmarks)");
   if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d not supported", d);
+  // (data term kind, vertices per cell) of each data_kind
+  static const int kinds[7] = {0, 1, 0, 1, 2, 2, 3};
+  const int cell = data_kind < 2 ? 3 : data_kind < 4 ? 2 : data_kind == 5 ? d + 1 : 1;
+  if (data_kind < 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "surface registration needs d = 3");
+  if (cell == 1) {
+    nf = nv;
+    nf_t = nv_t;
+  }
   if (ncp <= 0 || nv <= 0 || nf <= 0 || nv_t <= 0 || nf_t <= 0 || T < 2)
     return c->fail(GBK_ERR_ARG, "bad sizes");
   if (!(data_sigma2 > 0)) return c->fail(GBK_ERR_ARG, "data_sigma2 must be positive");
-  if (!tmpl_pts || !tmpl_tris || !tgt_pts || !tgt_tris) return c->fail(GBK_ERR_ARG, "null pointer");
+  if (!tmpl_pts || !tgt_pts || (cell > 1 && (!tmpl_tris || !tgt_tris))) return c->fail(GBK_ERR_ARG, "null pointer");
   gbk_registration *r = new gbk_registration();
   r->c = c;
   r->d = d;
@@ -164,15 +171,17 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   r->sigma_data = sigma_data;
   r->data_sigma2 = data_sigma2;
   int rc = c->cuda(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "stream");
-  std::vector<int> th((size_t)nf * cell), tth((size_t)nf_t * cell);
-  if (!rc) {
+  std::vector<int> th, tth;
+  if (!rc && cell > 1) {
+    th.resize((size_t)nf * cell);
+    tth.resize((size_t)nf_t * cell);
     cudaMemcpy(th.data(), tmpl_tris, th.size() * sizeof(int), cudaMemcpyDefault);
     cudaMemcpy(tth.data(), tgt_tris, tth.size() * sizeof(int), cudaMemcpyDefault);
-    rc = c->cuda(cudaGetLastError(), "copy triangles");
+    rc = c->cuda(cudaGetLastError(), "copy cells");
   }
   cudaStream_t saved = c->stream;
   c->stream = r->stream;
-  if (!rc) rc = r->surf.init(c, data_kind & 1, d, cell, sigma_data, nv, nf, th.data(), nv_t, nf_t, tth.data());
+  if (!rc) rc = r->surf.init(c, kinds[data_kind], d, cell, sigma_data, nv, nf, th.data(), nv_t, nf_t, tth.data());
   const long n = ncp * d, m = nv * d, rows = std::max(ncp, nv);
   struct {
     double **p;
@@ -200,6 +209,22 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   }
   *out = r;
   return GBK_OK;
+}
+
+int gbk_registration_set_point_weights(gbk_registration *r, const double *w_tmpl, const double *w_tgt) {
+  if (!r) return GBK_ERR_ARG;
+  gbk_ctx *c = r->c;
+  c->err.clear();
+  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
+  cudaStream_t saved = c->stream;
+  c->stream = r->stream;
+  int rc;
+  {
+    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    rc = r->surf.set_weights(c, w_tmpl, w_tgt);  // same buffers: a captured graph reads the new weights
+  }
+  c->stream = saved;
+  return rc;
 }
 
 int gbk_registration_set_graph(gbk_registration *r, int enable) {

@@ -121,27 +121,83 @@ def curve_varifold_match(pts, segs, pts_t, segs_t, sigma, grad=True, context: Co
     return _surface("gbk_curve_varifold_match", context, pts, segs, pts_t, segs_t, sigma, grad, True)
 
 
+def pointcloud_match(pts, w, pts_t, w_t, sigma, grad=True, context: Context | None = None):
+    """Weighted point-cloud distance and its gradient w.r.t. pts (PointCloud.cxx:104-198); w, w_t
+    are per-point weights (None: unit weights). The gradient follows the context's gradient mode."""
+    ctx = context or Context()
+    pts, pts_t = _f64(pts), _f64(pts_t)
+    w = None if w is None else _f64(w)
+    w_t = None if w_t is None else _f64(w_t)
+    if pts.shape[1] != pts_t.shape[1] or (w is not None and len(w) != len(pts)) or (
+            w_t is not None and len(w_t) != len(pts_t)):
+        raise ValueError("point and weight counts or dimensions disagree")
+    match = np.zeros(1)
+    g = np.zeros(pts.shape) if grad else None
+    ctx.bind_stream()
+    ctx.check(ctx.lib.gbk_pointcloud_match(ctx.h, pts.shape[1], pts.shape[0], _ptr(pts), _ptr(w), pts_t.shape[0],
+                                           _ptr(pts_t), _ptr(w_t), float(sigma), ctypes.c_void_p(match.ctypes.data),
+                                           _ptr(g)))
+    return float(match[0]), g
+
+
+def volume_match(pts, cells, pts_t, cells_t, sigma, grad=True, context: Context | None = None):
+    """Oriented volume-mesh distance (tetrahedra in 3-D, triangles in 2-D) and its gradient w.r.t.
+    pts (OrientedVolumeMesh.cxx:115-280). The gradient follows the context's gradient mode."""
+    return _surface("gbk_volume_match", context, pts, cells, pts_t, cells_t, sigma, grad, True)
+
+
+def landmark_match(pts, pts_t, grad=True, context: Context | None = None):
+    """|S - T|^2 and 2 (S - T) over corresponding points (Landmark.cxx:288-322)."""
+    ctx = context or Context()
+    pts, pts_t = _f64(pts), _f64(pts_t)
+    if tuple(pts.shape) != tuple(pts_t.shape):
+        raise ValueError("landmark objects need the same number of points")
+    match = np.zeros(1)
+    g = np.zeros(pts.shape) if grad else None
+    ctx.bind_stream()
+    ctx.check(ctx.lib.gbk_landmark_match(ctx.h, pts.shape[1], pts.shape[0], _ptr(pts), _ptr(pts_t),
+                                         ctypes.c_void_p(match.ctypes.data), _ptr(g)))
+    return float(match[0]), g
+
+
 class Registration:
     """One subject of DeterministicAtlas with a frozen template, replayed from a CUDA graph: a
-    triangle mesh in 3-D (kind "currents" / "varifold") or a polyline of 2-point segments in 2-D or
-    3-D ("curve_currents" / "curve_varifold"); the dimension is the template's."""
+    triangle mesh in 3-D (kind "currents" / "varifold"), a polyline of 2-point segments in 2-D or
+    3-D ("curve_currents" / "curve_varifold"), a weighted point cloud ("pointcloud": cells are
+    ignored, weights by `tmpl_weights` / `tgt_weights`), a volume mesh of (d + 1)-vertex cells
+    ("volume") or landmarks ("landmark"); the dimension is the template's."""
 
-    KINDS = {"currents": 0, "varifold": 1, "curve_currents": 2, "curve_varifold": 3}
+    KINDS = {"currents": 0, "varifold": 1, "curve_currents": 2, "curve_varifold": 3, "pointcloud": 4, "volume": 5,
+             "landmark": 6}
 
     def __init__(self, ncp: int, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T: int, sigma_def: float,
                  sigma_data: float, data_sigma2: float, kind: str = "currents", heun: bool = True,
-                 context: Context | None = None):
+                 context: Context | None = None, tmpl_weights=None, tgt_weights=None):
         self.ctx = context or Context()
         self.ncp, self.T = int(ncp), int(T)
-        tp, tt = _f64(tmpl_pts), _i32(tmpl_tris)
-        gp, gt = _f64(tgt_pts), _i32(tgt_tris)
-        self.nv, self.d = tp.shape[0], tp.shape[1]
+        tp, gp = _f64(tmpl_pts), _f64(tgt_pts)
+        pointwise = kind in ("pointcloud", "landmark")
+        tt = _i32(np.zeros((tp.shape[0], 1)) if pointwise else tmpl_tris)
+        gt = _i32(np.zeros((gp.shape[0], 1)) if pointwise else tgt_tris)
+        self.nv, self.d, self.nv_t = tp.shape[0], tp.shape[1], gp.shape[0]
+        if kind == "landmark" and gp.shape != tp.shape:
+            raise ValueError("landmark objects need the same number of points")
         h = ctypes.c_void_p()
         self.ctx.check(self.ctx.lib.gbk_registration_create(
             self.ctx.h, self.d, self.ncp, tp.shape[0], _ptr(tp), tt.shape[0], _ptr(tt), gp.shape[0], _ptr(gp),
             gt.shape[0], _ptr(gt), self.T, float(sigma_def), float(sigma_data), float(data_sigma2),
             self.KINDS[kind], int(heun), ctypes.byref(h)))
         self.h = h
+        if tmpl_weights is not None or tgt_weights is not None:
+            self.set_point_weights(tmpl_weights, tgt_weights)
+
+    def set_point_weights(self, tmpl_weights=None, tgt_weights=None):
+        """Point weights of a point-cloud registration (None keeps the current ones)."""
+        w = None if tmpl_weights is None else _f64(tmpl_weights)
+        wt = None if tgt_weights is None else _f64(tgt_weights)
+        if (w is not None and len(w) != self.nv) or (wt is not None and len(wt) != self.nv_t):
+            raise ValueError("one weight per point")
+        self.ctx.check(self.ctx.lib.gbk_registration_set_point_weights(self.h, _ptr(w), _ptr(wt)))
 
     def set_graph(self, enable: bool):
         self.ctx.check(self.ctx.lib.gbk_registration_set_graph(self.h, int(enable)))

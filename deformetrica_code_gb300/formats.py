@@ -1,7 +1,9 @@
 """On-disk formats of the reference used for end-to-end parity.
 
-* `read_vtk_polydata`: legacy VTK polydata (ASCII), the mesh format of the reference's data sets
-  (read by DeformableObjectReader.cxx through VTK): POINTS and POLYGONS / LINES sections.
+* `read_vtk_polydata`: legacy VTK polydata or unstructured grid (ASCII), the mesh format of the
+  reference's data sets (read by DeformableObjectReader.cxx through VTK): POINTS and POLYGONS /
+  LINES / VERTICES / CELLS sections; `read_vtk_point_weights`: the one-component point-data scalars
+  a point cloud takes its weights from (PointCloud.cxx:204-225).
 * `read_deformation_state`: the optimiser state the reference serialises at the end of an
   estimation (FastGradientAscent.cxx:296-305 and 313-322, written by DeformationState,
   SerializeDeformationState.h) as a Boost text archive. DeformationState keeps one queue per value
@@ -23,8 +25,9 @@ _B64 = re.compile(r"[A-Za-z0-9+/]+=*")
 
 def read_vtk_polydata(path: str):
     """Points (n x 3 float64) and cells (list of index tuples, or an int32 array when every cell has
-    the same size) of an ASCII legacy VTK polydata file. Points declared `float` are rounded to
-    single precision, as VTK stores them before the reference converts them to double."""
+    the same size) of an ASCII legacy VTK polydata or unstructured-grid file (tetrahedra of
+    OrientedVolumeMesh come as an unstructured grid's CELLS). Points declared `float` are rounded
+    to single precision, as VTK stores them before the reference converts them to double."""
     with open(path) as f:
         tokens = f.read().split()
     i = 0
@@ -39,7 +42,7 @@ def read_vtk_polydata(path: str):
                 vals = vals.astype(np.float32).astype(np.float64)
             pts = vals.reshape(n, 3)
             i += 3 + 3 * n
-        elif t in ("POLYGONS", "LINES", "TRIANGLE_STRIPS"):
+        elif t in ("POLYGONS", "LINES", "VERTICES", "CELLS", "TRIANGLE_STRIPS"):
             if t == "TRIANGLE_STRIPS":
                 raise ValueError("triangle strips are not supported")
             m = int(tokens[i + 1])
@@ -51,6 +54,10 @@ def read_vtk_polydata(path: str):
             i = j
         elif t == "BINARY":
             raise ValueError("binary VTK files are not supported")
+        elif t in ("CELL_TYPES", "POINT_DATA", "CELL_DATA"):
+            i += 2 + (int(tokens[i + 1]) if t == "CELL_TYPES" else 0)
+            if t != "CELL_TYPES":
+                break  # attribute data follows the geometry
         else:
             i += 1
     if pts is None:
@@ -58,6 +65,41 @@ def read_vtk_polydata(path: str):
     if cells and all(len(c) == len(cells[0]) for c in cells):
         return pts, np.array(cells, dtype=np.int32)
     return pts, cells
+
+
+def read_vtk_point_weights(path: str):
+    """The point-data SCALARS of a legacy VTK file as float64 (one component), or None when the
+    file has none or they do not match the point count (the reference then uses unit weights,
+    PointCloud.cxx:204-225)."""
+    with open(path) as f:
+        tokens = f.read().split()
+    n_pts = None
+    i = 0
+    while i < len(tokens):
+        t = tokens[i].upper()
+        if t == "POINTS":
+            n_pts = int(tokens[i + 1])
+            i += 3
+        elif t == "POINT_DATA":
+            n = int(tokens[i + 1])
+            j = i + 2
+            while j < len(tokens) and tokens[j].upper() not in ("SCALARS", "CELL_DATA"):
+                j += 1
+            if j >= len(tokens) or tokens[j].upper() != "SCALARS":
+                return None
+            ncomp = 1
+            j += 3  # SCALARS name type
+            if j < len(tokens) and tokens[j].isdigit():
+                ncomp = int(tokens[j])
+                j += 1
+            if j < len(tokens) and tokens[j].upper() == "LOOKUP_TABLE":
+                j += 2
+            if ncomp != 1 or n != n_pts:
+                return None
+            return np.array(tokens[j:j + n], dtype=np.float64)
+        else:
+            i += 1
+    return None
 
 
 def reorient_like_reader(pts, tris, flip: bool = True):

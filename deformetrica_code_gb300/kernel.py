@@ -92,6 +92,14 @@ class Context:
     def get_order(self) -> int:
         return int(self.lib.gbk_get_order(self.h))
 
+    def set_gradient_mode(self, mode: int):
+        """GBK_GRADIENT_REFERENCE (the reference's point-cloud and volume-mesh gradient formulas,
+        default) or GBK_GRADIENT_EXACT (the derivatives of their matches) (include/gbk.h)."""
+        self.check(self.lib.gbk_set_gradient_mode(self.h, mode))
+
+    def get_gradient_mode(self) -> int:
+        return int(self.lib.gbk_get_gradient_mode(self.h))
+
     def set_split(self, n: int):
         self.check(self.lib.gbk_set_split(self.h, n))
 

@@ -62,6 +62,15 @@ enum { GBK_MODE_F32C = 0, GBK_MODE_F64 = 1 };
  * The reference has no counterpart: ExactKernel always visits every pair in row order. */
 enum { GBK_ORDER_AUTO = 0, GBK_ORDER_OFF = 1, GBK_ORDER_SPATIAL = 2, GBK_ORDER_SPATIAL_NOPRUNE = 3 };
 
+/* Gradient formula of the point-cloud and volume-mesh data terms (gbk_set_gradient_mode).
+ *  REFERENCE: the reference's formulas. PointCloud::ComputeMatchGradient (PointCloud.cxx:150-198)
+ *    returns 2 (G_S + G_T), adding the target term the match subtracts; OrientedVolumeMesh
+ *    (OrientedVolumeMesh.cxx:159-280) differentiates the signed volume although the match uses its
+ *    absolute value, which agrees with EXACT on positively oriented cells only.
+ *  EXACT: the derivative of the match: 2 (G_S - G_T) for point clouds, the determinant's sign
+ *    applied per cell for volume meshes. */
+enum { GBK_GRADIENT_REFERENCE = 0, GBK_GRADIENT_EXACT = 1 };
+
 /* Operation identifiers (for gbk_autotune). */
 enum {
   GBK_OP_CONVOLVE = 0,
@@ -95,6 +104,10 @@ int gbk_get_mode(const gbk_ctx *ctx);
  * registration and atlas steps always use GBK_ORDER_OFF. No counterpart in the reference. */
 int gbk_set_order(gbk_ctx *ctx, int order);
 int gbk_get_order(const gbk_ctx *ctx);
+/* Sets the GBK_GRADIENT_* formula of later point-cloud and volume-mesh data terms (default
+ * GBK_GRADIENT_REFERENCE; a registration takes the mode current at its creation). */
+int gbk_set_gradient_mode(gbk_ctx *ctx, int mode);
+int gbk_get_gradient_mode(const gbk_ctx *ctx);
 /* Waits for all work queued on the context's stream. */
 int gbk_synchronize(gbk_ctx *ctx);
 /* Number of the library's own kernels launched on this context so far. */
@@ -240,6 +253,21 @@ int gbk_curve_currents_match(gbk_ctx *ctx, int d, long nv, const double *pts, lo
 int gbk_curve_varifold_match(gbk_ctx *ctx, int d, long nv, const double *pts, long nseg, const int *segs,
                              long nv_t, const double *pts_t, long nseg_t, const int *segs_t, double sigma,
                              double *match, double *grad);
+/* PointCloud::ComputeMatch / ComputeMatchGradient (PointCloud.cxx:104-198): weighted points
+ * (w, w_t: one weight per point, NULL = unit weights as UpdatePointWeights, :204-225),
+ * match = |T|^2 + |S|^2 - 2 sum_i (K_S w_S)(t_i) w_T,i, gradient per gbk_set_gradient_mode. */
+int gbk_pointcloud_match(gbk_ctx *ctx, int d, long n, const double *pts, const double *w, long n_t,
+                         const double *pts_t, const double *w_t, double sigma, double *match, double *grad);
+/* OrientedVolumeMesh::ComputeMatch / ComputeMatchGradient (OrientedVolumeMesh.cxx:115-280):
+ * cells of d + 1 vertices (tetrahedra in 3-D, triangles in 2-D) carry their centres and volumes
+ * |det(p_1 - p_0, ..., p_d - p_0)| / d!; gradient per gbk_set_gradient_mode. */
+int gbk_volume_match(gbk_ctx *ctx, int d, long nv, const double *pts, long ncell, const int *cells, long nv_t,
+                     const double *pts_t, long ncell_t, const int *cells_t, double sigma, double *match,
+                     double *grad);
+/* Landmark::ComputeMatch / ComputeMatchGradient (Landmark.cxx:288-322): |S - T|_F^2 and 2 (S - T)
+ * over n corresponding points. */
+int gbk_landmark_match(gbk_ctx *ctx, int d, long n, const double *pts, const double *pts_t, double *match,
+                       double *grad);
 
 /* ---- registration iteration (shooting + flow + data term + adjoint), CUDA-graph replay ---- */
 
@@ -248,8 +276,10 @@ typedef struct gbk_registration gbk_registration;
 /* One subject of DeterministicAtlas with a frozen template (DeterministicAtlas.cxx:99-154,
  * AbstractAtlas.cxx:559-613): template (nv points, nf cells) deformed by ncp control points over T
  * time points, matched to the target with data_kind 0 = surface currents, 1 = surface varifold
- * (triangles, d = 3), 2 = curve currents, 3 = curve varifold (2-point segments, d = 2 or 3). All
- * device memory is allocated here. */
+ * (triangles, d = 3), 2 = curve currents, 3 = curve varifold (2-point segments, d = 2 or 3),
+ * 4 = point cloud (nf = nv, nf_t = nv_t, the cell arrays are ignored and may be NULL; unit weights
+ * until gbk_registration_set_point_weights), 5 = volume mesh (cells of d + 1 vertices), 6 =
+ * landmarks (nv_t = nv, cells ignored). All device memory is allocated here. */
 int gbk_registration_create(gbk_ctx *ctx, int d, long ncp, long nv, const double *tmpl_pts,
                             long nf, const int *tmpl_tris, long nv_t, const double *tgt_pts,
                             long nf_t, const int *tgt_tris, int T, double sigma_def,
@@ -261,6 +291,10 @@ int gbk_registration_create(gbk_ctx *ctx, int d, long ncp, long nv, const double
  * graph, later calls replay it. */
 int gbk_registration_step(gbk_registration *reg, const double *cp, const double *mom,
                           double *loglik, double *grad_cp, double *grad_mom);
+/* Point weights of a point-cloud registration (data_kind 4): template (nv) and target (nv_t)
+ * weights, host or device; either may be NULL to keep the current ones. A captured iteration
+ * graph reads the new weights (same device buffers). */
+int gbk_registration_set_point_weights(gbk_registration *reg, const double *w_tmpl, const double *w_tgt);
 /* 0 disables graph capture (every step launches the kernels directly). */
 int gbk_registration_set_graph(gbk_registration *reg, int enable);
 /* Copies of the last step's trajectories (T x ncp x d or T x nv x d); any pointer may be NULL. */

@@ -2,8 +2,9 @@
 
 Surface currents: OrientedSurfaceMesh.cxx:124-352. Surface varifolds: NonOrientedSurfaceMesh.cxx:
 124-378. Curve currents: OrientedPolyLine.cxx (ComputeMatch, ComputeMatchGradient,
-UpdateCentersTangents, UpdateSelfNorm). Curve varifolds: NonOrientedPolyLine.cxx:125-300, 364-378.
-Every kernel sum goes through the kernel oracle, as the reference goes through its kernel object.
+UpdateCentersTangents, UpdateSelfNorm). Curve varifolds: NonOrientedPolyLine.cxx:125-300, 364-378. Point clouds:
+PointCloud.cxx:104-254. Volume meshes: OrientedVolumeMesh.cxx:115-367. Landmarks:
+Landmark.cxx:288-322. Every kernel sum goes through the kernel oracle, as the reference goes through its kernel object.
 Meshes are (points nv x d, cells nf x 3 or nf x 2 int) arrays; the reference reads them from VTK.
 """
 from __future__ import annotations
@@ -187,9 +188,112 @@ def curve_varifold_match_gradient(K: OracleLib, sigma, pts_s, segs_s, pts_t, seg
     return grad
 
 
+def point_weights(pts, w):
+    """PointCloud::UpdatePointWeights, :204-225: the point-data scalars, unit weights without them."""
+    return np.ones(len(pts)) if w is None else np.asarray(w, dtype=np.float64).reshape(-1)
+
+
+def pointcloud_match(K: OracleLib, sigma, pts_s, w_s, pts_t, w_t):
+    """PointCloud::ComputeMatch, :104-146: |T|^2 + |S|^2 - 2 sum_i (K_S w_S)(t_i) w_T,i, the norms
+    sum_i w_i (K w)(p_i) (UpdateSelfNorm, :229-250). The "cells" of a point cloud are its weights."""
+    ws, wt = point_weights(pts_s, w_s), point_weights(pts_t, w_t)
+    m = float(np.sum(K.convolve(pts_t, pts_t, wt[:, None], sigma)[:, 0] * wt))
+    m += float(np.sum(K.convolve(pts_s, pts_s, ws[:, None], sigma)[:, 0] * ws))
+    sdt = K.convolve(pts_t, pts_s, ws[:, None], sigma)[:, 0]
+    return m - float(np.sum(sdt * (2.0 * wt)))
+
+
+def pointcloud_match_gradient(K: OracleLib, sigma, pts_s, w_s, pts_t, w_t, exact: bool = False):
+    """PointCloud::ComputeMatchGradient, :150-198: 2 (G_S + G_T), G_X = ConvolveGradient(S, w_S)
+    with sources X and their weights. The reference adds the target term; the derivative of the
+    match subtracts it (exact=True)."""
+    ws, wt = point_weights(pts_s, w_s), point_weights(pts_t, w_t)
+    g_s = K.grad_alpha(pts_s, pts_s, ws[:, None], sigma, ws[:, None])
+    g_t = K.grad_alpha(pts_s, pts_t, wt[:, None], sigma, ws[:, None])
+    return (g_s - g_t) * 2.0 if exact else (g_s + g_t) * 2.0
+
+
+def volume_centers(pts, cells):
+    """OrientedVolumeMesh::UpdateCentersNormals, :299-335: c = mean of the d + 1 vertices (summed in
+    cell order), volume = |det(p_1 - p_0, ..., p_d - p_0)| / (6 in 3-D, 2 in 2-D); also returns
+    the sign of the determinant."""
+    d = pts.shape[1]
+    c = pts[cells[:, 0]].copy()
+    for k in range(1, d + 1):
+        c += pts[cells[:, k]]
+    c /= d + 1.0
+    edges = np.stack([pts[cells[:, k]] - pts[cells[:, 0]] for k in range(1, d + 1)], axis=1)
+    det = np.linalg.det(edges)
+    return c, np.abs(det) / (6.0 if d == 3 else 2.0), np.where(det < 0, -1.0, 1.0)
+
+
+def volume_match(K: OracleLib, sigma, pts_s, cells_s, pts_t, cells_t):
+    """OrientedVolumeMesh::ComputeMatch, :115-155: |T|^2 + |S|^2 - 2 sum_j V_T,j (K_S V_S)(c_T,j)."""
+    cs, vs, _ = volume_centers(pts_s, cells_s)
+    ct, vt, _ = volume_centers(pts_t, cells_t)
+    m = currents_norm(K, sigma, ct, vt[:, None]) + currents_norm(K, sigma, cs, vs[:, None])
+    return m - 2.0 * float(np.sum(K.convolve(ct, cs, vs[:, None], sigma)[:, 0] * vt))
+
+
+# the reference scales the 3-D volume term by the single-precision constant 1.0f / 3.0f
+THIRD_F32 = float(np.float32(1.0) / np.float32(3.0))
+
+
+def volume_corner_vectors(pts, cells):
+    """d det / d p_k of every cell, written as OrientedVolumeMesh::ComputeMatchGradient does
+    (:214-227 in 3-D, :254-266 in 2-D): (ncells, d + 1, d)."""
+    d = pts.shape[1]
+    p = [pts[cells[:, k]] for k in range(d + 1)]
+    if d == 3:
+        return np.stack([np.cross(p[3] - p[1], p[2] - p[1]), np.cross(p[2] - p[0], p[3] - p[0]),
+                         np.cross(p[3] - p[0], p[1] - p[0]), np.cross(p[1] - p[0], p[2] - p[0])], axis=1)
+    def perp(a, b):  # (a_y - b_y, b_x - a_x)
+        return np.stack([a[:, 1] - b[:, 1], b[:, 0] - a[:, 0]], axis=1)
+    return np.stack([perp(p[1], p[2]), perp(p[2], p[0]), perp(p[0], p[1])], axis=1)
+
+
+def volume_match_gradient(K: OracleLib, sigma, pts_s, cells_s, pts_t, cells_t, exact: bool = False):
+    """OrientedVolumeMesh::ComputeMatchGradient, :159-280: per cell Ktau = K_S V_S - K_T V_T at its
+    centre times d det / d p_k (times 1.0f/3.0f in 3-D) to every corner k, and
+    (G_S - G_T) / ((d + 1) / 2) to every corner, G_X = ConvolveGradient(c_S, V_S) with sources X.
+    The reference drops the sign of the determinant its volumes take the absolute value of; exact=True
+    keeps it (the two agree on positively oriented cells)."""
+    d = pts_s.shape[1]
+    cs, vs, sg = volume_centers(pts_s, cells_s)
+    ct, vt, _ = volume_centers(pts_t, cells_t)
+    ktau = K.convolve(cs, cs, vs[:, None], sigma)[:, 0] - K.convolve(cs, ct, vt[:, None], sigma)[:, 0]
+    gk = (K.grad_alpha(cs, cs, vs[:, None], sigma, vs[:, None])
+          - K.grad_alpha(cs, ct, vt[:, None], sigma, vs[:, None])) / ((d + 1.0) / 2.0)
+    if exact:
+        ktau = ktau * sg
+    vk = volume_corner_vectors(pts_s, cells_s)
+    grad = np.zeros_like(pts_s)
+    for f in range(len(cells_s)):  # cell order, as the reference accumulates
+        for k in range(d + 1):
+            v = cells_s[f, k]
+            grad[v] += (THIRD_F32 * vk[f, k] * ktau[f]) if d == 3 else vk[f, k] * ktau[f]
+            grad[v] += gk[f]
+    return grad
+
+
+def landmark_match(K, sigma, pts_s, cells_s, pts_t, cells_t):
+    """Landmark::ComputeMatch, :288-304: squared Frobenius norm of S - T (same point count)."""
+    if pts_s.shape != pts_t.shape:
+        raise ValueError("landmark objects need the same number of points")
+    return float(np.sum((pts_s - pts_t) ** 2))
+
+
+def landmark_match_gradient(K, sigma, pts_s, cells_s, pts_t, cells_t):
+    """Landmark::ComputeMatchGradient, :306-322: 2 (S - T)."""
+    return (pts_s - pts_t) * 2.0
+
+
 KINDS = {
     "currents": (currents_match, currents_match_gradient),
     "varifold": (varifold_match, varifold_match_gradient),
     "curve_currents": (curve_currents_match, curve_currents_match_gradient),
     "curve_varifold": (curve_varifold_match, curve_varifold_match_gradient),
+    "pointcloud": (pointcloud_match, pointcloud_match_gradient),
+    "volume": (volume_match, volume_match_gradient),
+    "landmark": (landmark_match, landmark_match_gradient),
 }

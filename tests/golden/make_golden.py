@@ -128,6 +128,8 @@ def main(ref_root: str = "/root/reference"):
     # 4. functional tests 5 and 6: landmark registrations of two skull curves, two amygdala meshes
     skull_fixture(ref_root)
     amygdala_fixture(ref_root)
+    # 5. volume-mesh gradient unit test and the point-cloud example's point sets
+    volume_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
 
 
@@ -179,6 +181,26 @@ def amygdala_fixture(ref_root: str = "/root/reference"):
         kernel_width=np.array(10.0), data_kernel_width=np.array(10.0), data_sigma2=np.array(0.01),
         number_of_time_points=np.array(10), initial_step=np.array(1e-7), max_iterations=np.array(10),
         **{f"state_{k}": np.asarray(v) for k, v in st.items()})
+
+
+def volume_fixture(ref_root: str = "/root/reference"):
+    """Meshes of the reference's volume-gradient unit test (TestVolumeGradient.cxx:86-120: kernel
+    width 1, forward differences of step 1e-5f, |analytic - numeric| <= 1e-5): a tetrahedral cube
+    deformed towards a ball in 3-D, a triangulated square towards a disk in 2-D (the 2-D objects keep
+    the first two coordinates), and the two 4-point sets of the 2-D point-cloud example."""
+    F = _formats()
+    g = os.path.join(ref_root, "tests", "unit_tests", "geometries", "data")
+    out = {}
+    for name, dim in (("VolumeCube", 3), ("VolumeBall", 3), ("VolumeSquare", 2), ("VolumeDisk", 2)):
+        p, c = F.read_vtk_polydata(os.path.join(g, name + ".vtk"))
+        out[f"{name}_pts"] = np.ascontiguousarray(p[:, :dim])
+        out[f"{name}_cells"] = np.asarray(c, dtype=np.int32)
+    e = os.path.join(ref_root, "examples", "registration", "landmark", "2d", "simple_point_cloud", "data")
+    for name in ("sourcePoints", "targetPoints"):
+        p, _ = F.read_vtk_polydata(os.path.join(e, name + ".vtk"))
+        out[f"{name}_pts"] = np.ascontiguousarray(p[:, :2])
+    np.savez_compressed(os.path.join(HERE, "volume_meshes.npz"), kernel_width=np.array(1.0),
+                        fd_step=np.array(float(np.float32(1e-5))), tolerance=np.array(1e-5), **out)
 
 
 if __name__ == "__main__":

@@ -190,8 +190,10 @@ def _archive_items(text: str):
 
 def read_state_blobs(path: str):
     """Every matrix and vector of a DeformationState archive in file order, as dicts with keys
-    `name` (the map key written before it, or None), `shape` and `value` (float64, shaped, matrices
-    converted from column-major). Also returns the scalar tokens that precede the first blob."""
+    `name` (the map key written before it, or None), `shape`, `value` (float64, shaped, matrices
+    converted from column-major) and `index` (position within a matrix list: the matrices of one
+    fixed or random effect, e.g. one per template object or per subject, follow the key that
+    names the first one). Also returns the scalar tokens that precede the first blob."""
     with open(path) as f:
         items = _archive_items(f.read())
     out = []
@@ -211,21 +213,29 @@ def read_state_blobs(path: str):
                 name = toks[k]
                 break
         ints = [int(t) for t in toks if t.lstrip("-").isdigit()]
-        if len(ints) >= 2 and ints[-2] * ints[-1] == a.size and ints[-1] > 0 and name is not None:
+        shaped = len(ints) >= 2 and ints[-2] * ints[-1] == a.size and ints[-1] > 0
+        prev = out[-1] if out else None
+        if shaped and name is not None:
             r, c = ints[-2], ints[-1]
-            out.append({"name": name, "shape": (r, c), "value": a.reshape(c, r).T.copy()})
+            out.append({"name": name, "shape": (r, c), "value": a.reshape(c, r).T.copy(), "index": 0})
+        elif shaped and prev is not None and len(prev["shape"]) == 2 and prev["name"] is not None:
+            r, c = ints[-2], ints[-1]  # the next matrix of the same list
+            out.append({"name": prev["name"], "shape": (r, c), "value": a.reshape(c, r).T.copy(),
+                        "index": prev["index"] + 1})
         else:
-            out.append({"name": name, "shape": (a.size,), "value": a})
+            out.append({"name": name, "shape": (a.size,), "value": a, "index": 0})
         toks = []
     return out, head or toks
 
 
 def read_deformation_state(path: str):
-    """The final FastGradientAscent state (FastGradientAscent.cxx:313-322) of a one-subject
-    landmark registration: fields iter, freeze_counter, tau (scalars), step, grad_sq_norms
-    (vectors), control_points, template (fixed effects), aux_control_points, aux_template, the
-    control-point gradient, momenta, aux_momenta, the momenta gradient, and history (one
-    [data, regularity] row per iteration)."""
+    """The final FastGradientAscent state (FastGradientAscent.cxx:313-322) of a landmark
+    registration or deterministic atlas: fields iter, freeze_counter, tau (scalars), step,
+    grad_sq_norms (vectors), control_points, template (fixed effects), aux_control_points,
+    aux_template, the control-point gradient (grad_control_points), grad_template, momenta,
+    aux_momenta, the momenta gradient, and history (one [data, regularity] row per iteration).
+    A multi-object template is a list of matrices (one per object); the momenta of several
+    subjects stack to (subjects, control points, d)."""
     blobs, head = read_state_blobs(path)
 
     def is_float(t):
@@ -246,14 +256,22 @@ def read_deformation_state(path: str):
     named = [b for b in blobs if b["name"] is not None]
     st["step"], st["grad_sq_norms"] = vecs[0]["value"], vecs[1]["value"]
     st["history"] = np.stack([b["value"] for b in vecs[2:]])
-    by_name: dict[str, list] = {}
+    groups: dict[str, list] = {}  # per name: one list of matrices per written effect map
     for b in named:
-        by_name.setdefault(b["name"], []).append(b["value"])
+        g = groups.setdefault(b["name"], [])
+        if b["index"] == 0:
+            g.append([])
+        g[-1].append(b["value"])
+    # a one-matrix list is that matrix; same-shaped lists (one per subject) stack; others stay lists
+    by_name = {k: [m[0] if len(m) == 1 else (np.stack(m) if len({x.shape for x in m}) == 1 and k == "Momenta"
+                                              else m) for m in v] for k, v in groups.items()}
     cps, tds, moms = by_name.get("ControlPoints", []), by_name.get("TemplateData", []), by_name.get("Momenta", [])
     st["control_points"], st["aux_control_points"] = cps[0], cps[1]
     if len(cps) > 2:
         st["grad_control_points"] = cps[2]
     if tds:
         st["template"], st["aux_template"] = tds[0], tds[1]
+        if len(tds) > 2:
+            st["grad_template"] = tds[2]
     st["momenta"], st["aux_momenta"], st["grad_momenta"] = moms[0], moms[1], moms[2]
     return st

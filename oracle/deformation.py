@@ -217,3 +217,34 @@ def registration(K: OracleLib, cp, mom, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, 
     g_cp = -xp[0] - K.grad_alpha(cp, cp, mom, sigma_def, mom)
     return L, g_cp, g_mom, {"match": match, "pos": pos, "mom": mo, "lm": lm, "theta": theta,
                             "xi_pos": xp, "xi_mom": xm}
+
+
+def registration_multi(K: OracleLib, cp, mom, tmpl_pts, objects, targets, T: int, sigma_def: float,
+                       heun: bool = True):
+    """registration() for a multi-object template (DeformableMultiObject): the points of every
+    object, concatenated in template order, flow together; object i (objects[i] = dict(kind, cells,
+    sigma, sigma2, n): data term, template cells, kernel width, data sigma^2, point count) is
+    matched to targets[i] = (points, cells). L_data = -0.5 sum_i match_i / sigma2_i
+    (DeterministicAtlas.cxx:121-125) and the adjoint is seeded with each object's match gradient
+    / (2 sigma2_i) (AbstractAtlas.cxx:585-590)."""
+    from . import geometry as G
+    pos, mo = shoot(K, sigma_def, cp, mom, T)
+    lm = flow_landmarks(K, sigma_def, pos, mo, tmpl_pts, heun)
+    matches, theta_T, off = [], [], 0
+    for ob, (tp, tc) in zip(objects, targets):
+        match_f, grad_f = G.KINDS[ob["kind"]]
+        x = lm[-1][off:off + ob["n"]]
+        matches.append(match_f(K, ob["sigma"], x, ob["cells"], tp, tc))
+        theta_T.append(grad_f(K, ob["sigma"], x, ob["cells"], tp, tc) / (2.0 * ob["sigma2"]))
+        off += ob["n"]
+    data = 0.0
+    for m, ob in zip(matches, objects):
+        data -= m / ob["sigma2"]
+    data *= 0.5
+    kp = K.convolve(cp, cp, mom, sigma_def)
+    reg = -0.5 * float(np.sum(kp * mom))
+    theta = adjoint_landmarks(K, sigma_def, pos, mo, lm, np.concatenate(theta_T), heun)
+    xp, xm = adjoint_diffeo(K, sigma_def, pos, mo, lm, theta, heun)
+    g_mom = -xm[0] - kp
+    g_cp = -xp[0] - K.grad_alpha(cp, cp, mom, sigma_def, mom)
+    return data, reg, g_cp, g_mom, {"matches": matches, "theta": theta, "lm": lm}

@@ -23,11 +23,22 @@ import numpy as np
 
 def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: int,
                          max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2,
-                         tolerance: float = 1e-4, nb_iter_freeze: int = 3, multivariate: bool = True):
+                         tolerance: float = 1e-4, nb_iter_freeze: int = 3, multivariate: bool = True,
+                         set_fixed=None):
+    """set_fixed(params), when given, is called wherever the reference calls
+    SetFixedEffects (before every evaluation at a new point, and around the per-iteration state
+    write, SaveEveryNIters = 1 by default, SparseDiffeoParameters.cxx:105), for models whose state
+    depends on that sequence; the log-likelihood at the extrapolated point and the gradient there
+    are then two evaluations, as in the reference (:245-258)."""
     fixed = [np.array(p, dtype=np.float64) for p in params]
     aux = [p.copy() for p in fixed]
     history = [None] * (max_iterations + 1)
-    terms0, grads, sq = evaluate(aux, True)
+    sf = set_fixed or (lambda p: None)
+    if set_fixed is None:
+        terms0, grads, sq = evaluate(aux, True)
+    else:
+        terms0 = evaluate(aux, False)[0]
+        _, grads, sq = evaluate(aux, True)
     history[0] = np.asarray(terms0, dtype=np.float64)
     lsq_ref = float(np.sum(history[0]))
     n = len(fixed)
@@ -47,6 +58,7 @@ def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: 
         new_terms = None
         for li in range(max_line_search):
             cand = ascent(step)
+            sf(cand)
             t, _, _ = evaluate(cand, False)
             evaluations += 1
             q = float(np.sum(t)) - lsq_ref - float(np.dot(sq, step)) * shrink
@@ -63,6 +75,7 @@ def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: 
                     local = step.copy()
                     local[k] /= shrink
                     ck = ascent(local)
+                    sf(ck)
                     tk, _, _ = evaluate(ck, False)
                     evaluations += 1
                     props.append(ck)
@@ -78,6 +91,7 @@ def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: 
                 freeze = 1
                 step = step * shrink
         if not found:
+            sf(fixed)
             stopped = "line_search"
             break
         history[it] = new_terms
@@ -89,7 +103,14 @@ def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: 
         aux = [new[k] + (new[k] - fixed[k]) * tau_scale for k in range(n)]
         fixed = new
         tau = tau_next
-        t_aux, grads, sq = evaluate(aux, True)
+        if set_fixed is None:
+            t_aux, grads, sq = evaluate(aux, True)
+        else:
+            sf(aux)
+            t_aux = evaluate(aux, False)[0]
+            sf(fixed)  # the state write of every iteration (:250-254)
+            sf(aux)
+            _, grads, sq = evaluate(aux, True)
         evaluations += 1
         lsq_ref = float(np.sum(t_aux))
         d_cur = float(np.sum(history[it - 1]) - np.sum(history[it]))
@@ -99,6 +120,7 @@ def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: 
             it += 1
             break
         it += 1
+    sf(fixed)
     done = [h for h in history if h is not None]
     return {"params": fixed, "aux": aux, "grads": grads, "grad_sq_norms": np.asarray(sq, dtype=np.float64),
             "step": step, "tau": tau, "freeze_counter": freeze, "iter": it, "history": np.stack(done),
@@ -169,6 +191,82 @@ def atlas_evaluator(K, tmpl_cells, targets, T: int, sigma_def: float, sigma_data
             sob = K.convolve(tmpl, tmpl, g_t, smoothing_width) if smoothing_width >= 1e-20 else g_t
             grads.append(sob)
             sq.append(float(np.sum(g_t * sob)))
+        grads.append(g_mom)
+        sq.append(float(np.sum(g_mom * g_mom)))
+        return terms, grads, np.array(sq)
+
+    return evaluate
+
+
+class LaggedTemplate:
+    """The template the reference deforms during an atlas estimation. AbstractAtlas::SetFixedEffects
+    (AbstractAtlas.cxx:52-65) reads the template data of the fixed effects BEFORE storing the new
+    map and writes that older copy into the template objects, so every evaluation deforms the
+    template of the previous SetFixedEffects call, while the smoothing of the template gradient
+    (ConvolveGradTemplate, :724-748) and the step use the current one. set_fixed(params) follows
+    the calls; `deformed` is the template the next evaluation deforms."""
+
+    def __init__(self, tmpl, index: int):
+        self.current = np.array(tmpl, dtype=np.float64)
+        self.deformed = self.current.copy()
+        self.index = index
+
+    def set_fixed(self, params):
+        self.deformed = self.current
+        self.current = np.array(params[self.index], dtype=np.float64)
+
+
+def multi_object_atlas_evaluator(K, objects, subjects, T: int, sigma_def: float, heun: bool = False,
+                                 smoothing_width: float = 0.0, optimize_cp: bool = True,
+                                 optimize_template: bool = True, cp=None, tmpl=None, lag: LaggedTemplate = None):
+    """evaluate() of a DeterministicAtlas with a multi-object template: objects[i] = dict(kind,
+    cells, sigma, sigma2, n) in template order (the template points are the objects' points
+    concatenated), subjects[s][i] = (points, cells) of object i of subject s. Groups as in
+    atlas_evaluator. Per subject the data term sums its objects (DeterministicAtlas.cxx:121-125:
+    subjects outer, objects inner, then * 0.5); the template gradient is sum_s -theta_s(0), smoothed
+    object by object on that object's own points (ConvolveGradTemplate, AbstractAtlas.cxx:724-748),
+    and its squared norm is the sum over objects of <L2, smoothed> (DeterministicAtlas.cxx:232).
+    With `lag` (a LaggedTemplate whose set_fixed goes to fast_gradient_ascent) the deformation uses
+    the lagged template as the reference does."""
+    from .deformation import registration_multi
+    cp_frozen, tmpl_frozen = cp, tmpl
+    offs = np.cumsum([0] + [ob["n"] for ob in objects])
+
+    def evaluate(params, need_grad):
+        k = 0
+        cp = params[k] if optimize_cp else cp_frozen
+        k += int(optimize_cp)
+        tmpl = params[k] if optimize_template else tmpl_frozen
+        k += int(optimize_template)
+        mom = params[k]
+        data = reg = 0.0
+        g_cp = np.zeros_like(cp)
+        g_t = np.zeros_like(tmpl)
+        g_mom = np.zeros_like(mom)
+        moved = tmpl if lag is None else lag.deformed
+        for s, targets in enumerate(subjects):
+            d_s, r_s, gc, gm, info = registration_multi(K, cp, mom[s], moved, objects, targets, T, sigma_def, heun)
+            data += d_s
+            reg += r_s
+            g_cp += gc
+            g_mom[s] = gm
+            g_t -= info["theta"][0]
+        terms = [data, reg]
+        if not need_grad:
+            return terms, None, None
+        grads, sq = [], []
+        if optimize_cp:
+            grads.append(g_cp)
+            sq.append(float(np.sum(g_cp * g_cp)))
+        if optimize_template:
+            sob = g_t.copy()
+            if smoothing_width >= 1e-20:
+                for i in range(len(objects)):
+                    a, b = offs[i], offs[i + 1]
+                    sob[a:b] = K.convolve(tmpl[a:b], tmpl[a:b], g_t[a:b], smoothing_width)
+            grads.append(sob)
+            sq.append(float(sum(np.sum(g_t[offs[i]:offs[i + 1]] * sob[offs[i]:offs[i + 1]])
+                                for i in range(len(objects)))))
         grads.append(g_mom)
         sq.append(float(np.sum(g_mom * g_mom)))
         return terms, grads, np.array(sq)

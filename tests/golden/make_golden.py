@@ -130,6 +130,8 @@ def main(ref_root: str = "/root/reference"):
     amygdala_fixture(ref_root)
     # 5. volume-mesh gradient unit test and the point-cloud example's point sets
     volume_fixture(ref_root)
+    # 6. functional test 8: a two-object curve atlas of three subjects
+    parabola_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
 
 
@@ -201,6 +203,36 @@ def volume_fixture(ref_root: str = "/root/reference"):
         out[f"{name}_pts"] = np.ascontiguousarray(p[:, :2])
     np.savez_compressed(os.path.join(HERE, "volume_meshes.npz"), kernel_width=np.array(1.0),
                         fd_step=np.array(float(np.float32(1e-5))), tolerance=np.array(1e-5), **out)
+
+
+def parabola_fixture(ref_root: str = "/root/reference"):
+    """Inputs and expected final state of the reference's parabola atlas (functional test 8,
+    model.xml: DeterministicAtlas, two OrientedPolyline objects "line" and "wave", object kernel
+    width 0.2, data-sigma 1, deformation kernel width 0.2, 10 time points; three subjects;
+    optimization_parameters.xml: FastGradientAscent (the default), initial step 1e-3,
+    10 iterations, 10 line-search iterations. Its smoothing-kernel-width-ratio element is not a key
+    the reference's XML converter reads (it reads smoothing-kernel-with-ratio,
+    XmlConfigurationConverter.cxx:228), so the ratio keeps its default 1: smoothing width 0.2)."""
+    F = _formats()
+    from oracle.optimize import initial_control_points
+    d = os.path.join(ref_root, "tests", "functional_tests", "atlas", "landmark", "2d", "parabola")
+    out = {}
+    centres = []
+    for i in (1, 2):
+        p, c = F.read_vtk_polydata(os.path.join(d, "data", f"{i}-meantemplate.vtk"))
+        out[f"tmpl{i}_pts"], out[f"tmpl{i}_segs"] = np.ascontiguousarray(p[:, :2]), c
+        centres.append(p[c].mean(axis=1)[:, :2])
+        for s in (1, 2, 3):
+            q, e = F.read_vtk_polydata(os.path.join(d, "data", f"{i}-subject{s}.vtk"))
+            out[f"subj{s}_obj{i}_pts"], out[f"subj{s}_obj{i}_segs"] = np.ascontiguousarray(q[:, :2]), e
+    st = F.read_deformation_state(os.path.join(d, "deformetrica-state.bin"))
+    for k in ("template", "aux_template", "grad_template"):
+        st[k] = np.concatenate(st[k])
+    np.savez_compressed(
+        os.path.join(HERE, "parabola_atlas.npz"), cp0=initial_control_points(np.concatenate(centres), 0.2),
+        kernel_width=np.array(0.2), data_kernel_width=np.array(0.2), data_sigma2=np.array(1.0),
+        smoothing_width=np.array(0.2), number_of_time_points=np.array(10), initial_step=np.array(1e-3),
+        max_iterations=np.array(10), **out, **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
 if __name__ == "__main__":

@@ -91,6 +91,17 @@ SIGNATURES = {
     "gbk_volume_match": (_I, [_P, _I, _L, _P, _L, _P, _L, _P, _L, _P, _D, _P, _P]),
     "gbk_landmark_match": (_I, [_P, _I, _L, _P, _P, _P, _P]),
     "gbk_registration_set_point_weights": (_I, [_P, _P, _P]),
+    "gbk_registration_create_multi": (_I, [_P, _I, _L, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _I, _D, _I,
+                                           ctypes.POINTER(_P)]),
+    "gbk_registration_set_template": (_I, [_P, _P]),
+    "gbk_mo_atlas_create": (_I, [_P, _I, _L, _I, _P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _I, _D, _I,
+                                 ctypes.POINTER(_P)]),
+    "gbk_mo_atlas_set_template_smoothing": (_I, [_P, _D]),
+    "gbk_mo_atlas_set_lagged_template": (_I, [_P, _I]),
+    "gbk_mo_atlas_step": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "gbk_mo_atlas_optimize": (_I, [_P, _P, _P, _P, _I, _I, _I, _D, _I, _D, _D, _D, _I, _P, _P, _P, _P, _P, _P, _P,
+                                   _P, _P]),
+    "gbk_mo_atlas_destroy": (None, [_P]),
     "gbk_registration_create": (_I, [_P, _I, _L, _L, _P, _L, _P, _L, _P, _L, _P, _I, _D, _D, _D, _I, _I,
                                      ctypes.POINTER(_P)]),
     "gbk_registration_step": (_I, [_P, _P, _P, _P, _P, _P]),

@@ -25,7 +25,7 @@ namespace gbk {
 
 int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes, double *const *params,
                          const FgaOptions &o, const FgaEvaluate &evaluate, FgaResult *res, double *const *aux_out,
-                         double *const *grad_out) {
+                         double *const *grad_out, const FgaSetFixed &set_fixed) {
   if (ng < 1 || ng > 4) return c->fail(GBK_ERR_ARG, "optimiser: %d parameter groups", ng);
   if (o.max_iterations < 0 || o.max_line_search < 1 || !(o.shrink > 0 && o.shrink < 1) || !(o.expand >= 1) ||
       !(o.initial_step > 0) || o.nb_iter_freeze < 0)
@@ -62,6 +62,20 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
     ++evaluations;
     return evaluate(p.data(), need_grad, t, grad.data(), sq.data());
   };
+  auto setf = [&](const std::vector<double *> &p) { return set_fixed ? set_fixed(p.data()) : GBK_OK; };
+  // the log-likelihood at aux and the gradient there: one evaluation, or, with set_fixed, the
+  // reference's sequence (evaluate; SetFixedEffects(fixed) and (aux) for the state write; gradient)
+  auto eval_aux = [&](double *t, bool after_step) {
+    if (!set_fixed) return eval(aux, true, t);
+    int e = after_step ? setf(aux) : GBK_OK;
+    if (!e) e = eval(aux, false, t);
+    if (!e && after_step) e = setf(fixed);
+    if (!e && after_step) e = setf(aux);
+    double ignored[2];
+    if (!e) e = eval(aux, true, ignored);
+    if (!e) --evaluations;  // one log-likelihood evaluation and one gradient
+    return e;
+  };
   auto ascent = [&](const std::vector<double *> &dst, const std::vector<double> &s) {  // GradientAscentStep
     int e = GBK_OK;
     for (int g = 0; g < ng && !e; ++g) e = c->cuda(lincomb(st, dst[g], aux[g], s[g], grad[g], 0.0, nullptr, sizes[g]), "ascent");
@@ -77,7 +91,7 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
     if (!rc) rc = c->cuda(cudaMemcpyAsync(aux[g], params[g], (size_t)sizes[g] * sizeof(double), cudaMemcpyDefault, st), "copy");
   }
   double t0[2] = {0, 0};
-  if (!rc) rc = eval(aux, true, t0);
+  if (!rc) rc = eval_aux(t0, false);
   if (rc) {
     cleanup();
     return rc;
@@ -93,6 +107,7 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
     for (int li = 0; li < o.max_line_search && !rc; ++li) {
       double t[2];
       if ((rc = ascent(nw, step))) break;
+      if ((rc = setf(nw))) break;
       if ((rc = eval(nw, false, t))) break;
       if (t[0] + t[1] - lsq_ref - dotsq(step) * shrink >= 0) {
         found = true;
@@ -109,6 +124,7 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
           std::vector<double> local(step);
           local[k] /= shrink;
           if ((rc = ascent(prop[k], local))) break;
+          if ((rc = setf(prop[k]))) break;
           if ((rc = eval(prop[k], false, ts[k].data()))) break;
           qs[k] = ts[k][0] + ts[k][1] - lsq_ref - dotsq(local) * shrink;
         }
@@ -131,6 +147,7 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
     }
     if (rc) break;
     if (!found) {
+      rc = setf(fixed);
       stop = 1;
       break;
     }
@@ -148,7 +165,7 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
     std::swap(fixed, nw);
     tau = tau_next;
     double ta[2];
-    if ((rc = eval(aux, true, ta))) break;
+    if ((rc = eval_aux(ta, true))) break;
     lsq_ref = ta[0] + ta[1];
     const double cur = (hist[(size_t)(it - 1) * 2] + hist[(size_t)(it - 1) * 2 + 1]) -
                        (hist[(size_t)it * 2] + hist[(size_t)it * 2 + 1]);
@@ -159,6 +176,7 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
       break;
     }
   }
+  if (!rc) rc = setf(fixed);
   for (int g = 0; g < ng && !rc; ++g) {
     const size_t nb = (size_t)sizes[g] * sizeof(double);
     rc = c->cuda(cudaMemcpyAsync(params[g], fixed[g], nb, cudaMemcpyDefault, st), "copy");

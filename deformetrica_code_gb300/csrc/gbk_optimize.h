@@ -39,11 +39,17 @@ struct FgaResult {
 typedef std::function<int(double *const *params, bool need_grad, double *terms, double *const *grads, double *sq)>
     FgaEvaluate;
 
+// set_fixed(params): called wherever the reference calls SetFixedEffects (before every evaluation
+// at a new point and around the per-iteration state write), for models whose state depends on that
+// sequence; with it the log-likelihood at the extrapolated point and the gradient there are two
+// evaluations, as in FastGradientAscent.cxx:245-258.
+typedef std::function<int(double *const *params)> FgaSetFixed;
+
 // Runs the ascent from the group vectors `params` (device, sizes[g] doubles each), which receive
 // the final fixed effects; aux_out / grad_out (optional, device or host, per group) receive the
 // extrapolated point and the gradient there.
 int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes, double *const *params,
                          const FgaOptions &o, const FgaEvaluate &evaluate, FgaResult *res, double *const *aux_out,
-                         double *const *grad_out);
+                         double *const *grad_out, const FgaSetFixed &set_fixed = nullptr);
 
 }  // namespace gbk

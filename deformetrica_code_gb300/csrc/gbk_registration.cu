@@ -1,7 +1,9 @@
-// One registration iteration of a subject of DeterministicAtlas with a frozen template (a triangle
-// mesh in 3-D or a polyline in 2-D / 3-D), on the device, replayed from a CUDA graph.
+// One registration iteration of a subject of DeterministicAtlas with a frozen template of one or
+// several objects (triangle meshes, polylines, point clouds, volume meshes, landmarks), on the
+// device, replayed from a CUDA graph.
 //
-// Log-likelihood (DeterministicAtlas.cxx:99-154) L = -0.5 match / data_sigma2 - 0.5 <K p, p>
+// Log-likelihood (DeterministicAtlas.cxx:99-154) L = -0.5 sum_k match_k / data_sigma2_k
+// - 0.5 <K p, p>
 // and its gradient (AbstractAtlas.cxx:559-613, DeterministicAtlas.cxx:246-280):
 //   1. Shoot the control points and momenta (Diffeos.cxx:589-660);
 //   2. flow the template vertices (Diffeos.cxx:661-712);
@@ -27,161 +29,200 @@
 #include "gbk_hostio.h"
 #include "gbk_ops.h"
 #include "gbk_optimize.h"
+#include "gbk_registration_impl.h"
 
 using namespace gbk;
 
-struct gbk_registration {
-  gbk_ctx *c = nullptr;
-  int d = 3, T = 2, heun = 1, use_graph = 1, steps = 0;
-  long ncp = 0, nv = 0;
-  double sigma_def = 1, sigma_data = 1, data_sigma2 = 1;
-  cudaStream_t stream = nullptr;
-  SurfaceTerm surf;
-  std::vector<void *> owned;
-  double *cp = nullptr, *mom = nullptr, *pos = nullptr, *momt = nullptr, *lm = nullptr, *lm0 = nullptr;
-  double *theta = nullptr, *thetaT = nullptr, *xp = nullptr, *xm = nullptr;
-  double *kp = nullptr, *greg = nullptr, *gcp = nullptr, *gmom = nullptr, *out = nullptr;
-  DeformScratch s;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+namespace {
 
-  int alloc(void **p, size_t bytes) {
-    cudaError_t e = cudaMalloc(p, std::max(bytes, (size_t)8));
-    if (e != cudaSuccess) return c->cuda(e, "cudaMalloc (registration)");
-    owned.push_back(*p);
-    return GBK_OK;
+// L_data = 0.5 * (-sum_k match_k / sigma2_k) in object order (DeterministicAtlas.cxx:121-125) and
+// the sum of the matches
+__global__ void data_terms_kernel(const double *match, const double *sigma2, int n, double *l_data,
+                                  double *match_sum) {
+  double acc = 0.0, m = 0.0;
+  for (int k = 0; k < n; ++k) {
+    acc -= match[k] / sigma2[k];
+    m += match[k];
   }
+  *l_data = acc * 0.5;
+  *match_sum = m;
+}
 
-  // The whole iteration on `stream`, device pointers only.
-  int body() {
-    const long n = ncp * d;
-    int rc;
-    if ((rc = shoot_device(c, d, ncp, cp, mom, T, sigma_def, pos, momt, s))) return rc;
-    if ((rc = flow_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm0, heun, lm, s))) return rc;
-    // data term on the deformed template; thetaT = d match / d x_T / (2 data_sigma2)
-    if ((rc = surf.evaluate(c, lm + (long)(T - 1) * nv * d, out + 3, thetaT, 0.5 / data_sigma2, 0))) return rc;
-    // regularity: K p and ConvolveGradient(cp, p) in one fused pass, <K p, p> in FP64
-    PairArgs a = pair_args(ncp, ncp, sigma_def);
-    a.x = cp;
-    a.y = cp;
-    a.w = mom;
-    a.w_ld = d;
-    a.ta = mom;
-    a.ta_ld = d;
-    a.out0 = kp;
-    a.out0_ld = d;
-    a.out1 = greg;
-    a.out1_ld = d;
-    if ((rc = c->launch(OP_CONV_GRADA, d, d, a))) return rc;
-    if ((rc = c->cuda(dot_f64(c->stream, kp, mom, n, out + 4, 0), "dot"))) return rc;
-    // out = [L, L_data, L_reg, match, <Kp,p>]
-    if ((rc = c->cuda(scalar_combine(c->stream, out + 1, out + 3, -0.5 / data_sigma2, nullptr, 0, nullptr, 0), "L"))) return rc;
-    if ((rc = c->cuda(scalar_combine(c->stream, out + 2, out + 4, -0.5, nullptr, 0, nullptr, 0), "L"))) return rc;
-    if ((rc = c->cuda(scalar_combine(c->stream, out + 0, out + 1, 1.0, out + 2, 1.0, nullptr, 0), "L"))) return rc;
-    c->launches += 4;
-    if ((rc = adjoint_landmarks_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm, thetaT, heun, theta, s))) return rc;
-    if ((rc = adjoint_diffeo_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm, theta, heun, xp, xm, s))) return rc;
-    if ((rc = c->cuda(lincomb(c->stream, gmom, nullptr, -1.0, xm, -1.0, kp, n), "grad"))) return rc;
-    if ((rc = c->cuda(lincomb(c->stream, gcp, nullptr, -1.0, xp, -1.0, greg, n), "grad"))) return rc;
-    c->launches += 2;
-    return GBK_OK;
+}  // namespace
+
+int gbk_registration::alloc(void **p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, std::max(bytes, (size_t)8));
+  if (e != cudaSuccess) return c->cuda(e, "cudaMalloc (registration)");
+  owned.push_back(*p);
+  return GBK_OK;
+}
+
+int gbk_registration::body() {
+  const long n = ncp * d;
+  int rc;
+  if ((rc = shoot_device(c, d, ncp, cp, mom, T, sigma_def, pos, momt, s))) return rc;
+  if ((rc = flow_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm0, heun, lm, s))) return rc;
+  // data terms on the deformed template objects; thetaT = d match_k / d x_T / (2 sigma2_k)
+  const double *xT = lm + (long)(T - 1) * nv * d;
+  for (size_t k = 0; k < objs.size(); ++k) {
+    RegObject &o = objs[k];
+    if ((rc = o.surf.evaluate(c, xT + o.off * d, out + 8 + k, thetaT + o.off * d, 0.5 / o.sigma2, 0))) return rc;
   }
+  data_terms_kernel<<<1, 1, 0, c->stream>>>(out + 8, sigma2_dev, (int)objs.size(), out + 1, out + 3);
+  if ((rc = c->cuda(cudaGetLastError(), "data terms"))) return rc;
+  // regularity: K p and ConvolveGradient(cp, p) in one fused pass, <K p, p> in FP64
+  PairArgs a = pair_args(ncp, ncp, sigma_def);
+  a.x = cp;
+  a.y = cp;
+  a.w = mom;
+  a.w_ld = d;
+  a.ta = mom;
+  a.ta_ld = d;
+  a.out0 = kp;
+  a.out0_ld = d;
+  a.out1 = greg;
+  a.out1_ld = d;
+  if ((rc = c->launch(OP_CONV_GRADA, d, d, a))) return rc;
+  if ((rc = c->cuda(dot_f64(c->stream, kp, mom, n, out + 4, 0), "dot"))) return rc;
+  // out = [L, L_data, L_reg, match, <Kp,p>]
+  if ((rc = c->cuda(scalar_combine(c->stream, out + 2, out + 4, -0.5, nullptr, 0, nullptr, 0), "L"))) return rc;
+  if ((rc = c->cuda(scalar_combine(c->stream, out + 0, out + 1, 1.0, out + 2, 1.0, nullptr, 0), "L"))) return rc;
+  c->launches += 4;
+  if ((rc = adjoint_landmarks_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm, thetaT, heun, theta, s))) return rc;
+  if ((rc = adjoint_diffeo_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm, theta, heun, xp, xm, s))) return rc;
+  if ((rc = c->cuda(lincomb(c->stream, gmom, nullptr, -1.0, xm, -1.0, kp, n), "grad"))) return rc;
+  if ((rc = c->cuda(lincomb(c->stream, gcp, nullptr, -1.0, xp, -1.0, greg, n), "grad"))) return rc;
+  c->launches += 2;
+  return GBK_OK;
+}
 
-  int run() {
-    cudaStream_t saved = c->stream;
-    c->stream = stream;
-    int rc = GBK_OK;
-    if (!use_graph || steps == 0) {
+int gbk_registration::run() {
+  cudaStream_t saved = c->stream;
+  c->stream = stream;
+  int rc = GBK_OK;
+  if (!use_graph || steps == 0) {
+    rc = body();
+  } else {
+    if (!exec) {
+      if ((rc = c->cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture"))) {
+        c->stream = saved;
+        return rc;
+      }
+      long long l0 = c->launches;
       rc = body();
-    } else {
-      if (!exec) {
-        if ((rc = c->cuda(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture"))) {
-          c->stream = saved;
-          return rc;
-        }
-        long long l0 = c->launches;
-        rc = body();
-        cudaGraph_t g = nullptr;
-        cudaError_t e = cudaStreamEndCapture(stream, &g);
-        if (!rc && e != cudaSuccess) rc = c->cuda(e, "end capture");
-        if (!rc) rc = c->cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate");
-        graph = g;
-        graph_launches = c->launches - l0;
-        c->launches = l0;
-      }
-      if (!rc) {
-        rc = c->cuda(cudaGraphLaunch(exec, stream), "graph launch");
-        c->launches += graph_launches;
-      }
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(stream, &g);
+      if (!rc && e != cudaSuccess) rc = c->cuda(e, "end capture");
+      if (!rc) rc = c->cuda(cudaGraphInstantiate(&exec, g, 0), "graph instantiate");
+      graph = g;
+      graph_launches = c->launches - l0;
+      c->launches = l0;
     }
-    c->stream = saved;
-    if (!rc) ++steps;
-    return rc;
+    if (!rc) {
+      rc = c->cuda(cudaGraphLaunch(exec, stream), "graph launch");
+      c->launches += graph_launches;
+    }
   }
-  long long graph_launches = 0;
+  c->stream = saved;
+  if (!rc) ++steps;
+  return rc;
+}
 
-  void release() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    exec = nullptr;
-    graph = nullptr;
-    surf.release();
-    for (void *p : owned) cudaFree(p);
-    owned.clear();
-    if (stream) cudaStreamDestroy(stream);
-    stream = nullptr;
-  }
-};
+void gbk_registration::drop_graph() {
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  exec = nullptr;
+  graph = nullptr;
+  steps = 0;
+}
 
-extern "C" {
+void gbk_registration::release() {
+  drop_graph();
+  for (RegObject &o : objs) o.surf.release();
+  for (void *p : owned) cudaFree(p);
+  owned.clear();
+  if (stream && own_stream) cudaStreamDestroy(stream);
+  stream = nullptr;
+}
 
-int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *tmpl_pts, long nf,
-                            const int *tmpl_tris, long nv_t, const double *tgt_pts, long nf_t,
-                            const int *tgt_tris, int T, double sigma_def, double sigma_data,
-                            double data_sigma2, int data_kind, int heun,
-                            gbk_registration **out) {
+namespace gbk {
+
+int registration_create(gbk_ctx *c, int d, long ncp, int nobj, const int *kinds, const long *nv_o,
+                        const double *tmpl_pts, const long *nf_o, const int *cells, const long *nv_t_o,
+                        const double *tgt_pts, const long *nf_t_o, const int *tgt_cells, const double *sigma_data,
+                        const double *data_sigma2, int T, double sigma_def, int heun, cudaStream_t stream,
+                        gbk_registration **out) {
   if (!c || !out) return GBK_ERR_ARG;
   *out = nullptr;
-  c->err.clear();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
-  if (data_kind < 0 || data_kind > 6)
-    return c->fail(GBK_ERR_ARG, "data_kind must be 0/1 (surface currents/varifold), 2/3 (curve currents/varifold), "
-                                "4 (point cloud), 5 (volume mesh) or 6 (landmarks)");
   if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d not supported", d);
-  // (data term kind, vertices per cell) of each data_kind
-  static const int kinds[7] = {0, 1, 0, 1, 2, 2, 3};
-  const int cell = data_kind < 2 ? 3 : data_kind < 4 ? 2 : data_kind == 5 ? d + 1 : 1;
-  if (data_kind < 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "surface registration needs d = 3");
-  if (cell == 1) {
-    nf = nv;
-    nf_t = nv_t;
+  if (nobj < 1 || !kinds || !nv_o || !nf_o || !nv_t_o || !nf_t_o || !sigma_data || !data_sigma2)
+    return c->fail(GBK_ERR_ARG, "bad object description");
+  if (ncp <= 0 || T < 2) return c->fail(GBK_ERR_ARG, "bad sizes");
+  if (!tmpl_pts || !tgt_pts) return c->fail(GBK_ERR_ARG, "null pointer");
+  // (data term kind) of each data_kind; vertices per cell follow from data_kind and d
+  static const int term_kind[7] = {0, 1, 0, 1, 2, 2, 3};
+  std::vector<int> cell(nobj);
+  long nv = 0, nv_t = 0, ncells = 0, ncells_t = 0;
+  for (int k = 0; k < nobj; ++k) {
+    const int dk = kinds[k];
+    if (dk < 0 || dk > 6)
+      return c->fail(GBK_ERR_ARG, "data_kind must be 0/1 (surface currents/varifold), 2/3 (curve currents/varifold), "
+                                  "4 (point cloud), 5 (volume mesh) or 6 (landmarks)");
+    if (dk < 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "surface data terms need d = 3");
+    cell[k] = dk < 2 ? 3 : dk < 4 ? 2 : dk == 5 ? d + 1 : 1;
+    const long nf = cell[k] == 1 ? nv_o[k] : nf_o[k], nf_t = cell[k] == 1 ? nv_t_o[k] : nf_t_o[k];
+    if (nv_o[k] <= 0 || nv_t_o[k] <= 0 || nf <= 0 || nf_t <= 0) return c->fail(GBK_ERR_ARG, "bad sizes");
+    if (!(data_sigma2[k] > 0)) return c->fail(GBK_ERR_ARG, "data_sigma2 must be positive");
+    if (cell[k] > 1 && (!cells || !tgt_cells)) return c->fail(GBK_ERR_ARG, "null pointer");
+    nv += nv_o[k];
+    nv_t += nv_t_o[k];
+    if (cell[k] > 1) {
+      ncells += nf * cell[k];
+      ncells_t += nf_t * cell[k];
+    }
   }
-  if (ncp <= 0 || nv <= 0 || nf <= 0 || nv_t <= 0 || nf_t <= 0 || T < 2)
-    return c->fail(GBK_ERR_ARG, "bad sizes");
-  if (!(data_sigma2 > 0)) return c->fail(GBK_ERR_ARG, "data_sigma2 must be positive");
-  if (!tmpl_pts || !tgt_pts || (cell > 1 && (!tmpl_tris || !tgt_tris))) return c->fail(GBK_ERR_ARG, "null pointer");
   gbk_registration *r = new gbk_registration();
   r->c = c;
   r->d = d;
   r->ncp = ncp;
   r->nv = nv;
+  r->nv_t = nv_t;
   r->T = T;
   r->heun = heun ? 1 : 0;
   r->sigma_def = sigma_def;
-  r->sigma_data = sigma_data;
-  r->data_sigma2 = data_sigma2;
-  int rc = c->cuda(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "stream");
-  std::vector<int> th, tth;
-  if (!rc && cell > 1) {
-    th.resize((size_t)nf * cell);
-    tth.resize((size_t)nf_t * cell);
-    cudaMemcpy(th.data(), tmpl_tris, th.size() * sizeof(int), cudaMemcpyDefault);
-    cudaMemcpy(tth.data(), tgt_tris, tth.size() * sizeof(int), cudaMemcpyDefault);
-    rc = c->cuda(cudaGetLastError(), "copy cells");
+  r->objs.resize(nobj);
+  int rc = GBK_OK;
+  if (stream) {
+    r->stream = stream;
+    r->own_stream = false;
+  } else {
+    rc = c->cuda(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "stream");
   }
+  std::vector<int> th(ncells), tth(ncells_t);
+  if (!rc && ncells) cudaMemcpy(th.data(), cells, th.size() * sizeof(int), cudaMemcpyDefault);
+  if (!rc && ncells_t) cudaMemcpy(tth.data(), tgt_cells, tth.size() * sizeof(int), cudaMemcpyDefault);
+  if (!rc) rc = c->cuda(cudaGetLastError(), "copy cells");
   cudaStream_t saved = c->stream;
   c->stream = r->stream;
-  if (!rc) rc = r->surf.init(c, kinds[data_kind], d, cell, sigma_data, nv, nf, th.data(), nv_t, nf_t, tth.data());
+  {
+    long off = 0, co = 0, co_t = 0;
+    for (int k = 0; k < nobj && !rc; ++k) {
+      RegObject &o = r->objs[k];
+      o.off = off;
+      o.nv = nv_o[k];
+      o.nv_t = nv_t_o[k];
+      o.sigma2 = data_sigma2[k];
+      const long nf = cell[k] == 1 ? nv_o[k] : nf_o[k], nf_t = cell[k] == 1 ? nv_t_o[k] : nf_t_o[k];
+      rc = o.surf.init(c, term_kind[kinds[k]], d, cell[k], sigma_data[k], o.nv, nf, cell[k] > 1 ? th.data() + co : nullptr,
+                       o.nv_t, nf_t, cell[k] > 1 ? tth.data() + co_t : nullptr);
+      off += o.nv;
+      if (cell[k] > 1) {
+        co += nf * cell[k];
+        co_t += nf_t * cell[k];
+      }
+    }
+  }
   const long n = ncp * d, m = nv * d, rows = std::max(ncp, nv);
   struct {
     double **p;
@@ -189,17 +230,24 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   } bufs[] = {{&r->cp, (size_t)n}, {&r->mom, (size_t)n}, {&r->pos, (size_t)T * n}, {&r->momt, (size_t)T * n},
               {&r->lm, (size_t)T * m}, {&r->lm0, (size_t)m}, {&r->theta, (size_t)T * m}, {&r->thetaT, (size_t)m},
               {&r->xp, (size_t)T * n}, {&r->xm, (size_t)T * n}, {&r->kp, (size_t)n}, {&r->greg, (size_t)n},
-              {&r->gcp, (size_t)n}, {&r->gmom, (size_t)n}, {&r->out, 8},
+              {&r->gcp, (size_t)n}, {&r->gmom, (size_t)n}, {&r->out, (size_t)8 + nobj},
+              {&r->sigma2_dev, (size_t)nobj}, {&r->tgt, (size_t)nv_t * d},
               {&r->s.va, (size_t)rows * d}, {&r->s.vb, (size_t)rows * d}, {&r->s.vc, (size_t)rows * d},
               {&r->s.vd, (size_t)rows * d}};
   for (auto &b : bufs)
     if (!rc) rc = r->alloc((void **)b.p, b.count * sizeof(double));
   if (!rc) rc = r->alloc((void **)&r->s.flag, 16);
-  double *tgt_dev = nullptr;
-  if (!rc) rc = r->alloc((void **)&tgt_dev, (size_t)nv_t * d * sizeof(double));
-  if (!rc) rc = c->cuda(cudaMemcpyAsync(tgt_dev, tgt_pts, (size_t)nv_t * d * sizeof(double), cudaMemcpyDefault, r->stream), "copy target");
+  if (!rc) rc = c->cuda(cudaMemcpyAsync(r->sigma2_dev, data_sigma2, nobj * sizeof(double), cudaMemcpyHostToDevice, r->stream), "copy sigma2");
+  if (!rc) rc = c->cuda(cudaMemcpyAsync(r->tgt, tgt_pts, (size_t)nv_t * d * sizeof(double), cudaMemcpyDefault, r->stream), "copy target");
   if (!rc) rc = c->cuda(cudaMemcpyAsync(r->lm0, tmpl_pts, (size_t)m * sizeof(double), cudaMemcpyDefault, r->stream), "copy template");
-  if (!rc) rc = r->surf.set_target(c, tgt_dev);
+  {
+    long off_t = 0;
+    for (int k = 0; k < nobj && !rc; ++k) {
+      gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+      rc = r->objs[k].surf.set_target(c, r->tgt + off_t * d);
+      off_t += r->objs[k].nv_t;
+    }
+  }
   if (!rc) rc = c->cuda(cudaStreamSynchronize(r->stream), "sync");
   c->stream = saved;
   if (rc) {
@@ -211,6 +259,44 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
   return GBK_OK;
 }
 
+}  // namespace gbk
+
+extern "C" {
+
+int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *tmpl_pts, long nf,
+                            const int *tmpl_tris, long nv_t, const double *tgt_pts, long nf_t,
+                            const int *tgt_tris, int T, double sigma_def, double sigma_data,
+                            double data_sigma2, int data_kind, int heun,
+                            gbk_registration **out) {
+  if (!c || !out) return GBK_ERR_ARG;
+  c->err.clear();
+  return registration_create(c, d, ncp, 1, &data_kind, &nv, tmpl_pts, &nf, tmpl_tris, &nv_t, tgt_pts, &nf_t, tgt_tris,
+                             &sigma_data, &data_sigma2, T, sigma_def, heun, nullptr, out);
+}
+
+int gbk_registration_create_multi(gbk_ctx *c, int d, long ncp, int nobj, const int *data_kinds, const long *nv,
+                                  const double *tmpl_pts, const long *ncell, const int *tmpl_cells, const long *nv_t,
+                                  const double *tgt_pts, const long *ncell_t, const int *tgt_cells,
+                                  const double *sigma_data, const double *data_sigma2, int T, double sigma_def,
+                                  int heun, gbk_registration **out) {
+  if (!c || !out) return GBK_ERR_ARG;
+  c->err.clear();
+  return registration_create(c, d, ncp, nobj, data_kinds, nv, tmpl_pts, ncell, tmpl_cells, nv_t, tgt_pts, ncell_t,
+                             tgt_cells, sigma_data, data_sigma2, T, sigma_def, heun, nullptr, out);
+}
+
+int gbk_registration_set_template(gbk_registration *r, const double *pts) {
+  if (!r) return GBK_ERR_ARG;
+  gbk_ctx *c = r->c;
+  c->err.clear();
+  if (!pts) return c->fail(GBK_ERR_ARG, "null pointer");
+  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
+  int rc = c->cuda(cudaMemcpyAsync(r->lm0, pts, (size_t)r->nv * r->d * sizeof(double), cudaMemcpyDefault, r->stream),
+                   "copy template");
+  if (!rc) rc = c->cuda(cudaStreamSynchronize(r->stream), "sync");
+  return rc;
+}
+
 int gbk_registration_set_point_weights(gbk_registration *r, const double *w_tmpl, const double *w_tgt) {
   if (!r) return GBK_ERR_ARG;
   gbk_ctx *c = r->c;
@@ -218,12 +304,20 @@ int gbk_registration_set_point_weights(gbk_registration *r, const double *w_tmpl
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   cudaStream_t saved = c->stream;
   c->stream = r->stream;
-  int rc;
+  int rc = GBK_OK, clouds = 0;
   {
     gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
-    rc = r->surf.set_weights(c, w_tmpl, w_tgt);  // same buffers: a captured graph reads the new weights
+    long off_t = 0;
+    for (RegObject &o : r->objs) {
+      if (o.surf.kind == 2 && o.surf.cell == 1) {  // same buffers: a captured graph reads the new weights
+        ++clouds;
+        if (!rc) rc = o.surf.set_weights(c, w_tmpl ? w_tmpl + o.off : nullptr, w_tgt ? w_tgt + off_t : nullptr);
+      }
+      off_t += o.nv_t;
+    }
   }
   c->stream = saved;
+  if (!rc && !clouds) rc = c->fail(GBK_ERR_STATE, "the registration has no point-cloud object");
   return rc;
 }
 

@@ -191,6 +191,37 @@ class Registration:
         if tmpl_weights is not None or tgt_weights is not None:
             self.set_point_weights(tmpl_weights, tgt_weights)
 
+    @classmethod
+    def from_objects(cls, ncp: int, objects, targets, T: int, sigma_def: float, heun: bool = True,
+                     context: Context | None = None):
+        """A registration whose template has several objects (gbk_registration_create_multi):
+        `objects` as for MultiObjectAtlas, `targets` one (points, cells) per object. Point weights of
+        point-cloud objects go through set_point_weights over all template / target points."""
+        self = cls.__new__(cls)
+        self.ctx = context or Context()
+        self.ncp, self.T = int(ncp), int(T)
+        d = int(np.asarray(objects[0]["pts"]).shape[1])
+        kinds, nv, pts, nc, cells = _objects_arrays(objects, d, cls.KINDS)
+        objs_t = [dict(o, pts=t[0], cells=t[1]) for o, t in zip(objects, targets)]
+        _, nv_t, pts_t, nc_t, cells_t = _objects_arrays(objs_t, d, cls.KINDS)
+        sd = np.array([float(o["sigma"]) for o in objects])
+        s2 = np.array([float(o["sigma2"]) for o in objects])
+        self.nv, self.d, self.nv_t = int(nv.sum()), d, int(nv_t.sum())
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbk_registration_create_multi(
+            self.ctx.h, d, self.ncp, len(objects), c(kinds), c(nv), c(pts), c(nc), c(cells), c(nv_t), c(pts_t), c(nc_t),
+            c(cells_t), c(sd), c(s2), self.T, float(sigma_def), int(heun), ctypes.byref(h)))
+        self.h = h
+        return self
+
+    def set_template(self, pts):
+        """Replaces the template points (all objects)."""
+        pts = _f64(pts)
+        if tuple(pts.shape) != (self.nv, self.d):
+            raise ValueError("template shape")
+        self.ctx.check(self.ctx.lib.gbk_registration_set_template(self.h, _ptr(pts)))
+
     def set_point_weights(self, tmpl_weights=None, tgt_weights=None):
         """Point weights of a point-cloud registration (None keeps the current ones)."""
         w = None if tmpl_weights is None else _f64(tmpl_weights)
@@ -250,6 +281,110 @@ class Registration:
     def close(self):
         if getattr(self, "h", None):
             self.ctx.lib.gbk_registration_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _objects_arrays(objects, d, kinds):
+    """Per-object arrays of a multi-object description: kinds, point counts, concatenated points,
+    cell counts, concatenated cells (int32, cell-free kinds contribute none)."""
+    k = np.array([kinds[o["kind"]] for o in objects], dtype=np.int32)
+    nv = np.array([len(o["pts"]) for o in objects], dtype=np.int64)
+    pts = np.ascontiguousarray(np.concatenate([np.asarray(o["pts"], np.float64).reshape(-1, d) for o in objects]))
+    cells, nc = [], []
+    for o in objects:
+        if o["kind"] in ("pointcloud", "landmark") or o.get("cells") is None:
+            nc.append(len(o["pts"]))
+        else:
+            c = np.asarray(o["cells"], dtype=np.int32)
+            nc.append(len(c))
+            cells.append(c.reshape(-1))
+    cells = np.ascontiguousarray(np.concatenate(cells) if cells else np.zeros(1, np.int32), dtype=np.int32)
+    return k, nv, pts, np.array(nc, dtype=np.int64), cells
+
+
+class MultiObjectAtlas:
+    """DeterministicAtlas with a template of several objects (gbk_mo_atlas_*): `objects` is a list
+    of dict(kind, pts, cells, sigma, sigma2) (kind as Registration.KINDS, sigma the data kernel width,
+    sigma2 the data sigma^2), `subjects` a list over subjects of [(points, cells) per object]. One
+    registration per subject, replayed from CUDA graphs; the optimiser deforms the reference's lagged
+    template unless set_lagged_template(False)."""
+
+    def __init__(self, ncp: int, objects, subjects, T: int, sigma_def: float, heun: bool = False,
+                 context: Context | None = None):
+        self.ctx = context or Context()
+        self.d = int(np.asarray(objects[0]["pts"]).shape[1])
+        self.ncp, self.S, self.nobj = int(ncp), len(subjects), len(objects)
+        kinds, nv, pts, nc, cells = _objects_arrays(objects, self.d, Registration.KINDS)
+        self.nv = int(nv.sum())
+        sd = np.array([float(o["sigma"]) for o in objects])
+        s2 = np.array([float(o["sigma2"]) for o in objects])
+        tn, tp, tnc, tc = [], [], [], []
+        for subj in subjects:
+            if len(subj) != self.nobj:
+                raise ValueError("every subject needs one target per template object")
+            objs = [dict(o, pts=t[0], cells=t[1]) for o, t in zip(objects, subj)]
+            _, n_t, p_t, c_n, c_t = _objects_arrays(objs, self.d, Registration.KINDS)
+            tn.append(n_t), tp.append(p_t), tnc.append(c_n)
+            if any(o["kind"] not in ("pointcloud", "landmark") for o in objects):
+                tc.append(c_t)
+        nv_t, ncell_t = np.concatenate(tn), np.concatenate(tnc)
+        tgt = np.ascontiguousarray(np.concatenate(tp))
+        tcells = np.ascontiguousarray(np.concatenate(tc) if tc else np.zeros(1, np.int32), dtype=np.int32)
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbk_mo_atlas_create(
+            self.ctx.h, self.d, self.ncp, self.nobj, c(kinds), c(nv), c(pts), c(nc), c(cells), c(sd), c(s2), self.S,
+            c(nv_t), c(tgt), c(ncell_t), c(tcells), int(T), float(sigma_def), int(heun), ctypes.byref(h)))
+        self.h = h
+
+    def set_template_smoothing(self, width: float):
+        self.ctx.check(self.ctx.lib.gbk_mo_atlas_set_template_smoothing(self.h, float(width)))
+
+    def set_lagged_template(self, enable: bool):
+        self.ctx.check(self.ctx.lib.gbk_mo_atlas_set_lagged_template(self.h, int(enable)))
+
+    def step(self, cp, tmpl, mom):
+        """Returns loglik [L, L_data, L_reg], dL/dcp, the smoothed template gradient, dL/dp."""
+        cp, tmpl, mom = (np.ascontiguousarray(a, dtype=np.float64) for a in (cp, tmpl, mom))
+        ll = np.zeros(3)
+        gc, gt, gm = np.zeros_like(cp), np.zeros_like(tmpl), np.zeros_like(mom)
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_mo_atlas_step(self.h, c(cp), c(tmpl), c(mom), c(ll), c(gc), c(gt), c(gm)))
+        return ll, gc, gt, gm
+
+    def optimize(self, cp, tmpl, mom, max_iterations: int, initial_step: float = 1e-3, optimize_cp: bool = True,
+                 optimize_template: bool = True, max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2,
+                 tolerance: float = 1e-4, nb_iter_freeze: int = 3):
+        """The reference's FastGradientAscent over [control points] [template] momenta on the device.
+        Returns a dict like Atlas.optimize plus aux_* and grad_* (extrapolated point, gradient there)."""
+        cp, tmpl, mom = (np.array(a, dtype=np.float64) for a in (cp, tmpl, mom))
+        hist = np.zeros((max_iterations + 1, 2))
+        info = np.zeros(10)
+        aux = [np.zeros_like(a) for a in (cp, tmpl, mom)]
+        grd = [np.zeros_like(a) for a in (cp, tmpl, mom)]
+        iters = ctypes.c_int(0)
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_mo_atlas_optimize(
+            self.h, c(cp), c(tmpl), c(mom), int(optimize_cp), int(optimize_template), int(max_iterations),
+            float(initial_step), int(max_line_search), float(shrink), float(expand), float(tolerance),
+            int(nb_iter_freeze), c(hist), ctypes.byref(iters), c(info), *[c(a) for a in aux], *[c(a) for a in grd]))
+        groups = [k for k, on in (("cp", optimize_cp), ("template", optimize_template), ("momenta", True)) if on]
+        idx = {"cp": (0, 5), "template": (1, 6), "momenta": (2, 7)}
+        return {"cp": cp, "template": tmpl, "mom": mom, "aux_cp": aux[0], "aux_template": aux[1], "aux_mom": aux[2],
+                "grad_cp": grd[0], "grad_template": grd[1], "grad_mom": grd[2], "history": hist[:iters.value],
+                "step": np.array([info[idx[g][0]] for g in groups]), "tau": float(info[3]),
+                "freeze_counter": int(info[4]), "grad_sq_norms": np.array([info[idx[g][1]] for g in groups]),
+                "evaluations": int(info[8]), "stopped": Registration.STOP[int(info[9])]}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbk_mo_atlas_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -285,14 +285,30 @@ int gbk_registration_create(gbk_ctx *ctx, int d, long ncp, long nv, const double
                             long nf_t, const int *tgt_tris, int T, double sigma_def,
                             double sigma_data, double data_sigma2, int data_kind, int heun,
                             gbk_registration **out);
+/* A registration whose template has nobj objects (DeformableMultiObject): object k has data_kinds[k]
+ * (as data_kind above), nv[k] template points and ncell[k] cells (points and cells concatenated
+ * over the objects in tmpl_pts / tmpl_cells, cell indices local to their object), its target's
+ * nv_t[k] points and ncell_t[k] cells likewise, data kernel width sigma_data[k] and data sigma^2
+ * data_sigma2[k] (the per-object arrays on the host). All template points flow together;
+ * L_data = -0.5 sum_k match_k / data_sigma2_k (DeterministicAtlas.cxx:121-125) and loglik[3] is the
+ * sum of the matches. */
+int gbk_registration_create_multi(gbk_ctx *ctx, int d, long ncp, int nobj, const int *data_kinds, const long *nv,
+                                  const double *tmpl_pts, const long *ncell, const int *tmpl_cells, const long *nv_t,
+                                  const double *tgt_pts, const long *ncell_t, const int *tgt_cells,
+                                  const double *sigma_data, const double *data_sigma2, int T, double sigma_def,
+                                  int heun, gbk_registration **out);
+/* Replaces the template points (all objects, nv x d, host or device); a captured iteration graph
+ * reads the new points. */
+int gbk_registration_set_template(gbk_registration *reg, const double *pts);
 /* Log-likelihood and gradient at (cp, mom): loglik[5] = {L, L_data, L_reg, match, <K p, p>},
  * grad_cp / grad_mom = dL/dcp, dL/dp (ncp x d). Any output may be NULL. Returns when the outputs
  * are written. The first call runs the kernels directly, the second captures them into a CUDA
  * graph, later calls replay it. */
 int gbk_registration_step(gbk_registration *reg, const double *cp, const double *mom,
                           double *loglik, double *grad_cp, double *grad_mom);
-/* Point weights of a point-cloud registration (data_kind 4): template (nv) and target (nv_t)
- * weights, host or device; either may be NULL to keep the current ones. A captured iteration
+/* Point weights of the point-cloud objects (data_kind 4) of a registration: template weights over
+ * all template points (nv, entries of other objects ignored) and target weights over all target
+ * points, host or device; either may be NULL to keep the current ones. A captured iteration
  * graph reads the new weights (same device buffers). */
 int gbk_registration_set_point_weights(gbk_registration *reg, const double *w_tmpl, const double *w_tgt);
 /* 0 disables graph capture (every step launches the kernels directly). */
@@ -332,6 +348,42 @@ void gbk_registration_destroy(gbk_registration *reg);
  * calls that overlap on the GPU race: serialise them. Queued on the context's stream. */
 int gbk_kernel_norm_noalloc(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
                             double sigma, double *out);
+
+/* ---- atlas with a multi-object template, one registration per subject ------------------- */
+
+typedef struct gbk_mo_atlas gbk_mo_atlas;
+
+/* DeterministicAtlas (DeterministicAtlas.cxx:99-280, AbstractAtlas.cxx:492-748) of nsubj subjects
+ * with a template of nobj objects, described as for gbk_registration_create_multi: template
+ * objects by data_kinds, nv, tmpl_pts, ncell, tmpl_cells, sigma_data, data_sigma2; the subjects'
+ * objects by nv_t[s * nobj + k] points and ncell_t[s * nobj + k] cells, their points and cells
+ * concatenated subject by subject, object by object, in tgt_pts / tgt_cells. Every subject runs as
+ * one replayed iteration graph, subjects in order on the atlas's stream. */
+int gbk_mo_atlas_create(gbk_ctx *ctx, int d, long ncp, int nobj, const int *data_kinds, const long *nv,
+                        const double *tmpl_pts, const long *ncell, const int *tmpl_cells, const double *sigma_data,
+                        const double *data_sigma2, int nsubj, const long *nv_t, const double *tgt_pts,
+                        const long *ncell_t, const int *tgt_cells, int T, double sigma_def, int heun,
+                        gbk_mo_atlas **out);
+/* Template-gradient smoothing width (ConvolveGradTemplate, AbstractAtlas.cxx:724-748), applied
+ * object by object over that object's template points; 0 (default) keeps the L2 gradient. */
+int gbk_mo_atlas_set_template_smoothing(gbk_mo_atlas *atlas, double width);
+/* 1 (default): the optimiser deforms the template of the previous SetFixedEffects call, as the
+ * reference's AbstractAtlas::SetFixedEffects (AbstractAtlas.cxx:52-65) does, while the step and the
+ * smoothing use the current template; 0: every evaluation deforms its own template. */
+int gbk_mo_atlas_set_lagged_template(gbk_mo_atlas *atlas, int enable);
+/* loglik[3] = {L, L_data, L_reg} at (cp: ncp x d, tmpl: nv x d, mom: nsubj x ncp x d), host or
+ * device; grad_cp, grad_tmpl (smoothed), grad_mom: the gradients (any may be NULL). */
+int gbk_mo_atlas_step(gbk_mo_atlas *atlas, const double *cp, const double *tmpl, const double *mom, double *loglik,
+                      double *grad_cp, double *grad_tmpl, double *grad_mom);
+/* FastGradientAscent (FastGradientAscent.cxx:48-300) over [control points] [template] momenta, as
+ * gbk_atlas_optimize (same info layout); aux_* / grad_* (optional) receive the extrapolated point
+ * and the gradient there. */
+int gbk_mo_atlas_optimize(gbk_mo_atlas *atlas, double *cp, double *tmpl, double *mom, int optimize_cp,
+                          int optimize_template, int max_iterations, double initial_step, int max_line_search,
+                          double shrink, double expand, double tolerance, int nb_iter_freeze, double *history,
+                          int *iterations, double *info, double *aux_cp, double *aux_tmpl, double *aux_mom,
+                          double *grad_cp, double *grad_tmpl, double *grad_mom);
+void gbk_mo_atlas_destroy(gbk_mo_atlas *atlas);
 
 /* ---- batched atlas iteration (all subjects per launch), CUDA-graph replay ---------------- */
 

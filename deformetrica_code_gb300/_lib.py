@@ -118,6 +118,7 @@ SIGNATURES = {
     "gbk_atlas_set_template_smoothing": (_I, [_P, _D]),
     "gbk_atlas_optimize": (_I, [_P, _P, _P, _P, _I, _I, _I, _D, _I, _D, _D, _D, _I, _P, _P, _P]),
     "gbk_atlas_destroy": (None, [_P]),
+    "gbk_atlas_set_lagged_template": (_I, [_P, _I]),
 }
 
 _lib = None

@@ -241,6 +241,7 @@ struct gbk_atlas {
   long ncp = 0, nv = 0, nf = 0;
   double sigma_def = 1, sigma_data = 1, data_sigma2 = 1;
   double smoothing = 0.0;  // template-gradient smoothing width (0: the L2 gradient)
+  int lag = 1;             // the optimiser deforms the reference's lagged template
   std::vector<long> nft;  // target faces per subject
   cudaStream_t stream = nullptr;
   std::vector<void *> owned;
@@ -254,6 +255,9 @@ struct gbk_atlas {
   double *lm0 = nullptr, *lm = nullptr, *theta = nullptr;       // nv x 3, S x T x nv x 3
   double *va = nullptr, *vb = nullptr, *vc = nullptr, *vd = nullptr;  // S x max(ncp, nv) x 3
   double *kp = nullptr, *greg = nullptr, *gmom = nullptr, *gcp = nullptr, *gtmpl = nullptr, *gtmpl_l2 = nullptr;
+  // the points the template gradient is smoothed over (the current fixed-effect template, = lm0
+  // outside the optimiser), and the optimiser's current fixed-effect template (lag)
+  double *smooth = nullptr, *tmpl_fe = nullptr;
   double *thT = nullptr;                                        // S x nv x 3
   int *flag = nullptr, *tris = nullptr, *csr_ptr = nullptr, *csr_fc = nullptr;
   double *cs = nullptr, *ns = nullptr, *mns = nullptr, *ws = nullptr;   // S x nf x {3,6}
@@ -654,8 +658,8 @@ int gbk_atlas::body() {
   if ((rc = ok(cudaGetLastError(), "atlas gradients"))) return rc;
   if (smoothing > 0) {  // Sobolev template gradient: K_smooth(template, template) L2 (ConvolveGradTemplate)
     PairArgs q = pa(nv, nv, smoothing);
-    q.x = lm0;
-    q.y = lm0;
+    q.x = smooth;
+    q.y = smooth;
     q.w = gtmpl_l2;
     q.w_ld = 3;
     q.out0 = gtmpl;
@@ -764,6 +768,7 @@ int gbk_atlas_create(gbk_ctx *c, long ncp, const double *cp, long nv, const doub
               {&a->theta, S * TT * m}, {&a->va, S * rows3}, {&a->vb, S * rows3}, {&a->vc, S * rows3},
               {&a->vd, S * rows3}, {&a->kp, S * rows3}, {&a->greg, S * rows3}, {&a->gmom, S * n},
               {&a->gcp, (size_t)n}, {&a->gtmpl, (size_t)m}, {&a->gtmpl_l2, (size_t)m},
+              {&a->smooth, (size_t)m}, {&a->tmpl_fe, (size_t)m},
               {&a->cs, S * nf * 3}, {&a->ns, S * nf * 3},
               {&a->mns, S * nf * 6}, {&a->ws, S * nf * 6}, {&a->kts, S * nf * 6}, {&a->ktt, S * nf * 6},
               {&a->gs, S * nf * 3}, {&a->gt, S * nf * 3}, {&a->kt, S * nf * 3}, {&a->gk, S * nf * 3},
@@ -781,6 +786,7 @@ int gbk_atlas_create(gbk_ctx *c, long ncp, const double *cp, long nv, const doub
     cudaStream_t st = a->stream;
     rc = c->cuda(cudaMemcpyAsync(a->cp, cp, n * sizeof(double), cudaMemcpyDefault, st), "copy");
     if (!rc) rc = c->cuda(cudaMemcpyAsync(a->lm0, tmpl_pts, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+    if (!rc) rc = c->cuda(cudaMemcpyAsync(a->smooth, tmpl_pts, m * sizeof(double), cudaMemcpyDefault, st), "copy");
     if (!rc) rc = c->cuda(cudaMemcpyAsync(a->tris, th.data(), th.size() * sizeof(int), cudaMemcpyHostToDevice, st), "copy");
     if (!rc) rc = c->cuda(cudaMemcpyAsync(a->csr_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice, st), "copy");
     if (!rc) rc = c->cuda(cudaMemcpyAsync(a->csr_fc, fc.data(), fc.size() * sizeof(int), cudaMemcpyHostToDevice, st), "copy");
@@ -866,6 +872,12 @@ int gbk_atlas_step(gbk_atlas *a, const double *mom, double *loglik, double *grad
 
 long long gbk_atlas_graph_launches(const gbk_atlas *a) { return a ? a->graph_kernels : 0; }
 
+int gbk_atlas_set_lagged_template(gbk_atlas *a, int enable) {
+  if (!a) return GBK_ERR_ARG;
+  a->lag = enable ? 1 : 0;
+  return GBK_OK;
+}
+
 int gbk_atlas_set_template_smoothing(gbk_atlas *a, double width) {
   if (!a) return GBK_ERR_ARG;
   if (!(width >= 0)) return a->c->fail(GBK_ERR_ARG, "smoothing width must be >= 0");
@@ -891,8 +903,12 @@ int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int 
   double *sq_dev = nullptr;
   int rc = c->cuda(cudaMalloc(&sq_dev, 4 * sizeof(double)), "cudaMalloc (optimiser)");
   if (!rc && !optimize_cp) rc = c->cuda(cudaMemcpyAsync(a->cp, cp, n * sizeof(double), cudaMemcpyDefault, st), "copy");
-  if (!rc && !optimize_template)
-    rc = c->cuda(cudaMemcpyAsync(a->lm0, tmpl, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+  // the deformed template (lm0), the smoothing points and the current fixed-effect template all
+  // start at the initial template
+  if (!rc) rc = c->cuda(cudaMemcpyAsync(a->lm0, tmpl, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+  if (!rc) rc = c->cuda(cudaMemcpyAsync(a->smooth, tmpl, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+  if (!rc) rc = c->cuda(cudaMemcpyAsync(a->tmpl_fe, tmpl, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+  const bool lag = a->lag && optimize_template;
   int ng = 0, gcp = -1, gt = -1;
   long sizes[3];
   double *params[3];
@@ -912,7 +928,11 @@ int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int 
   FgaEvaluate ev = [&](double *const *p, bool need_grad, double *terms, double *const *g, double *sq) -> int {
     int e = GBK_OK;
     if (gcp >= 0) e = c->cuda(cudaMemcpyAsync(a->cp, p[gcp], n * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
-    if (!e && gt >= 0) e = c->cuda(cudaMemcpyAsync(a->lm0, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+    // without the lag the evaluation deforms its own template; with it, lm0 holds the template of
+    // the previous SetFixedEffects call (set_fixed below)
+    if (!e && gt >= 0 && !lag)
+      e = c->cuda(cudaMemcpyAsync(a->lm0, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+    if (!e && gt >= 0) e = c->cuda(cudaMemcpyAsync(a->smooth, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
     if (!e) e = c->cuda(cudaMemcpyAsync(a->mom, p[gm], nm * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
     if (!e) e = a->run();
     double out[3];
@@ -949,7 +969,18 @@ int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int 
   o.expand = expand;
   o.tolerance = tolerance;
   FgaResult res;
-  if (!rc) rc = fast_gradient_ascent(c, st, ng, sizes, params, o, ev, &res, nullptr, nullptr);
+  // SetFixedEffects (AbstractAtlas.cxx:52-65): the template objects take the previous fixed-effect
+  // template
+  FgaSetFixed sf = [&](double *const *p) -> int {
+    int e = c->cuda(cudaMemcpyAsync(a->lm0, a->tmpl_fe, m * sizeof(double), cudaMemcpyDeviceToDevice, st), "lag");
+    if (!e) e = c->cuda(cudaMemcpyAsync(a->tmpl_fe, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "lag");
+    return e;
+  };
+  if (!rc) rc = fast_gradient_ascent(c, st, ng, sizes, params, o, ev, &res, nullptr, nullptr, lag ? sf : FgaSetFixed());
+  // later steps deform and smooth over the final template
+  if (!rc && optimize_template) rc = c->cuda(cudaMemcpyAsync(a->lm0, tmpl, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+  if (!rc && optimize_template) rc = c->cuda(cudaMemcpyAsync(a->smooth, tmpl, m * sizeof(double), cudaMemcpyDefault, st), "copy");
+  if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
   if (sq_dev) cudaFree(sq_dev);
   if (rc) return rc;
   std::copy(res.history.begin(), res.history.end(), history);

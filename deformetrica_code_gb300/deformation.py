@@ -418,6 +418,10 @@ class Atlas:
             ctypes.byref(h)))
         self.h = h
 
+    def set_lagged_template(self, enable: bool):
+        """True (default): optimize() deforms the reference's lagged template (gbk_atlas_set_lagged_template)."""
+        self.ctx.check(self.ctx.lib.gbk_atlas_set_lagged_template(self.h, int(enable)))
+
     def set_graph(self, enable: bool):
         self.ctx.check(self.ctx.lib.gbk_atlas_set_graph(self.h, int(enable)))
 

@@ -413,6 +413,10 @@ long long gbk_atlas_graph_launches(const gbk_atlas *atlas);
  * smoothing-kernel-width-ratio x deformation kernel width, estimate_atlas.cxx:457); 0 (default)
  * returns the L2 gradient. */
 int gbk_atlas_set_template_smoothing(gbk_atlas *atlas, double width);
+/* 1 (default): gbk_atlas_optimize deforms the template of the previous SetFixedEffects call, as
+ * the reference's AbstractAtlas::SetFixedEffects (AbstractAtlas.cxx:52-65) does, while the step and
+ * the smoothing use the current template; 0: every evaluation deforms its own template. */
+int gbk_atlas_set_lagged_template(gbk_atlas *atlas, int enable);
 /* FastGradientAscent (FastGradientAscent.cxx:48-300) of the atlas over its control points
  * (optimize_cp), template points (optimize_template) and all subjects' momenta, on the device.
  * cp (ncp x 3), tmpl (nv x 3), mom (nsub x ncp x 3): start point in, final fixed effects out (host or

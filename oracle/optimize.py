@@ -149,14 +149,14 @@ def registration_evaluator(K, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T: int, si
 
 def atlas_evaluator(K, tmpl_cells, targets, T: int, sigma_def: float, sigma_data: float, data_sigma2: float,
                     kind: str = "currents", heun: bool = True, smoothing_width: float = 0.0,
-                    optimize_cp: bool = True, optimize_template: bool = True, cp=None, tmpl=None):
+                    optimize_cp: bool = True, optimize_template: bool = True, cp=None, tmpl=None, lag=None):
     """evaluate() of a DeterministicAtlas over the subjects `targets` ([(points, cells)]): parameter
     groups in the reference's order [ControlPoints] [TemplateData] Momenta (one ncp x d block per
     subject, stacked). The template gradient is the sum over subjects of -theta_s(0)
     (AbstractAtlas.cxx:559-613) smoothed by a Gaussian of width smoothing_width over the template
     points (ConvolveGradTemplate, :724-748; no smoothing at width 0), and its squared norm is
     <L2, smoothed> (DeterministicAtlas.cxx:232). Frozen groups take their values from `cp` /
-    `tmpl`."""
+    `tmpl`. With `lag` (a LaggedTemplate) the subjects deform the reference's lagged template."""
     from .deformation import registration
     cp_frozen, tmpl_frozen = cp, tmpl
 
@@ -171,8 +171,9 @@ def atlas_evaluator(K, tmpl_cells, targets, T: int, sigma_def: float, sigma_data
         g_cp = np.zeros_like(cp)
         g_t = np.zeros_like(tmpl)
         g_mom = np.zeros_like(mom)
+        moved = tmpl if lag is None or not optimize_template else lag.deformed
         for s, (pts, cells) in enumerate(targets):
-            L, gc, gm, info = registration(K, cp, mom[s], tmpl, tmpl_cells, pts, cells, T, sigma_def, sigma_data,
+            L, gc, gm, info = registration(K, cp, mom[s], moved, tmpl_cells, pts, cells, T, sigma_def, sigma_data,
                                            data_sigma2, kind=kind, heun=heun)
             d_s = -0.5 * info["match"] / data_sigma2
             data += d_s
@@ -243,7 +244,7 @@ def multi_object_atlas_evaluator(K, objects, subjects, T: int, sigma_def: float,
         g_cp = np.zeros_like(cp)
         g_t = np.zeros_like(tmpl)
         g_mom = np.zeros_like(mom)
-        moved = tmpl if lag is None else lag.deformed
+        moved = tmpl if lag is None or not optimize_template else lag.deformed
         for s, targets in enumerate(subjects):
             d_s, r_s, gc, gm, info = registration_multi(K, cp, mom[s], moved, objects, targets, T, sigma_def, heun)
             data += d_s

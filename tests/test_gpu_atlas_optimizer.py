@@ -30,23 +30,27 @@ def problem():
     return cp, tp, tf, targets, mom, dict(T=5, sigma_def=0.25, sigma_data=0.15, data_sigma2=0.01)
 
 
-@pytest.mark.parametrize("groups", [(True, True), (False, True), (True, False)])
-def test_atlas_optimizer_matches_oracle(gb, groups):
+@pytest.mark.parametrize("groups,lag", [((True, True), True), ((True, True), False), ((False, True), True),
+                                        ((True, False), True)])
+def test_atlas_optimizer_matches_oracle(gb, groups, lag):
+    """lag: the reference's lagged template (AbstractAtlas.cxx:52-65, the default) or not."""
     import oracle
-    from oracle.optimize import atlas_evaluator, fast_gradient_ascent
+    from oracle.optimize import LaggedTemplate, atlas_evaluator, fast_gradient_ascent
     from deformetrica_code_gb300.deformation import Atlas
     opt_cp, opt_t = groups
     K = oracle.load("port")
     cp, tp, tf, targets, mom, kw = problem()
     smoothing, iters, step0 = 0.1, 4, 1e-3
+    lt = LaggedTemplate(tp, int(opt_cp)) if lag and opt_t else None
     ev = atlas_evaluator(K, tf, targets, kw["T"], kw["sigma_def"], kw["sigma_data"], kw["data_sigma2"], "currents",
-                         True, smoothing, opt_cp, opt_t, cp=cp, tmpl=tp)
+                         True, smoothing, opt_cp, opt_t, cp=cp, tmpl=tp, lag=lt)
     start = ([cp] if opt_cp else []) + ([tp] if opt_t else []) + [mom]
-    ref = fast_gradient_ascent(ev, start, step0, iters)
+    ref = fast_gradient_ascent(ev, start, step0, iters, set_fixed=lt.set_fixed if lt else None)
     for mode, tol in ((gb.GBK_MODE_F64, 1e-9), (gb.GBK_MODE_F32C, 1e-5)):
         ctx = gb.Context(mode=mode)
         atlas = Atlas(cp, tp, tf, targets, kind="currents", context=ctx, **kw)
         atlas.set_template_smoothing(smoothing)
+        atlas.set_lagged_template(lag)
         r = atlas.optimize(cp, tp, mom, iters, step0, optimize_cp=opt_cp, optimize_template=opt_t)
         atlas.close()
         h, hr = r["history"], ref["history"]

@@ -8,7 +8,12 @@
 // compensation terms in shared memory 605-636 ms (removed). Longer plain-FP32 runs before each
 // compensated fold are faster but less accurate (spatial order, 1e6: MERGE 64 534 ms, normwise
 // 1.9e-7; 128: 524 ms, 2.7e-7; 256: 519 ms, 4.0e-7), so every variant keeps runs of 64 and the
-// autotuner only trades speed for speed. FP64 uses one target per thread.
+// autotuner only trades speed for speed. An expanded exponent, -|x'|^2 - |y'|^2 + 2 x'.y' with the
+// two norms precomputed (two FP32 lane instructions fewer per pair, one more 16-byte shared load
+// per source), measured 519 ms in every CTA (normwise error 9.8e-7: the expansion loses accuracy
+// when the CTA's target box is wide) and 533 ms when restricted to CTAs whose box has a
+// half-diagonal of at most one scaled unit, so the difference form stays. FP64 uses one target per
+// thread.
 #include "gbk_dispatch.h"
 
 namespace gbk {

@@ -308,6 +308,29 @@ def data_term_bench(steps: int, cpu: bool = True, nu: int = 500, nv: int = 200, 
         sec = statistics.median(ts)
         res[kind] = {"s_per_call": sec, "pairs_per_s": pairs / sec, "evaluated_pairs_per_call": ev,
                      "match": m, "includes": "host->device copy of both meshes, device->host gradient"}
+    # point clouds (the tori's vertices, unit weights) and volume meshes (jittered tetrahedral grids)
+    from deformetrica_code_gb300.deformation import pointcloud_match, volume_match
+    from deformetrica_code_gb300.meshes import tet_grid
+    ng = max(4, 30 * nv // 200)
+    vs, cs_v = tet_grid(ng, seed=7)
+    vt, ct_v = tet_grid(ng, seed=8)
+    extra = {
+        "pointcloud": (lambda: pointcloud_match(ps, None, pt, None, sigma, context=ctx), ps.shape[0],
+                       f"two point clouds of {ps.shape[0]} points (the tori's vertices), unit weights"),
+        "volume": (lambda: volume_match(vs, cs_v, vt, ct_v, sigma, context=ctx), cs_v.shape[0],
+                   f"two jittered tetrahedral grids of {cs_v.shape[0]} tetrahedra"),
+    }
+    for kind, (fn, n_el, what) in extra.items():
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            m, _ = fn()
+            ts.append(time.perf_counter() - t0)
+        sec = statistics.median(ts)
+        res[kind] = {"workload": what + f", sigma {sigma}", "s_per_call": sec, "pairs_per_s": 3.0 * n_el * n_el / sec,
+                     "match": m, "includes": "host->device copy of both objects, device->host gradient"}
     if cpu:
         import oracle
         from oracle import geometry as G
@@ -315,6 +338,7 @@ def data_term_bench(steps: int, cpu: bool = True, nu: int = 500, nv: int = 200, 
         cs, cfs = torus(100, 40, seed=5)
         ct, cft = torus(100, 40, seed=6)
         Fc = cfs.shape[0]
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
         for kind in ("currents", "varifold"):
             om = G.currents_match if kind == "currents" else G.varifold_match
             og = G.currents_match_gradient if kind == "currents" else G.varifold_match_gradient
@@ -323,8 +347,21 @@ def data_term_bench(steps: int, cpu: bool = True, nu: int = 500, nv: int = 200, 
             og(K, sigma, cs, cfs, ct, cft)
             dt = time.perf_counter() - t0
             res[kind]["cpu_oracle"] = {"s_per_call": dt, "pairs_per_s": 3.0 * Fc * Fc / dt, "triangles": Fc,
-                                       "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
-                                       "kind": "port (FP64)"}
+                                       "cores": cores, "kind": "port (FP64)"}
+        t0 = time.perf_counter()
+        G.pointcloud_match(K, sigma, cs, None, ct, None)
+        G.pointcloud_match_gradient(K, sigma, cs, None, ct, None)
+        dt = time.perf_counter() - t0
+        res["pointcloud"]["cpu_oracle"] = {"s_per_call": dt, "pairs_per_s": 3.0 * len(cs) ** 2 / dt,
+                                           "points": len(cs), "cores": cores, "kind": "port (FP64)"}
+        qs, qcs = tet_grid(8, seed=7)
+        qt, qct = tet_grid(8, seed=8)
+        t0 = time.perf_counter()
+        G.volume_match(K, sigma, qs, qcs, qt, qct)
+        G.volume_match_gradient(K, sigma, qs, qcs, qt, qct)
+        dt = time.perf_counter() - t0
+        res["volume"]["cpu_oracle"] = {"s_per_call": dt, "pairs_per_s": 3.0 * len(qcs) ** 2 / dt,
+                                       "tetrahedra": len(qcs), "cores": cores, "kind": "port (FP64)"}
     return res
 
 
@@ -379,6 +416,44 @@ def optimizer_bench(cpu: bool = True, reg_iters: int = 10):
                                   "evaluations": r["evaluations"], "s_per_evaluation": dt / max(1, r["evaluations"]),
                                   "loglik_first_last": [float(r["history"][0].sum()), float(r["history"][-1].sum())],
                                   "stopped": r["stopped"]}
+    # the reference's functional test 8: a two-object curve atlas of three subjects
+    from deformetrica_code_gb300.deformation import MultiObjectAtlas
+    pb = dict(np.load(os.path.join(ROOT, "tests", "golden", "parabola_atlas.npz")))
+    objs = [dict(kind="curve_currents", pts=pb[f"tmpl{i}_pts"], cells=pb[f"tmpl{i}_segs"],
+                 sigma=float(pb["data_kernel_width"]), sigma2=float(pb["data_sigma2"])) for i in (1, 2)]
+    subjects = [[(pb[f"subj{s}_obj{i}_pts"], pb[f"subj{s}_obj{i}_segs"]) for i in (1, 2)] for s in (1, 2, 3)]
+    tmpl = np.concatenate([pb["tmpl1_pts"], pb["tmpl2_pts"]])
+    mom0 = np.zeros((3,) + pb["cp0"].shape)
+    hist = pb["state_history"]
+    res["parabola_atlas"] = {"workload": "reference functional test 8: two OrientedPolyline objects (60 points each), "
+                                         "3 subjects, 40 CP, T = 10, 10 FastGradientAscent iterations over control "
+                                         "points, template and momenta, lagged template"}
+    for mode, name in ((g.GBK_MODE_F64, "f64"), (g.GBK_MODE_F32C, "f32c")):
+        a = MultiObjectAtlas(len(pb["cp0"]), objs, subjects, int(pb["number_of_time_points"]),
+                             float(pb["kernel_width"]), heun=False, context=g.Context(mode=mode))
+        a.set_template_smoothing(float(pb["smoothing_width"]))
+        a.optimize(pb["cp0"], tmpl, mom0, 1, 1e-3)  # warm-up: graphs captured
+        t0 = time.perf_counter()
+        r = a.optimize(pb["cp0"], tmpl, mom0, int(pb["max_iterations"]), float(pb["initial_step"]))
+        dt = time.perf_counter() - t0
+        a.close()
+        res["parabola_atlas"][name] = {"s_total": dt, "evaluations": r["evaluations"],
+                                       "history_max_rel_err_vs_reference_state":
+                                           float(np.abs(r["history"] - hist).max() / np.abs(hist).max())}
+    if cpu:
+        from oracle.optimize import LaggedTemplate, fast_gradient_ascent, multi_object_atlas_evaluator
+        import oracle
+        K = oracle.load("port")
+        oobj = [dict(kind="curve_currents", cells=pb[f"tmpl{i}_segs"], sigma=float(pb["data_kernel_width"]),
+                     sigma2=float(pb["data_sigma2"]), n=len(pb[f"tmpl{i}_pts"])) for i in (1, 2)]
+        lt = LaggedTemplate(tmpl, 1)
+        ev = multi_object_atlas_evaluator(K, oobj, subjects, int(pb["number_of_time_points"]), float(pb["kernel_width"]),
+                                          heun=False, smoothing_width=float(pb["smoothing_width"]), lag=lt)
+        t0 = time.perf_counter()
+        r = fast_gradient_ascent(ev, [pb["cp0"], tmpl, mom0], float(pb["initial_step"]), int(pb["max_iterations"]),
+                                 set_fixed=lt.set_fixed)
+        res["parabola_atlas"]["cpu_oracle"] = {"s_total": time.perf_counter() - t0, "evaluations": r["evaluations"],
+                                               "kind": "port (FP64)"}
     return res
 
 

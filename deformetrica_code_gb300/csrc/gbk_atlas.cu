@@ -925,16 +925,30 @@ int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int 
   const int gm = ng;
   sizes[ng] = nm;
   params[ng++] = mom;
+  // With the lag the ascent evaluates the extrapolated point twice in a row, the log-likelihood and
+  // then the gradient, with only SetFixedEffects calls between (which write no parameter buffer).
+  // A run computes both, so the second evaluation reuses the first run when the parameter buffers
+  // and the buffer the deformed template was copied from are the same.
+  const double *fe_src = tmpl, *def_src = tmpl;  // parameter buffers behind tmpl_fe and lm0
+  const double *last_p[3] = {nullptr, nullptr, nullptr}, *last_def = nullptr;
+  bool last_nograd = false;
   FgaEvaluate ev = [&](double *const *p, bool need_grad, double *terms, double *const *g, double *sq) -> int {
     int e = GBK_OK;
-    if (gcp >= 0) e = c->cuda(cudaMemcpyAsync(a->cp, p[gcp], n * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
-    // without the lag the evaluation deforms its own template; with it, lm0 holds the template of
-    // the previous SetFixedEffects call (set_fixed below)
-    if (!e && gt >= 0 && !lag)
-      e = c->cuda(cudaMemcpyAsync(a->lm0, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
-    if (!e && gt >= 0) e = c->cuda(cudaMemcpyAsync(a->smooth, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
-    if (!e) e = c->cuda(cudaMemcpyAsync(a->mom, p[gm], nm * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
-    if (!e) e = a->run();
+    bool reuse = lag && need_grad && last_nograd && def_src == last_def;
+    for (int k = 0; k < ng; ++k) reuse = reuse && last_p[k] == p[k];
+    for (int k = 0; k < ng; ++k) last_p[k] = p[k];
+    last_def = def_src;
+    last_nograd = !need_grad;
+    if (!reuse) {
+      if (gcp >= 0) e = c->cuda(cudaMemcpyAsync(a->cp, p[gcp], n * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+      // without the lag the evaluation deforms its own template; with it, lm0 holds the template
+      // of the previous SetFixedEffects call (set_fixed below)
+      if (!e && gt >= 0 && !lag)
+        e = c->cuda(cudaMemcpyAsync(a->lm0, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+      if (!e && gt >= 0) e = c->cuda(cudaMemcpyAsync(a->smooth, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+      if (!e) e = c->cuda(cudaMemcpyAsync(a->mom, p[gm], nm * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+      if (!e) e = a->run();
+    }
     double out[3];
     if (!e) e = c->cuda(cudaMemcpyAsync(out, a->out, sizeof out, cudaMemcpyDeviceToHost, st), "read L");
     double h[3] = {0, 0, 0};
@@ -972,6 +986,8 @@ int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int 
   // SetFixedEffects (AbstractAtlas.cxx:52-65): the template objects take the previous fixed-effect
   // template
   FgaSetFixed sf = [&](double *const *p) -> int {
+    def_src = fe_src;
+    fe_src = p[gt];
     int e = c->cuda(cudaMemcpyAsync(a->lm0, a->tmpl_fe, m * sizeof(double), cudaMemcpyDeviceToDevice, st), "lag");
     if (!e) e = c->cuda(cudaMemcpyAsync(a->tmpl_fe, p[gt], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "lag");
     return e;

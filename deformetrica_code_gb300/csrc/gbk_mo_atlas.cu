@@ -52,16 +52,19 @@ struct gbk_mo_atlas {
     return GBK_OK;
   }
 
+  std::vector<double> outs;  // the last run's log-likelihood terms per subject
+
   // terms[2] = {L_data, L_reg} at (cp, deformed template `moved`, mom: S x ncp x d), all device; with
   // gcp / gmom / gtmpl non-null also the gradients (the template one smoothed over the points
-  // `smooth_pts`) and sq[3] = the squared norms.
+  // `smooth_pts`) and sq[3] = the squared norms. rerun = false: the subjects' last runs (same
+  // inputs) are still in their buffers.
   int evaluate(const double *cp, const double *moved, const double *smooth_pts, const double *mom, double *terms,
-               double *gcp, double *gtmpl, double *gmom, double *sq) {
+               double *gcp, double *gtmpl, double *gmom, double *sq, bool rerun = true) {
     const long n = ncp * d, m = nv * d;
     const size_t nb = (size_t)n * sizeof(double);
     int rc = GBK_OK;
-    std::vector<double> outs((size_t)S * 5);
-    for (int s = 0; s < S && !rc; ++s) {
+    outs.resize((size_t)S * 5);
+    for (int s = 0; s < S && !rc && rerun; ++s) {
       gbk_registration *r = subj[s];
       rc = c->cuda(cudaMemcpyAsync(r->cp, cp, nb, cudaMemcpyDeviceToDevice, stream), "copy cp");
       if (!rc) rc = c->cuda(cudaMemcpyAsync(r->mom, mom + (long)s * n, nb, cudaMemcpyDeviceToDevice, stream), "copy mom");
@@ -281,13 +284,25 @@ int gbk_mo_atlas_optimize(gbk_mo_atlas *a, double *cp, double *tmpl, double *mom
   sizes[ng] = nm, params[ng] = mom, aux_o[ng] = aux_mom, grad_o[ng] = grad_mom;
   ++ng;
   const bool lag = a->lag && optimize_template;
+  // With the lag the ascent evaluates the extrapolated point twice in a row, the log-likelihood and
+  // then the gradient, with only SetFixedEffects calls between (which write no parameter buffer);
+  // the second evaluation reuses the subjects' runs when the parameter buffers and the buffer the
+  // deformed template was copied from are the same.
+  const double *fe_src = tmpl, *def_src = tmpl;
+  const double *last_p[3] = {nullptr, nullptr, nullptr}, *last_def = nullptr;
+  bool last_nograd = false;
   FgaEvaluate ev = [&](double *const *p, bool need_grad, double *terms, double *const *g, double *sq) -> int {
     const double *pcp = optimize_cp ? p[gi_cp] : cp_frozen;
     const double *pt = optimize_template ? p[gi_t] : tmpl_frozen;
+    bool reuse = lag && need_grad && last_nograd && def_src == last_def;
+    for (int k = 0; k < ng; ++k) reuse = reuse && last_p[k] == p[k];
+    for (int k = 0; k < ng; ++k) last_p[k] = p[k];
+    last_def = def_src;
+    last_nograd = !need_grad;
     double h[3] = {0, 0, 0};
     int e = a->evaluate(pcp, lag ? a->tmpl_def : pt, pt, p[gi_m], terms, need_grad && optimize_cp ? g[gi_cp] : nullptr,
                         need_grad && optimize_template ? g[gi_t] : nullptr, need_grad ? g[gi_m] : nullptr,
-                        need_grad ? h : nullptr);
+                        need_grad ? h : nullptr, !reuse);
     if (!e && need_grad) {
       if (optimize_cp) sq[gi_cp] = h[0];
       if (optimize_template) sq[gi_t] = h[1];
@@ -297,6 +312,8 @@ int gbk_mo_atlas_optimize(gbk_mo_atlas *a, double *cp, double *tmpl, double *mom
   };
   // SetFixedEffects: the template objects take the previous fixed-effect template
   FgaSetFixed sf = [&](double *const *p) -> int {
+    def_src = fe_src;
+    fe_src = p[gi_t];
     int e = c->cuda(cudaMemcpyAsync(a->tmpl_def, a->tmpl_fe, m * sizeof(double), cudaMemcpyDeviceToDevice, st), "lag");
     if (!e) e = c->cuda(cudaMemcpyAsync(a->tmpl_fe, p[gi_t], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "lag");
     return e;

@@ -6,7 +6,9 @@
   (the registration target);
 * torus(nu, nv, R, r, noise, seed): a (u, v) grid torus with 2 nu nv faces (500 x 200 -> 200,000);
 * perturbed_sphere(n, noise, seed): Fibonacci points on the unit sphere perturbed radially and
-  triangulated by their convex hull (2 n - 4 faces), the atlas subjects.
+  triangulated by their convex hull (2 n - 4 faces), the atlas subjects;
+* tet_grid(n, noise, seed): the unit cube cut into n^3 cells of six tetrahedra each (6 n^3 cells,
+  all positively oriented), vertices jittered, for the volume-mesh data term.
 
 Faces are oriented so that the reference's face normal (p2 - p0) x (p1 - p0) / 2 points outward;
 the currents data term depends on orientation (OrientedSurfaceMesh.cxx:298-328).
@@ -105,3 +107,32 @@ def perturbed_sphere(n: int, noise: float = 0.02, seed: int = 4, radius: float =
     rng = np.random.default_rng(seed)
     pts = np.asarray(center, float) + radius * v * (1.0 + noise * rng.standard_normal((n, 1)))
     return pts, orient_outward_faces(pts, f, np.asarray(center, float))
+
+
+def tet_grid(n: int = 30, noise: float = 0.1, seed: int = 7, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0)):
+    """(n+1)^3 grid vertices over [lo, hi] moved by noise x cell size (uniform, seeded), and the six
+    tetrahedra p0, p_a, p_ab, p7 of every cell along the monotone paths of its main diagonal, each
+    ordered so that det(p1 - p0, p2 - p0, p3 - p0) > 0 (OrientedVolumeMesh's volumes)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.asarray(lo, float), np.asarray(hi, float)
+    g = np.linspace(0.0, 1.0, n + 1)
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    pts = pts + rng.uniform(-noise, noise, pts.shape) / n
+    pts = lo + pts * (hi - lo)
+    idx = lambda i, j, k: (i * (n + 1) + j) * (n + 1) + k
+    i, j, k = (a.ravel() for a in np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"))
+    corner = {c: idx(i + c[0], j + c[1], k + c[2]) for c in np.ndindex(2, 2, 2)}
+    tets = []
+    for a in range(3):
+        for b in range(3):
+            if a == b:
+                continue
+            ea = tuple(1 if t == a else 0 for t in range(3))
+            eab = tuple(1 if t in (a, b) else 0 for t in range(3))
+            tets.append(np.stack([corner[(0, 0, 0)], corner[ea], corner[eab], corner[(1, 1, 1)]], axis=1))
+    cells = np.concatenate(tets).astype(np.int32)
+    e = pts[cells[:, 1:]] - pts[cells[:, :1]]
+    neg = np.linalg.det(e) < 0
+    cells[neg, 1], cells[neg, 2] = cells[neg, 2].copy(), cells[neg, 1].copy()
+    return pts, cells

@@ -44,6 +44,7 @@ struct gbk_mo_atlas {
   // the template the evaluations deform and the current fixed-effect template (lag), the L2 and
   // smoothed template gradients, scalars
   double *tmpl_def = nullptr, *tmpl_fe = nullptr, *gt_l2 = nullptr, *gt_sob = nullptr, *scal = nullptr;
+  double *outs_dev = nullptr;  // S x 5 log-likelihood terms of the subjects' last runs
 
   int alloc(double **p, size_t n) {
     cudaError_t e = cudaMalloc(p, std::max(n, (size_t)1) * sizeof(double));
@@ -70,8 +71,10 @@ struct gbk_mo_atlas {
       if (!rc) rc = c->cuda(cudaMemcpyAsync(r->mom, mom + (long)s * n, nb, cudaMemcpyDeviceToDevice, stream), "copy mom");
       if (!rc) rc = c->cuda(cudaMemcpyAsync(r->lm0, moved, (size_t)m * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy template");
       if (!rc) rc = r->run();
-      if (!rc) rc = c->cuda(cudaMemcpyAsync(outs.data() + 5 * s, r->out, 5 * sizeof(double), cudaMemcpyDeviceToHost, stream), "read L");
+      if (!rc) rc = c->cuda(cudaMemcpyAsync(outs_dev + 5 * s, r->out, 5 * sizeof(double), cudaMemcpyDeviceToDevice, stream), "gather L");
     }
+    // one read of every subject's terms (a pageable read per subject would wait for each subject)
+    if (!rc && rerun) rc = c->cuda(cudaMemcpyAsync(outs.data(), outs_dev, (size_t)S * 5 * sizeof(double), cudaMemcpyDeviceToHost, stream), "read L");
     const bool grad = gcp || gtmpl || gmom;
     cudaStream_t saved = c->stream;
     c->stream = stream;
@@ -182,6 +185,7 @@ int gbk_mo_atlas_create(gbk_ctx *c, int d, long ncp, int nobj, const int *data_k
   if (!rc) rc = a->alloc(&a->gt_l2, m);
   if (!rc) rc = a->alloc(&a->gt_sob, m);
   if (!rc) rc = a->alloc(&a->scal, 8);
+  if (!rc) rc = a->alloc(&a->outs_dev, (size_t)nsubj * 5);
   if (!rc) rc = c->cuda(cudaMemcpyAsync(a->tmpl_fe, tmpl_pts, m * sizeof(double), cudaMemcpyDefault, a->stream), "copy template");
   if (!rc) rc = c->cuda(cudaStreamSynchronize(a->stream), "sync");
   if (rc) {

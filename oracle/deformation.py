@@ -248,3 +248,99 @@ def registration_multi(K: OracleLib, cp, mom, tmpl_pts, objects, targets, T: int
     g_mom = -xm[0] - kp
     g_cp = -xp[0] - K.grad_alpha(cp, cp, mom, sigma_def, mom)
     return data, reg, g_cp, g_mom, {"matches": matches, "theta": theta, "lm": lm}
+
+
+def adjoint_landmarks_jumps(K: OracleLib, sigma: float, pos, mom, lm, grads, times, heun: bool = True,
+                            t0=0.0, tn=1.0, corrected: bool = False):
+    """IntegrateAdjointOfLandmarkPointsEquations with observations (AdjointEquationsIntegrator.cxx:
+    59-136, jumps at the observations' time indices `times`, increasing, with match gradients
+    `grads`). The reference: with one observation, theta_{T-1} is its gradient; with several,
+    theta_{T-1} is the last one's gradient if its index is T - 1, else 0 (:71-87); walking t from
+    T - 1 down to 1, the gradient of the observation whose index is t is added to the rate dTheta,
+    so it enters multiplied by dt (:104-109); the observation cursor moves back only in the Heun
+    branch (:123-128), so the explicit Euler scheme adds at most one observation inside the loop, and
+    an observation at index 0 is never added. corrected=True adds every gradient to theta at its own
+    index instead (the jump condition of the continuous adjoint, which the registration's adjoint
+    discretises the same way)."""
+    T = len(pos)
+    dt = _dt(T, t0, tn)
+    theta = [None] * T
+    if corrected:
+        theta[T - 1] = np.zeros_like(np.asarray(lm[T - 1], float))
+        for g, ti in zip(grads, times):
+            if ti == T - 1:
+                theta[T - 1] = theta[T - 1] + g
+        for t in range(T - 1, 0, -1):
+            dth = K.grad_alpha(lm[t], pos[t], mom[t], sigma, theta[t])
+            theta[t - 1] = theta[t] + dth * dt
+            if heun:
+                dth2 = K.grad_alpha(lm[t - 1], pos[t - 1], mom[t - 1], sigma, theta[t - 1])
+                theta[t - 1] = theta[t] + (dth + dth2) * (dt * 0.5)
+            for g, ti in zip(grads, times):
+                if ti == t - 1:
+                    theta[t - 1] = theta[t - 1] + g
+        return theta
+    jumps = len(grads) > 1
+    si = len(times) - 1
+    if jumps:
+        if times[si] == T - 1:
+            theta[T - 1] = np.asarray(grads[si], float).copy()
+            si = max(si - 1, 0)
+        else:
+            theta[T - 1] = np.zeros_like(np.asarray(grads[0], float))
+    else:
+        theta[T - 1] = np.asarray(grads[0], float).copy()
+    for t in range(T - 1, 0, -1):
+        dth = K.grad_alpha(lm[t], pos[t], mom[t], sigma, theta[t])
+        if jumps and t == times[si]:
+            dth = dth + grads[si]
+        theta[t - 1] = theta[t] + dth * dt
+        if heun:
+            dth2 = K.grad_alpha(lm[t - 1], pos[t - 1], mom[t - 1], sigma, theta[t - 1])
+            if jumps and t == times[si]:
+                dth2 = dth2 + grads[si]
+                si = max(si - 1, 0)
+            theta[t - 1] = theta[t] + (dth + dth2) * (dt * 0.5)
+    return theta
+
+
+def geodesic_regression(K: OracleLib, cp, mom, tmpl, objects, observations, times, T: int, sigma_def: float,
+                        t0: float, tn: float, heun: bool = False, corrected: bool = False):
+    """Log-likelihood and gradient of the reference's geodesic Regression (Regression.cxx:150-232,
+    598-673): the template (objects as in registration_multi) flows along the geodesic of (cp, mom)
+    from t0 to tn over T time points; observation s (one (points, cells) per object) is matched to
+    the deformed template at time index times[s]. L_data = -sum_s sum_k 0.5 match / sigma2 (:212-214),
+    L_reg = -0.5 <K p, p>. The reference's gradient: dL/dp = -xi_mom(0) and dL/dcp = -xi_pos(0)
+    only, because AddGradientRegularityTerm (:676-686) takes both gradients by value and its
+    subtractions are lost; the landmark adjoint with the reference's jumps; template L2 gradient
+    -theta(0). corrected=True: the regularity gradients are subtracted and every observation enters
+    the adjoint at its own index; the result then differs from the derivative of the discretised
+    log-likelihood only by the O(dt) of the discretised continuous adjoint, as the registration's
+    gradient does. Returns (data, reg, g_cp, g_mom, g_tmpl, info)."""
+    from . import geometry as G
+    pos, mo = shoot(K, sigma_def, cp, mom, T, t0, tn)
+    lm = flow_landmarks(K, sigma_def, pos, mo, tmpl, heun, t0, tn)
+    data, grads, matches = 0.0, [], []
+    for s, targets in enumerate(observations):
+        gs, off = [], 0
+        for ob, (tp, tc) in zip(objects, targets):
+            match_f, grad_f = G.KINDS[ob["kind"]]
+            x = lm[times[s]][off:off + ob["n"]]
+            r = match_f(K, ob["sigma"], x, ob["cells"], tp, tc)
+            matches.append(r)
+            data -= 0.5 * r / ob["sigma2"]
+            gs.append(grad_f(K, ob["sigma"], x, ob["cells"], tp, tc) / (2.0 * ob["sigma2"]))
+            off += ob["n"]
+        grads.append(np.concatenate(gs))
+    kp = K.convolve(cp, cp, mom, sigma_def)
+    reg = 0.0
+    for i in range(len(cp)):
+        reg -= float(np.dot(kp[i], mom[i]))
+    reg *= 0.5
+    theta = adjoint_landmarks_jumps(K, sigma_def, pos, mo, lm, grads, times, heun, t0, tn, corrected)
+    xp, xm = adjoint_diffeo(K, sigma_def, pos, mo, lm, theta, heun, t0, tn)
+    g_cp, g_mom = -xp[0], -xm[0]
+    if corrected:
+        g_mom = g_mom - kp
+        g_cp = g_cp - K.grad_alpha(cp, cp, mom, sigma_def, mom)
+    return data, reg, g_cp, g_mom, -theta[0], {"matches": matches, "theta": theta, "lm": lm}

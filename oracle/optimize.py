@@ -275,6 +275,34 @@ def multi_object_atlas_evaluator(K, objects, subjects, T: int, sigma_def: float,
     return evaluate
 
 
+def regression_evaluator(K, objects, observations, times, T: int, sigma_def: float, t0: float, tn: float,
+                         heun: bool = False, smoothing_width: float = 0.0, corrected: bool = False):
+    """evaluate() of the reference's geodesic Regression (oracle.deformation.geodesic_regression) for
+    fast_gradient_ascent: groups in the reference's order ControlPoints, InitialMomenta, TemplateData
+    (Regression.cxx:279-286); the template gradient smoothed object by object
+    (Regression::ConvolveGradTemplate, :688-712); squared norms |g_cp|^2, |g_mom|^2, <L2, smoothed>.
+    Regression::SetFixedEffects (:55-66) writes the new template into the template objects, so no
+    lag."""
+    from .deformation import geodesic_regression
+    offs = np.cumsum([0] + [ob["n"] for ob in objects])
+
+    def evaluate(params, need_grad):
+        cp, mom, tmpl = params
+        data, reg, g_cp, g_mom, g_t, _ = geodesic_regression(K, cp, mom, tmpl, objects, observations, times, T,
+                                                             sigma_def, t0, tn, heun, corrected)
+        if not need_grad:
+            return [data, reg], None, None
+        sob = g_t.copy()
+        if smoothing_width >= 1e-20:
+            for i in range(len(objects)):
+                a, b = offs[i], offs[i + 1]
+                sob[a:b] = K.convolve(tmpl[a:b], tmpl[a:b], g_t[a:b], smoothing_width)
+        sq = np.array([float(np.sum(g_cp * g_cp)), float(np.sum(g_mom * g_mom)), float(np.sum(g_t * sob))])
+        return [data, reg], [g_cp, g_mom, sob], sq
+
+    return evaluate
+
+
 def initial_control_points(points, spacing: float):
     """Regular grid over a bounding box (AbstractAtlas.cxx:240-330 without the image criterion):
     per axis, spacing apart, centred so the leftover extent is split evenly; x outermost."""

@@ -132,6 +132,8 @@ def main(ref_root: str = "/root/reference"):
     volume_fixture(ref_root)
     # 6. functional test 8: a two-object curve atlas of three subjects
     parabola_fixture(ref_root)
+    # 7. functional test 7: a geodesic regression of three skull curves
+    regression_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
 
 
@@ -233,6 +235,43 @@ def parabola_fixture(ref_root: str = "/root/reference"):
         kernel_width=np.array(0.2), data_kernel_width=np.array(0.2), data_sigma2=np.array(1.0),
         smoothing_width=np.array(0.2), number_of_time_points=np.array(10), initial_step=np.array(1e-3),
         max_iterations=np.array(10), **out, **{f"state_{k}": np.asarray(v) for k, v in st.items()})
+
+
+def regression_fixture(ref_root: str = "/root/reference"):
+    """Inputs and expected final state of the reference's geodesic regression (functional test 7,
+    model.xml: Regression, initial CP spacing 40, one NonOrientedPolyline object with data kernel
+    width 40 and data-sigma 1, deformation kernel width 60, 5 time points from t0 = 0 to tn = 5;
+    data_set.xml: observations at ages 0, 3, 5, i.e. time indices int((age - t0)(T - 1)/(tn - t0)
+    + 0.5) = 0, 2, 4 (estimate_geodesic_regression.cxx:229-237); optimization_parameters.xml:
+    FastGradientAscent, 10 iterations, tolerance 1e-3, default initial step 1e-3; smoothing width
+    1 x 60, the default ratio). The state's fixed effects are ControlPoints, InitialMomenta and
+    TemplateData (fixed, extrapolated, gradient)."""
+    F = _formats()
+    from oracle.optimize import initial_control_points
+    d = os.path.join(ref_root, "tests", "functional_tests", "regression", "landmark", "2d", "skulls")
+    tp, tc = F.read_vtk_polydata(os.path.join(d, "data", "template.vtk"))
+    out = {"tmpl_pts": np.ascontiguousarray(tp[:, :2]), "tmpl_segs": tc}
+    for k, name in enumerate(("skull_australopithecus", "skull_habilis", "skull_sapiens")):
+        p, c = F.read_vtk_polydata(os.path.join(d, "data", name + ".vtk"))
+        out[f"obs{k}_pts"], out[f"obs{k}_segs"] = np.ascontiguousarray(p[:, :2]), c
+    blobs, head = F.read_state_blobs(os.path.join(d, "deformetrica-state.bin"))
+    named = [b for b in blobs if b["name"] is not None]
+    vecs = [b for b in blobs if b["name"] is None]
+    st = {"step": vecs[0]["value"], "grad_sq_norms": vecs[1]["value"],
+          "history": np.stack([b["value"] for b in vecs[2:]])}
+    for i, what in enumerate(("", "aux_", "grad_")):
+        for j, key in enumerate(("control_points", "momenta", "template")):
+            assert named[3 * i + j]["name"] == ("ControlPoints", "InitialMomenta", "TemplateData")[j]
+            st[what + key] = named[3 * i + j]["value"]
+    tau_i = next(i for i, t in enumerate(head) if "." in t)
+    uints = [int(t) for t in head[:tau_i] if t.isdigit()]
+    st["tau"], st["iter"], st["freeze_counter"] = float(head[tau_i]), uints[-6], uints[-5]
+    np.savez_compressed(
+        os.path.join(HERE, "regression_skulls.npz"), cp0=initial_control_points(tp[tc].mean(axis=1)[:, :2], 40.0),
+        times=np.array([0, 2, 4]), t0=np.array(0.0), tn=np.array(5.0), number_of_time_points=np.array(5),
+        kernel_width=np.array(60.0), data_kernel_width=np.array(40.0), data_sigma2=np.array(1.0),
+        smoothing_width=np.array(60.0), initial_step=np.array(1e-3), max_iterations=np.array(10),
+        tolerance=np.array(1e-3), **out, **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
 if __name__ == "__main__":

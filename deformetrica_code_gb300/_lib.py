@@ -102,6 +102,15 @@ SIGNATURES = {
     "gbk_mo_atlas_optimize": (_I, [_P, _P, _P, _P, _I, _I, _I, _D, _I, _D, _D, _D, _I, _P, _P, _P, _P, _P, _P, _P,
                                    _P, _P]),
     "gbk_mo_atlas_destroy": (None, [_P]),
+    "gbk_geodesic_regression_create": (_I, [_P, _I, _L, _I, _P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P, _I, _D,
+                                            _D, _D, _I, ctypes.POINTER(_P)]),
+    "gbk_geodesic_regression_set_template_smoothing": (_I, [_P, _D]),
+    "gbk_geodesic_regression_set_corrected_gradient": (_I, [_P, _I]),
+    "gbk_geodesic_regression_set_graph": (_I, [_P, _I]),
+    "gbk_geodesic_regression_step": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "gbk_geodesic_regression_optimize": (_I, [_P, _P, _P, _P, _I, _I, _I, _D, _I, _D, _D, _D, _I, _P, _P, _P, _P, _P,
+                                              _P, _P, _P, _P]),
+    "gbk_geodesic_regression_destroy": (None, [_P]),
     "gbk_registration_create": (_I, [_P, _I, _L, _L, _P, _L, _P, _L, _P, _L, _P, _I, _D, _D, _D, _I, _I,
                                      ctypes.POINTER(_P)]),
     "gbk_registration_step": (_I, [_P, _P, _P, _P, _P, _P]),

@@ -118,9 +118,9 @@ cudaError_t scalar_combine(cudaStream_t st, double *out, const double *a, double
 // loop bodies (device pointers only; shared with the registration object)
 // ---------------------------------------------------------------------------------------------
 int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *mom0, int T,
-                 double sigma, double *pos, double *mom, const DeformScratch &s) {
+                 double sigma, double *pos, double *mom, const DeformScratch &s, double span) {
   const long n = ncp * d;
-  const double dt = 1.0 / (T - 1);
+  const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
   int rc;
   if ((rc = c->cuda(cudaMemcpyAsync(pos, cp0, n * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy")))
@@ -159,9 +159,9 @@ int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *m
 
 int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                 double sigma, long nlm, const double *lm0, int heun, double *lm,
-                const DeformScratch &s) {
+                const DeformScratch &s, double span) {
   const long n = ncp * d, m = nlm * d;
-  const double dt = 1.0 / (T - 1);
+  const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
   int rc;
   if ((rc = c->cuda(cudaMemcpyAsync(lm, lm0, m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy"))) return rc;
@@ -199,14 +199,35 @@ int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mo
 int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
                              int T, double sigma, long nlm, const double *lm,
                              const double *theta_final, int heun, double *theta,
-                             const DeformScratch &s) {
+                             const DeformScratch &s, double span, const AdjointJumps *jumps) {
   const long n = ncp * d, m = nlm * d;
-  const double dt = 1.0 / (T - 1);
+  const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
   int rc;
-  if ((rc = c->cuda(cudaMemcpyAsync(theta + (T - 1) * m, theta_final, m * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, st), "copy")))
-    return rc;
+  // observations: the reference's jumps (several observations), or each gradient added at its own
+  // time index; one reference observation is the plain final condition
+  const bool obs = jumps && jumps->n > 0;
+  const bool ref_jumps = obs && jumps->reference && jumps->n > 1;
+  const bool own_index = obs && !jumps->reference;
+  int si = obs ? jumps->n - 1 : 0;
+  double *thT = theta + (T - 1) * m;
+  if (obs && jumps->reference && jumps->n == 1) {
+    rc = c->cuda(cudaMemcpyAsync(thT, jumps->grads[0], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+  } else if (ref_jumps && jumps->times[si] == T - 1) {
+    rc = c->cuda(cudaMemcpyAsync(thT, jumps->grads[si], m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+    si = si > 0 ? si - 1 : 0;
+  } else if (obs) {
+    rc = c->cuda(lincomb(st, thT, nullptr, 0.0, nullptr, 0.0, nullptr, m), "zero");
+    c->launches += 1;
+    for (int k = 0; k < jumps->n && !rc && own_index; ++k)
+      if (jumps->times[k] == T - 1) {
+        rc = c->cuda(lincomb(st, thT, thT, 1.0, jumps->grads[k], 0.0, nullptr, m), "jump");
+        c->launches += 1;
+      }
+  } else {
+    rc = c->cuda(cudaMemcpyAsync(thT, theta_final, m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy");
+  }
+  if (rc) return rc;
   for (int t = T - 1; t > 0; --t) {
     PairArgs a = pair_args(nlm, ncp, sigma);
     a.x = lm + t * m;
@@ -218,6 +239,12 @@ int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, con
     a.out1 = s.vc;
     a.out1_ld = d;
     if ((rc = c->launch(OP_GRADA, d, d, a))) return rc;
+    // the reference adds the observation's gradient to the rate (AdjointEquationsIntegrator.cxx:104-109)
+    const bool jump_here = ref_jumps && t == jumps->times[si];
+    if (jump_here) {
+      if ((rc = c->cuda(lincomb(st, s.vc, s.vc, 1.0, jumps->grads[si], 0.0, nullptr, m), "jump"))) return rc;
+      c->launches += 1;
+    }
     double *th1 = theta + (t - 1) * m;
     if ((rc = c->cuda(lincomb(st, th1, theta + t * m, dt, s.vc, 0, nullptr, m), "euler"))) return rc;
     c->launches += 1;
@@ -232,9 +259,19 @@ int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, con
       b.out1 = s.vd;
       b.out1_ld = d;
       if ((rc = c->launch(OP_GRADA, d, d, b))) return rc;
+      if (jump_here) {  // and the cursor moves back in this branch only (:123-128)
+        if ((rc = c->cuda(lincomb(st, s.vd, s.vd, 1.0, jumps->grads[si], 0.0, nullptr, m), "jump"))) return rc;
+        c->launches += 1;
+        si = si > 0 ? si - 1 : 0;
+      }
       if ((rc = c->cuda(lincomb(st, th1, theta + t * m, 0.5 * dt, s.vc, 0.5 * dt, s.vd, m), "heun"))) return rc;
       c->launches += 1;
     }
+    for (int k = 0; k < (own_index ? jumps->n : 0); ++k)
+      if (jumps->times[k] == t - 1) {
+        if ((rc = c->cuda(lincomb(st, th1, th1, 1.0, jumps->grads[k], 0.0, nullptr, m), "jump"))) return rc;
+        c->launches += 1;
+      }
   }
   return GBK_OK;
 }
@@ -279,9 +316,9 @@ int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const doubl
 
 int adjoint_diffeo_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                           double sigma, long nlm, const double *lm, const double *theta, int heun,
-                          double *xp, double *xm, const DeformScratch &s) {
+                          double *xp, double *xm, const DeformScratch &s, double span) {
   const long n = ncp * d, m = nlm * d;
-  const double dt = 1.0 / (T - 1);
+  const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
   int rc;
   if ((rc = c->cuda(cudaMemsetAsync(xp + (T - 1) * n, 0, n * sizeof(double), st), "memset"))) return rc;

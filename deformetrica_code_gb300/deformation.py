@@ -394,6 +394,92 @@ class MultiObjectAtlas:
             pass
 
 
+class GeodesicRegression:
+    """The reference's geodesic Regression (gbk_geodesic_regression_*): `objects` as for
+    MultiObjectAtlas, `observations` a list of [(points, cells) per object] at the time indices
+    `times` of T time points over [t0, tn]. The gradient is the reference's unless
+    set_corrected_gradient(True)."""
+
+    def __init__(self, ncp: int, objects, observations, times, T: int, sigma_def: float, t0: float, tn: float,
+                 heun: bool = False, context: Context | None = None):
+        self.ctx = context or Context()
+        self.d = int(np.asarray(objects[0]["pts"]).shape[1])
+        self.ncp, self.nobs = int(ncp), len(observations)
+        kinds, nv, pts, nc, cells = _objects_arrays(objects, self.d, Registration.KINDS)
+        self.nv = int(nv.sum())
+        sd = np.array([float(o["sigma"]) for o in objects])
+        s2 = np.array([float(o["sigma2"]) for o in objects])
+        tn_, tp, tnc, tc = [], [], [], []
+        for ob in observations:
+            objs = [dict(o, pts=t[0], cells=t[1]) for o, t in zip(objects, ob)]
+            _, n_t, p_t, c_n, c_t = _objects_arrays(objs, self.d, Registration.KINDS)
+            tn_.append(n_t), tp.append(p_t), tnc.append(c_n)
+            if any(o["kind"] not in ("pointcloud", "landmark") for o in objects):
+                tc.append(c_t)
+        nv_t, ncell_t = np.concatenate(tn_), np.concatenate(tnc)
+        tgt = np.ascontiguousarray(np.concatenate(tp))
+        tcells = np.ascontiguousarray(np.concatenate(tc) if tc else np.zeros(1, np.int32), dtype=np.int32)
+        ti = np.ascontiguousarray(times, dtype=np.int32)
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.gbk_geodesic_regression_create(
+            self.ctx.h, self.d, self.ncp, len(objects), c(kinds), c(nv), c(pts), c(nc), c(cells), c(sd), c(s2),
+            self.nobs, c(ti), c(nv_t), c(tgt), c(ncell_t), c(tcells), int(T), float(sigma_def), float(t0), float(tn),
+            int(heun), ctypes.byref(h)))
+        self.h = h
+
+    def set_template_smoothing(self, width: float):
+        self.ctx.check(self.ctx.lib.gbk_geodesic_regression_set_template_smoothing(self.h, float(width)))
+
+    def set_corrected_gradient(self, enable: bool):
+        self.ctx.check(self.ctx.lib.gbk_geodesic_regression_set_corrected_gradient(self.h, int(enable)))
+
+    def step(self, cp, mom, tmpl=None):
+        """Returns loglik [L, L_data, L_reg, sum of matches, <Kp,p>], dL/dcp, dL/dp, the smoothed
+        template gradient."""
+        cp, mom = np.ascontiguousarray(cp, np.float64), np.ascontiguousarray(mom, np.float64)
+        t = None if tmpl is None else np.ascontiguousarray(tmpl, np.float64)
+        ll = np.zeros(5)
+        gc, gm, gt = np.zeros_like(cp), np.zeros_like(mom), np.zeros((self.nv, self.d))
+        c = lambda a: None if a is None else ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_geodesic_regression_step(self.h, c(cp), c(mom), c(t), c(ll), c(gc), c(gm),
+                                                                 c(gt)))
+        return ll, gc, gm, gt
+
+    def optimize(self, cp, mom, tmpl, max_iterations: int, initial_step: float = 1e-3, optimize_cp: bool = True,
+                 optimize_template: bool = True, max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2,
+                 tolerance: float = 1e-4, nb_iter_freeze: int = 3):
+        cp, mom, tmpl = (np.array(a, dtype=np.float64) for a in (cp, mom, tmpl))
+        hist = np.zeros((max_iterations + 1, 2))
+        info = np.zeros(10)
+        aux = [np.zeros_like(a) for a in (cp, mom, tmpl)]
+        grd = [np.zeros_like(a) for a in (cp, mom, tmpl)]
+        iters = ctypes.c_int(0)
+        c = lambda a: ctypes.c_void_p(a.ctypes.data)
+        self.ctx.check(self.ctx.lib.gbk_geodesic_regression_optimize(
+            self.h, c(cp), c(mom), c(tmpl), int(optimize_cp), int(optimize_template), int(max_iterations),
+            float(initial_step), int(max_line_search), float(shrink), float(expand), float(tolerance),
+            int(nb_iter_freeze), c(hist), ctypes.byref(iters), c(info), *[c(a) for a in aux], *[c(a) for a in grd]))
+        groups = [k for k, on in (("cp", optimize_cp), ("momenta", True), ("template", optimize_template)) if on]
+        idx = {"cp": (0, 5), "momenta": (1, 6), "template": (2, 7)}
+        return {"cp": cp, "mom": mom, "template": tmpl, "aux_cp": aux[0], "aux_mom": aux[1], "aux_template": aux[2],
+                "grad_cp": grd[0], "grad_mom": grd[1], "grad_template": grd[2], "history": hist[:iters.value],
+                "step": np.array([info[idx[g][0]] for g in groups]), "tau": float(info[3]),
+                "freeze_counter": int(info[4]), "grad_sq_norms": np.array([info[idx[g][1]] for g in groups]),
+                "evaluations": int(info[8]), "stopped": Registration.STOP[int(info[9])]}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.gbk_geodesic_regression_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Atlas:
     """DeterministicAtlas iteration over many subjects, every stage one launch for all subjects
     (uneven target meshes balanced by source chunks), replayed from a CUDA graph."""

@@ -349,6 +349,48 @@ void gbk_registration_destroy(gbk_registration *reg);
 int gbk_kernel_norm_noalloc(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
                             double sigma, double *out);
 
+/* ---- geodesic regression (the reference's Regression model), CUDA-graph replay ------------ */
+
+typedef struct gbk_geodesic_regression gbk_geodesic_regression;
+
+/* Regression.cxx: a template of nobj objects (described as for gbk_registration_create_multi) flows
+ * along the geodesic of (control points, initial momenta) from t0 to tn over T time points;
+ * observation o (nobs of them, time indices time_index[o], not decreasing: the reference's
+ * int((age - t0)(T - 1)/(tn - t0) + 0.5f), estimate_geodesic_regression.cxx:229-237) has, per object
+ * k, nv_t[o * nobj + k] points and ncell_t[o * nobj + k] cells, concatenated observation by
+ * observation, object by object. */
+int gbk_geodesic_regression_create(gbk_ctx *ctx, int d, long ncp, int nobj, const int *data_kinds, const long *nv,
+                                   const double *tmpl_pts, const long *ncell, const int *tmpl_cells,
+                                   const double *sigma_data, const double *data_sigma2, int nobs, const int *time_index,
+                                   const long *nv_t, const double *tgt_pts, const long *ncell_t, const int *tgt_cells,
+                                   int T, double sigma_def, double t0, double tn, int heun,
+                                   gbk_geodesic_regression **out);
+/* Template-gradient smoothing width (Regression::ConvolveGradTemplate, Regression.cxx:688-712;
+ * the reference uses smoothing-kernel-width-ratio x deformation kernel width); 0 keeps L2. */
+int gbk_geodesic_regression_set_template_smoothing(gbk_geodesic_regression *reg, double width);
+/* 0 (default): the reference's gradient -- no regularity gradient (AddGradientRegularityTerm,
+ * Regression.cxx:676-686, works on copies), observations entering the landmark adjoint as rates
+ * times dt, at most one of them inside the explicit-Euler loop, none at time index 0
+ * (AdjointEquationsIntegrator.cxx:59-136). 1: the regularity gradients applied and every
+ * observation added to the adjoint at its own time index. */
+int gbk_geodesic_regression_set_corrected_gradient(gbk_geodesic_regression *reg, int enable);
+int gbk_geodesic_regression_set_graph(gbk_geodesic_regression *reg, int enable);
+/* loglik[5] = {L, L_data, L_reg, sum of matches, <K p, p>} at (cp, mom: ncp x d; tmpl: nv x d or
+ * NULL to keep the current template), and the gradients (the template one smoothed); any output
+ * may be NULL. */
+int gbk_geodesic_regression_step(gbk_geodesic_regression *reg, const double *cp, const double *mom, const double *tmpl,
+                                 double *loglik, double *grad_cp, double *grad_mom, double *grad_tmpl);
+/* FastGradientAscent over the reference's groups [ControlPoints] InitialMomenta [TemplateData]
+ * (Regression.cxx:279-286). info (10 doubles): final steps (cp, momenta, template), tau, freeze
+ * counter, squared norms (cp, momenta, template as <L2, smoothed>), evaluations, stop reason. */
+int gbk_geodesic_regression_optimize(gbk_geodesic_regression *reg, double *cp, double *mom, double *tmpl,
+                                     int optimize_cp, int optimize_template, int max_iterations, double initial_step,
+                                     int max_line_search, double shrink, double expand, double tolerance,
+                                     int nb_iter_freeze, double *history, int *iterations, double *info,
+                                     double *aux_cp, double *aux_mom, double *aux_tmpl, double *grad_cp,
+                                     double *grad_mom, double *grad_tmpl);
+void gbk_geodesic_regression_destroy(gbk_geodesic_regression *reg);
+
 /* ---- atlas with a multi-object template, one registration per subject ------------------- */
 
 typedef struct gbk_mo_atlas gbk_mo_atlas;

@@ -454,6 +454,43 @@ def optimizer_bench(cpu: bool = True, reg_iters: int = 10):
                                  set_fixed=lt.set_fixed)
         res["parabola_atlas"]["cpu_oracle"] = {"s_total": time.perf_counter() - t0, "evaluations": r["evaluations"],
                                                "kind": "port (FP64)"}
+    # the reference's functional test 7: a geodesic regression of three skull curves
+    from deformetrica_code_gb300.deformation import GeodesicRegression
+    rg = dict(np.load(os.path.join(ROOT, "tests", "golden", "regression_skulls.npz")))
+    gobj = [dict(kind="curve_varifold", pts=rg["tmpl_pts"], cells=rg["tmpl_segs"], sigma=float(rg["data_kernel_width"]),
+                 sigma2=float(rg["data_sigma2"]))]
+    observations = [[(rg[f"obs{k}_pts"], rg[f"obs{k}_segs"])] for k in range(3)]
+    times = [int(t) for t in rg["times"]]
+    res["skull_regression"] = {"workload": "reference functional test 7: geodesic regression of a 150-point "
+                                           "NonOrientedPolyline through 3 observations, 16 CP, T = 5 over [0, 5], "
+                                           "10 FastGradientAscent iterations over control points, momenta and template"}
+    for mode, name in ((g.GBK_MODE_F64, "f64"), (g.GBK_MODE_F32C, "f32c")):
+        reg = GeodesicRegression(16, gobj, observations, times, int(rg["number_of_time_points"]),
+                                 float(rg["kernel_width"]), float(rg["t0"]), float(rg["tn"]), heun=False,
+                                 context=g.Context(mode=mode))
+        reg.set_template_smoothing(float(rg["smoothing_width"]))
+        reg.optimize(rg["cp0"], np.zeros_like(rg["cp0"]), rg["tmpl_pts"], 1, 1e-3)  # warm-up: graph captured
+        t0 = time.perf_counter()
+        r = reg.optimize(rg["cp0"], np.zeros_like(rg["cp0"]), rg["tmpl_pts"], int(rg["max_iterations"]),
+                         float(rg["initial_step"]), tolerance=float(rg["tolerance"]))
+        dt = time.perf_counter() - t0
+        reg.close()
+        hist = rg["state_history"]
+        res["skull_regression"][name] = {"s_total": dt, "evaluations": r["evaluations"],
+                                         "history_max_rel_err_vs_reference_state":
+                                             float(np.abs(r["history"] - hist).max() / np.abs(hist).max())}
+    if cpu:
+        from oracle.optimize import regression_evaluator
+        oobj = [dict(kind="curve_varifold", cells=rg["tmpl_segs"], sigma=float(rg["data_kernel_width"]),
+                     sigma2=float(rg["data_sigma2"]), n=len(rg["tmpl_pts"]))]
+        ev = regression_evaluator(K, oobj, observations, times, int(rg["number_of_time_points"]),
+                                  float(rg["kernel_width"]), float(rg["t0"]), float(rg["tn"]), heun=False,
+                                  smoothing_width=float(rg["smoothing_width"]))
+        t0 = time.perf_counter()
+        r = fast_gradient_ascent(ev, [rg["cp0"], np.zeros_like(rg["cp0"]), rg["tmpl_pts"]], float(rg["initial_step"]),
+                                 int(rg["max_iterations"]), tolerance=float(rg["tolerance"]))
+        res["skull_regression"]["cpu_oracle"] = {"s_total": time.perf_counter() - t0, "evaluations": r["evaluations"],
+                                                 "kind": "port (FP64)"}
     return res
 
 

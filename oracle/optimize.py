@@ -127,6 +127,80 @@ def fast_gradient_ascent(evaluate, params, initial_step: float, max_iterations: 
             "evaluations": evaluations, "stopped": stopped}
 
 
+def gradient_ascent(evaluate, params, initial_step: float, max_iterations: int, max_line_search: int = 10,
+                    shrink: float = 0.5, expand: float = 1.2, tolerance: float = 1e-4, multivariate: bool = True,
+                    set_fixed=None):
+    """The reference's GradientAscent estimator (GradientAscent.cxx:48-240): from the fixed point,
+    a trial fixed + grad * step is accepted when its log-likelihood is not below the current one
+    (no sufficient-increase term); otherwise every step shrinks and, with several groups, the
+    "all but one shrunk" proposals are tried and the best acceptable one kept (its group's step
+    restored); after an accepted step every step expands; stop on |dL| < tolerance |L_0 - L| or when
+    the line search fails. The gradient is evaluated at each new fixed point. set_fixed as in
+    fast_gradient_ascent (the reference calls SetFixedEffects before every trial and before each
+    gradient, :154-218)."""
+    fixed = [np.array(p, dtype=np.float64) for p in params]
+    sf = set_fixed or (lambda p: None)
+    history = [None] * (max_iterations + 1)
+    t0, _, _ = evaluate(fixed, False)
+    history[0] = np.asarray(t0, dtype=np.float64)
+    lsq_ref = float(np.sum(history[0]))
+    _, grads, sq = evaluate(fixed, True)
+    n = len(fixed)
+    step = np.full(n, float(initial_step))
+    evaluations, it, stopped = 2, 1, "max_iterations"
+    step_at = lambda local: [fixed[k] + grads[k] * local[k] for k in range(n)]
+    while it < max_iterations + 1:
+        found = False
+        for li in range(max_line_search):
+            cand = step_at(step)
+            sf(cand)
+            t, _, _ = evaluate(cand, False)
+            evaluations += 1
+            if float(np.sum(t)) - lsq_ref >= 0:
+                found, new, new_terms = True, cand, np.asarray(t, dtype=np.float64)
+                break
+            elif n > 1 and multivariate:
+                step = step * shrink
+                props, ts, qs = [], [], np.empty(n)
+                for k in range(n):
+                    local = step.copy()
+                    local[k] /= shrink
+                    ck = step_at(local)
+                    sf(ck)
+                    tk, _, _ = evaluate(ck, False)
+                    evaluations += 1
+                    props.append(ck)
+                    ts.append(np.asarray(tk, dtype=np.float64))
+                    qs[k] = float(np.sum(tk)) - lsq_ref
+                idx = int(np.argmax(qs))
+                if qs[idx] >= 0:
+                    found, new, new_terms = True, props[idx], ts[idx]
+                    step[idx] /= shrink
+                    break
+            else:
+                step = step * shrink
+        if not found:
+            sf(fixed)
+            stopped = "line_search"
+            break
+        history[it] = new_terms
+        fixed = new
+        step = step * expand
+        lsq_ref = float(np.sum(new_terms))
+        d_cur = float(np.sum(history[it - 1]) - np.sum(history[it]))
+        d_ref = float(np.sum(history[0]) - np.sum(history[it]))
+        if abs(d_cur) < tolerance * abs(d_ref):
+            stopped = "tolerance"
+            break
+        sf(fixed)
+        _, grads, sq = evaluate(fixed, True)
+        evaluations += 1
+        it += 1
+    done = [h for h in history if h is not None]
+    return {"params": fixed, "grads": grads, "grad_sq_norms": np.asarray(sq, dtype=np.float64), "step": step,
+            "iter": it, "history": np.stack(done), "evaluations": evaluations, "stopped": stopped}
+
+
 def registration_evaluator(K, tmpl_pts, tmpl_tris, tgt_pts, tgt_tris, T: int, sigma_def: float,
                            sigma_data: float, data_sigma2: float, kind: str = "currents", heun: bool = True):
     """evaluate() of one landmark registration with control points and momenta optimised (the

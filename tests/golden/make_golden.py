@@ -134,6 +134,8 @@ def main(ref_root: str = "/root/reference"):
     parabola_fixture(ref_root)
     # 7. functional test 7: a geodesic regression of three skull curves
     regression_fixture(ref_root)
+    # 8. functional test 2: a banana surface atlas estimated by GradientAscent
+    banana_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
 
 
@@ -272,6 +274,40 @@ def regression_fixture(ref_root: str = "/root/reference"):
         kernel_width=np.array(60.0), data_kernel_width=np.array(40.0), data_sigma2=np.array(1.0),
         smoothing_width=np.array(60.0), initial_step=np.array(1e-3), max_iterations=np.array(10),
         tolerance=np.array(1e-3), **out, **{f"state_{k}": np.asarray(v) for k, v in st.items()})
+
+
+def banana_fixture(ref_root: str = "/root/reference"):
+    """Inputs and expected final state of the reference's banana atlas (functional test 2,
+    model.xml: DeterministicAtlas, OrientedSurfaceMesh with data kernel width 0.5 and data-sigma
+    0.5, re-oriented normals, initial CP spacing 0.3, deformation kernel width 1, 20 time points;
+    three subjects; optimization_parameters.xml: GradientAscent, 150 iterations, 20 line-search
+    iterations, step expand 2; default initial step 1e-3, shrink 0.5, tolerance 1e-4, smoothing
+    ratio 1). GradientAscent stores the step, the history, the fixed effects (ControlPoints,
+    TemplateData), the momenta and the gradients at the final point (GradientAscent.cxx:226-236)."""
+    F = _formats()
+    from oracle.optimize import initial_control_points
+    d = os.path.join(ref_root, "tests", "functional_tests", "atlas", "landmark", "3d", "banana")
+    tp, tf_raw = F.read_vtk_polydata(os.path.join(d, "data", "template.vtk"))
+    tf = F.reorient_like_reader(tp, tf_raw)
+    out = {"tmpl_pts": tp, "tmpl_tris": tf}
+    for i in (1, 2, 3):
+        p, f = F.read_vtk_polydata(os.path.join(d, "data", f"banana_{i}.vtk"))
+        out[f"subj{i}_pts"], out[f"subj{i}_tris"] = p, F.reorient_like_reader(p, f)
+    blobs, head = F.read_state_blobs(os.path.join(d, "deformetrica-state.bin"))
+    vecs = [b["value"] for b in blobs if b["name"] is None]
+    named = [b for b in blobs if b["name"] is not None]
+    cps = [b["value"] for b in named if b["name"] == "ControlPoints"]
+    tds = [b["value"] for b in named if b["name"] == "TemplateData"]
+    moms = [b["value"] for b in named if b["name"] == "Momenta"]
+    st = {"step": vecs[0], "history": np.stack(vecs[1:]), "control_points": cps[0], "grad_control_points": cps[1],
+          "template": tds[0], "grad_template": tds[1], "momenta": np.stack(moms[:3]),
+          "grad_momenta": np.stack(moms[3:6]), "iter": [int(t) for t in head if t.isdigit()][-16]}
+    np.savez_compressed(
+        os.path.join(HERE, "banana_atlas.npz"), cp0=initial_control_points(tp[tf].mean(axis=1), 0.3),
+        kernel_width=np.array(1.0), data_kernel_width=np.array(0.5), data_sigma2=np.array(0.25),
+        smoothing_width=np.array(1.0), number_of_time_points=np.array(20), initial_step=np.array(1e-3),
+        max_iterations=np.array(150), max_line_search=np.array(20), expand=np.array(2.0), **out,
+        **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
 if __name__ == "__main__":

@@ -77,3 +77,49 @@ def test_without_the_lag_the_history_departs(pb):
     h = pb["state_history"]
     assert np.abs(r["history"][1] - h[1]).max() <= 1e-12 * np.abs(h[1]).max()
     assert abs(r["history"][2][0] - h[2][0]) > 1e-3 * abs(h[2][0])
+
+
+@pytest.fixture(scope="module")
+def bn():
+    return dict(np.load(os.path.join(GOLDEN, "banana_atlas.npz")))
+
+
+def banana_run(bn, lag=True, max_iterations=None):
+    """The reference's functional test 2 (atlas/landmark/3d/banana): a DeterministicAtlas of three
+    banana surfaces (OrientedSurfaceMesh currents, data kernel 0.5, data-sigma 0.5), deformation
+    kernel 1 over 20 time points, control points on the 0.3 grid, estimated by the reference's
+    GradientAscent (150 iterations, 20 line-search iterations, step expand 2)."""
+    import oracle
+    from oracle.optimize import LaggedTemplate, atlas_evaluator, gradient_ascent
+    K = oracle.load("port")
+    subjects = [(bn[f"subj{i}_pts"], bn[f"subj{i}_tris"]) for i in (1, 2, 3)]
+    lt = LaggedTemplate(bn["tmpl_pts"], 1) if lag else None
+    ev = atlas_evaluator(K, bn["tmpl_tris"], subjects, int(bn["number_of_time_points"]), float(bn["kernel_width"]),
+                         float(bn["data_kernel_width"]), float(bn["data_sigma2"]), "currents", False,
+                         float(bn["smoothing_width"]), True, True, cp=bn["cp0"], tmpl=bn["tmpl_pts"], lag=lt)
+    return gradient_ascent(ev, [bn["cp0"], bn["tmpl_pts"], np.zeros((3,) + bn["cp0"].shape)], float(bn["initial_step"]),
+                           int(max_iterations or bn["max_iterations"]), int(bn["max_line_search"]),
+                           expand=float(bn["expand"]), set_fixed=lt.set_fixed if lag else None)
+
+
+def test_oracle_reproduces_banana_state(bn):
+    """Every stored field: the history (9 rows; the line search fails at iteration 9, as in the
+    reference's run), the final steps, the fixed effects, the momenta and the gradients."""
+    r = banana_run(bn)
+    rel = lambda a, b: np.abs(np.asarray(a) - b).max() / max(np.abs(b).max(), 1e-300)
+    assert r["stopped"] == "line_search" and r["iter"] == int(bn["state_iter"])
+    assert rel(r["history"], bn["state_history"]) <= 1e-10
+    assert rel(r["step"], bn["state_step"]) <= 1e-12
+    assert rel(r["params"][0], bn["state_control_points"]) <= 1e-10
+    assert rel(r["params"][1], bn["state_template"]) <= 1e-10
+    assert rel(r["params"][2], bn["state_momenta"]) <= 1e-10
+    assert rel(r["grads"][0], bn["state_grad_control_points"]) <= 1e-9
+    assert rel(r["grads"][1], bn["state_grad_template"]) <= 1e-9
+    assert rel(r["grads"][2], bn["state_grad_momenta"]) <= 1e-9
+
+
+def test_banana_needs_the_lag(bn):
+    r = banana_run(bn, lag=False, max_iterations=2)
+    h = bn["state_history"]
+    assert np.abs(r["history"][1] - h[1]).max() <= 1e-12 * np.abs(h[1]).max()
+    assert abs(r["history"][2][0] - h[2][0]) > 1e-2 * abs(h[2][0])

@@ -5,7 +5,8 @@ if it has not been built: there is no CPU or PyTorch fallback.
 """
 from . import _lib
 from ._lib import (GBKError, GBK_MODE_F32C, GBK_MODE_F64, GBK_ORDER_AUTO, GBK_ORDER_OFF, GBK_ORDER_SPATIAL,
-                   GBK_ORDER_SPATIAL_NOPRUNE, GBK_GRADIENT_REFERENCE, GBK_GRADIENT_EXACT)
+                   GBK_ORDER_SPATIAL_NOPRUNE, GBK_GRADIENT_REFERENCE, GBK_GRADIENT_EXACT,
+                   GBK_ESTIMATOR_FAST_GRADIENT_ASCENT, GBK_ESTIMATOR_GRADIENT_ASCENT)
 
 _lib.load()
 
@@ -13,4 +14,4 @@ from .kernel import Context, GB300ExactKernel  # noqa: E402
 
 __all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64", "GBK_ORDER_AUTO",
            "GBK_ORDER_OFF", "GBK_ORDER_SPATIAL", "GBK_ORDER_SPATIAL_NOPRUNE", "GBK_GRADIENT_REFERENCE",
-           "GBK_GRADIENT_EXACT"]
+           "GBK_GRADIENT_EXACT", "GBK_ESTIMATOR_FAST_GRADIENT_ASCENT", "GBK_ESTIMATOR_GRADIENT_ASCENT"]

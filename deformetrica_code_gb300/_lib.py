@@ -27,6 +27,8 @@ GBK_ORDER_SPATIAL = 2
 GBK_ORDER_SPATIAL_NOPRUNE = 3
 GBK_GRADIENT_REFERENCE = 0
 GBK_GRADIENT_EXACT = 1
+GBK_ESTIMATOR_FAST_GRADIENT_ASCENT = 0
+GBK_ESTIMATOR_GRADIENT_ASCENT = 1
 
 OPS = {
     "convolve": 0,
@@ -59,6 +61,8 @@ SIGNATURES = {
     "gbk_get_order": (_I, [_P]),
     "gbk_set_gradient_mode": (_I, [_P, _I]),
     "gbk_get_gradient_mode": (_I, [_P]),
+    "gbk_set_estimator": (_I, [_P, _I]),
+    "gbk_get_estimator": (_I, [_P]),
     "gbk_synchronize": (_I, [_P]),
     "gbk_launch_count": (ctypes.c_longlong, [_P]),
     "gbk_convolve": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P]),

@@ -975,6 +975,7 @@ int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int 
     return e;
   };
   FgaOptions o;
+  o.estimator = c->estimator;
   o.max_iterations = max_iterations;
   o.max_line_search = max_line_search;
   o.nb_iter_freeze = nb_iter_freeze;

@@ -443,6 +443,16 @@ int gbk_set_gradient_mode(gbk_ctx *c, int mode) {
 
 int gbk_get_gradient_mode(const gbk_ctx *c) { return c ? c->gradient_mode : -1; }
 
+int gbk_set_estimator(gbk_ctx *c, int estimator) {
+  if (!c) return GBK_ERR_ARG;
+  if (estimator != GBK_ESTIMATOR_FAST_GRADIENT_ASCENT && estimator != GBK_ESTIMATOR_GRADIENT_ASCENT)
+    return c->fail(GBK_ERR_ARG, "unknown estimator %d", estimator);
+  c->estimator = estimator;
+  return GBK_OK;
+}
+
+int gbk_get_estimator(const gbk_ctx *c) { return c ? c->estimator : -1; }
+
 int gbk_synchronize(gbk_ctx *c) {
   GBK_GUARD(c);
   return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");

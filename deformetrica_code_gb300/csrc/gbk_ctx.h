@@ -36,6 +36,7 @@ struct gbk_ctx {
   DevBuf tmp;                 // op temporaries (e.g. K w for the kernel norm)
   int order = 0;              // GBK_ORDER_* (0 = automatic)
   int gradient_mode = 0;      // GBK_GRADIENT_* of the point-cloud and volume data terms
+  int estimator = 0;          // GBK_ESTIMATOR_* of the *_optimize calls
   struct SortSlot {           // a point set in spatial order: perm, sorted keys, box
     DevBuf buf;
     const double *ptr = nullptr;

@@ -428,6 +428,7 @@ int gbk_geodesic_regression_optimize(gbk_geodesic_regression *r, double *cp, dou
     return e;
   };
   FgaOptions o;
+  o.estimator = c->estimator;
   o.max_iterations = max_iterations;
   o.max_line_search = max_line_search;
   o.nb_iter_freeze = nb_iter_freeze;

@@ -323,6 +323,7 @@ int gbk_mo_atlas_optimize(gbk_mo_atlas *a, double *cp, double *tmpl, double *mom
     return e;
   };
   FgaOptions o;
+  o.estimator = c->estimator;
   o.max_iterations = max_iterations;
   o.max_line_search = max_line_search;
   o.nb_iter_freeze = nb_iter_freeze;

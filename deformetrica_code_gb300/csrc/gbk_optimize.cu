@@ -23,6 +23,150 @@
 
 namespace gbk {
 
+// GradientAscent::Update (GradientAscent.cxx:48-240): the trial fixed + grad * step is accepted when
+// the log-likelihood does not decrease; otherwise every step shrinks and, with several groups,
+// each "all but one shrunk" proposal is tried and the best acceptable one kept (its step
+// restored); after an accepted step every step expands, the tolerance is tested, and the gradient
+// is evaluated at the new fixed point (after SetFixedEffects, as the reference).
+static int gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes, double *const *params,
+                           const FgaOptions &o, const FgaEvaluate &evaluate, FgaResult *res,
+                           double *const *grad_out, const FgaSetFixed &set_fixed) {
+  std::vector<double *> owned;
+  auto dev = [&](long n, double **p) {
+    int e = c->cuda(cudaMalloc(p, (size_t)std::max(n, 1L) * sizeof(double)), "cudaMalloc (optimiser)");
+    if (!e) owned.push_back(*p);
+    return e;
+  };
+  std::vector<double *> fixed(ng), nw(ng), grad(ng);
+  std::vector<std::vector<double *>> prop(ng, std::vector<double *>(ng));
+  int rc = GBK_OK;
+  for (int g = 0; g < ng && !rc; ++g) {
+    if (!rc) rc = dev(sizes[g], &fixed[g]);
+    if (!rc) rc = dev(sizes[g], &nw[g]);
+    if (!rc) rc = dev(sizes[g], &grad[g]);
+    for (int k = 0; k < ng && !rc; ++k) rc = dev(sizes[g], &prop[k][g]);
+  }
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(st);
+    for (double *p : owned) cudaFree(p);
+  };
+  if (rc) {
+    cleanup();
+    return rc;
+  }
+  const double shrink = o.shrink;
+  std::vector<double> sq(ng, 0.0), step(ng, o.initial_step), hist((size_t)(o.max_iterations + 1) * 2, 0.0);
+  long evaluations = 0;
+  auto eval = [&](const std::vector<double *> &p, bool need_grad, double *t) {
+    ++evaluations;
+    return evaluate(p.data(), need_grad, t, grad.data(), sq.data());
+  };
+  auto setf = [&](const std::vector<double *> &p) { return set_fixed ? set_fixed(p.data()) : GBK_OK; };
+  auto ascent = [&](const std::vector<double *> &dst, const std::vector<double> &s) {
+    int e = GBK_OK;
+    for (int g = 0; g < ng && !e; ++g) e = c->cuda(lincomb(st, dst[g], fixed[g], s[g], grad[g], 0.0, nullptr, sizes[g]), "ascent");
+    return e;
+  };
+  for (int g = 0; g < ng && !rc; ++g)
+    rc = c->cuda(cudaMemcpyAsync(fixed[g], params[g], (size_t)sizes[g] * sizeof(double), cudaMemcpyDefault, st), "copy");
+  double t0[2] = {0, 0}, ignored[2];
+  if (!rc) rc = eval(fixed, false, t0);
+  if (!rc) rc = eval(fixed, true, ignored);
+  if (rc) {
+    cleanup();
+    return rc;
+  }
+  hist[0] = t0[0];
+  hist[1] = t0[1];
+  double lsq_ref = t0[0] + t0[1];
+  int it = 1, stop = 0, rows = 0;
+  while (it < o.max_iterations + 1 && !rc) {
+    bool found = false;
+    double new_terms[2] = {0, 0};
+    for (int li = 0; li < o.max_line_search && !rc; ++li) {
+      double t[2];
+      if ((rc = ascent(nw, step))) break;
+      if ((rc = setf(nw))) break;
+      if ((rc = eval(nw, false, t))) break;
+      if (t[0] + t[1] - lsq_ref >= 0) {
+        found = true;
+        new_terms[0] = t[0];
+        new_terms[1] = t[1];
+        break;
+      } else if (ng > 1) {
+        for (int g = 0; g < ng; ++g) step[g] *= shrink;
+        std::vector<double> qs(ng);
+        std::vector<std::array<double, 2>> ts(ng);
+        for (int k = 0; k < ng && !rc; ++k) {
+          std::vector<double> local(step);
+          local[k] /= shrink;
+          if ((rc = ascent(prop[k], local))) break;
+          if ((rc = setf(prop[k]))) break;
+          if ((rc = eval(prop[k], false, ts[k].data()))) break;
+          qs[k] = ts[k][0] + ts[k][1] - lsq_ref;
+        }
+        if (rc) break;
+        int idx = 0;
+        for (int k = 1; k < ng; ++k)
+          if (qs[k] > qs[idx]) idx = k;
+        if (qs[idx] >= 0) {
+          std::swap(nw, prop[idx]);
+          new_terms[0] = ts[idx][0];
+          new_terms[1] = ts[idx][1];
+          step[idx] /= shrink;
+          found = true;
+          break;
+        }
+      } else {
+        for (int g = 0; g < ng; ++g) step[g] *= shrink;
+      }
+    }
+    if (rc) break;
+    if (!found) {
+      rc = setf(fixed);
+      stop = 1;
+      rows = it;
+      break;
+    }
+    hist[(size_t)it * 2] = new_terms[0];
+    hist[(size_t)it * 2 + 1] = new_terms[1];
+    std::swap(fixed, nw);
+    for (int g = 0; g < ng; ++g) step[g] *= o.expand;
+    lsq_ref = new_terms[0] + new_terms[1];
+    const double cur = (hist[(size_t)(it - 1) * 2] + hist[(size_t)(it - 1) * 2 + 1]) -
+                       (hist[(size_t)it * 2] + hist[(size_t)it * 2 + 1]);
+    const double ref = (hist[0] + hist[1]) - (hist[(size_t)it * 2] + hist[(size_t)it * 2 + 1]);
+    if (std::fabs(cur) < o.tolerance * std::fabs(ref)) {
+      stop = 2;
+      rows = it + 1;
+      break;
+    }
+    if ((rc = setf(fixed))) break;
+    if ((rc = eval(fixed, true, ignored))) break;
+    ++it;
+    rows = it;
+  }
+  for (int g = 0; g < ng && !rc; ++g) {
+    const size_t nb = (size_t)sizes[g] * sizeof(double);
+    rc = c->cuda(cudaMemcpyAsync(params[g], fixed[g], nb, cudaMemcpyDefault, st), "copy");
+    if (!rc && grad_out && grad_out[g]) rc = c->cuda(cudaMemcpyAsync(grad_out[g], grad[g], nb, cudaMemcpyDefault, st), "copy");
+  }
+  if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
+  if (!rc) {
+    res->rows = stop == 0 ? o.max_iterations + 1 : rows;
+    res->history.assign(hist.begin(), hist.begin() + (size_t)res->rows * 2);
+    res->step = step;
+    res->sq = sq;
+    res->tau = 0.0;
+    res->freeze = 0;
+    res->evaluations = evaluations;
+    res->stop = stop;
+    res->iter = it;
+  }
+  cleanup();
+  return rc;
+}
+
 int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes, double *const *params,
                          const FgaOptions &o, const FgaEvaluate &evaluate, FgaResult *res, double *const *aux_out,
                          double *const *grad_out, const FgaSetFixed &set_fixed) {
@@ -30,6 +174,9 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
   if (o.max_iterations < 0 || o.max_line_search < 1 || !(o.shrink > 0 && o.shrink < 1) || !(o.expand >= 1) ||
       !(o.initial_step > 0) || o.nb_iter_freeze < 0)
     return c->fail(GBK_ERR_ARG, "bad optimiser parameters");
+  if (o.estimator == GBK_ESTIMATOR_GRADIENT_ASCENT)
+    return gradient_ascent(c, st, ng, sizes, params, o, evaluate, res, grad_out, set_fixed);
+  if (o.estimator != GBK_ESTIMATOR_FAST_GRADIENT_ASCENT) return c->fail(GBK_ERR_ARG, "unknown estimator %d", o.estimator);
   // per group: fixed, aux, new, gradient, and one candidate per multivariate proposal
   std::vector<double *> owned;
   auto dev = [&](long n, double **p) {
@@ -193,6 +340,7 @@ int fast_gradient_ascent(gbk_ctx *c, cudaStream_t st, int ng, const long *sizes,
     res->freeze = freeze;
     res->evaluations = evaluations;
     res->stop = stop;
+    res->iter = it;
   }
   cleanup();
   return rc;

@@ -424,6 +424,7 @@ int gbk_registration_optimize(gbk_registration *r, double *cp, double *mom, int 
     return e;
   };
   FgaOptions o;
+  o.estimator = c->estimator;
   o.max_iterations = max_iterations;
   o.max_line_search = max_line_search;
   o.nb_iter_freeze = nb_iter_freeze;

@@ -251,7 +251,8 @@ class Registration:
     def optimize(self, cp, mom, max_iterations: int, initial_step: float = 1e-3, optimize_cp: bool = True,
                  max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2, tolerance: float = 1e-4,
                  nb_iter_freeze: int = 3):
-        """The reference's FastGradientAscent over control points and momenta, on the device
+        """The context's estimator (the reference's FastGradientAscent by default, or GradientAscent)
+        over control points and momenta, on the device
         (gbk_registration_optimize). Returns a dict: cp, mom (final fixed effects), aux_cp, aux_mom,
         grad_cp, grad_mom (extrapolated point and gradient there), history ([data, regularity] per
         iteration), step, tau, freeze_counter, grad_sq_norms, evaluations, stopped."""
@@ -361,7 +362,8 @@ class MultiObjectAtlas:
     def optimize(self, cp, tmpl, mom, max_iterations: int, initial_step: float = 1e-3, optimize_cp: bool = True,
                  optimize_template: bool = True, max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2,
                  tolerance: float = 1e-4, nb_iter_freeze: int = 3):
-        """The reference's FastGradientAscent over [control points] [template] momenta on the device.
+        """The context's estimator (FastGradientAscent by default, or GradientAscent) over [control
+        points] [template] momenta on the device.
         Returns a dict like Atlas.optimize plus aux_* and grad_* (extrapolated point, gradient there)."""
         cp, tmpl, mom = (np.array(a, dtype=np.float64) for a in (cp, tmpl, mom))
         hist = np.zeros((max_iterations + 1, 2))
@@ -532,7 +534,8 @@ class Atlas:
     def optimize(self, cp, tmpl, mom, max_iterations: int, initial_step: float = 1e-3, optimize_cp: bool = True,
                  optimize_template: bool = True, max_line_search: int = 10, shrink: float = 0.5,
                  expand: float = 1.2, tolerance: float = 1e-4, nb_iter_freeze: int = 3):
-        """The reference's FastGradientAscent over control points, template points and momenta, on
+        """The context's estimator (the reference's FastGradientAscent by default, or its
+        GradientAscent: Context.set_estimator) over control points, template points and momenta, on
         the device (gbk_atlas_optimize). Returns a dict: cp, tmpl, mom (final), history, step and
         grad_sq_norms per optimised group, tau, freeze_counter, evaluations, stopped."""
         cp, tmpl, mom = (np.array(v, dtype=np.float64) for v in (cp, tmpl, mom))

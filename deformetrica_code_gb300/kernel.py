@@ -100,6 +100,14 @@ class Context:
     def get_gradient_mode(self) -> int:
         return int(self.lib.gbk_get_gradient_mode(self.h))
 
+    def set_estimator(self, estimator: int):
+        """GBK_ESTIMATOR_FAST_GRADIENT_ASCENT (default) or GBK_ESTIMATOR_GRADIENT_ASCENT for the
+        optimize() methods (include/gbk.h)."""
+        self.check(self.lib.gbk_set_estimator(self.h, estimator))
+
+    def get_estimator(self) -> int:
+        return int(self.lib.gbk_get_estimator(self.h))
+
     def set_split(self, n: int):
         self.check(self.lib.gbk_set_split(self.h, n))
 

@@ -71,6 +71,11 @@ enum { GBK_ORDER_AUTO = 0, GBK_ORDER_OFF = 1, GBK_ORDER_SPATIAL = 2, GBK_ORDER_S
  *    applied per cell for volume meshes. */
 enum { GBK_GRADIENT_REFERENCE = 0, GBK_GRADIENT_EXACT = 1 };
 
+/* Estimator of the *_optimize calls (gbk_set_estimator): the reference's FastGradientAscent
+ * (FastGradientAscent.cxx:48-300, its default) or GradientAscent (GradientAscent.cxx:48-240:
+ * no extrapolation, no sufficient-increase term, every step expanded after an accepted step). */
+enum { GBK_ESTIMATOR_FAST_GRADIENT_ASCENT = 0, GBK_ESTIMATOR_GRADIENT_ASCENT = 1 };
+
 /* Operation identifiers (for gbk_autotune). */
 enum {
   GBK_OP_CONVOLVE = 0,
@@ -108,6 +113,10 @@ int gbk_get_order(const gbk_ctx *ctx);
  * GBK_GRADIENT_REFERENCE; a registration takes the mode current at its creation). */
 int gbk_set_gradient_mode(gbk_ctx *ctx, int mode);
 int gbk_get_gradient_mode(const gbk_ctx *ctx);
+/* Sets the GBK_ESTIMATOR_* of later *_optimize calls (default FastGradientAscent). With
+ * GradientAscent the optimisers' tau, freeze-counter and aux outputs are not set. */
+int gbk_set_estimator(gbk_ctx *ctx, int estimator);
+int gbk_get_estimator(const gbk_ctx *ctx);
 /* Waits for all work queued on the context's stream. */
 int gbk_synchronize(gbk_ctx *ctx);
 /* Number of the library's own kernels launched on this context so far. */

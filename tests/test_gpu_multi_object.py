@@ -160,3 +160,42 @@ def test_mo_atlas_without_lag_matches_oracle(gb, K, pb):
     assert normwise_rel(r["template"], ref["params"][1]) <= 1e-10
     assert r["evaluations"] == ref["evaluations"]
     a.close()
+
+
+@pytest.fixture(scope="module")
+def bn():
+    return dict(np.load(os.path.join(GOLDEN, "banana_atlas.npz")))
+
+
+@pytest.mark.parametrize("engine", ["batched", "multi_object"])
+@pytest.mark.parametrize("mode,tol", [("F64", 1e-9), ("F32C", 1e-4)])
+def test_reproduces_functional_test_2(gb, bn, engine, mode, tol):
+    """The reference's banana atlas (three OrientedSurfaceMesh subjects) estimated by its
+    GradientAscent with the lagged template, on the batched atlas and on the multi-object atlas:
+    the history (the line search fails at iteration 9, as in the reference's run), the final steps
+    and fixed effects."""
+    from deformetrica_code_gb300 import deformation as D
+    ctx = _ctx(gb, mode)
+    ctx.set_estimator(gb.GBK_ESTIMATOR_GRADIENT_ASCENT)
+    subjects = [(bn[f"subj{i}_pts"], bn[f"subj{i}_tris"]) for i in (1, 2, 3)]
+    kw = dict(T=int(bn["number_of_time_points"]), sigma_def=float(bn["kernel_width"]), heun=False)
+    if engine == "batched":
+        a = D.Atlas(bn["cp0"], bn["tmpl_pts"], bn["tmpl_tris"], subjects, sigma_data=float(bn["data_kernel_width"]),
+                    data_sigma2=float(bn["data_sigma2"]), kind="currents", context=ctx, **kw)
+    else:
+        obj = [dict(kind="currents", pts=bn["tmpl_pts"], cells=bn["tmpl_tris"], sigma=float(bn["data_kernel_width"]),
+                    sigma2=float(bn["data_sigma2"]))]
+        a = D.MultiObjectAtlas(len(bn["cp0"]), obj, [[s] for s in subjects], context=ctx, **kw)
+    a.set_template_smoothing(float(bn["smoothing_width"]))
+    r = a.optimize(bn["cp0"], bn["tmpl_pts"], np.zeros((3,) + bn["cp0"].shape), int(bn["max_iterations"]),
+                   float(bn["initial_step"]), max_line_search=int(bn["max_line_search"]), expand=float(bn["expand"]))
+    a.close()
+    rel = lambda x, y: np.abs(np.asarray(x) - y).max() / np.abs(y).max()
+    assert r["stopped"] == "line_search"
+    assert r["history"].shape == bn["state_history"].shape
+    assert rel(r["history"], bn["state_history"]) <= tol
+    assert rel(r["step"], bn["state_step"]) <= 1e-12
+    tk = "tmpl" if engine == "batched" else "template"
+    assert rel(r["cp"], bn["state_control_points"]) <= 10 * tol
+    assert rel(r[tk], bn["state_template"]) <= 10 * tol
+    assert rel(r["mom"], bn["state_momenta"]) <= 10 * tol

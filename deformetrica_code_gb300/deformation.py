@@ -236,6 +236,8 @@ class Registration:
     def step(self, cp, mom):
         """Returns (loglik[5] = L, L_data, L_reg, match, <Kp,p>), dL/dcp, dL/dp."""
         cp, mom = _f64(cp), _f64(mom)
+        if tuple(cp.shape) != (self.ncp, self.d) or tuple(mom.shape) != (self.ncp, self.d):
+            raise ValueError(f"expected control points and momenta of shape {(self.ncp, self.d)}")
         ll = np.zeros(5)
         gcp = _empty_like(cp, cp.shape)
         gmom = _empty_like(cp, cp.shape)
@@ -258,6 +260,8 @@ class Registration:
         iteration), step, tau, freeze_counter, grad_sq_norms, evaluations, stopped."""
         cp = np.array(cp, dtype=np.float64)
         mom = np.array(mom, dtype=np.float64)
+        if cp.shape != (self.ncp, self.d) or mom.shape != (self.ncp, self.d):
+            raise ValueError(f"expected control points and momenta of shape {(self.ncp, self.d)}")
         hist = np.zeros((max_iterations + 1, 2))
         info = np.zeros(8)
         aux_cp, aux_mom, g_cp, g_mom = (np.zeros_like(cp) for _ in range(4))
@@ -344,6 +348,11 @@ class MultiObjectAtlas:
             c(nv_t), c(tgt), c(ncell_t), c(tcells), int(T), float(sigma_def), int(heun), ctypes.byref(h)))
         self.h = h
 
+    def _check_shapes(self, cp, tmpl, mom):
+        if cp.shape != (self.ncp, self.d) or tmpl.shape != (self.nv, self.d) or mom.shape != (self.S, self.ncp, self.d):
+            raise ValueError(f"expected cp {(self.ncp, self.d)}, template {(self.nv, self.d)}, "
+                             f"momenta {(self.S, self.ncp, self.d)}")
+
     def set_template_smoothing(self, width: float):
         self.ctx.check(self.ctx.lib.gbk_mo_atlas_set_template_smoothing(self.h, float(width)))
 
@@ -353,6 +362,7 @@ class MultiObjectAtlas:
     def step(self, cp, tmpl, mom):
         """Returns loglik [L, L_data, L_reg], dL/dcp, the smoothed template gradient, dL/dp."""
         cp, tmpl, mom = (np.ascontiguousarray(a, dtype=np.float64) for a in (cp, tmpl, mom))
+        self._check_shapes(cp, tmpl, mom)
         ll = np.zeros(3)
         gc, gt, gm = np.zeros_like(cp), np.zeros_like(tmpl), np.zeros_like(mom)
         c = lambda a: ctypes.c_void_p(a.ctypes.data)
@@ -366,6 +376,7 @@ class MultiObjectAtlas:
         points] [template] momenta on the device.
         Returns a dict like Atlas.optimize plus aux_* and grad_* (extrapolated point, gradient there)."""
         cp, tmpl, mom = (np.array(a, dtype=np.float64) for a in (cp, tmpl, mom))
+        self._check_shapes(cp, tmpl, mom)
         hist = np.zeros((max_iterations + 1, 2))
         info = np.zeros(10)
         aux = [np.zeros_like(a) for a in (cp, tmpl, mom)]
@@ -433,6 +444,11 @@ class GeodesicRegression:
     def set_template_smoothing(self, width: float):
         self.ctx.check(self.ctx.lib.gbk_geodesic_regression_set_template_smoothing(self.h, float(width)))
 
+    def _check_shapes(self, cp, mom, tmpl):
+        if cp.shape != (self.ncp, self.d) or mom.shape != (self.ncp, self.d) or (
+                tmpl is not None and tmpl.shape != (self.nv, self.d)):
+            raise ValueError(f"expected cp and momenta {(self.ncp, self.d)}, template {(self.nv, self.d)}")
+
     def set_corrected_gradient(self, enable: bool):
         self.ctx.check(self.ctx.lib.gbk_geodesic_regression_set_corrected_gradient(self.h, int(enable)))
 
@@ -441,6 +457,7 @@ class GeodesicRegression:
         template gradient."""
         cp, mom = np.ascontiguousarray(cp, np.float64), np.ascontiguousarray(mom, np.float64)
         t = None if tmpl is None else np.ascontiguousarray(tmpl, np.float64)
+        self._check_shapes(cp, mom, t)
         ll = np.zeros(5)
         gc, gm, gt = np.zeros_like(cp), np.zeros_like(mom), np.zeros((self.nv, self.d))
         c = lambda a: None if a is None else ctypes.c_void_p(a.ctypes.data)
@@ -452,6 +469,7 @@ class GeodesicRegression:
                  optimize_template: bool = True, max_line_search: int = 10, shrink: float = 0.5, expand: float = 1.2,
                  tolerance: float = 1e-4, nb_iter_freeze: int = 3):
         cp, mom, tmpl = (np.array(a, dtype=np.float64) for a in (cp, mom, tmpl))
+        self._check_shapes(cp, mom, tmpl)
         hist = np.zeros((max_iterations + 1, 2))
         info = np.zeros(10)
         aux = [np.zeros_like(a) for a in (cp, mom, tmpl)]
@@ -516,6 +534,8 @@ class Atlas:
     def step(self, mom):
         """mom: S x ncp x 3. Returns loglik (3 + S), dL/dp (S x ncp x 3), dL/dcp, template gradient."""
         mom = np.ascontiguousarray(mom, dtype=np.float64)
+        if mom.shape != (self.S, self.ncp, 3):
+            raise ValueError(f"expected momenta of shape {(self.S, self.ncp, 3)}")
         ll = np.zeros(3 + self.S)
         gm = np.zeros((self.S, self.ncp, 3))
         gc = np.zeros((self.ncp, 3))
@@ -539,6 +559,8 @@ class Atlas:
         the device (gbk_atlas_optimize). Returns a dict: cp, tmpl, mom (final), history, step and
         grad_sq_norms per optimised group, tau, freeze_counter, evaluations, stopped."""
         cp, tmpl, mom = (np.array(v, dtype=np.float64) for v in (cp, tmpl, mom))
+        if cp.shape != (self.ncp, 3) or tmpl.shape != (self.nv, 3) or mom.shape != (self.S, self.ncp, 3):
+            raise ValueError(f"expected cp {(self.ncp, 3)}, template {(self.nv, 3)}, momenta {(self.S, self.ncp, 3)}")
         hist = np.zeros((max_iterations + 1, 2))
         info = np.zeros(10)
         iters = ctypes.c_int(0)

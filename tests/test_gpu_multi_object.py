@@ -199,3 +199,18 @@ def test_reproduces_functional_test_2(gb, bn, engine, mode, tol):
     assert rel(r["cp"], bn["state_control_points"]) <= 10 * tol
     assert rel(r[tk], bn["state_template"]) <= 10 * tol
     assert rel(r["mom"], bn["state_momenta"]) <= 10 * tol
+
+
+def test_wrappers_reject_bad_shapes(gb, pb):
+    from deformetrica_code_gb300 import deformation as D
+    objects, subjects, tmpl, gobj = _parabola(pb)
+    a = D.MultiObjectAtlas(40, gobj, subjects, 10, 0.2, heun=False, context=_ctx(gb, "F64"))
+    with pytest.raises(ValueError):
+        a.step(pb["cp0"], tmpl[:-1], np.zeros((3, 40, 2)))
+    with pytest.raises(ValueError):
+        a.optimize(pb["cp0"], tmpl, np.zeros((2, 40, 2)), 1)
+    a.close()
+    r = D.Registration.from_objects(40, gobj, subjects[0], 10, 0.2, heun=False, context=_ctx(gb, "F64"))
+    with pytest.raises(ValueError):
+        r.step(pb["cp0"][:-1], np.zeros((39, 2)))
+    r.close()

@@ -2,8 +2,9 @@
 
 Every ``csrc/*.cu`` file is compiled by nvcc in parallel with
 ``-gencode arch=compute_103a,code=sm_103a -lineinfo -O3`` and linked into
-``deformetrica_code_gb300/libgbkernel.so``. Rebuilds only when a source is newer than the
-library. No CMake, no torch extension machinery: the library is plain C ABI.
+``deformetrica_code_gb300/libgbkernel.so`` (with cuFFT for the particle-mesh kernel). Rebuilds only
+when a source is newer than the library. No CMake, no torch extension machinery: the library is
+plain C ABI.
 """
 from __future__ import annotations
 
@@ -72,7 +73,9 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+    # cuFFT (the particle-mesh kernel) from the toolkit this nvcc belongs to, found at run time by rpath
+    cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "lib64")
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcufft", "-Xlinker", "-rpath", "-Xlinker", cudalib]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr[-4000:]}")

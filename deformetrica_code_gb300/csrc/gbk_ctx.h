@@ -86,7 +86,13 @@ struct gbk_ctx {
     ~OrderScope() { c->order = saved; }
   };
 
+  // the particle-mesh kernel's cached FFT plans and kernel spectra (gbk_p3m.cu)
+  void *p3m = nullptr;
+  void (*p3m_free)(void *) = nullptr;
+
   void release() {
+    if (p3m && p3m_free) p3m_free(p3m);
+    p3m = nullptr;
     auto fr = [](DevBuf &b) {
       if (b.p) cudaFree(b.p);
       b.p = nullptr;

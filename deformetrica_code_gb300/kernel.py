@@ -342,3 +342,52 @@ class GB300ExactKernel:
 
 
 __all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64"]
+
+
+def _p3m(name, x, y, w, sigma, alpha, domain, spacing_ratio, padding_factor, out_cols, context):
+    ctx = context or Context()
+    d = x.shape[1]
+    _check(x, "x")
+    _check(y, "y", d)
+    _check(w, "w")
+    if w.shape[0] != y.shape[0]:
+        raise ValueError("sources and weights count mismatch")
+    if alpha is not None:
+        _check(alpha, "alpha", w.shape[1])
+        if alpha.shape[0] != x.shape[0]:
+            raise ValueError("alpha needs one row per target")
+    dom = None if domain is None else np.ascontiguousarray(np.concatenate([np.asarray(domain[0], float).ravel(),
+                                                                            np.asarray(domain[1], float).ravel()]))
+    if dom is not None and dom.size != 2 * d:
+        raise ValueError("domain: (lo[d], hi[d])")
+    out = _empty_like(x, (x.shape[0],) + out_cols)
+    ctx.bind_stream(x, y, w)
+    args = [ctx.h, d, w.shape[1], _ptr(x), x.shape[0], _ptr(y), _ptr(w), y.shape[0], float(sigma)]
+    if alpha is not None:
+        args.append(_ptr(alpha))
+    args += [None if dom is None else ctypes.c_void_p(dom.ctypes.data), float(spacing_ratio), float(padding_factor),
+             _ptr(out)]
+    ctx.check(getattr(ctx.lib, name)(*args))
+    return out
+
+
+def p3m_convolve(x, y, w, sigma, domain=None, spacing_ratio: float = 0.2, padding_factor: float = 3.0,
+                 context: Context | None = None):
+    """The reference's P3MKernel::Convolve on the device (gbk_p3m_convolve): a particle-mesh
+    approximation of sum_j K(x_i, y_j) w_j. domain = (lo, hi) or None for the bounding box of x, y."""
+    return _p3m("gbk_p3m_convolve", x, y, w, sigma, None, domain, spacing_ratio, padding_factor, (w.shape[1],),
+                context)
+
+
+def p3m_convolve_gradient(x, y, w, sigma, domain=None, spacing_ratio: float = 0.2, padding_factor: float = 3.0,
+                          context: Context | None = None):
+    """P3MKernel::ConvolveGradient(X): nx x dv x d."""
+    return _p3m("gbk_p3m_convolve_gradient", x, y, w, sigma, None, domain, spacing_ratio, padding_factor,
+                (w.shape[1], x.shape[1]), context)
+
+
+def p3m_convolve_gradient_alpha(x, y, w, sigma, alpha, domain=None, spacing_ratio: float = 0.2,
+                                padding_factor: float = 3.0, context: Context | None = None):
+    """P3MKernel::ConvolveGradient(X, alpha): nx x d."""
+    return _p3m("gbk_p3m_convolve_gradient_alpha", x, y, w, sigma, alpha, domain, spacing_ratio, padding_factor,
+                (x.shape[1],), context)

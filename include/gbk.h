@@ -358,6 +358,26 @@ void gbk_registration_destroy(gbk_registration *reg);
 int gbk_kernel_norm_noalloc(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
                             double sigma, double *out);
 
+/* ---- particle-mesh approximation (the reference's P3MKernel) -------------------------------- */
+
+/* P3MKernel::Convolve (P3MKernel.cxx:1245-1355): the sources' weights splatted multilinearly onto a
+ * grid of spacing spacing_ratio x sigma covering the data domain padded by padding_factor x sigma on
+ * each side (sizes rounded up to powers of two, DetermineGrids :371-432), convolved with the
+ * sampled Gaussian by FFT (cuFFT), interpolated multilinearly at the targets. domain: 2 d doubles on
+ * the host (lo[0..d-1], hi[0..d-1]), or NULL for the bounding box of targets and sources. The
+ * reference's defaults are spacing_ratio 0.2 and padding_factor 3 (SparseDiffeoParameters.cxx:25-27).
+ * An approximation: a few percent relative error against the exact sums. d = 2 or 3, FP64. */
+int gbk_p3m_convolve(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                     double sigma, const double *domain, double spacing_ratio, double padding_factor, double *out);
+/* P3MKernel::ConvolveGradient(X) (:1386-1447): out nx x dv x d from the sampled kernel gradient. */
+int gbk_p3m_convolve_gradient(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y, const double *w,
+                              long ny, double sigma, const double *domain, double spacing_ratio, double padding_factor,
+                              double *out);
+/* P3MKernel::ConvolveGradient(X, alpha) (:1357-1366): out nx x d, the gradient contracted with alpha. */
+int gbk_p3m_convolve_gradient_alpha(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                                    const double *w, long ny, double sigma, const double *alpha, const double *domain,
+                                    double spacing_ratio, double padding_factor, double *out);
+
 /* ---- geodesic regression (the reference's Regression model), CUDA-graph replay ------------ */
 
 typedef struct gbk_geodesic_regression gbk_geodesic_regression;

@@ -1,0 +1,60 @@
+"""GPU particle-mesh kernel (gbk_p3m_*, the reference's P3MKernel with cuFFT) against its FP64
+restatement (oracle/p3m.py) and against the exact kernel sums (the reference's P3M tolerance,
+8e-2). Parity with the reference's own P3M binary is unpinned: it needs ITK/FFTW."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gb():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import deformetrica_code_gb300 as g
+    return g
+
+
+@pytest.fixture(scope="module")
+def K():
+    import oracle
+    return oracle.load("port")
+
+
+@pytest.mark.parametrize("d,sigma", [(2, 0.1), (2, 0.3), (3, 0.3), (3, 0.15)])
+def test_p3m_matches_restatement_and_exact(gb, K, d, sigma):
+    from oracle import p3m
+    from deformetrica_code_gb300 import kernel as KM
+    rng = np.random.default_rng(11 + d)
+    x, y = rng.random((200, d)), rng.random((250, d))
+    w, a = rng.normal(size=(250, 3)), rng.normal(size=(200, 3))
+    ctx = gb.Context(mode=gb.GBK_MODE_F64)
+    v = KM.p3m_convolve(x, y, w, sigma, context=ctx)
+    gv = KM.p3m_convolve_gradient(x, y, w, sigma, context=ctx)
+    ga = KM.p3m_convolve_gradient_alpha(x, y, w, sigma, a, context=ctx)
+    rv, rg = p3m.convolve(x, y, w, sigma), p3m.convolve_gradient(x, y, w, sigma)
+    assert np.linalg.norm(v - rv) <= 1e-10 * np.linalg.norm(rv)
+    assert np.linalg.norm(gv - rg) <= 1e-10 * np.linalg.norm(rg)
+    np.testing.assert_allclose(ga, np.einsum("ikp,ik->ip", gv, a), rtol=1e-12, atol=1e-12 * np.abs(ga).max())
+    ve, ge = K.convolve(x, y, w, sigma), K.grad_alpha(x, y, w, sigma, a)
+    assert np.linalg.norm(v - ve) <= 8e-2 * np.linalg.norm(ve)
+    assert np.linalg.norm(ga - ge) <= 8e-2 * np.linalg.norm(ge)
+
+
+def test_p3m_domain_and_cache(gb):
+    """An explicit data domain equal to the bounding box gives the same sums; a second width after
+    the first rebuilds the cached plans and spectra."""
+    from oracle import p3m
+    from deformetrica_code_gb300 import kernel as KM
+    rng = np.random.default_rng(3)
+    x, y, w = rng.random((100, 3)), rng.random((120, 3)), rng.normal(size=(120, 2))
+    ctx = gb.Context(mode=gb.GBK_MODE_F64)
+    lo, hi = p3m.domain_of(x, y)
+    a = KM.p3m_convolve(x, y, w, 0.3, context=ctx)
+    b = KM.p3m_convolve(x, y, w, 0.3, domain=(lo, hi), context=ctx)
+    assert np.array_equal(a, b) or np.abs(a - b).max() <= 1e-14 * np.abs(a).max()
+    c = KM.p3m_convolve(x, y, w, 0.25, context=ctx)
+    assert np.linalg.norm(c - p3m.convolve(x, y, w, 0.25)) <= 1e-10 * np.linalg.norm(c)
+    with pytest.raises(ValueError):
+        KM.p3m_convolve(x, y, w[:5], 0.3, context=ctx)

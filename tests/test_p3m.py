@@ -1,0 +1,34 @@
+"""The particle-mesh (P3M) oracle (oracle/p3m.py, a restatement of the reference's P3MKernel,
+whose own build needs ITK/FFTW): the grid rule and the approximation error against the exact
+kernel, within the 8e-2 the reference's tests accept for P3M. No GPU."""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def K():
+    import oracle
+    return oracle.load("port")
+
+
+def test_grid_rule():
+    from oracle import p3m
+    origin, size, s = p3m.grid([0.0, 0.0, 0.0], [1.0, 1.0, 1.0], 0.1)
+    assert s == pytest.approx(0.02) and list(size) == [128, 128, 128]  # 1.6 / 0.02 = 80 -> 128
+    assert origin[0] == pytest.approx(-(128 * 0.02 - 1.0) / 2)
+    origin, size, s = p3m.grid([0.0, -1.0], [2.0, 1.0], 0.5, ratio=0.25, padding=1.0)
+    assert list(size) == [32, 32]  # (2 + 1) / 0.125 = 24 -> 32
+
+
+@pytest.mark.parametrize("d,sigma", [(2, 0.1), (2, 0.3), (3, 0.3)])
+def test_approximation_error(K, d, sigma):
+    from oracle import p3m
+    rng = np.random.default_rng(7 + d)
+    x, y = rng.random((120, d)), rng.random((150, d))
+    w, a = rng.normal(size=(150, 3)), rng.normal(size=(120, 3))
+    v, ve = p3m.convolve(x, y, w, sigma), K.convolve(x, y, w, sigma)
+    g, ge = p3m.convolve_gradient_alpha(x, y, w, sigma, a), K.grad_alpha(x, y, w, sigma, a)
+    assert np.linalg.norm(v - ve) <= 8e-2 * np.linalg.norm(ve)
+    assert np.linalg.norm(g - ge) <= 8e-2 * np.linalg.norm(ge)
+    gv = p3m.convolve_gradient(x, y, w, sigma)
+    np.testing.assert_allclose(np.einsum("ikp,ik->ip", gv, a), g, rtol=1e-12, atol=1e-12)

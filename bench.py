@@ -557,6 +557,65 @@ def small_kernel_bench(n: int = 4096, sigma: float = 0.2, reps: int = 50, cpu: b
     return res
 
 
+def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float = 0.1, n_check: int = 4096,
+              n_cpu: int = 20_000):
+    """The particle-mesh kernel (the reference's P3MKernel: grid spacing 0.2 sigma, padding 3 sigma)
+    on the headline workload: N = M = 1e6 points of the 8-Gaussian mixture, sigma 0.1, Convolve
+    and ConvolveGradient(X, alpha) from device arrays, timed per call with FP32 grids (f32c, the
+    default context mode) and FP64 grids (f64); relative L2 errors against the exact FP64 sum on
+    the first n_check targets; the FP64 numpy restatement timed on
+    n_cpu targets and sources on the same grid (a bounded CPU sample: the FFTs are the same size,
+    the splat and interpolation loops scale with the points)."""
+    import torch
+    import deformetrica_code_gb300 as g
+    x, y, w, a = make_workload(n, n)
+    lo, hi = np.minimum(x.min(0), y.min(0)), np.maximum(x.max(0), y.max(0))
+    dom = (lo, hi)
+    ctx, ctx64 = g.Context(), g.Context(mode=g.GBK_MODE_F64)
+    X, Y, W, A = (torch.from_numpy(v).cuda() for v in (x, y, w, a))
+    res = {"workload": f"N = M = {n}, d = 3, 8-Gaussian mixture in [0,1]^3, sigma {sigma}, spacing 0.2 sigma, "
+                       "padding 3 sigma, cuFFT; grids FP32 (f32c) or FP64 (f64)",
+           "grid": None, "convolve": {}, "gradient_alpha": {}}
+    # exact FP64 sums on a subsample of targets
+    k = g.GB300ExactKernel(3, sigma, context=ctx64)
+    k.SetSources(Y)
+    k.SetWeights(W)
+    Xs, As = X[:n_check].contiguous(), A[:n_check].contiguous()
+    exact = {"convolve": k.Convolve(Xs).cpu().numpy(), "gradient_alpha": k.ConvolveGradient(Xs, As).cpu().numpy()}
+    for mode, c in (("f32c", ctx), ("f64", ctx64)):
+        calls = (("convolve", lambda: g.p3m_convolve(X, Y, W, sigma, domain=dom, context=c)),
+                 ("gradient_alpha", lambda: g.p3m_convolve_gradient_alpha(X, Y, W, sigma, A, domain=dom, context=c)))
+        for name, fn in calls:
+            for _ in range(3):
+                out = fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / reps
+            e = exact[name]
+            err = float(np.linalg.norm(out[:n_check].cpu().numpy() - e) / np.linalg.norm(e))
+            res[name][mode] = {"s_per_call": dt, "pairs_per_s_equivalent": float(n) * n / dt,
+                               "rel_l2_err_vs_exact": err}
+    res["err_sample"] = f"first {n_check} targets vs the exact FP64 GPU sum over all {n} sources"
+    from oracle import p3m as p3m_oracle
+    origin, size, s = p3m_oracle.grid(lo, hi, sigma)
+    res["grid"] = [int(v) for v in size]
+    if cpu:
+        xs, ys, ws, as_ = x[:n_cpu], y[:n_cpu], w[:n_cpu], a[:n_cpu]
+        for name, fn in (("convolve", lambda: p3m_oracle.convolve(xs, ys, ws, sigma, lo, hi)),
+                         ("gradient_alpha", lambda: p3m_oracle.convolve_gradient_alpha(xs, ys, ws, sigma, as_, lo, hi))):
+            t0 = time.perf_counter()
+            fn()
+            dt = time.perf_counter() - t0
+            res[name]["cpu_oracle"] = {"s_per_call": dt, "sample": f"{n_cpu} targets and sources, same grid",
+                                       "kind": "port (FP64 numpy)", "cores": 1}
+    ctx.close()
+    ctx64.close()
+    return res
+
+
 def fp64_gpu_pairs(n: int, sigma: float):
     """The same fused forward+adjoint step in the FP64 mode (plain FP64 kernel sums) at N = M = n."""
     import torch
@@ -718,6 +777,7 @@ def main():
     ap.add_argument("--no-data-terms", action="store_true")
     ap.add_argument("--no-small", action="store_true", help="skip the 4096-point kernel-sum case")
     ap.add_argument("--no-optimizer", action="store_true", help="skip the registration optimiser runs")
+    ap.add_argument("--no-p3m", action="store_true", help="skip the particle-mesh kernel case")
     ap.add_argument("--data-term-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
@@ -881,6 +941,8 @@ def main():
             line["data_terms"] = data_term_bench(args.data_term_steps, cpu=not args.no_cpu_baseline)
         if not args.no_small:
             line["small_kernel_sum"] = small_kernel_bench(cpu=not args.no_cpu_baseline)
+        if not args.no_p3m:
+            line["p3m"] = p3m_bench(cpu=not args.no_cpu_baseline)
         if not args.no_optimizer:
             line["optimizer"] = optimizer_bench(cpu=not args.no_cpu_baseline)
             if not args.no_atlas:

@@ -10,8 +10,10 @@ from ._lib import (GBKError, GBK_MODE_F32C, GBK_MODE_F64, GBK_ORDER_AUTO, GBK_OR
 
 _lib.load()
 
-from .kernel import Context, GB300ExactKernel  # noqa: E402
+from .kernel import (Context, GB300ExactKernel, p3m_convolve, p3m_convolve_gradient,  # noqa: E402
+                     p3m_convolve_gradient_alpha)
 
 __all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64", "GBK_ORDER_AUTO",
            "GBK_ORDER_OFF", "GBK_ORDER_SPATIAL", "GBK_ORDER_SPATIAL_NOPRUNE", "GBK_GRADIENT_REFERENCE",
-           "GBK_GRADIENT_EXACT", "GBK_ESTIMATOR_FAST_GRADIENT_ASCENT", "GBK_ESTIMATOR_GRADIENT_ASCENT"]
+           "GBK_GRADIENT_EXACT", "GBK_ESTIMATOR_FAST_GRADIENT_ASCENT", "GBK_ESTIMATOR_GRADIENT_ASCENT", "p3m_convolve",
+           "p3m_convolve_gradient", "p3m_convolve_gradient_alpha"]

@@ -8,8 +8,13 @@
 //     gradient at the non-border grid points around the grid centre, inverse-FFT-shifted, FFT;
 //   convolution (ApplyKernelFFT, :1088-1178): inverse FFT of the product of the spectra;
 //   interpolation (Interpolate, :641-662): multilinear at the targets.
-// Everything is FP64. The splat accumulates with atomic adds (grid sums in arbitrary order, last-bit
-// differences between runs); plans and kernel spectra are cached in the context per grid and width.
+// Coordinates, interpolation weights and outputs are FP64; the grids, spectra and transforms are
+// FP64 in GBK_MODE_F64 and FP32 in GBK_MODE_F32C (FP64 transforms are bound by the FP64 pipe, which
+// is a small fraction of the FP32 one; FP32 grids add ~1e-6 relative to a method whose own error
+// against the exact sum is ~1e-2). The splat accumulates with atomic adds (grid sums in arbitrary
+// order, last-bit differences between runs). Each call runs one batched forward transform over
+// the weight grids and one batched inverse transform over the images; plans, kernel spectra and
+// scratch are cached in the context per grid, width and precision.
 #include <cuda_runtime.h>
 #include <cufft.h>
 
@@ -32,37 +37,57 @@ struct P3MGrid {
   long ccells() const { return n[0] * (d == 3 ? n[1] * (n[2] / 2 + 1) : (n[1] / 2 + 1)); }
 };
 
+struct P3MPlan {
+  cufftType type;
+  int batch;
+  cufftHandle h;
+};
+
 struct P3MCache {
-  bool valid = false;
+  bool valid = false;  // kspec holds the spectra of (d, n, s, sigma, f64)
   int d = 0;
   long n[3] = {0, 0, 0};
   double s = 0, sigma = 0;
-  cufftHandle fwd = 0, inv = 0;
-  bool plans = false;
-  cufftDoubleComplex *kspec = nullptr;  // (1 + d) kernel spectra: Gaussian, then its gradient components
+  bool f64 = true;
+  std::vector<P3MPlan> plans;  // for the grid n of d
+  void *kspec = nullptr;       // (1 + d) kernel spectra: Gaussian, then its gradient components
+  void *work = nullptr;        // grow-only scratch: grids, images, spectra, products, box
+  size_t work_bytes = 0;
+
+  void drop_plans() {
+    for (auto &p : plans) cufftDestroy(p.h);
+    plans.clear();
+  }
 };
 
 void p3m_cache_free(void *p) {
   P3MCache *c = (P3MCache *)p;
   if (!c) return;
-  if (c->plans) {
-    cufftDestroy(c->fwd);
-    cufftDestroy(c->inv);
-  }
+  c->drop_plans();
   if (c->kspec) cudaFree(c->kspec);
+  if (c->work) cudaFree(c->work);
   delete c;
+}
+
+// grows the cached scratch to at least `bytes` (contents not kept)
+int p3m_work(gbk_ctx *c, P3MCache *pc, size_t bytes) {
+  if (pc->work_bytes >= bytes) return 0;
+  if (pc->work) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(pc->work);
+  }
+  pc->work = nullptr;
+  pc->work_bytes = 0;
+  int rc = c->cuda(cudaMalloc(&pc->work, bytes), "cudaMalloc (P3M)");
+  if (!rc) pc->work_bytes = bytes;
+  return rc;
 }
 
 unsigned nblk(long n, int bs = 256) { return (unsigned)std::max(1L, (n + bs - 1) / bs); }
 
-template <int D>
-__device__ inline long lin(const long *ind, const long *n) {
-  return D == 3 ? (ind[0] * n[1] + ind[1]) * n[2] + ind[2] : ind[0] * n[1] + ind[1];
-}
-
 // Kernel images in inverse-FFT-shifted layout: slot j holds the value at grid index (j + n/2) mod n.
-template <int D>
-__global__ void p3m_kernel_images(P3MGrid g, double sigma, double *img, long cells) {
+template <int D, typename G>
+__global__ void p3m_kernel_images(P3MGrid g, double sigma, G *img, long cells) {
   long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= cells) return;
   long slot[3], ind[3];
@@ -82,92 +107,114 @@ __global__ void p3m_kernel_images(P3MGrid g, double sigma, double *img, long cel
     d2 += diff[k] * diff[k];
   }
   const double kv = exp(-d2 / (sigma * sigma));
-  img[j] = border ? 0.0 : kv;
-  for (int k = 0; k < D; ++k) img[(1 + k) * cells + j] = border ? 0.0 : diff[k] * (-2.0 * kv / (sigma * sigma));
+  img[j] = (G)(border ? 0.0 : kv);
+  for (int k = 0; k < D; ++k) img[(1 + k) * cells + j] = (G)(border ? 0.0 : diff[k] * (-2.0 * kv / (sigma * sigma)));
 }
 
-// multilinear corners of one point: returns their count, in the reference's order (first
-// dimension slowest), outside points and zero weights dropped
+// multilinear corners of one point, slot b = corner b in the reference's order (first dimension
+// slowest): linear index, weight, `use` (inside the grid and weight > 0) and `interior` (no index
+// <= 0, the splat's border rule). Fixed slots keep the arrays in registers.
 template <int D>
-__device__ inline int p3m_corners(const double *p, const P3MGrid &g, long (*ind)[3], double *w) {
-  long i1[3];
-  double f[3], h[3];
+struct P3MCorners {
+  long l[1 << D];
+  double w[1 << D];
+  bool use[1 << D], interior[1 << D];
+};
+
+template <int D>
+__device__ inline void p3m_corners(const double *p, const P3MGrid &g, P3MCorners<D> &cs) {
+  long i1[D];
+  double f[D], h[D];
+#pragma unroll
   for (int k = 0; k < D; ++k) {
     const double c = (p[k] - g.origin[k]) / g.s;
     i1[k] = (long)floor(c);
     f[k] = c - i1[k];
     h[k] = (i1[k] + 1) - c;
   }
-  int m = 0;
+#pragma unroll
   for (int b = 0; b < (1 << D); ++b) {
     double wt = 1.0;
-    bool in = true;
+    bool in = true, inner = true;
+    long l = 0;
+#pragma unroll
     for (int k = 0; k < D; ++k) {
       const int bit = (b >> (D - 1 - k)) & 1;
       const long q = i1[k] + bit;
       wt *= bit ? f[k] : h[k];
       in = in && q >= 0 && q < g.n[k];
-      ind[m][k] = q;
+      inner = inner && q > 0;
+      l = l * g.n[k] + q;
     }
-    if (in && wt > 0) w[m++] = wt;
+    cs.l[b] = l;
+    cs.w[b] = wt;
+    cs.use[b] = in && wt > 0;
+    cs.interior[b] = inner;
   }
-  return m;
 }
 
-template <int D>
-__global__ void p3m_splat(const double *y, const double *wts, long ny, int dv, P3MGrid g, double *grids, long cells) {
+template <int D, typename G>
+__global__ void p3m_splat(const double *y, const double *wts, long ny, int dv, P3MGrid g, G *grids, long cells) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ny) return;
-  long ind[1 << D][3];
-  double w[1 << D];
-  const int m = p3m_corners<D>(y + i * D, g, ind, w);
-  for (int c = 0; c < m; ++c) {
-    bool border = false;
-    for (int k = 0; k < D; ++k) border = border || ind[c][k] <= 0;
-    if (border) continue;
-    const long l = lin<D>(ind[c], g.n);
-    for (int k = 0; k < dv; ++k) atomicAdd(grids + (long)k * cells + l, w[c] * wts[i * dv + k]);
+  P3MCorners<D> cs;
+  p3m_corners<D>(y + i * D, g, cs);
+#pragma unroll
+  for (int c = 0; c < (1 << D); ++c) {
+    if (!cs.use[c] || !cs.interior[c]) continue;
+    for (int k = 0; k < dv; ++k) atomicAdd(grids + (long)k * cells + cs.l[c], (G)(cs.w[c] * wts[i * dv + k]));
   }
 }
 
 // out[img] = spec[grid_of(img)] * kspec[kernel_of(img)] / N for img < nimg
-__global__ void p3m_multiply(const cufftDoubleComplex *spec, const cufftDoubleComplex *kspec, int nimg, int per_grid,
-                             int kernel0, long ccells, double scale, cufftDoubleComplex *out) {
+template <typename C, typename G>
+__global__ void p3m_multiply(const C *spec, const C *kspec, int nimg, int per_grid, int kernel0, long ccells, G scale,
+                             C *out) {
   long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= ccells) return;
   for (int m = 0; m < nimg; ++m) {
-    const cufftDoubleComplex a = spec[(long)(m / per_grid) * ccells + j];
-    const cufftDoubleComplex b = kspec[(long)(kernel0 + m % per_grid) * ccells + j];
-    out[(long)m * ccells + j] = make_cuDoubleComplex((a.x * b.x - a.y * b.y) * scale, (a.x * b.y + a.y * b.x) * scale);
+    const C a = spec[(long)(m / per_grid) * ccells + j];
+    const C b = kspec[(long)(kernel0 + m % per_grid) * ccells + j];
+    C r;
+    r.x = (a.x * b.x - a.y * b.y) * scale;
+    r.y = (a.x * b.y + a.y * b.x) * scale;
+    out[(long)m * ccells + j] = r;
   }
 }
 
 // values at the targets: mode 0 the nimg images; mode 2 contracted with alpha (images ordered
 // p + D k, out nx x D)
-template <int D>
-__global__ void p3m_interp(const double *x, long nx, const double *imgs, int nimg, long cells, P3MGrid g, int mode,
+template <int D, typename G>
+__global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, long cells, P3MGrid g, int mode,
                            const double *alpha, int dv, double *out) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nx) return;
-  long ind[1 << D][3];
-  double w[1 << D];
-  const int m = p3m_corners<D>(x + i * D, g, ind, w);
-  long l[1 << D];
-  for (int c = 0; c < m; ++c) l[c] = lin<D>(ind[c], g.n);
+  P3MCorners<D> cs;
+  p3m_corners<D>(x + i * D, g, cs);
   if (mode == 0) {
     for (int q = 0; q < nimg; ++q) {
       double v = 0.0;
-      for (int c = 0; c < m; ++c) v += w[c] * imgs[(long)q * cells + l[c]];
+#pragma unroll
+      for (int c = 0; c < (1 << D); ++c)
+        if (cs.use[c]) v += cs.w[c] * imgs[(long)q * cells + cs.l[c]];
       out[i * nimg + q] = v;
     }
   } else {
-    double r[3] = {0, 0, 0};
-    for (int k = 0; k < dv; ++k)
+    double r[D];
+#pragma unroll
+    for (int p = 0; p < D; ++p) r[p] = 0.0;
+    for (int k = 0; k < dv; ++k) {
+      const double a = alpha[i * dv + k];
+#pragma unroll
       for (int p = 0; p < D; ++p) {
         double v = 0.0;
-        for (int c = 0; c < m; ++c) v += w[c] * imgs[(long)(p + D * k) * cells + l[c]];
-        r[p] += v * alpha[i * dv + k];
+#pragma unroll
+        for (int c = 0; c < (1 << D); ++c)
+          if (cs.use[c]) v += cs.w[c] * imgs[(long)(p + D * k) * cells + cs.l[c]];
+        r[p] += v * a;
       }
+    }
+#pragma unroll
     for (int p = 0; p < D; ++p) out[i * D + p] = r[p];
   }
 }
@@ -212,6 +259,119 @@ int fft_error(gbk_ctx *c, cufftResult r, const char *what) {
   return r == CUFFT_SUCCESS ? GBK_OK : c->fail(GBK_ERR_CUDA, "cuFFT %s failed (%d)", what, (int)r);
 }
 
+template <typename G>
+struct P3MFFT;
+template <>
+struct P3MFFT<double> {
+  typedef cufftDoubleComplex C;
+  static constexpr cufftType R2C = CUFFT_D2Z, C2R = CUFFT_Z2D;
+  static cufftResult fwd(cufftHandle h, double *in, C *out) { return cufftExecD2Z(h, in, out); }
+  static cufftResult inv(cufftHandle h, C *in, double *out) { return cufftExecZ2D(h, in, out); }
+};
+template <>
+struct P3MFFT<float> {
+  typedef cufftComplex C;
+  static constexpr cufftType R2C = CUFFT_R2C, C2R = CUFFT_C2R;
+  static cufftResult fwd(cufftHandle h, float *in, C *out) { return cufftExecR2C(h, in, out); }
+  static cufftResult inv(cufftHandle h, C *in, float *out) { return cufftExecC2R(h, in, out); }
+};
+
+// a cached batched plan over `batch` contiguous grids of g (real distance cells, complex ccells)
+int p3m_plan(gbk_ctx *c, P3MCache *pc, const P3MGrid &g, cufftType type, int batch, cufftHandle *out) {
+  for (const P3MPlan &p : pc->plans)
+    if (p.type == type && p.batch == batch) {
+      *out = p.h;
+      return fft_error(c, cufftSetStream(p.h, c->stream), "stream");
+    }
+  int n[3] = {(int)g.n[0], (int)g.n[1], (int)g.n[2]};
+  cufftHandle h;
+  const cufftResult r = cufftPlanMany(&h, g.d, n, nullptr, 1, 0, nullptr, 1, 0, type, batch);
+  if (r != CUFFT_SUCCESS) return fft_error(c, r, "plan");
+  pc->plans.push_back({type, batch, h});
+  *out = h;
+  return fft_error(c, cufftSetStream(h, c->stream), "stream");
+}
+
+size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// kernel spectra (cached), splat, one batched forward transform, spectrum products, one batched
+// inverse transform, interpolation
+template <typename G>
+int p3m_exec(gbk_ctx *c, P3MCache *pc, const P3MGrid &g, int mode, int dv, const double *dx, long nx,
+             const double *dy, const double *dw, long ny, double sigma, const double *da, double *dout, HostIO &io) {
+  typedef typename P3MFFT<G>::C C;
+  const int d = g.d;
+  cudaStream_t st = c->stream;
+  const long cells = g.cells(), ccells = g.ccells();
+  const int nimg = mode == 0 ? dv : dv * d;
+  const bool f64 = sizeof(G) == 8;
+  int rc = 0;
+  if (!(pc->valid && pc->s == g.s && pc->sigma == sigma && pc->f64 == f64)) {
+    pc->valid = false;
+    if (pc->kspec) {
+      cudaStreamSynchronize(st);
+      cudaFree(pc->kspec);
+      pc->kspec = nullptr;
+    }
+    cufftHandle kp;
+    if ((rc = p3m_plan(c, pc, g, P3MFFT<G>::R2C, 1 + d, &kp))) return rc;
+    if ((rc = c->cuda(cudaMalloc(&pc->kspec, (size_t)ccells * (1 + d) * sizeof(C)), "cudaMalloc (P3M)"))) return rc;
+    if ((rc = p3m_work(c, pc, (size_t)cells * (1 + d) * sizeof(G)))) return rc;
+    G *kimg = (G *)pc->work;
+    if (d == 3)
+      p3m_kernel_images<3, G><<<nblk(cells), 256, 0, st>>>(g, sigma, kimg, cells);
+    else
+      p3m_kernel_images<2, G><<<nblk(cells), 256, 0, st>>>(g, sigma, kimg, cells);
+    c->launches += 1;
+    if ((rc = c->cuda(cudaGetLastError(), "kernel images"))) return rc;
+    if ((rc = fft_error(c, P3MFFT<G>::fwd(kp, kimg, (C *)pc->kspec), "forward"))) return rc;
+    pc->valid = true;
+    pc->s = g.s;
+    pc->sigma = sigma;
+    pc->f64 = f64;
+  }
+  cufftHandle fwd, inv;
+  if ((rc = p3m_plan(c, pc, g, P3MFFT<G>::R2C, dv, &fwd))) return rc;
+  if ((rc = p3m_plan(c, pc, g, P3MFFT<G>::C2R, nimg, &inv))) return rc;
+  const size_t b_spec = up256((size_t)ccells * dv * sizeof(C)), b_prod = up256((size_t)ccells * nimg * sizeof(C));
+  const size_t b_grid = up256((size_t)cells * dv * sizeof(G)), b_img = up256((size_t)cells * nimg * sizeof(G));
+  if ((rc = p3m_work(c, pc, b_spec + b_prod + b_grid + b_img))) return rc;
+  char *base = (char *)pc->work;
+  C *spec = (C *)base;
+  C *prod = (C *)(base + b_spec);
+  G *grids = (G *)(base + b_spec + b_prod);
+  G *imgs = (G *)(base + b_spec + b_prod + b_grid);
+  rc = c->cuda(cudaMemsetAsync(grids, 0, (size_t)cells * dv * sizeof(G), st), "memset");
+  if (!rc) {
+    if (d == 3)
+      p3m_splat<3, G><<<nblk(ny), 256, 0, st>>>(dy, dw, ny, dv, g, grids, cells);
+    else
+      p3m_splat<2, G><<<nblk(ny), 256, 0, st>>>(dy, dw, ny, dv, g, grids, cells);
+    c->launches += 1;
+    rc = c->cuda(cudaGetLastError(), "splat");
+  }
+  if (!rc) rc = fft_error(c, P3MFFT<G>::fwd(fwd, grids, spec), "forward");
+  if (!rc) {
+    p3m_multiply<C, G><<<nblk(ccells), 256, 0, st>>>(spec, (const C *)pc->kspec, nimg, mode == 0 ? 1 : d,
+                                                    mode == 0 ? 0 : 1, ccells, (G)(1.0 / (double)cells), prod);
+    c->launches += 1;
+    rc = c->cuda(cudaGetLastError(), "multiply");
+  }
+  if (!rc) rc = fft_error(c, P3MFFT<G>::inv(inv, prod, imgs), "inverse");
+  if (!rc) {
+    if (d == 3)
+      p3m_interp<3, G><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, mode == 2 ? 2 : 0, da, dv, dout);
+    else
+      p3m_interp<2, G><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, mode == 2 ? 2 : 0, da, dv, dout);
+    c->launches += 1;
+    rc = c->cuda(cudaGetLastError(), "interpolate");
+  }
+  if (!rc) rc = io.finish();
+  if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
+  cudaStreamSynchronize(st);  // the scratch is reused by the next call
+  return rc;
+}
+
 // mode 0 Convolve (out nx x dv), 1 ConvolveGradient(X) (out nx x dv x d), 2 alpha-contracted (nx x d)
 int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const double *y, const double *w, long ny,
             double sigma, const double *alpha, const double *domain, double ratio, double padding, double *out) {
@@ -234,13 +394,19 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
   int rc = io.rc;
   if (rc) return rc;
   // the data domain: given, or the bounding box of targets and sources
+  P3MCache *pc = (P3MCache *)c->p3m;
+  if (!pc) {
+    pc = new P3MCache();
+    c->p3m = pc;
+    c->p3m_free = p3m_cache_free;
+  }
   double box[6];
   if (domain) {
     for (int k = 0; k < 2 * d; ++k) box[k] = domain[k];
   } else {
-    double *dbox = nullptr;
-    rc = c->cuda(cudaMalloc(&dbox, 6 * sizeof(double)), "cudaMalloc");
+    rc = p3m_work(c, pc, 6 * sizeof(double));
     if (!rc) {
+      double *dbox = (double *)pc->work;
       if (d == 3)
         p3m_box<3><<<1, 256, 0, st>>>(dx, nx, dy, ny, dbox);
       else
@@ -249,7 +415,6 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
       rc = c->cuda(cudaMemcpyAsync(box, dbox, 2 * d * sizeof(double), cudaMemcpyDeviceToHost, st), "read box");
       if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
     }
-    if (dbox) cudaFree(dbox);
     if (rc) return rc;
   }
   // DetermineGrids
@@ -258,7 +423,9 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
   g.s = ratio * sigma;
   for (int k = 0; k < d; ++k) {
     const double length = box[d + k] - box[k];
-    long n = (long)((length + 2 * padding * sigma) / g.s);
+    const double nd = (length + 2 * padding * sigma) / g.s;
+    if (!(nd < 1073741824.0)) return c->fail(GBK_ERR_ARG, "P3M grid of more than 2^30 points along an axis");
+    long n = (long)nd;
     if (n < 1) n = 1;
     double l2 = std::log((double)n) / std::log(2.0);
     const long t = (long)l2;
@@ -269,102 +436,19 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
   }
   const long cells = g.cells(), ccells = g.ccells();
   const int nimg = mode == 0 ? dv : dv * d;
-  const double bytes = 8.0 * cells * (dv + nimg) + 16.0 * ccells * (dv + nimg + 1 + d);
+  const bool f64 = c->mode == GBK_MODE_F64;
+  const double re = f64 ? 8.0 : 4.0;  // grids, images, spectra, products, kernel spectra, cuFFT work areas
+  const double bytes = re * cells * (dv + nimg) + 2 * re * ccells * (dv + nimg + 1 + d + std::max(nimg, 1 + d));
   if (bytes > 64e9) return c->fail(GBK_ERR_ARG, "P3M grid of %ld points needs %.0f GB", cells, bytes / 1e9);
-  // plans and kernel spectra, cached per grid size, spacing and width
-  P3MCache *pc = (P3MCache *)c->p3m;
-  if (!pc) {
-    pc = new P3MCache();
-    c->p3m = pc;
-    c->p3m_free = p3m_cache_free;
-  }
-  const bool same = pc->valid && pc->d == d && pc->n[0] == g.n[0] && pc->n[1] == g.n[1] &&
-                    (d == 2 || pc->n[2] == g.n[2]) && pc->s == g.s && pc->sigma == sigma;
-  if (!same) {
-    if (pc->plans) {
-      cufftDestroy(pc->fwd);
-      cufftDestroy(pc->inv);
-      pc->plans = false;
-    }
-    if (pc->kspec) cudaFree(pc->kspec);
-    pc->kspec = nullptr;
+  if (!(pc->d == d && pc->n[0] == g.n[0] && pc->n[1] == g.n[1] && pc->n[2] == g.n[2])) {
+    cudaStreamSynchronize(st);
+    pc->drop_plans();
     pc->valid = false;
-    cufftResult fr = d == 3 ? cufftPlan3d(&pc->fwd, (int)g.n[0], (int)g.n[1], (int)g.n[2], CUFFT_D2Z)
-                            : cufftPlan2d(&pc->fwd, (int)g.n[0], (int)g.n[1], CUFFT_D2Z);
-    if ((rc = fft_error(c, fr, "plan"))) return rc;
-    fr = d == 3 ? cufftPlan3d(&pc->inv, (int)g.n[0], (int)g.n[1], (int)g.n[2], CUFFT_Z2D)
-                : cufftPlan2d(&pc->inv, (int)g.n[0], (int)g.n[1], CUFFT_Z2D);
-    if ((rc = fft_error(c, fr, "plan"))) {
-      cufftDestroy(pc->fwd);
-      return rc;
-    }
-    pc->plans = true;
-    double *kimg = nullptr;
-    rc = c->cuda(cudaMalloc(&kimg, (size_t)cells * (1 + d) * sizeof(double)), "cudaMalloc (P3M)");
-    if (!rc) rc = c->cuda(cudaMalloc(&pc->kspec, (size_t)ccells * (1 + d) * sizeof(cufftDoubleComplex)), "cudaMalloc (P3M)");
-    if (!rc) {
-      if (d == 3)
-        p3m_kernel_images<3><<<nblk(cells), 256, 0, st>>>(g, sigma, kimg, cells);
-      else
-        p3m_kernel_images<2><<<nblk(cells), 256, 0, st>>>(g, sigma, kimg, cells);
-      c->launches += 1;
-      rc = c->cuda(cudaGetLastError(), "kernel images");
-    }
-    for (int k = 0; k <= d && !rc; ++k) {
-      rc = fft_error(c, cufftSetStream(pc->fwd, st), "stream");
-      if (!rc) rc = fft_error(c, cufftExecD2Z(pc->fwd, kimg + (long)k * cells, pc->kspec + (long)k * ccells), "D2Z");
-    }
-    if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
-    if (kimg) cudaFree(kimg);
-    if (rc) return rc;
-    pc->valid = true;
     pc->d = d;
     for (int k = 0; k < 3; ++k) pc->n[k] = g.n[k];
-    pc->s = g.s;
-    pc->sigma = sigma;
   }
-  // splat, transform, multiply, transform back, interpolate
-  double *grids = nullptr, *imgs = nullptr;
-  cufftDoubleComplex *spec = nullptr, *prod = nullptr;
-  rc = c->cuda(cudaMalloc(&grids, (size_t)cells * dv * sizeof(double)), "cudaMalloc (P3M)");
-  if (!rc) rc = c->cuda(cudaMalloc(&imgs, (size_t)cells * nimg * sizeof(double)), "cudaMalloc (P3M)");
-  if (!rc) rc = c->cuda(cudaMalloc(&spec, (size_t)ccells * dv * sizeof(cufftDoubleComplex)), "cudaMalloc (P3M)");
-  if (!rc) rc = c->cuda(cudaMalloc(&prod, (size_t)ccells * nimg * sizeof(cufftDoubleComplex)), "cudaMalloc (P3M)");
-  if (!rc) rc = c->cuda(cudaMemsetAsync(grids, 0, (size_t)cells * dv * sizeof(double), st), "memset");
-  if (!rc) {
-    if (d == 3)
-      p3m_splat<3><<<nblk(ny), 256, 0, st>>>(dy, dw, ny, dv, g, grids, cells);
-    else
-      p3m_splat<2><<<nblk(ny), 256, 0, st>>>(dy, dw, ny, dv, g, grids, cells);
-    c->launches += 1;
-    rc = c->cuda(cudaGetLastError(), "splat");
-  }
-  if (!rc) rc = fft_error(c, cufftSetStream(pc->fwd, st), "stream");
-  if (!rc) rc = fft_error(c, cufftSetStream(pc->inv, st), "stream");
-  for (int k = 0; k < dv && !rc; ++k)
-    rc = fft_error(c, cufftExecD2Z(pc->fwd, grids + (long)k * cells, spec + (long)k * ccells), "D2Z");
-  if (!rc) {
-    p3m_multiply<<<nblk(ccells), 256, 0, st>>>(spec, pc->kspec, nimg, mode == 0 ? 1 : d, mode == 0 ? 0 : 1, ccells,
-                                               1.0 / (double)cells, prod);
-    c->launches += 1;
-    rc = c->cuda(cudaGetLastError(), "multiply");
-  }
-  for (int m = 0; m < nimg && !rc; ++m)
-    rc = fft_error(c, cufftExecZ2D(pc->inv, prod + (long)m * ccells, imgs + (long)m * cells), "Z2D");
-  if (!rc) {
-    if (d == 3)
-      p3m_interp<3><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, mode == 2 ? 2 : 0, da, dv, dout);
-    else
-      p3m_interp<2><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, mode == 2 ? 2 : 0, da, dv, dout);
-    c->launches += 1;
-    rc = c->cuda(cudaGetLastError(), "interpolate");
-  }
-  if (!rc) rc = io.finish();
-  if (!rc) rc = c->cuda(cudaStreamSynchronize(st), "sync");
-  cudaStreamSynchronize(st);
-  for (void *p : {(void *)grids, (void *)imgs, (void *)spec, (void *)prod})
-    if (p) cudaFree(p);
-  return rc;
+  return f64 ? p3m_exec<double>(c, pc, g, mode, dv, dx, nx, dy, dw, ny, sigma, da, dout, io)
+             : p3m_exec<float>(c, pc, g, mode, dv, dx, nx, dy, dw, ny, sigma, da, dout, io);
 }
 
 }  // namespace

@@ -58,3 +58,44 @@ def test_p3m_domain_and_cache(gb):
     assert np.linalg.norm(c - p3m.convolve(x, y, w, 0.25)) <= 1e-10 * np.linalg.norm(c)
     with pytest.raises(ValueError):
         KM.p3m_convolve(x, y, w[:5], 0.3, context=ctx)
+
+
+@pytest.mark.parametrize("d,sigma", [(2, 0.1), (3, 0.15)])
+def test_p3m_f32c_grids(gb, K, d, sigma):
+    """GBK_MODE_F32C runs the grids, spectra and transforms in FP32: within 1e-5 (normwise) of the
+    FP64 restatement, far inside the method's own error against the exact sums."""
+    from oracle import p3m
+    from deformetrica_code_gb300 import kernel as KM
+    rng = np.random.default_rng(21 + d)
+    x, y = rng.random((300, d)), rng.random((280, d))
+    w, a = rng.normal(size=(280, 3)), rng.normal(size=(300, 3))
+    ctx = gb.Context(mode=gb.GBK_MODE_F32C)
+    v = KM.p3m_convolve(x, y, w, sigma, context=ctx)
+    gv = KM.p3m_convolve_gradient(x, y, w, sigma, context=ctx)
+    ga = KM.p3m_convolve_gradient_alpha(x, y, w, sigma, a, context=ctx)
+    rv, rg = p3m.convolve(x, y, w, sigma), p3m.convolve_gradient(x, y, w, sigma)
+    assert np.linalg.norm(v - rv) <= 1e-5 * np.linalg.norm(rv)
+    assert np.linalg.norm(gv - rg) <= 1e-5 * np.linalg.norm(rg)
+    rga = np.einsum("ikp,ik->ip", rg, a)
+    assert np.linalg.norm(ga - rga) <= 1e-5 * np.linalg.norm(rga)
+    ve = K.convolve(x, y, w, sigma)
+    assert np.linalg.norm(v - ve) <= 8e-2 * np.linalg.norm(ve)
+
+
+def test_p3m_precision_switch(gb):
+    """Switching the context's precision between calls rebuilds the cached spectra for that
+    precision; switching back reproduces the first result."""
+    from oracle import p3m
+    from deformetrica_code_gb300 import kernel as KM
+    rng = np.random.default_rng(5)
+    x, y, w = rng.random((150, 3)), rng.random((160, 3)), rng.normal(size=(160, 3))
+    ctx = gb.Context(mode=gb.GBK_MODE_F64)
+    a = KM.p3m_convolve(x, y, w, 0.2, context=ctx)
+    ctx.set_mode(gb.GBK_MODE_F32C)
+    b = KM.p3m_convolve(x, y, w, 0.2, context=ctx)
+    ctx.set_mode(gb.GBK_MODE_F64)
+    c = KM.p3m_convolve(x, y, w, 0.2, context=ctx)
+    r = p3m.convolve(x, y, w, 0.2)
+    assert np.linalg.norm(a - r) <= 1e-10 * np.linalg.norm(r)
+    assert 0 < np.linalg.norm(b - r) <= 1e-5 * np.linalg.norm(r)
+    assert np.abs(c - a).max() <= 1e-13 * np.abs(a).max()

@@ -616,6 +616,64 @@ def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float 
     return res
 
 
+def image_bench(reps: int = 5, cpu: bool = True, n: int = 128, sigma: float = 4.0, T: int = 11):
+    """The image-grid path: a 128^3 image (unit spacing, origin 0), 1,000 control points on the
+    cell-centred 10^3 grid of spacing 12.8, momenta N(0, 1) x 0.5, sigma 4 pixels (windows of 24^3
+    pixels). ConvolveImageFast on the image points displaced by 0.2 N(0,1) (device arrays), the full
+    Convolve over the same pixels beside it, and the backward image-map flow with T = 11, Heun, with
+    windowed sums (FP64) and with full sums (FP32C). The FP64 numpy restatement of
+    ConvolveImageFast runs on the same case (1 core)."""
+    import torch
+    import deformetrica_code_gb300 as g
+    rng = np.random.default_rng(12)
+    im = g.ImageGrid([0.0] * 3, [1.0] * 3, [n] * 3)
+    c = (np.arange(10) + 0.5) * (n / 10)
+    cp = np.stack(np.meshgrid(c, c, c, indexing="ij"), -1).reshape(-1, 3)
+    mom = 0.5 * rng.standard_normal(cp.shape)
+    ctx = g.Context()
+    pts = im.points(context=ctx)
+    x = pts + 0.2 * rng.standard_normal(pts.shape)
+    X, Y, W = (torch.from_numpy(v).cuda() for v in (x, cp, mom))
+    k = g.GB300ExactKernel(3, sigma, context=ctx)
+    k.SetSources(Y)
+    k.SetWeights(W)
+    L = int(6 * sigma)
+    from oracle import image as IM
+    _, _, lo, hi, _ = IM.windows(cp, sigma, im.origin, im.spacing, im.size)
+    win_pairs = float(np.prod(hi - lo, axis=1).sum())
+    res = {"workload": f"{n}^3 image, {len(cp)} control points, sigma {sigma} pixels (windows of {L}^3), "
+                       f"T = {T} Heun for the flow",
+           "window_pairs_per_call": win_pairs, "full_pairs_per_call": float(im.pixels) * len(cp)}
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    dt = timed(lambda: k.ConvolveImageFast(X, im))
+    res["convolve_image_fast"] = {"s_per_call": dt, "window_pairs_per_s": win_pairs / dt, "precision": "FP64"}
+    dt = timed(lambda: k.Convolve(X))
+    res["convolve_full"] = {"s_per_call": dt, "pairs_per_s": res["full_pairs_per_call"] / dt, "precision": "FP32C"}
+    pos = np.repeat(cp[None], T, axis=0) + 0.5 * rng.standard_normal((T, len(cp), 3))
+    momt = np.repeat(mom[None], T, axis=0)
+    P, M = torch.from_numpy(pos).cuda(), torch.from_numpy(momt).cuda()
+    for name, fast in (("flow_windowed", True), ("flow_full_sums", False)):
+        dt = timed(lambda: g.flow_image_maps(P, M, sigma, im, heun=True, fast=fast, context=ctx))
+        res[name] = {"s_per_flow": dt, "kernel_sums": 2 * (T - 1)}
+    if cpu:
+        t0 = time.perf_counter()
+        IM.convolve_image_fast(x, cp, mom, sigma, im.origin, im.spacing, im.size)
+        dt = time.perf_counter() - t0
+        res["convolve_image_fast"]["cpu_oracle"] = {"s_per_call": dt, "window_pairs_per_s": win_pairs / dt,
+                                                    "kind": "port (FP64 numpy)", "cores": 1}
+    return res
+
+
 def fp64_gpu_pairs(n: int, sigma: float):
     """The same fused forward+adjoint step in the FP64 mode (plain FP64 kernel sums) at N = M = n."""
     import torch
@@ -778,6 +836,7 @@ def main():
     ap.add_argument("--no-small", action="store_true", help="skip the 4096-point kernel-sum case")
     ap.add_argument("--no-optimizer", action="store_true", help="skip the registration optimiser runs")
     ap.add_argument("--no-p3m", action="store_true", help="skip the particle-mesh kernel case")
+    ap.add_argument("--no-image", action="store_true", help="skip the image-grid case")
     ap.add_argument("--data-term-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
@@ -943,6 +1002,8 @@ def main():
             line["small_kernel_sum"] = small_kernel_bench(cpu=not args.no_cpu_baseline)
         if not args.no_p3m:
             line["p3m"] = p3m_bench(cpu=not args.no_cpu_baseline)
+        if not args.no_image:
+            line["image_grid"] = image_bench(cpu=not args.no_cpu_baseline)
         if not args.no_optimizer:
             line["optimizer"] = optimizer_bench(cpu=not args.no_cpu_baseline)
             if not args.no_atlas:

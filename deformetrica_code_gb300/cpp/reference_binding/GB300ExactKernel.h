@@ -159,6 +159,33 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
   }
 
  private:
+  // ExactKernel::ConvolveImageFast (ExactKernel.cxx:76-129) on the device: the image's origin,
+  // spacing and size go to the C ABI; images with a non-identity direction are refused (the
+  // library's pixel geometry is origin + spacing x index).
+  virtual MatrixType ConvolveImageFast(const MatrixType &X, const typename Superclass::ImageTypePointer image) {
+    Buffers b(this, X);
+    if (b.dv != PointDim) throw std::runtime_error("ConvolveImageFast needs weights with PointDim columns");
+    const auto origin = image->GetOrigin();
+    const auto spacing = image->GetSpacing();
+    const auto direction = image->GetDirection();
+    const auto size = image->GetLargestPossibleRegion().GetSize();
+    double o[PointDim], s[PointDim];
+    long n[PointDim];
+    for (unsigned i = 0; i < PointDim; ++i) {
+      o[i] = origin[i];
+      s[i] = spacing[i];
+      n[i] = (long)size[i];
+      for (unsigned j = 0; j < PointDim; ++j)
+        if (direction[i][j] != (i == j ? 1.0 : 0.0))
+          throw std::runtime_error("GB300ExactKernel::ConvolveImageFast: non-identity image direction");
+    }
+    std::vector<double> out((size_t)X.rows() * PointDim);
+    gb300_binding::check(gbk_convolve_image_fast(gb300_binding::thread_context(), PointDim, b.x.memptr(), X.rows(),
+                                                 b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(), o, s, n,
+                                                 out.data()));
+    return from_rows(out, X.rows(), PointDim);
+  }
+
   struct Buffers {
     VectorType x, y, w;
     unsigned ny, dv;

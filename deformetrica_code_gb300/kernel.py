@@ -148,6 +148,11 @@ class Context:
         self.check(self.lib.gbk_tune_load(self.h, path.encode()))
 
 
+def _hptr(a: np.ndarray):
+    """A host array's address for the C ABI's small host-side arguments."""
+    return ctypes.c_void_p(a.ctypes.data)
+
+
 def _empty_like(ref, shape):
     if _is_torch(ref):
         return torch.empty(shape, dtype=torch.float64, device=ref.device)
@@ -314,6 +319,24 @@ class GB300ExactKernel:
         self.ctx.bind_stream(Y, W, xi)
         self._call(self.ctx.lib.gbk_convolve_special_hessian, self.d, _ptr(Y), _ptr(W), Y.shape[0],
                    self.m_KernelWidth, _ptr(xi), _ptr(out))
+        return out
+
+    def ConvolveImageFast(self, X, image):
+        """ExactKernel::ConvolveImageFast (ExactKernel.cxx:76-129): the sum over each control point's
+        window of int(6 sigma) pixels per axis around it. `image` is an ImageGrid (origin, spacing,
+        size) and X holds one (deformed) point per pixel, first index fastest; weights need
+        PointDim columns. Raises GBKError when a window misses the image."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        if W.shape[1] != self.d:
+            raise RuntimeError("ConvolveImageFast needs weights with PointDim columns")
+        origin, spacing, size = image.arrays(self.d)
+        if X.shape[0] != int(np.prod(size)):
+            raise ValueError(f"X has {X.shape[0]} rows for an image of {int(np.prod(size))} pixels")
+        out = _empty_like(X, (X.shape[0], self.d))
+        self.ctx.bind_stream(X, Y, W)
+        self._call(self.ctx.lib.gbk_convolve_image_fast, self.d, _ptr(X), X.shape[0], _ptr(Y), _ptr(W), Y.shape[0],
+                   self.m_KernelWidth, _hptr(origin), _hptr(spacing), _hptr(size), _ptr(out))
         return out
 
     def ForwardAdjoint(self, X, alpha):

@@ -378,6 +378,34 @@ int gbk_p3m_convolve_gradient_alpha(gbk_ctx *ctx, int d, int dv, const double *x
                                     const double *w, long ny, double sigma, const double *alpha, const double *domain,
                                     double spacing_ratio, double padding_factor, double *out);
 
+/* ---- the image grid (ExactKernel::ConvolveImageFast and the Diffeos image maps) ------------ *
+ * An image is its geometry on the host: origin[d], spacing[d] and size[d] (pixels per axis,
+ * identity direction); its points are listed first index fastest (GridFunctions::ImageToPoints,
+ * GridFunctions.cxx:41-60). FP64 in every precision mode for the windowed sums. */
+
+/* The physical points of the pixels: points (prod(size) x d) = origin + spacing * index. */
+int gbk_image_points(gbk_ctx *ctx, int d, const double *origin, const double *spacing, const long *size,
+                     double *points);
+/* ExactKernel::ConvolveImageFast (src/support/kernels/ExactKernel.cxx:76-129): out (nx x d) =
+ * sum over control points y_j (ny x d, momenta w ny x d) of w_j K(x_p, y_j) over the pixels p of the
+ * window of int(6 sigma) pixels per axis starting at the index of y_j - 3 sigma (rounded half up),
+ * cropped to the image. x holds one (deformed) point per pixel: nx = prod(size). A window that
+ * misses the image returns GBK_ERR_ARG (the reference's ITK region iterator throws), as does
+ * 6 sigma < 1. */
+int gbk_convolve_image_fast(gbk_ctx *ctx, int d, const double *x, long nx, const double *y, const double *w, long ny,
+                            double sigma, const double *origin, const double *spacing, const long *size,
+                            double *out);
+/* The backward integration of the image maps (Diffeos.cxx:725-770, non-regression branch): all T
+ * maps (T x prod(size) x d) start as the image points; unless |mom_traj[0]| < 1e-20, from
+ * t = T-1 down, maps[t-1] = maps[t] - dt V(maps[t]; pos[t], mom[t]) (Heun: the average of both
+ * ends), dt = span / (T-1), V the windowed sum (fast = 1) or the full kernel sum in the context's
+ * precision (fast = 0). bbox (host, d x 2: lo, hi per axis, or NULL) stops the integration after
+ * the first step whose map leaves it (Diffeos::CheckBoundingBox); *stopped_at = that time index,
+ * or -1. */
+int gbk_flow_image_maps(gbk_ctx *ctx, int d, long ncp, const double *pos_traj, const double *mom_traj, int T,
+                        double sigma, double span, int heun, int fast, const double *origin, const double *spacing,
+                        const long *size, const double *bbox, double *maps_traj, int *stopped_at);
+
 /* ---- geodesic regression (the reference's Regression model), CUDA-graph replay ------------ */
 
 typedef struct gbk_geodesic_regression gbk_geodesic_regression;

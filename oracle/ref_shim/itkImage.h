@@ -33,6 +33,17 @@ template <class T, unsigned D> class Image {
   typedef T PixelType;
   static constexpr unsigned ImageDimension = D;
   ImageRegion<D> GetLargestPossibleRegion() const { throw std::runtime_error("ITK stand-in: not available in the oracle"); }
+  struct Vec {
+    double v[D];
+    double operator[](unsigned i) const { return v[i]; }
+  };
+  struct Mat {
+    double v[D][D];
+    const double *operator[](unsigned i) const { return v[i]; }
+  };
+  Vec GetOrigin() const { throw std::runtime_error("ITK stand-in: not available in the oracle"); }
+  Vec GetSpacing() const { throw std::runtime_error("ITK stand-in: not available in the oracle"); }
+  Mat GetDirection() const { throw std::runtime_error("ITK stand-in: not available in the oracle"); }
   template <class P, class I> bool TransformPhysicalPointToIndex(const P &, I &) const {
     throw std::runtime_error("ITK stand-in: not available in the oracle");
   }

@@ -619,10 +619,10 @@ def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float 
 def image_bench(reps: int = 5, cpu: bool = True, n: int = 128, sigma: float = 4.0, T: int = 11):
     """The image-grid path: a 128^3 image (unit spacing, origin 0), 1,000 control points on the
     cell-centred 10^3 grid of spacing 12.8, momenta N(0, 1) x 0.5, sigma 4 pixels (windows of 24^3
-    pixels). ConvolveImageFast on the image points displaced by 0.2 N(0,1) (device arrays), the full
-    Convolve over the same pixels beside it, and the backward image-map flow with T = 11, Heun, with
-    windowed sums (FP64) and with full sums (FP32C). The FP64 numpy restatement of
-    ConvolveImageFast runs on the same case (1 core)."""
+    pixels). ConvolveImageFast (FP32C and FP64) on the image points displaced by 0.2 N(0,1) (device
+    arrays), the full FP32C Convolve over the same pixels beside it, and the backward image-map flow
+    with T = 11, Heun, with windowed sums (FP32C and FP64) and with full sums (FP32C). The FP64 numpy
+    restatement of ConvolveImageFast runs on the same case (1 core)."""
     import torch
     import deformetrica_code_gb300 as g
     rng = np.random.default_rng(12)
@@ -655,15 +655,24 @@ def image_bench(reps: int = 5, cpu: bool = True, n: int = 128, sigma: float = 4.
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) / reps
 
-    dt = timed(lambda: k.ConvolveImageFast(X, im))
-    res["convolve_image_fast"] = {"s_per_call": dt, "window_pairs_per_s": win_pairs / dt, "precision": "FP64"}
+    ctx64 = g.Context(mode=g.GBK_MODE_F64)
+    k64 = g.GB300ExactKernel(3, sigma, context=ctx64)
+    k64.SetSources(Y)
+    k64.SetWeights(W)
+    res["convolve_image_fast"] = {}
+    for prec, kk in (("f32c", k), ("f64", k64)):
+        dt = timed(lambda: kk.ConvolveImageFast(X, im))
+        res["convolve_image_fast"][prec] = {"s_per_call": dt, "window_pairs_per_s": win_pairs / dt}
+    v32, v64 = k.ConvolveImageFast(X, im).cpu().numpy(), k64.ConvolveImageFast(X, im).cpu().numpy()
+    res["convolve_image_fast"]["f32c_rel_err_vs_f64"] = float(np.linalg.norm(v32 - v64) / np.linalg.norm(v64))
     dt = timed(lambda: k.Convolve(X))
     res["convolve_full"] = {"s_per_call": dt, "pairs_per_s": res["full_pairs_per_call"] / dt, "precision": "FP32C"}
     pos = np.repeat(cp[None], T, axis=0) + 0.5 * rng.standard_normal((T, len(cp), 3))
     momt = np.repeat(mom[None], T, axis=0)
     P, M = torch.from_numpy(pos).cuda(), torch.from_numpy(momt).cuda()
-    for name, fast in (("flow_windowed", True), ("flow_full_sums", False)):
-        dt = timed(lambda: g.flow_image_maps(P, M, sigma, im, heun=True, fast=fast, context=ctx))
+    for name, fast, c in (("flow_windowed_f32c", True, ctx), ("flow_windowed_f64", True, ctx64),
+                          ("flow_full_sums_f32c", False, ctx)):
+        dt = timed(lambda: g.flow_image_maps(P, M, sigma, im, heun=True, fast=fast, context=c))
         res[name] = {"s_per_flow": dt, "kernel_sums": 2 * (T - 1)}
     if cpu:
         t0 = time.perf_counter()

@@ -8,7 +8,8 @@
 // loops over control points and scatters; here each CTA owns a tile of pixels, keeps the control
 // points whose window meets the tile (in control-point order, compacted through shared memory) and
 // each thread gathers its pixel's sum in that order, so every pixel sees the reference's order of
-// additions. FP64 throughout, without contracted multiply-adds, as the reference's scalar loop.
+// additions. GBK_MODE_F64 evaluates in FP64 without contracted multiply-adds, as the reference's
+// scalar loop; GBK_MODE_F32C evaluates the exponentials in FP32 with compensated per-pixel sums.
 //
 // gbk_flow_image_maps restates the backward integration of the image maps
 // (src/core/model_tools/deformations/Diffeos.cxx:725-770, non-regression branch) with either the
@@ -71,12 +72,22 @@ __global__ void image_windows_kernel(const double *y, long n, long per, double s
   if (!ok) atomicMin(bad + r / per, (int)(r % per));
 }
 
-template <int D>
+__device__ __forceinline__ float image_ex2(float v) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+
+// F32 = false: FP64 as the reference (exp, no contracted multiply-adds). F32 = true (GBK_MODE_F32C):
+// offsets from the tile's centre formed in FP64 and scaled by sqrt(log2 e) / sigma, then FP32 distances,
+// K = 2^-r2 on the MUFU unit and per-pixel compensated FP32 sums (TwoSum), added up in FP64 at the end.
+template <int D, bool F32>
 __global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, const double *y, const double *w,
-                                                              const int *start, long ny, double s2, ImageGeom g,
-                                                              double *out) {
+                                                              const int *start, long ny, double s2, double pre,
+                                                              ImageGeom g, double *out) {
   typedef Tile<D> T;
-  __shared__ double s_y[kThreads][D], s_w[kThreads][D];
+  __shared__ double s_y[F32 ? 1 : kThreads][D], s_w[F32 ? 1 : kThreads][D];
+  __shared__ float s_yf[F32 ? kThreads : 1][D], s_wf[F32 ? kThreads : 1][D];
   __shared__ int s_start[kThreads][D];
   __shared__ int s_warp[kThreads / 32 + 1];
   const int tid = threadIdx.x;
@@ -88,10 +99,15 @@ __global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, c
   const long q[3] = {lo[0] + tid % T::X, lo[1] + (tid / T::X) % T::Y, lo[2] + tid / (T::X * T::Y)};
   const bool valid = q[0] < hi[0] && q[1] < hi[1] && (D == 2 || q[2] < hi[2]);
   const long row = q[0] + g.n[0] * (q[1] + (D == 3 ? g.n[1] * q[2] : 0));
-  double xp[D], acc[D];
+  double xp[D], acc[D], ctr[D];
+  float xf[D], fs[D], fc[D];
   for (int k = 0; k < D; ++k) {
     xp[k] = valid ? x[row * D + k] : 0.0;
     acc[k] = 0.0;
+    ctr[k] = g.origin[k] + g.spacing[k] * 0.5 * (double)(lo[k] + hi[k] - 1);
+    xf[k] = (float)((xp[k] - ctr[k]) * pre);
+    fs[k] = 0.f;
+    fc[k] = 0.f;
   }
   const int lane = tid & 31, warp = tid >> 5;
   for (long c0 = 0; c0 < ny; c0 += kThreads) {
@@ -115,8 +131,13 @@ __global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, c
     if (keep) {
       const int pos = base + __popc(ball & ((1u << lane) - 1u));
       for (int k = 0; k < D; ++k) {
-        s_y[pos][k] = y[j * D + k];
-        s_w[pos][k] = w[j * D + k];
+        if (F32) {
+          s_yf[pos][k] = (float)((y[j * D + k] - ctr[k]) * pre);
+          s_wf[pos][k] = (float)w[j * D + k];
+        } else {
+          s_y[pos][k] = y[j * D + k];
+          s_w[pos][k] = w[j * D + k];
+        }
         s_start[pos][k] = st[k];
       }
     }
@@ -126,18 +147,33 @@ __global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, c
         bool in = true;
         for (int k = 0; k < D; ++k) in = in && q[k] >= s_start[m][k] && q[k] < (long)s_start[m][k] + g.L;
         if (!in) continue;
-        double sq = 0.0;
-        for (int k = 0; k < D; ++k) {
-          const double diff = __dsub_rn(xp[k], s_y[m][k]);
-          sq = __dadd_rn(sq, __dmul_rn(diff, diff));
+        if (F32) {
+          float r2 = 0.f;
+          for (int k = 0; k < D; ++k) {
+            const float df = xf[k] - s_yf[m][k];
+            r2 = fmaf(df, df, r2);
+          }
+          const float K = image_ex2(-r2);
+          for (int k = 0; k < D; ++k) {  // TwoSum into (fs, fc)
+            const float v = s_wf[m][k] * K;
+            const float t = fs[k] + v, bp = t - fs[k];
+            fc[k] += (fs[k] - (t - bp)) + (v - bp);
+            fs[k] = t;
+          }
+        } else {
+          double sq = 0.0;
+          for (int k = 0; k < D; ++k) {
+            const double diff = __dsub_rn(xp[k], s_y[m][k]);
+            sq = __dadd_rn(sq, __dmul_rn(diff, diff));
+          }
+          const double K = exp(-sq / s2);
+          for (int k = 0; k < D; ++k) acc[k] = __dadd_rn(acc[k], __dmul_rn(s_w[m][k], K));
         }
-        const double K = exp(-sq / s2);
-        for (int k = 0; k < D; ++k) acc[k] = __dadd_rn(acc[k], __dmul_rn(s_w[m][k], K));
       }
     __syncthreads();
   }
   if (valid)
-    for (int k = 0; k < D; ++k) out[row * D + k] = acc[k];
+    for (int k = 0; k < D; ++k) out[row * D + k] = F32 ? (double)fs[k] + (double)fc[k] : acc[k];
 }
 
 template <int D>
@@ -221,11 +257,20 @@ int launch_fast(gbk_ctx *c, const ImageGeom &g, const double *x, const double *y
   const long tiles = g.d == 3 ? ((g.n[0] + 7) / 8) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4)
                               : ((g.n[0] + 15) / 16) * ((g.n[1] + 15) / 16);
   if (tiles > 2147483647L) return c->fail(GBK_ERR_ARG, "image too large");
-  const double s2 = sigma * sigma;
-  if (g.d == 3)
-    image_fast_kernel<3><<<(unsigned)tiles, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, g, out);
-  else
-    image_fast_kernel<2><<<(unsigned)tiles, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, g, out);
+  const double s2 = sigma * sigma, pre = std::sqrt(1.4426950408889634) / sigma;  // sqrt(log2 e) / sigma
+  const bool f32 = c->mode != GBK_MODE_F64;
+  const unsigned nb = (unsigned)tiles;
+  if (g.d == 3) {
+    if (f32)
+      image_fast_kernel<3, true><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
+    else
+      image_fast_kernel<3, false><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
+  } else {
+    if (f32)
+      image_fast_kernel<2, true><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
+    else
+      image_fast_kernel<2, false><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
+  }
   c->launches += 1;
   return c->cuda(cudaGetLastError(), "image convolution");
 }

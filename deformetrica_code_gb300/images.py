@@ -57,7 +57,7 @@ def flow_image_maps(pos_traj, mom_traj, sigma: float, image: ImageGrid, heun: bo
     """The reference's backward integration of the image maps (Diffeos.cxx:725-770) on the device:
     returns (maps T x pixels x d, stopped_at) with stopped_at the time index at which the bounding
     box (d x 2: lo, hi per axis) stopped it, or None. fast = True uses ConvolveImageFast's windowed
-    sums (FP64), False the full kernel sums in the context's precision."""
+    sums, False the full kernel sums; both in the context's precision."""
     ctx = context or Context()
     d = image.d
     if pos_traj.ndim != 3 or pos_traj.shape[2] != d or mom_traj.shape != pos_traj.shape:

@@ -381,7 +381,9 @@ int gbk_p3m_convolve_gradient_alpha(gbk_ctx *ctx, int d, int dv, const double *x
 /* ---- the image grid (ExactKernel::ConvolveImageFast and the Diffeos image maps) ------------ *
  * An image is its geometry on the host: origin[d], spacing[d] and size[d] (pixels per axis,
  * identity direction); its points are listed first index fastest (GridFunctions::ImageToPoints,
- * GridFunctions.cxx:41-60). FP64 in every precision mode for the windowed sums. */
+ * GridFunctions.cxx:41-60). The windowed sums follow the context's precision: GBK_MODE_F64 is the
+ * reference's FP64 arithmetic in its order of additions per pixel, GBK_MODE_F32C FP32 exponentials
+ * with compensated per-pixel sums (~1e-7 relative). */
 
 /* The physical points of the pixels: points (prod(size) x d) = origin + spacing * index. */
 int gbk_image_points(gbk_ctx *ctx, int d, const double *origin, const double *spacing, const long *size,
@@ -398,8 +400,8 @@ int gbk_convolve_image_fast(gbk_ctx *ctx, int d, const double *x, long nx, const
 /* The backward integration of the image maps (Diffeos.cxx:725-770, non-regression branch): all T
  * maps (T x prod(size) x d) start as the image points; unless |mom_traj[0]| < 1e-20, from
  * t = T-1 down, maps[t-1] = maps[t] - dt V(maps[t]; pos[t], mom[t]) (Heun: the average of both
- * ends), dt = span / (T-1), V the windowed sum (fast = 1) or the full kernel sum in the context's
- * precision (fast = 0). bbox (host, d x 2: lo, hi per axis, or NULL) stops the integration after
+ * ends), dt = span / (T-1), V the windowed sum (fast = 1) or the full kernel sum (fast = 0), in the
+ * context's precision. bbox (host, d x 2: lo, hi per axis, or NULL) stops the integration after
  * the first step whose map leaves it (Diffeos::CheckBoundingBox); *stopped_at = that time index,
  * or -1. */
 int gbk_flow_image_maps(gbk_ctx *ctx, int d, long ncp, const double *pos_traj, const double *mom_traj, int T,

@@ -1,7 +1,8 @@
 """GPU image-grid path (gbk_image_points, gbk_convolve_image_fast, gbk_flow_image_maps) against the
 oracle's restatement of ExactKernel::ConvolveImageFast and Diffeos' image-map integration
-(oracle/image.py). The windowed sums are FP64 in every mode and follow the reference's order of
-additions per pixel; they differ from the oracle only through exp (1e-13 normwise)."""
+(oracle/image.py). In GBK_MODE_F64 the windowed sums follow the reference's arithmetic and order of
+additions per pixel and differ from the oracle only through exp (1e-13 normwise); GBK_MODE_F32C
+evaluates them in FP32 with compensated sums (1e-6)."""
 import numpy as np
 import pytest
 
@@ -40,8 +41,11 @@ def test_image_points(gb, d):
     np.testing.assert_array_equal(im.points(), IM.image_points(origin, spacing, size))
 
 
-@pytest.mark.parametrize("d,sigma", [(2, 1.7), (3, 1.2), (3, 2.5)])
-def test_convolve_image_fast(gb, d, sigma):
+@pytest.mark.parametrize("d,sigma,mode,tol", [(2, 1.7, "F64", 1e-13), (3, 1.2, "F64", 1e-13), (3, 2.5, "F64", 1e-13),
+                                               (2, 1.7, "F32C", 1e-6), (3, 2.5, "F32C", 1e-6)])
+def test_convolve_image_fast(gb, d, sigma, mode, tol):
+    """FP64: the reference's arithmetic (differences from the oracle through exp only); FP32C:
+    FP32 exponentials with compensated sums."""
     import torch
     from oracle import image as IM
     size, origin, spacing, pos, mom = _case(d)
@@ -49,11 +53,11 @@ def test_convolve_image_fast(gb, d, sigma):
     rng = np.random.default_rng(3)
     x = IM.image_points(origin, spacing, size) + 0.2 * rng.normal(size=(im.pixels, d))
     ref = IM.convolve_image_fast(x, pos[0], mom[0], sigma, origin, spacing, size)
-    k = gb.GB300ExactKernel(d, sigma, mode=gb.GBK_MODE_F32C)  # windowed sums are FP64 in every mode
+    k = gb.GB300ExactKernel(d, sigma, mode=getattr(gb, f"GBK_MODE_{mode}"))
     k.SetSources(pos[0])
     k.SetWeights(mom[0])
     got = k.ConvolveImageFast(x, im)
-    assert _nrm(got, ref) <= 1e-13
+    assert _nrm(got, ref) <= tol
     kd = gb.GB300ExactKernel(d, sigma, context=k.ctx)
     kd.SetSources(torch.from_numpy(pos[0]).cuda())
     kd.SetWeights(torch.from_numpy(mom[0]).cuda())
@@ -93,6 +97,17 @@ def test_flow_image_maps_fast(gb, d, heun):
     for t in range(pos.shape[0]):
         assert _nrm(maps[t], ref[t]) <= 1e-13
     np.testing.assert_array_equal(maps[-1], ref[-1])
+
+
+def test_flow_image_maps_fast_f32c(gb):
+    from oracle import image as IM
+    size, origin, spacing, pos, mom = _case(3, seed=5)
+    im = gb.ImageGrid(origin, spacing, size)
+    ctx = gb.Context(mode=gb.GBK_MODE_F32C)
+    maps, _ = gb.flow_image_maps(pos, 0.3 * mom, 1.6, im, fast=True, context=ctx)
+    ref, _ = IM.flow_image_maps(pos, 0.3 * mom, 1.6, origin, spacing, size, fast=True)
+    pts = ref[-1]
+    assert np.linalg.norm((maps[0] - pts) - (ref[0] - pts)) <= 1e-6 * np.linalg.norm(ref[0] - pts)
 
 
 @pytest.mark.parametrize("mode,tol", [("F64", 1e-12), ("F32C", 1e-6)])

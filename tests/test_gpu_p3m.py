@@ -99,3 +99,23 @@ def test_p3m_precision_switch(gb):
     assert np.linalg.norm(a - r) <= 1e-10 * np.linalg.norm(r)
     assert 0 < np.linalg.norm(b - r) <= 1e-5 * np.linalg.norm(r)
     assert np.abs(c - a).max() <= 1e-13 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_p3m_points_outside_the_domain(gb, d):
+    """A data domain smaller than the points: corners that fall off the grid are dropped by the
+    splat and the interpolation alike (P3MKernel.cxx:473-593), on the GPU as in the restatement."""
+    from oracle import p3m
+    from deformetrica_code_gb300 import kernel as KM
+    rng = np.random.default_rng(30 + d)
+    x, y = rng.uniform(-0.5, 1.5, size=(150, d)), rng.uniform(-0.5, 1.5, size=(170, d))
+    w, a = rng.normal(size=(170, 2)), rng.normal(size=(150, 2))
+    lo, hi = np.full(d, 0.2), np.full(d, 0.8)
+    ctx = gb.Context(mode=gb.GBK_MODE_F64)
+    v = KM.p3m_convolve(x, y, w, 0.05, domain=(lo, hi), context=ctx)
+    ga = KM.p3m_convolve_gradient_alpha(x, y, w, 0.05, a, domain=(lo, hi), context=ctx)
+    rv = p3m.convolve(x, y, w, 0.05, lo, hi)
+    rga = p3m.convolve_gradient_alpha(x, y, w, 0.05, a, lo, hi)
+    assert np.linalg.norm(v - rv) <= 1e-10 * np.linalg.norm(rv)
+    assert np.linalg.norm(ga - rga) <= 1e-10 * np.linalg.norm(rga)
+    assert np.count_nonzero(np.all(v == 0, axis=1)) > 0  # targets off the grid get nothing

@@ -221,7 +221,13 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     // sorted copies of the source rows the op reads (y, the weight columns, the special Hessian's
     // xi); OpAdjointCP's source extras share arrays with its targets, so it gathers while staging
     SourceCopies want;
-    if (op != OP_ADJCP) {
+    if (op == OP_ADJCP) {  // p, xi_pos, xi_mom of the sources, read through the permutation
+      const double *ex[3] = {a.w, a.tb, a.sb};
+      for (int k = 0; k < 3; ++k) {
+        want.chk[k] = ex[k];
+        want.chk_ld[k] = want.chk_cols[k] = d;
+      }
+    } else {
       want.na = op == OP_SPECIAL ? 3 : 2;
       want.src[0] = a.y;
       want.ld[0] = want.cols[0] = d;
@@ -244,6 +250,18 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     a.nxtiles = tv.ntiles;
     a.xtile_bound = tv.grid;
     a.ybox = prune ? sv.boxes : nullptr;
+    if (prune) {
+      // the reference's sums are NaN or infinite wherever a target coordinate or extra is, however
+      // small its kernel values: such a launch visits every chunk (source chunks holding a
+      // non-finite value are never pruned either, see order_sources)
+      const bool adj = op == OP_ADJCP;
+      if (int rc = cuda(unbound_boxes_if_nonfinite(stream, d, a.x, a.nx, a.ta, a.ta_ld, a.tb, a.tb_ld,
+                                                   adj ? a.sb : nullptr, adj ? a.sb_ld : 0, nonfinite,
+                                                   const_cast<double *>(sv.boxes), (a.ny + e.tj - 1) / e.tj),
+                        "non-finite check"))
+        return rc;
+      launches += 2;
+    }
     launches += tv.launches + sv.launches;
     if (op == OP_ADJCP) {
       a.yperm = sv.perm;
@@ -380,8 +398,8 @@ int gbk_create(int device, gbk_ctx **out) {
   }
   c->stream = c->own_stream;
   // pair counter and the spatial order's self-resetting ticket
-  if (cudaMalloc(&c->pair_counter, 2 * sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMemset(c->pair_counter, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+  if (cudaMalloc(&c->pair_counter, 3 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(c->pair_counter, 0, 3 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     c->release();
     cudaStreamDestroy(c->own_stream);
@@ -390,6 +408,7 @@ int gbk_create(int device, gbk_ctx **out) {
     return GBK_ERR_ALLOC;
   }
   c->order_ticket = reinterpret_cast<unsigned *>(c->pair_counter + 1);
+  c->nonfinite = reinterpret_cast<unsigned *>(c->pair_counter + 2);
   *out = c;
   return GBK_OK;
 }

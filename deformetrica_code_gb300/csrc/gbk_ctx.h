@@ -56,6 +56,7 @@ struct gbk_ctx {
   DevBuf order_src;           // source rows in sorted order
   unsigned long long *pair_counter = nullptr;  // device: pairs evaluated by launch(), then a ticket
   unsigned *order_ticket = nullptr;            // device: in the pair counter's allocation
+  unsigned *nonfinite = nullptr;               // device: a pruned launch's targets hold a NaN or inf
 
   typedef std::tuple<int, int, int, int, int, int> TuneKey;  // op, mode, d, dv, log2 nx, log2 ny
   std::map<TuneKey, std::pair<int, int>> tune;                // -> (variant, nsplit)
@@ -114,6 +115,7 @@ struct gbk_ctx {
     if (pair_counter) cudaFree(pair_counter);
     pair_counter = nullptr;
     order_ticket = nullptr;
+    nonfinite = nullptr;
     for (auto &b : stage) fr(b);
   }
 };

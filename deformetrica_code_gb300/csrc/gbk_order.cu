@@ -275,6 +275,7 @@ __global__ void source_pack_kernel(const double *y, const int *perm, long n, int
     hi[l] = -1e300;
   }
   const long end = (c + 1) * chunk < n ? (c + 1) * chunk : n;
+  bool bad = false;  // a non-finite coordinate or source value in the chunk
   for (long q = c * chunk + threadIdx.x; q < end; q += blockDim.x) {
     const long r = perm[q];
 #pragma unroll
@@ -282,11 +283,20 @@ __global__ void source_pack_kernel(const double *y, const int *perm, long n, int
       const double v = y[r * D + l];
       lo[l] = fmin(lo[l], v);
       hi[l] = fmax(hi[l], v);
+      bad = bad || !isfinite(v);
       if (sc.dst[0]) sc.dst[0][q * D + l] = v;
     }
     for (int k = 1; k < sc.na; ++k)
-      for (int j = 0; j < sc.cols[k]; ++j) sc.dst[k][q * sc.cols[k] + j] = sc.src[k][r * sc.ld[k] + j];
+      for (int j = 0; j < sc.cols[k]; ++j) {
+        const double v = sc.src[k][r * sc.ld[k] + j];
+        bad = bad || !isfinite(v);
+        sc.dst[k][q * sc.cols[k] + j] = v;
+      }
+    for (int k = 0; k < 3; ++k)
+      if (sc.chk[k])
+        for (int j = 0; j < sc.chk_cols[k]; ++j) bad = bad || !isfinite(sc.chk[k][r * sc.chk_ld[k] + j]);
   }
+  const bool chunk_bad = __syncthreads_or(bad) != 0;
 #pragma unroll
   for (int l = 0; l < D; ++l)
 #pragma unroll
@@ -310,9 +320,9 @@ __global__ void source_pack_kernel(const double *y, const int *perm, long n, int
         hi[l] = fmax(hi[l], s[D + l][w]);
       }
 #pragma unroll
-    for (int l = 0; l < D; ++l) {
-      boxes[c * 2 * D + l] = lo[l];
-      boxes[c * 2 * D + D + l] = hi[l];
+    for (int l = 0; l < D; ++l) {  // an unbounded box for a chunk that must be visited
+      boxes[c * 2 * D + l] = chunk_bad ? -INFINITY : lo[l];
+      boxes[c * 2 * D + D + l] = chunk_bad ? INFINITY : hi[l];
     }
   }
 }
@@ -392,6 +402,43 @@ int sort_into(gbk_ctx *c, gbk_ctx::SortSlot &s, const double *x, long n, SortedS
 }
 
 }  // namespace
+
+__global__ void __launch_bounds__(kThreads) nonfinite_kernel(int d, const double *x, long n, const double *a, int lda,
+                                                             const double *b, int ldb, const double *e, int lde,
+                                                             unsigned *flag) {
+  bool bad = false;
+  for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+    for (int k = 0; k < d; ++k) bad = bad || !isfinite(x[i * d + k]);
+    if (a)
+      for (int k = 0; k < lda; ++k) bad = bad || !isfinite(a[i * lda + k]);
+    if (b)
+      for (int k = 0; k < ldb; ++k) bad = bad || !isfinite(b[i * ldb + k]);
+    if (e)
+      for (int k = 0; k < lde; ++k) bad = bad || !isfinite(e[i * lde + k]);
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1u);
+}
+
+// boxes: lo[d], hi[d] per chunk -> (-inf, +inf) when *flag
+__global__ void unbound_boxes_kernel(const unsigned *flag, double *boxes, long nvals, int d) {
+  if (!*flag) return;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nvals; i += (long)gridDim.x * blockDim.x)
+    boxes[i] = (i % (2 * d)) < d ? -INFINITY : INFINITY;
+}
+
+cudaError_t unbound_boxes_if_nonfinite(cudaStream_t st, int d, const double *x, long n, const double *a, int lda,
+                                       const double *b, int ldb, const double *e, int lde, unsigned *flag,
+                                       double *boxes, long nchunks) {
+  cudaError_t err = cudaMemsetAsync(flag, 0, sizeof(unsigned), st);
+  if (err != cudaSuccess) return err;
+  const long blocks = std::min<long>(std::max<long>((n + kThreads - 1) / kThreads, 1), 1216);
+  nonfinite_kernel<<<(unsigned)blocks, kThreads, 0, st>>>(d, x, n, a, lda, b, ldb, e, lde, flag);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  const long nvals = nchunks * 2 * d;
+  const long bb = std::min<long>(std::max<long>((nvals + kThreads - 1) / kThreads, 1), 1216);
+  unbound_boxes_kernel<<<(unsigned)bb, kThreads, 0, st>>>(flag, boxes, nvals, d);
+  return cudaGetLastError();
+}
 
 int order_sort(gbk_ctx *c, int d, const double *x, long n, SortedSet *out) {
   *out = SortedSet();

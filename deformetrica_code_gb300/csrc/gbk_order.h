@@ -22,6 +22,12 @@ struct SourceCopies {
   int ld[3] = {0, 0, 0};
   int cols[3] = {0, 0, 0};
   double *dst[3] = {nullptr, nullptr, nullptr};  // filled by order_sources
+  // arrays only read, to find non-finite source values (rows perm[p], first chk_cols[k] of
+  // chk_ld[k] columns): a chunk holding one is never pruned, as every pair term it feeds is NaN or
+  // infinite in the reference's sums however small the kernel value
+  const double *chk[3] = {nullptr, nullptr, nullptr};
+  int chk_ld[3] = {0, 0, 0};
+  int chk_cols[3] = {0, 0, 0};
 };
 
 // A point set in spatial order (device memory of the context, valid until the slot is reused).
@@ -58,5 +64,12 @@ int order_targets(gbk_ctx *c, int d, const SortedSet &s, int tile, double sigma,
 // `copies` asks for (the context's source-box and sorted-source buffers).
 int order_sources(gbk_ctx *c, int d, const double *y, const SortedSet &s, int chunk, const SourceCopies &copies,
                   OrderView *out);
+
+// If any of the n rows of x (d columns), a (lda columns), b (ldb), e (lde) holds a NaN or an
+// infinity (null arrays skipped), every one of the nchunks source-chunk boxes becomes unbounded, so
+// the launch that reads them prunes nothing. `flag` is device scratch; asynchronous on `st`.
+cudaError_t unbound_boxes_if_nonfinite(cudaStream_t st, int d, const double *x, long n, const double *a, int lda,
+                                       const double *b, int ldb, const double *e, int lde, unsigned *flag,
+                                       double *boxes, long nchunks);
 
 }  // namespace gbk

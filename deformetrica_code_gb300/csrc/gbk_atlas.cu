@@ -855,6 +855,7 @@ int gbk_atlas_step(gbk_atlas *a, const double *mom, double *loglik, double *grad
   if (!a) return GBK_ERR_ARG;
   gbk_ctx *c = a->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!mom) return c->fail(GBK_ERR_ARG, "null momenta");
   const size_t nb_mom = (size_t)a->S * a->ncp * 3 * sizeof(double);
@@ -896,6 +897,7 @@ int gbk_atlas_optimize(gbk_atlas *a, double *cp, double *tmpl, double *mom, int 
   if (!a) return GBK_ERR_ARG;
   gbk_ctx *c = a->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !tmpl || !mom || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = a->ncp * 3, m = a->nv * 3, nm = (long)a->S * n;

@@ -474,6 +474,7 @@ int gbk_get_estimator(const gbk_ctx *c) { return c ? c->estimator : -1; }
 
 int gbk_synchronize(gbk_ctx *c) {
   GBK_GUARD(c);
+  GBK_RANGE();
   return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
 }
 
@@ -503,6 +504,7 @@ int gbk_set_split(gbk_ctx *c, int nsplit) {
 int gbk_convolve(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
                  const double *w, long ny, double sigma, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
   HostIO io(c);
@@ -522,6 +524,7 @@ int gbk_convolve_gradient_alpha(gbk_ctx *c, int d, int dv, const double *x, long
                                 const double *y, const double *w, long ny, double sigma,
                                 const double *alpha, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if ((nx && (!x || !out || !alpha)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
   HostIO io(c);
@@ -542,6 +545,7 @@ int gbk_convolve_and_gradient_alpha(gbk_ctx *c, int d, int dv, const double *x, 
                                     const double *y, const double *w, long ny, double sigma,
                                     const double *alpha, double *out_v, double *out_g) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if ((nx && (!x || !out_v || !out_g || !alpha)) || (ny && (!y || !w)))
     return c->fail(GBK_ERR_ARG, "null pointer");
@@ -563,6 +567,7 @@ int gbk_convolve_and_gradient_alpha(gbk_ctx *c, int d, int dv, const double *x, 
 int gbk_convolve_gradient(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
                           const double *w, long ny, double sigma, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
   HostIO io(c);
@@ -582,6 +587,7 @@ int gbk_convolve_gradient_dim(gbk_ctx *c, int d, int dv, const double *x, long n
                               const double *y, const double *w, long ny, double sigma, int dim,
                               double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if (dim < 0 || dim >= d) return c->fail(GBK_ERR_ARG, "dimension index out of bounds");
   if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
@@ -603,6 +609,7 @@ int gbk_convolve_gradient_kdp(gbk_ctx *c, int d, int dv, const double *x, long n
                               const double *y, const double *w, long ny, double sigma, int k,
                               int dp, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if (k < 0 || k >= dv) return c->fail(GBK_ERR_ARG, "Invalid weight index");
   if (dp < 0 || dp >= d) return c->fail(GBK_ERR_ARG, "Invalid derivative direction");
@@ -630,6 +637,7 @@ int gbk_convolve_gradient_kdp(gbk_ctx *c, int d, int dv, const double *x, long n
 int gbk_convolve_hessian(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
                          const double *w, long ny, double sigma, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
   HostIO io(c);
@@ -649,6 +657,7 @@ int gbk_convolve_hessian_rowcol(gbk_ctx *c, int d, int dv, const double *x, long
                                 const double *y, const double *w, long ny, double sigma, int row,
                                 int col, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if (row < 0 || col < 0 || row >= d || col >= d) return c->fail(GBK_ERR_ARG, "Dimension index out of bounds");
   if ((nx && (!x || !out)) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
@@ -671,6 +680,7 @@ int gbk_convolve_hessian_kdpdq(gbk_ctx *c, int d, int dv, const double *x, long 
                                const double *y, const double *w, long ny, double sigma, int k,
                                int dp, int dq, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if (k < 0 || k >= dv) return c->fail(GBK_ERR_ARG, "Invalid weight index");
   if (dp < 0 || dq < 0 || dp >= d || dq >= d) return c->fail(GBK_ERR_ARG, "Invalid derivative direction");
@@ -697,6 +707,7 @@ int gbk_convolve_hessian_kdpdq(gbk_ctx *c, int d, int dv, const double *x, long 
 int gbk_convolve_special_hessian(gbk_ctx *c, int d, const double *y, const double *w, long n,
                                  double sigma, const double *xi, double *out) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, d, n, n, sigma)) return rc;
   if (n && (!y || !w || !xi || !out)) return c->fail(GBK_ERR_ARG, "null pointer");
   HostIO io(c);
@@ -726,6 +737,7 @@ int gbk_forward_adjoint(gbk_ctx *c, int d, int dv, const double *x, long nx, con
                         const double *w, long ny, double sigma, const double *alpha, double *v,
                         double *gx, double *gy, double *gw) {
   GBK_GUARD(c);
+  GBK_RANGE();
   if (int rc = check_common(c, d, dv, nx, ny, sigma)) return rc;
   if ((nx && !x) || (ny && (!y || !w))) return c->fail(GBK_ERR_ARG, "null pointer");
   if ((gx || gy || gw) && nx && !alpha) return c->fail(GBK_ERR_ARG, "alpha is required for the adjoint");

@@ -6,6 +6,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <map>
 #include <string>
@@ -13,6 +14,16 @@
 #include <utility>
 
 #include "gbk_dispatch.h"
+
+// A profiler range (NVTX) over the scope of one C ABI call, named after the call; inert unless a
+// profiling tool is attached.
+struct GbkRange {
+  explicit GbkRange(const char *name) { nvtxRangePushA(name); }
+  ~GbkRange() { nvtxRangePop(); }
+  GbkRange(const GbkRange &) = delete;
+  GbkRange &operator=(const GbkRange &) = delete;
+};
+#define GBK_RANGE() GbkRange gbk_nvtx_range_(__func__)
 
 struct gbk_ctx {
   struct DevBuf {

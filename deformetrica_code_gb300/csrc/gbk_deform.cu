@@ -384,6 +384,7 @@ extern "C" {
 int gbk_shoot(gbk_ctx *c, int d, long ncp, const double *cp0, const double *mom0, int T,
               double sigma, double *pos_traj, double *mom_traj) {
   GBK_GUARD2(c);
+  GBK_RANGE();
   if (int rc = check_traj(c, d, ncp, T)) return rc;
   if (!cp0 || !mom0 || !pos_traj || !mom_traj) return c->fail(GBK_ERR_ARG, "null pointer");
   HostIO io(c);
@@ -403,6 +404,7 @@ int gbk_flow_landmarks(gbk_ctx *c, int d, long ncp, const double *pos_traj, cons
                        int T, double sigma, long nlm, const double *lm0, int heun,
                        double *lm_traj) {
   GBK_GUARD2(c);
+  GBK_RANGE();
   if (int rc = check_traj(c, d, ncp, T)) return rc;
   if (nlm < 0) return c->fail(GBK_ERR_ARG, "negative landmark count");
   if (!pos_traj || !mom_traj || (nlm && (!lm0 || !lm_traj))) return c->fail(GBK_ERR_ARG, "null pointer");
@@ -425,6 +427,7 @@ int gbk_adjoint_landmarks(gbk_ctx *c, int d, long ncp, const double *pos_traj,
                           const double *lm_traj, const double *theta_final, int heun,
                           double *theta_traj) {
   GBK_GUARD2(c);
+  GBK_RANGE();
   if (int rc = check_traj(c, d, ncp, T)) return rc;
   if (nlm <= 0) return c->fail(GBK_ERR_ARG, "need at least one landmark");
   if (!pos_traj || !mom_traj || !lm_traj || !theta_final || !theta_traj)
@@ -447,6 +450,7 @@ int gbk_compute_update_at(gbk_ctx *c, int d, long ncp, const double *pos, const 
                           const double *xi_pos, const double *xi_mom, long nlm, const double *lm,
                           const double *theta, double sigma, double *dpos, double *dmom) {
   GBK_GUARD2(c);
+  GBK_RANGE();
   if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d not supported", d);
   if (ncp <= 0 || nlm < 0) return c->fail(GBK_ERR_ARG, "bad point counts");
   if (!pos || !mom || !xi_pos || !xi_mom || !dpos || !dmom || (nlm && (!lm || !theta)))
@@ -467,6 +471,7 @@ int gbk_adjoint_diffeo(gbk_ctx *c, int d, long ncp, const double *pos_traj, cons
                        const double *theta_traj, int heun, double *xipos_traj,
                        double *ximom_traj) {
   GBK_GUARD2(c);
+  GBK_RANGE();
   if (int rc = check_traj(c, d, ncp, T)) return rc;
   if (nlm < 0) return c->fail(GBK_ERR_ARG, "negative landmark count");
   if (!pos_traj || !mom_traj || !xipos_traj || !ximom_traj || (nlm && (!lm_traj || !theta_traj)))

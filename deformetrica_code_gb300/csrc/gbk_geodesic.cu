@@ -341,6 +341,7 @@ int gbk_geodesic_regression_step(gbk_geodesic_regression *r, const double *cp, c
   if (!r) return GBK_ERR_ARG;
   gbk_ctx *c = r->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !mom) return c->fail(GBK_ERR_ARG, "null pointer");
   const size_t nb = (size_t)r->ncp * r->d * sizeof(double), mb = (size_t)r->nv * r->d * sizeof(double);
@@ -372,6 +373,7 @@ int gbk_geodesic_regression_optimize(gbk_geodesic_regression *r, double *cp, dou
   if (!r) return GBK_ERR_ARG;
   gbk_ctx *c = r->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !mom || !tmpl || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = r->ncp * r->d, m = r->nv * r->d;

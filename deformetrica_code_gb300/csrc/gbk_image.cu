@@ -294,6 +294,7 @@ extern "C" {
 int gbk_image_points(gbk_ctx *c, int d, const double *origin, const double *spacing, const long *size,
                      double *points) {
   GBK_IMAGE_GUARD(c);
+  GBK_RANGE();
   ImageGeom g;
   if (int rc = geom_from(c, d, origin, spacing, size, 1.0, &g)) return rc;
   if (!points) return c->fail(GBK_ERR_ARG, "null pointer");
@@ -313,6 +314,7 @@ int gbk_convolve_image_fast(gbk_ctx *c, int d, const double *x, long nx, const d
                             double sigma, const double *origin, const double *spacing, const long *size,
                             double *out) {
   GBK_IMAGE_GUARD(c);
+  GBK_RANGE();
   if (sigma < 1e-10) sigma = 1e-10;  // AbstractKernel::SetKernelWidth
   ImageGeom g;
   if (int rc = geom_from(c, d, origin, spacing, size, sigma, &g)) return rc;
@@ -342,6 +344,7 @@ int gbk_flow_image_maps(gbk_ctx *c, int d, long ncp, const double *pos_traj, con
                         double sigma, double span, int heun, int fast, const double *origin, const double *spacing,
                         const long *size, const double *bbox, double *maps_traj, int *stopped_at) {
   GBK_IMAGE_GUARD(c);
+  GBK_RANGE();
   if (sigma < 1e-10) sigma = 1e-10;
   if (stopped_at) *stopped_at = -1;
   ImageGeom g;

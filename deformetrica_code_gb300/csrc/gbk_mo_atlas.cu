@@ -215,6 +215,7 @@ int gbk_mo_atlas_step(gbk_mo_atlas *a, const double *cp, const double *tmpl, con
   if (!a) return GBK_ERR_ARG;
   gbk_ctx *c = a->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !tmpl || !mom) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = a->ncp * a->d, m = a->nv * a->d, nm = (long)a->S * n;
@@ -256,6 +257,7 @@ int gbk_mo_atlas_optimize(gbk_mo_atlas *a, double *cp, double *tmpl, double *mom
   if (!a) return GBK_ERR_ARG;
   gbk_ctx *c = a->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !tmpl || !mom || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = a->ncp * a->d, m = a->nv * a->d, nm = (long)a->S * n;

@@ -377,6 +377,8 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
             double sigma, const double *alpha, const double *domain, double ratio, double padding, double *out) {
   if (!c) return GBK_ERR_ARG;
   c->err.clear();
+  static const char *const kNames[3] = {"gbk_p3m_convolve", "gbk_p3m_convolve_gradient", "gbk_p3m_convolve_gradient_alpha"};
+  GbkRange range(kNames[mode < 0 || mode > 2 ? 0 : mode]);
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "P3M needs d = 2 or 3");
   if (nx <= 0 || ny <= 0 || dv <= 0) return c->fail(GBK_ERR_ARG, "empty input");

@@ -289,6 +289,7 @@ int gbk_registration_set_template(gbk_registration *r, const double *pts) {
   if (!r) return GBK_ERR_ARG;
   gbk_ctx *c = r->c;
   c->err.clear();
+  GBK_RANGE();
   if (!pts) return c->fail(GBK_ERR_ARG, "null pointer");
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   int rc = c->cuda(cudaMemcpyAsync(r->lm0, pts, (size_t)r->nv * r->d * sizeof(double), cudaMemcpyDefault, r->stream),
@@ -301,6 +302,7 @@ int gbk_registration_set_point_weights(gbk_registration *r, const double *w_tmpl
   if (!r) return GBK_ERR_ARG;
   gbk_ctx *c = r->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   cudaStream_t saved = c->stream;
   c->stream = r->stream;
@@ -332,6 +334,7 @@ int gbk_registration_step(gbk_registration *r, const double *cp, const double *m
   if (!r) return GBK_ERR_ARG;
   gbk_ctx *c = r->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !mom) return c->fail(GBK_ERR_ARG, "null pointer");
   const size_t nb = (size_t)r->ncp * r->d * sizeof(double);
@@ -382,6 +385,7 @@ int gbk_registration_optimize(gbk_registration *r, double *cp, double *mom, int 
   if (!r) return GBK_ERR_ARG;
   gbk_ctx *c = r->c;
   c->err.clear();
+  GBK_RANGE();
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (!cp || !mom || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = r->ncp * r->d;

@@ -118,6 +118,7 @@ SIGNATURES = {
     "gbk_p3m_convolve": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _D, _D, _P]),
     "gbk_p3m_convolve_gradient": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _D, _D, _P]),
     "gbk_p3m_convolve_gradient_alpha": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P, _D, _D, _P]),
+    "gbk_set_alloc_limit": (_I, [_P, ctypes.c_size_t]),
     "gbk_image_points": (_I, [_P, _I, _P, _P, _P, _P]),
     "gbk_convolve_image_fast": (_I, [_P, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P]),
     "gbk_flow_image_maps": (_I, [_P, _I, _L, _P, _P, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P]),

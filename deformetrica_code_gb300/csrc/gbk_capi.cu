@@ -106,6 +106,8 @@ int gbk_ctx::ensure(DevBuf &b, size_t bytes, const char *what) {
   if (capturing())
     return fail(GBK_ERR_STATE, "%s: needs %zu bytes of device scratch while the stream is being captured; "
                 "run the call once before capture", what, bytes);
+  if (alloc_limit && bytes > alloc_limit)
+    return fail(GBK_ERR_ALLOC, "%s: %zu bytes refused (injected allocation limit %zu)", what, bytes, alloc_limit);
   if (b.p) {
     int rc = cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     if (rc) return rc;
@@ -451,6 +453,12 @@ int gbk_set_order(gbk_ctx *c, int order) {
 }
 
 int gbk_get_order(const gbk_ctx *c) { return c ? c->order : -1; }
+
+int gbk_set_alloc_limit(gbk_ctx *c, size_t bytes) {
+  if (!c) return GBK_ERR_ARG;
+  c->alloc_limit = bytes;
+  return GBK_OK;
+}
 
 int gbk_set_gradient_mode(gbk_ctx *c, int mode) {
   if (!c) return GBK_ERR_ARG;

@@ -38,6 +38,7 @@ struct gbk_ctx {
   cudaStream_t stream = nullptr;
   int mode = 0;         // GBK_MODE_F32C / GBK_MODE_F64
   int force_split = 0;  // 0 = automatic
+  size_t alloc_limit = 0;  // fault injection: buffer growth beyond this fails (0 = none)
   long long launches = 0;
   std::string err;
 

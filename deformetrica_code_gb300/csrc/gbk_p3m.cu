@@ -72,6 +72,8 @@ void p3m_cache_free(void *p) {
 // grows the cached scratch to at least `bytes` (contents not kept)
 int p3m_work(gbk_ctx *c, P3MCache *pc, size_t bytes) {
   if (pc->work_bytes >= bytes) return 0;
+  if (c->alloc_limit && bytes > c->alloc_limit)
+    return c->fail(GBK_ERR_ALLOC, "P3M scratch: %zu bytes refused (injected allocation limit)", bytes);
   if (pc->work) {
     cudaStreamSynchronize(c->stream);
     cudaFree(pc->work);

@@ -111,6 +111,11 @@ class Context:
     def set_split(self, n: int):
         self.check(self.lib.gbk_set_split(self.h, n))
 
+    def set_alloc_limit(self, nbytes: int):
+        """Fault injection for tests: device-buffer growth beyond nbytes fails with GBK_ERR_ALLOC
+        (0 lifts the limit)."""
+        self.check(self.lib.gbk_set_alloc_limit(self.h, int(nbytes)))
+
     def launch_count(self) -> int:
         return int(self.lib.gbk_launch_count(self.h))
 

@@ -32,6 +32,8 @@
 #ifndef GBK_H
 #define GBK_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -541,6 +543,10 @@ int gbk_tune_save(const gbk_ctx *ctx, const char *path);
 int gbk_tune_load(gbk_ctx *ctx, const char *path);
 /* Forces the number of source splits (0 = automatic) -- for tests and tuning. */
 int gbk_set_split(gbk_ctx *ctx, int nsplit);
+/* Fault injection for tests: from now on every growth of one of the context's device buffers
+ * beyond `bytes` fails with GBK_ERR_ALLOC as if cudaMalloc had failed (0 = no limit). The context
+ * stays usable: lift the limit and the same call succeeds. */
+int gbk_set_alloc_limit(gbk_ctx *ctx, size_t bytes);
 
 #ifdef __cplusplus
 }

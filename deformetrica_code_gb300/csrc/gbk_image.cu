@@ -232,8 +232,9 @@ int geom_from(gbk_ctx *c, int d, const double *origin, const double *spacing, co
   return GBK_OK;
 }
 
-// windows of `groups` x `per` control points (rows of y); fails at the first group with a window
-// that misses the image when `check_group` < 0, else returns the per-group verdicts in bad_host
+// Window starts of `groups` x `per` control points (rows of y) into `start`; bad_host[g] = the first
+// control point of group g whose window misses the image, or 0x7f7f7f7f when none does (the
+// caller turns a miss into GBK_ERR_ARG when it needs that group). Waits for the stream.
 int windows(gbk_ctx *c, const ImageGeom &g, const double *y, long per, int groups, double sigma, int *start,
             int *bad_dev, std::vector<int> &bad_host) {
   cudaStream_t st = c->stream;

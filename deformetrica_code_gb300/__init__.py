@@ -10,11 +10,13 @@ from ._lib import (GBKError, GBK_MODE_F32C, GBK_MODE_F64, GBK_ORDER_AUTO, GBK_OR
 
 _lib.load()
 
-from .kernel import (Context, GB300ExactKernel, p3m_convolve, p3m_convolve_gradient,  # noqa: E402
-                     p3m_convolve_gradient_alpha)
+from .kernel import (Context, GB300ExactKernel, GB300P3MKernel, p3m_convolve, p3m_convolve_gradient,  # noqa: E402
+                     p3m_convolve_gradient_alpha, p3m_convolve_gradient_dim, p3m_convolve_hessian,
+                     p3m_convolve_hessian_rowcol)
 from .images import ImageGrid, flow_image_maps  # noqa: E402
 
 __all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64", "GBK_ORDER_AUTO",
            "GBK_ORDER_OFF", "GBK_ORDER_SPATIAL", "GBK_ORDER_SPATIAL_NOPRUNE", "GBK_GRADIENT_REFERENCE",
            "GBK_GRADIENT_EXACT", "GBK_ESTIMATOR_FAST_GRADIENT_ASCENT", "GBK_ESTIMATOR_GRADIENT_ASCENT", "p3m_convolve",
-           "p3m_convolve_gradient", "p3m_convolve_gradient_alpha", "ImageGrid", "flow_image_maps"]
+           "p3m_convolve_gradient", "p3m_convolve_gradient_alpha", "p3m_convolve_gradient_dim", "p3m_convolve_hessian",
+           "p3m_convolve_hessian_rowcol", "GB300P3MKernel", "ImageGrid", "flow_image_maps"]

@@ -118,6 +118,11 @@ SIGNATURES = {
     "gbk_p3m_convolve": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _D, _D, _P]),
     "gbk_p3m_convolve_gradient": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _D, _D, _P]),
     "gbk_p3m_convolve_gradient_alpha": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P, _D, _D, _P]),
+    "gbk_p3m_convolve_gradient_dim": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _I, _P, _D, _D, _P]),
+    "gbk_p3m_convolve_hessian": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _D, _D, _P]),
+    "gbk_p3m_convolve_hessian_rowcol": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _I, _I, _P, _D, _D, _P]),
+    "gbk_p3m_convolve_gradient_kdp": (_I, [_P, _I, _I, _L, _L, _I, _I, _P]),
+    "gbk_p3m_convolve_hessian_kdpdq": (_I, [_P, _I, _I, _L, _L, _I, _I, _I, _P]),
     "gbk_set_alloc_limit": (_I, [_P, ctypes.c_size_t]),
     "gbk_image_points": (_I, [_P, _I, _P, _P, _P, _P]),
     "gbk_convolve_image_fast": (_I, [_P, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P]),

@@ -50,7 +50,7 @@ struct P3MCache {
   double s = 0, sigma = 0;
   bool f64 = true;
   std::vector<P3MPlan> plans;  // for the grid n of d
-  void *kspec = nullptr;       // (1 + d) kernel spectra: Gaussian, then its gradient components
+  void *kspec = nullptr;       // kernel spectra: Gaussian, its d gradient components, its d(d+1)/2 Hessian entries
   void *work = nullptr;        // grow-only scratch: grids, images, spectra, products, box
   size_t work_bytes = 0;
 
@@ -87,6 +87,10 @@ int p3m_work(gbk_ctx *c, P3MCache *pc, size_t bytes) {
 
 unsigned nblk(long n, int bs = 256) { return (unsigned)std::max(1L, (n + bs - 1) / bs); }
 
+// kernel images per grid: the Gaussian, its d gradient components, its d(d+1)/2 Hessian entries
+// (r <= c, first row first: the reference's BuildFFTHessianKernels order)
+inline int p3m_kernels(int d) { return 1 + d + d * (d + 1) / 2; }
+
 // Kernel images in inverse-FFT-shifted layout: slot j holds the value at grid index (j + n/2) mod n.
 template <int D, typename G>
 __global__ void p3m_kernel_images(P3MGrid g, double sigma, G *img, long cells) {
@@ -108,9 +112,17 @@ __global__ void p3m_kernel_images(P3MGrid g, double sigma, G *img, long cells) {
     diff[k] = x - c;
     d2 += diff[k] * diff[k];
   }
-  const double kv = exp(-d2 / (sigma * sigma));
+  const double s2 = sigma * sigma, kv = exp(-d2 / s2);
   img[j] = (G)(border ? 0.0 : kv);
-  for (int k = 0; k < D; ++k) img[(1 + k) * cells + j] = (G)(border ? 0.0 : diff[k] * (-2.0 * kv / (sigma * sigma)));
+  for (int k = 0; k < D; ++k) img[(1 + k) * cells + j] = (G)(border ? 0.0 : diff[k] * (-2.0 * kv / s2));
+  // ExactKernel::EvaluateKernelHessian (ExactKernel.h:113-132): (x - c)(x - c)^T 4K/s^4 - 2K/s^2 I
+  int q = 1 + D;
+  for (int r = 0; r < D; ++r)
+    for (int cc = r; cc < D; ++cc, ++q) {
+      double h = diff[r] * diff[cc] * (4.0 * kv / (s2 * s2));
+      if (r == cc) h -= 2.0 * kv / s2;
+      img[(long)q * cells + j] = (G)(border ? 0.0 : h);
+    }
 }
 
 // multilinear corners of one point, slot b = corner b in the reference's order (first dimension
@@ -185,7 +197,8 @@ __global__ void p3m_multiply(const C *spec, const C *kspec, int nimg, int per_gr
 }
 
 // values at the targets: mode 0 the nimg images; mode 2 contracted with alpha (images ordered
-// p + D k, out nx x D)
+// p + D k, out nx x D); mode 3 the symmetric Hessians (images ordered q + D(D+1)/2 k, q the upper
+// entry, out nx x dv x D x D)
 template <int D, typename G>
 __global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, long cells, P3MGrid g, int mode,
                            const double *alpha, int dv, double *out) {
@@ -200,6 +213,20 @@ __global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, lo
       for (int c = 0; c < (1 << D); ++c)
         if (cs.use[c]) v += cs.w[c] * imgs[(long)q * cells + cs.l[c]];
       out[i * nimg + q] = v;
+    }
+  } else if (mode == 3) {
+    constexpr int H = D * (D + 1) / 2;
+    for (int k = 0; k < dv; ++k) {
+      int q = 0;
+      for (int r = 0; r < D; ++r)
+        for (int cc = r; cc < D; ++cc, ++q) {
+          double v = 0.0;
+#pragma unroll
+          for (int c = 0; c < (1 << D); ++c)
+            if (cs.use[c]) v += cs.w[c] * imgs[(long)(q + H * k) * cells + cs.l[c]];
+          out[((i * dv + k) * D + r) * D + cc] = v;
+          out[((i * dv + k) * D + cc) * D + r] = v;
+        }
     }
   } else {
     double r[D];
@@ -299,13 +326,27 @@ size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 // kernel spectra (cached), splat, one batched forward transform, spectrum products, one batched
 // inverse transform, interpolation
 template <typename G>
-int p3m_exec(gbk_ctx *c, P3MCache *pc, const P3MGrid &g, int mode, int dv, const double *dx, long nx,
+int p3m_exec(gbk_ctx *c, P3MCache *pc, const P3MGrid &g, int mode, int p0, int p1, int dv, const double *dx, long nx,
              const double *dy, const double *dw, long ny, double sigma, const double *da, double *dout, HostIO &io) {
   typedef typename P3MFFT<G>::C C;
-  const int d = g.d;
+  const int d = g.d, nk = p3m_kernels(d), H = d * (d + 1) / 2;
   cudaStream_t st = c->stream;
   const long cells = g.cells(), ccells = g.ccells();
-  const int nimg = mode == 0 ? dv : dv * d;
+  // images per weight grid and the first kernel they use, and the interpolation's output form
+  int per_grid = 1, kernel0 = 0, interp = 0;
+  switch (mode) {
+    case 1: per_grid = d, kernel0 = 1; break;                  // ConvolveGradient(X)
+    case 2: per_grid = d, kernel0 = 1, interp = 2; break;      // ConvolveGradient(X, alpha)
+    case 3: kernel0 = 1 + p0; break;                           // ConvolveGradient(X, dim)
+    case 4: per_grid = H, kernel0 = 1 + d, interp = 3; break;  // ConvolveHessian(X)
+    case 5: {                                                  // ConvolveHessian(X, row, col)
+      const int r = std::min(p0, p1), cc = std::max(p0, p1);
+      kernel0 = 1 + d + cc + d * r - r * (r + 1) / 2;
+      break;
+    }
+    default: break;                                            // Convolve
+  }
+  const int nimg = dv * per_grid;
   const bool f64 = sizeof(G) == 8;
   int rc = 0;
   if (!(pc->valid && pc->s == g.s && pc->sigma == sigma && pc->f64 == f64)) {
@@ -316,9 +357,9 @@ int p3m_exec(gbk_ctx *c, P3MCache *pc, const P3MGrid &g, int mode, int dv, const
       pc->kspec = nullptr;
     }
     cufftHandle kp;
-    if ((rc = p3m_plan(c, pc, g, P3MFFT<G>::R2C, 1 + d, &kp))) return rc;
-    if ((rc = c->cuda(cudaMalloc(&pc->kspec, (size_t)ccells * (1 + d) * sizeof(C)), "cudaMalloc (P3M)"))) return rc;
-    if ((rc = p3m_work(c, pc, (size_t)cells * (1 + d) * sizeof(G)))) return rc;
+    if ((rc = p3m_plan(c, pc, g, P3MFFT<G>::R2C, nk, &kp))) return rc;
+    if ((rc = c->cuda(cudaMalloc(&pc->kspec, (size_t)ccells * nk * sizeof(C)), "cudaMalloc (P3M)"))) return rc;
+    if ((rc = p3m_work(c, pc, (size_t)cells * nk * sizeof(G)))) return rc;
     G *kimg = (G *)pc->work;
     if (d == 3)
       p3m_kernel_images<3, G><<<nblk(cells), 256, 0, st>>>(g, sigma, kimg, cells);
@@ -354,17 +395,17 @@ int p3m_exec(gbk_ctx *c, P3MCache *pc, const P3MGrid &g, int mode, int dv, const
   }
   if (!rc) rc = fft_error(c, P3MFFT<G>::fwd(fwd, grids, spec), "forward");
   if (!rc) {
-    p3m_multiply<C, G><<<nblk(ccells), 256, 0, st>>>(spec, (const C *)pc->kspec, nimg, mode == 0 ? 1 : d,
-                                                    mode == 0 ? 0 : 1, ccells, (G)(1.0 / (double)cells), prod);
+    p3m_multiply<C, G><<<nblk(ccells), 256, 0, st>>>(spec, (const C *)pc->kspec, nimg, per_grid, kernel0, ccells,
+                                                    (G)(1.0 / (double)cells), prod);
     c->launches += 1;
     rc = c->cuda(cudaGetLastError(), "multiply");
   }
   if (!rc) rc = fft_error(c, P3MFFT<G>::inv(inv, prod, imgs), "inverse");
   if (!rc) {
     if (d == 3)
-      p3m_interp<3, G><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, mode == 2 ? 2 : 0, da, dv, dout);
+      p3m_interp<3, G><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, interp, da, dv, dout);
     else
-      p3m_interp<2, G><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, mode == 2 ? 2 : 0, da, dv, dout);
+      p3m_interp<2, G><<<nblk(nx), 256, 0, st>>>(dx, nx, imgs, nimg, cells, g, interp, da, dv, dout);
     c->launches += 1;
     rc = c->cuda(cudaGetLastError(), "interpolate");
   }
@@ -375,17 +416,22 @@ int p3m_exec(gbk_ctx *c, P3MCache *pc, const P3MGrid &g, int mode, int dv, const
 }
 
 // mode 0 Convolve (out nx x dv), 1 ConvolveGradient(X) (out nx x dv x d), 2 alpha-contracted (nx x d)
-int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const double *y, const double *w, long ny,
-            double sigma, const double *alpha, const double *domain, double ratio, double padding, double *out) {
+int p3m_run(gbk_ctx *c, int mode, int p0, int p1, int d, int dv, const double *x, long nx, const double *y,
+            const double *w, long ny, double sigma, const double *alpha, const double *domain, double ratio,
+            double padding, double *out) {
   if (!c) return GBK_ERR_ARG;
   c->err.clear();
-  static const char *const kNames[3] = {"gbk_p3m_convolve", "gbk_p3m_convolve_gradient", "gbk_p3m_convolve_gradient_alpha"};
-  GbkRange range(kNames[mode < 0 || mode > 2 ? 0 : mode]);
+  static const char *const kNames[6] = {"gbk_p3m_convolve",          "gbk_p3m_convolve_gradient",
+                                        "gbk_p3m_convolve_gradient_alpha", "gbk_p3m_convolve_gradient_dim",
+                                        "gbk_p3m_convolve_hessian",  "gbk_p3m_convolve_hessian_rowcol"};
+  GbkRange range(kNames[mode < 0 || mode > 5 ? 0 : mode]);
   if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
   if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "P3M needs d = 2 or 3");
   if (nx <= 0 || ny <= 0 || dv <= 0) return c->fail(GBK_ERR_ARG, "empty input");
   if (!x || !y || !w || !out || (mode == 2 && !alpha)) return c->fail(GBK_ERR_ARG, "null pointer");
   if (!(sigma > 1e-20) || !(ratio > 0) || !(padding >= 0)) return c->fail(GBK_ERR_ARG, "bad P3M parameters");
+  if (mode == 3 && (p0 < 0 || p0 >= d)) return c->fail(GBK_ERR_ARG, "dimension parameter out of bounds");
+  if (mode == 5 && (p0 < 0 || p0 >= d || p1 < 0 || p1 >= d)) return c->fail(GBK_ERR_ARG, "dimension index out of bounds");
   if (c->capturing()) return c->fail(GBK_ERR_STATE, "P3M allocates and plans FFTs; not under stream capture");
   cudaStream_t st = c->stream;
   HostIO io(c);
@@ -393,7 +439,7 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
   const double *dy = io.in(y, (size_t)ny * d, "y");
   const double *dw = io.in(w, (size_t)ny * dv, "w");
   const double *da = mode == 2 ? io.in(alpha, (size_t)nx * dv, "alpha") : nullptr;
-  const size_t nout = (size_t)nx * (mode == 0 ? dv : mode == 1 ? dv * d : d);
+  const size_t nout = (size_t)nx * (mode == 1 ? dv * d : mode == 2 ? d : mode == 4 ? dv * d * d : dv);
   double *dout = io.out(out, nout, "out");
   int rc = io.rc;
   if (rc) return rc;
@@ -439,10 +485,10 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
     g.origin[k] = box[k] - (n * g.s - length) / 2;
   }
   const long cells = g.cells(), ccells = g.ccells();
-  const int nimg = mode == 0 ? dv : dv * d;
+  const int nimg = dv * (mode == 1 || mode == 2 ? d : mode == 4 ? d * (d + 1) / 2 : 1), nk = p3m_kernels(d);
   const bool f64 = c->mode == GBK_MODE_F64;
   const double re = f64 ? 8.0 : 4.0;  // grids, images, spectra, products, kernel spectra, cuFFT work areas
-  const double bytes = re * cells * (dv + nimg) + 2 * re * ccells * (dv + nimg + 1 + d + std::max(nimg, 1 + d));
+  const double bytes = re * cells * (dv + nimg) + 2 * re * ccells * (dv + nimg + nk + std::max(nimg, nk));
   if (bytes > 64e9) return c->fail(GBK_ERR_ARG, "P3M grid of %ld points needs %.0f GB", cells, bytes / 1e9);
   if (!(pc->d == d && pc->n[0] == g.n[0] && pc->n[1] == g.n[1] && pc->n[2] == g.n[2])) {
     cudaStreamSynchronize(st);
@@ -451,8 +497,8 @@ int p3m_run(gbk_ctx *c, int mode, int d, int dv, const double *x, long nx, const
     pc->d = d;
     for (int k = 0; k < 3; ++k) pc->n[k] = g.n[k];
   }
-  return f64 ? p3m_exec<double>(c, pc, g, mode, dv, dx, nx, dy, dw, ny, sigma, da, dout, io)
-             : p3m_exec<float>(c, pc, g, mode, dv, dx, nx, dy, dw, ny, sigma, da, dout, io);
+  return f64 ? p3m_exec<double>(c, pc, g, mode, p0, p1, dv, dx, nx, dy, dw, ny, sigma, da, dout, io)
+             : p3m_exec<float>(c, pc, g, mode, p0, p1, dv, dx, nx, dy, dw, ny, sigma, da, dout, io);
 }
 
 }  // namespace
@@ -461,19 +507,65 @@ extern "C" {
 
 int gbk_p3m_convolve(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y, const double *w, long ny,
                      double sigma, const double *domain, double spacing_ratio, double padding_factor, double *out) {
-  return p3m_run(c, 0, d, dv, x, nx, y, w, ny, sigma, nullptr, domain, spacing_ratio, padding_factor, out);
+  return p3m_run(c, 0, 0, 0, d, dv, x, nx, y, w, ny, sigma, nullptr, domain, spacing_ratio, padding_factor, out);
 }
 
 int gbk_p3m_convolve_gradient(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y, const double *w,
                               long ny, double sigma, const double *domain, double spacing_ratio, double padding_factor,
                               double *out) {
-  return p3m_run(c, 1, d, dv, x, nx, y, w, ny, sigma, nullptr, domain, spacing_ratio, padding_factor, out);
+  return p3m_run(c, 1, 0, 0, d, dv, x, nx, y, w, ny, sigma, nullptr, domain, spacing_ratio, padding_factor, out);
 }
 
 int gbk_p3m_convolve_gradient_alpha(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
                                     const double *w, long ny, double sigma, const double *alpha, const double *domain,
                                     double spacing_ratio, double padding_factor, double *out) {
-  return p3m_run(c, 2, d, dv, x, nx, y, w, ny, sigma, alpha, domain, spacing_ratio, padding_factor, out);
+  return p3m_run(c, 2, 0, 0, d, dv, x, nx, y, w, ny, sigma, alpha, domain, spacing_ratio, padding_factor, out);
+}
+
+int gbk_p3m_convolve_gradient_dim(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                                  const double *w, long ny, double sigma, int dim, const double *domain,
+                                  double spacing_ratio, double padding_factor, double *out) {
+  return p3m_run(c, 3, dim, 0, d, dv, x, nx, y, w, ny, sigma, nullptr, domain, spacing_ratio, padding_factor, out);
+}
+
+int gbk_p3m_convolve_hessian(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y, const double *w,
+                             long ny, double sigma, const double *domain, double spacing_ratio, double padding_factor,
+                             double *out) {
+  return p3m_run(c, 4, 0, 0, d, dv, x, nx, y, w, ny, sigma, nullptr, domain, spacing_ratio, padding_factor, out);
+}
+
+int gbk_p3m_convolve_hessian_rowcol(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                                    const double *w, long ny, double sigma, int row, int col, const double *domain,
+                                    double spacing_ratio, double padding_factor, double *out) {
+  return p3m_run(c, 5, row, col, d, dv, x, nx, y, w, ny, sigma, nullptr, domain, spacing_ratio, padding_factor,
+                 out);
+}
+
+// P3MKernel::ConvolveGradient(X, k, dp) and ConvolveHessian(X, k, dp, dq) (P3MKernel.cxx:1506-1547,
+// 1689-1729) check their indices and return nx zeros.
+static int p3m_zeros(gbk_ctx *c, int d, int dv, long nx, long ny, int k, int dp, int dq, double *out) {
+  if (!c) return GBK_ERR_ARG;
+  c->err.clear();
+  if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "P3M needs d = 2 or 3");
+  if (nx < 0 || ny < 0 || dv <= 0) return c->fail(GBK_ERR_ARG, "bad sizes");
+  if (k < 0 || k >= dv) return c->fail(GBK_ERR_ARG, "Invalid weight index");
+  if (dp < 0 || dp >= d || dq < 0 || dq >= d) return c->fail(GBK_ERR_ARG, "Invalid derivative direction");
+  if (nx == 0) return GBK_OK;
+  if (!out) return c->fail(GBK_ERR_ARG, "null pointer");
+  if (is_device_pointer(out)) {
+    if (int rc = c->cuda(cudaMemsetAsync(out, 0, (size_t)nx * sizeof(double), c->stream), "memset")) return rc;
+    return c->cuda(cudaStreamSynchronize(c->stream), "sync");
+  }
+  std::fill(out, out + nx, 0.0);
+  return GBK_OK;
+}
+
+int gbk_p3m_convolve_gradient_kdp(gbk_ctx *c, int d, int dv, long nx, long ny, int k, int dp, double *out) {
+  return p3m_zeros(c, d, dv, nx, ny, k, dp, 0, out);
+}
+
+int gbk_p3m_convolve_hessian_kdpdq(gbk_ctx *c, int d, int dv, long nx, long ny, int k, int dp, int dq, double *out) {
+  return p3m_zeros(c, d, dv, nx, ny, k, dp, dq, out);
 }
 
 }  // extern "C"

@@ -372,7 +372,7 @@ class GB300ExactKernel:
 __all__ = ["Context", "GB300ExactKernel", "GBKError", "GBK_MODE_F32C", "GBK_MODE_F64"]
 
 
-def _p3m(name, x, y, w, sigma, alpha, domain, spacing_ratio, padding_factor, out_cols, context):
+def _p3m(name, x, y, w, sigma, alpha, domain, spacing_ratio, padding_factor, out_cols, context, ints=()):
     ctx = context or Context()
     d = x.shape[1]
     _check(x, "x")
@@ -393,6 +393,7 @@ def _p3m(name, x, y, w, sigma, alpha, domain, spacing_ratio, padding_factor, out
     args = [ctx.h, d, w.shape[1], _ptr(x), x.shape[0], _ptr(y), _ptr(w), y.shape[0], float(sigma)]
     if alpha is not None:
         args.append(_ptr(alpha))
+    args += [int(v) for v in ints]
     args += [None if dom is None else ctypes.c_void_p(dom.ctypes.data), float(spacing_ratio), float(padding_factor),
              _ptr(out)]
     ctx.check(getattr(ctx.lib, name)(*args))
@@ -419,3 +420,108 @@ def p3m_convolve_gradient_alpha(x, y, w, sigma, alpha, domain=None, spacing_rati
     """P3MKernel::ConvolveGradient(X, alpha): nx x d."""
     return _p3m("gbk_p3m_convolve_gradient_alpha", x, y, w, sigma, alpha, domain, spacing_ratio, padding_factor,
                 (x.shape[1],), context)
+
+
+def p3m_convolve_gradient_dim(x, y, w, sigma, dim: int, domain=None, spacing_ratio: float = 0.2,
+                              padding_factor: float = 3.0, context: Context | None = None):
+    """P3MKernel::ConvolveGradient(X, dim): nx x dv."""
+    return _p3m("gbk_p3m_convolve_gradient_dim", x, y, w, sigma, None, domain, spacing_ratio, padding_factor,
+                (w.shape[1],), context, ints=(dim,))
+
+
+def p3m_convolve_hessian(x, y, w, sigma, domain=None, spacing_ratio: float = 0.2, padding_factor: float = 3.0,
+                         context: Context | None = None):
+    """P3MKernel::ConvolveHessian(X): nx x dv x d x d."""
+    return _p3m("gbk_p3m_convolve_hessian", x, y, w, sigma, None, domain, spacing_ratio, padding_factor,
+                (w.shape[1], x.shape[1], x.shape[1]), context)
+
+
+def p3m_convolve_hessian_rowcol(x, y, w, sigma, row: int, col: int, domain=None, spacing_ratio: float = 0.2,
+                                padding_factor: float = 3.0, context: Context | None = None):
+    """P3MKernel::ConvolveHessian(X, row, col): nx x dv."""
+    return _p3m("gbk_p3m_convolve_hessian_rowcol", x, y, w, sigma, None, domain, spacing_ratio, padding_factor,
+                (w.shape[1],), context, ints=(row, col))
+
+
+class GB300P3MKernel:
+    """The reference's P3MKernel<double, PointDim> (P3MKernel.h:32-286) on the device: the same
+    method names and overloads as the exact kernel object, every sum a particle-mesh approximation
+    (grid spacing = working_spacing_ratio x width, padding_factor x width of padding). The data
+    domain is the bounding box of targets and sources unless set with SetDataDomain."""
+
+    def __init__(self, point_dim: int, kernel_width: float = 1.0, context: Context | None = None,
+                 working_spacing_ratio: float = 0.2, padding_factor: float = 3.0):
+        if point_dim not in (2, 3):
+            raise ValueError("PointDim must be 2 or 3")
+        self.d = point_dim
+        self.ctx = context or Context()
+        self.ratio, self.padding = float(working_spacing_ratio), float(padding_factor)
+        self.domain = None
+        self.m_Sources = self.m_Weights = None
+        self.SetKernelWidth(kernel_width)
+
+    def SetKernelWidth(self, h: float):
+        self.m_KernelWidth = float(max(h, 1e-10))
+
+    def GetKernelWidth(self) -> float:
+        return self.m_KernelWidth
+
+    def SetSources(self, Y):
+        self.m_Sources = _check(Y, "sources", self.d)
+
+    def SetWeights(self, W):
+        self.m_Weights = _check(W, "weights")
+
+    def SetDataDomain(self, lo, hi):
+        self.domain = (np.asarray(lo, float), np.asarray(hi, float))
+
+    def _yw(self):
+        Y, W = self.m_Sources, self.m_Weights
+        if Y is None or W is None:
+            raise RuntimeError("sources and weights must be set")
+        if Y.shape[0] != W.shape[0]:
+            raise RuntimeError("Sources and weights count mismatch")
+        return Y, W
+
+    def _kw(self):
+        return dict(domain=self.domain, spacing_ratio=self.ratio, padding_factor=self.padding, context=self.ctx)
+
+    def Convolve(self, X):
+        Y, W = self._yw()
+        return p3m_convolve(_check(X, "X", self.d), Y, W, self.m_KernelWidth, **self._kw())
+
+    def ConvolveGradient(self, X, *args):
+        """(X) -> (nx, dv, d); (X, alpha) -> (nx, d); (X, dim) -> (nx, dv); (X, k, dp) -> nx zeros,
+        as the reference's stub."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        if len(args) == 0:
+            return p3m_convolve_gradient(X, Y, W, self.m_KernelWidth, **self._kw())
+        if len(args) == 1 and not isinstance(args[0], (int, np.integer)):
+            return p3m_convolve_gradient_alpha(X, Y, W, self.m_KernelWidth, args[0], **self._kw())
+        if len(args) == 1:
+            return p3m_convolve_gradient_dim(X, Y, W, self.m_KernelWidth, int(args[0]), **self._kw())
+        if len(args) == 2:
+            out = np.zeros(X.shape[0])
+            self.ctx.check(self.ctx.lib.gbk_p3m_convolve_gradient_kdp(self.ctx.h, self.d, W.shape[1], X.shape[0],
+                                                                      Y.shape[0], int(args[0]), int(args[1]),
+                                                                      _hptr(out)))
+            return out
+        raise TypeError("ConvolveGradient takes (X), (X, alpha), (X, dim) or (X, k, dp)")
+
+    def ConvolveHessian(self, X, *args):
+        """(X) -> (nx, dv, d, d); (X, row, col) -> (nx, dv); (X, k, dp, dq) -> nx zeros, as the
+        reference's stub."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        if len(args) == 0:
+            return p3m_convolve_hessian(X, Y, W, self.m_KernelWidth, **self._kw())
+        if len(args) == 2:
+            return p3m_convolve_hessian_rowcol(X, Y, W, self.m_KernelWidth, int(args[0]), int(args[1]), **self._kw())
+        if len(args) == 3:
+            out = np.zeros(X.shape[0])
+            self.ctx.check(self.ctx.lib.gbk_p3m_convolve_hessian_kdpdq(self.ctx.h, self.d, W.shape[1], X.shape[0],
+                                                                       Y.shape[0], int(args[0]), int(args[1]),
+                                                                       int(args[2]), _hptr(out)))
+            return out
+        raise TypeError("ConvolveHessian takes (X), (X, row, col) or (X, k, dp, dq)")

@@ -379,6 +379,23 @@ int gbk_p3m_convolve_gradient(gbk_ctx *ctx, int d, int dv, const double *x, long
 int gbk_p3m_convolve_gradient_alpha(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
                                     const double *w, long ny, double sigma, const double *alpha, const double *domain,
                                     double spacing_ratio, double padding_factor, double *out);
+/* P3MKernel::ConvolveGradient(X, dim) (:1443-1504): out nx x dv from the gradient kernel `dim`. */
+int gbk_p3m_convolve_gradient_dim(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                                  const double *w, long ny, double sigma, int dim, const double *domain,
+                                  double spacing_ratio, double padding_factor, double *out);
+/* P3MKernel::ConvolveHessian(X) (:1549-1620; Hessian kernels :947-1085): out nx x dv x d x d
+ * (symmetric), from the d(d+1)/2 sampled Hessian entries of the kernel. */
+int gbk_p3m_convolve_hessian(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y, const double *w,
+                             long ny, double sigma, const double *domain, double spacing_ratio, double padding_factor,
+                             double *out);
+/* P3MKernel::ConvolveHessian(X, row, col) (:1622-1687): out nx x dv. */
+int gbk_p3m_convolve_hessian_rowcol(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                                    const double *w, long ny, double sigma, int row, int col, const double *domain,
+                                    double spacing_ratio, double padding_factor, double *out);
+/* P3MKernel::ConvolveGradient(X, k, dp) and ConvolveHessian(X, k, dp, dq) (:1506-1547, :1689-1729):
+ * the reference checks the indices and returns nx zeros; so do these (out: nx doubles). */
+int gbk_p3m_convolve_gradient_kdp(gbk_ctx *ctx, int d, int dv, long nx, long ny, int k, int dp, double *out);
+int gbk_p3m_convolve_hessian_kdpdq(gbk_ctx *ctx, int d, int dv, long nx, long ny, int k, int dp, int dq, double *out);
 
 /* ---- the image grid (ExactKernel::ConvolveImageFast and the Diffeos image maps) ------------ *
  * An image is its geometry on the host: origin[d], spacing[d] and size[d] (pixels per axis,

@@ -63,18 +63,33 @@ def corners(p, origin, size, s):
     return out
 
 
-def _kernel_images(origin, size, s, sigma):
+def upper_pairs(d):
+    """The Hessian entries (r, c), r <= c, in the reference's order (BuildFFTHessianKernels)."""
+    return [(r, c) for r in range(d) for c in range(r, d)]
+
+
+def _kernel_images(origin, size, s, sigma, hessian=False):
     d = len(size)
     idx = np.indices(size)
     border = np.any(idx <= 0, axis=0)
     x = origin.reshape((d,) + (1,) * d) + idx * s
     c = origin + 0.5 * size * s
     diff = x - c.reshape((d,) + (1,) * d)
-    k = np.exp(-np.sum(diff * diff, axis=0) / (sigma * sigma))
+    s2 = sigma * sigma
+    k = np.exp(-np.sum(diff * diff, axis=0) / s2)
     k[border] = 0.0
-    grads = [np.where(border, 0.0, diff[p] * (-2.0 * k / (sigma * sigma))) for p in range(d)]
+    grads = [np.where(border, 0.0, diff[p] * (-2.0 * k / s2)) for p in range(d)]
     shift = lambda a: np.fft.ifftshift(a)
-    return shift(k), [shift(g) for g in grads]
+    if not hessian:
+        return shift(k), [shift(g) for g in grads]
+    # ExactKernel::EvaluateKernelHessian (ExactKernel.h:113-132) at every non-border grid point
+    hess = []
+    for r, cc in upper_pairs(d):
+        h = diff[r] * diff[cc] * (4.0 * k / (s2 * s2))
+        if r == cc:
+            h = h - 2.0 * k / s2
+        hess.append(shift(np.where(border, 0.0, h)))
+    return shift(k), [shift(g) for g in grads], hess
 
 
 def _splat(y, w, origin, size, s):
@@ -135,3 +150,40 @@ def convolve_gradient_alpha(x, y, w, sigma, alpha, lo=None, hi=None, ratio: floa
     """P3MKernel::ConvolveGradient(X, alpha) = G_i^T alpha_i."""
     g = convolve_gradient(x, y, w, sigma, lo, hi, ratio, padding)
     return np.einsum("ikp,ik->ip", g, np.asarray(alpha, float))
+
+
+def convolve_gradient_dim(x, y, w, sigma, dim, lo=None, hi=None, ratio: float = 0.2, padding: float = 3.0):
+    """P3MKernel::ConvolveGradient(X, dim) (:1443-1504): nx x dv, the gradient kernel `dim`."""
+    if lo is None:
+        lo, hi = domain_of(x, y)
+    origin, size, s = grid(lo, hi, sigma, ratio, padding)
+    _, gk = _kernel_images(origin, size, s, sigma)
+    grids = _splat(y, np.asarray(w, float), origin, size, s)
+    return _interp(x, [_conv(g, gk[dim]) for g in grids], origin, size, s)
+
+
+def convolve_hessian(x, y, w, sigma, lo=None, hi=None, ratio: float = 0.2, padding: float = 3.0):
+    """P3MKernel::ConvolveHessian(X) (:1549-1620): (nx, dv, d, d), symmetric."""
+    if lo is None:
+        lo, hi = domain_of(x, y)
+    origin, size, s = grid(lo, hi, sigma, ratio, padding)
+    _, _, hk = _kernel_images(origin, size, s, sigma, hessian=True)
+    grids = _splat(y, np.asarray(w, float), origin, size, s)
+    d, dv, pairs = len(size), grids.shape[0], upper_pairs(len(size))
+    vals = _interp(x, [_conv(grids[k], hk[p]) for p in range(len(pairs)) for k in range(dv)], origin, size, s)
+    out = np.zeros((len(x), dv, d, d))
+    for p, (r, c) in enumerate(pairs):
+        for k in range(dv):
+            out[:, k, r, c] = out[:, k, c, r] = vals[:, k + dv * p]
+    return out
+
+
+def convolve_hessian_rowcol(x, y, w, sigma, row, col, lo=None, hi=None, ratio: float = 0.2, padding: float = 3.0):
+    """P3MKernel::ConvolveHessian(X, row, col) (:1622-1687): nx x dv."""
+    if lo is None:
+        lo, hi = domain_of(x, y)
+    origin, size, s = grid(lo, hi, sigma, ratio, padding)
+    _, _, hk = _kernel_images(origin, size, s, sigma, hessian=True)
+    grids = _splat(y, np.asarray(w, float), origin, size, s)
+    p = upper_pairs(len(size)).index((min(row, col), max(row, col)))
+    return _interp(x, [_conv(g, hk[p]) for g in grids], origin, size, s)

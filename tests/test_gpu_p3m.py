@@ -119,3 +119,39 @@ def test_p3m_points_outside_the_domain(gb, d):
     assert np.linalg.norm(v - rv) <= 1e-10 * np.linalg.norm(rv)
     assert np.linalg.norm(ga - rga) <= 1e-10 * np.linalg.norm(rga)
     assert np.count_nonzero(np.all(v == 0, axis=1)) > 0  # targets off the grid get nothing
+
+
+@pytest.mark.parametrize("d,mode,tol", [(2, "F64", 1e-10), (3, "F64", 1e-10), (3, "F32C", 1e-5)])
+def test_p3m_kernel_object_all_overloads(gb, K, d, mode, tol):
+    """GB300P3MKernel: every overload of the reference's P3MKernel against the restatement (the two
+    stubs return zeros, as the reference's), Hessians within 8e-2 of the exact sums."""
+    from oracle import p3m
+    rng = np.random.default_rng(40 + d)
+    x, y = rng.random((220, d)), rng.random((240, d))
+    w, a = rng.normal(size=(240, 2)), rng.normal(size=(220, 2))
+    sigma = 0.25
+    k = gb.GB300P3MKernel(d, sigma, context=gb.Context(mode=getattr(gb, f"GBK_MODE_{mode}")))
+    k.SetSources(y)
+    k.SetWeights(w)
+    nrm = lambda got, ref: np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert nrm(k.Convolve(x), p3m.convolve(x, y, w, sigma)) <= tol
+    rg = p3m.convolve_gradient(x, y, w, sigma)
+    assert nrm(k.ConvolveGradient(x), rg) <= tol
+    assert nrm(k.ConvolveGradient(x, a), np.einsum("ikp,ik->ip", rg, a)) <= tol
+    for dim in range(d):
+        assert nrm(k.ConvolveGradient(x, dim), rg[:, :, dim]) <= tol
+    rh = p3m.convolve_hessian(x, y, w, sigma)
+    h = k.ConvolveHessian(x)
+    assert h.shape == (220, 2, d, d) and nrm(h, rh) <= tol
+    assert np.array_equal(h, np.swapaxes(h, 2, 3))
+    assert nrm(k.ConvolveHessian(x, d - 1, 0), rh[:, :, 0, d - 1]) <= tol
+    he = np.asarray(K.hess_full(x, y, w, sigma)).reshape(rh.shape)
+    assert np.linalg.norm(h - he) <= 8e-2 * np.linalg.norm(he)
+    assert np.array_equal(k.ConvolveGradient(x, 1, 0), np.zeros(220))
+    assert np.array_equal(k.ConvolveHessian(x, 1, 0, d - 1), np.zeros(220))
+    with pytest.raises(gb.GBKError):
+        k.ConvolveGradient(x, 2, 0)  # weight index out of range, as the reference throws
+    with pytest.raises(gb.GBKError):
+        k.ConvolveGradient(x, d)  # dimension out of range
+    with pytest.raises(gb.GBKError):
+        k.ConvolveHessian(x, 0, d)

@@ -32,3 +32,24 @@ def test_approximation_error(K, d, sigma):
     assert np.linalg.norm(g - ge) <= 8e-2 * np.linalg.norm(ge)
     gv = p3m.convolve_gradient(x, y, w, sigma)
     np.testing.assert_allclose(np.einsum("ikp,ik->ip", gv, a), g, rtol=1e-12, atol=1e-12)
+
+
+def test_gradient_dim_and_hessian_restatements():
+    """P3MKernel::ConvolveGradient(X, dim) is the dim column of ConvolveGradient(X); ConvolveHessian(X)
+    is symmetric and its (row, col) entry is ConvolveHessian(X, row, col); both within the
+    reference's 8e-2 of the exact sums."""
+    import oracle
+    from oracle import p3m
+    K = oracle.load("port")
+    rng = np.random.default_rng(8)
+    x, y, w = rng.random((60, 3)), rng.random((70, 3)), rng.normal(size=(70, 2))
+    g = p3m.convolve_gradient(x, y, w, 0.3)
+    for dim in range(3):
+        assert np.array_equal(p3m.convolve_gradient_dim(x, y, w, 0.3, dim), g[:, :, dim])
+    h = p3m.convolve_hessian(x, y, w, 0.3)
+    assert np.array_equal(h, np.swapaxes(h, 2, 3))
+    assert np.array_equal(p3m.convolve_hessian_rowcol(x, y, w, 0.3, 2, 1), h[:, :, 1, 2])
+    he = np.asarray(K.hess_full(x, y, w, 0.3)).reshape(h.shape)
+    assert np.linalg.norm(h - he) <= 8e-2 * np.linalg.norm(he)
+    ge = np.asarray(K.grad_dim(x, y, w, 0.3, 1)).reshape(60, 2)
+    assert np.linalg.norm(g[:, :, 1] - ge) <= 8e-2 * np.linalg.norm(ge)

@@ -313,6 +313,39 @@ class GB300ExactKernel:
         raise TypeError("ConvolveHessian takes (X), (X, row, col) or (X, k, dp, dq)")
 
     def ConvolveSpecialHessian(self, xi):
+        """AbstractKernel::ConvolveSpecialHessian (AbstractKernel.cxx:22-88), which P3MKernel
+        inherits: composed on the host, as the reference does, from ConvolveHessian(Y) and
+        ConvolveHessian(Y, r, q) with the weights beta x xi[:, r] (and their pairs), each a device
+        particle-mesh sum. Host arrays (N x PointDim)."""
+        Y, beta = self._yw()
+        Y, beta = np.asarray(Y.cpu() if _is_torch(Y) else Y), np.asarray(beta.cpu() if _is_torch(beta) else beta)
+        xi = np.ascontiguousarray(np.asarray(xi.cpu() if _is_torch(xi) else xi, dtype=np.float64))
+        d = self.d
+        if beta.shape[1] != d:
+            raise RuntimeError("ConvolveSpecialHessian needs weights with PointDim columns")
+        if xi.shape != Y.shape:
+            raise RuntimeError("Y and Xi count mismatch")
+        n = Y.shape[0]
+        kw = self._kw()
+        ha = p3m_convolve_hessian(Y, Y, beta, self.m_KernelWidth, **kw)
+        out = np.zeros((n, d))
+        for i in range(n):
+            aux = np.zeros((d, d))
+            for dim in range(d):
+                aux -= ha[i, dim] * beta[i, dim]
+            out[i] = aux @ xi[i]
+        H = np.zeros((n, d, d))
+        for r in range(d):
+            wd = np.ascontiguousarray(beta * xi[:, r:r + 1])
+            H[:, r, :] += p3m_convolve_hessian_rowcol(Y, Y, wd, self.m_KernelWidth, r, r, **kw)
+            for q in range(r + 1, d):
+                wt = np.ascontiguousarray(np.concatenate([wd, beta * xi[:, q:q + 1]], axis=1))
+                hrq = p3m_convolve_hessian_rowcol(Y, Y, wt, self.m_KernelWidth, r, q, **kw)
+                H[:, q, :] += hrq[:, :d]
+                H[:, r, :] += hrq[:, d:]
+        return out + np.einsum("irc,ic->ir", H, beta)
+
+    def ConvolveSpecialHessian(self, xi):
         """AbstractKernel::ConvolveSpecialHessian (AbstractKernel.cxx:22-88)."""
         Y, W = self._yw()
         if W.shape[1] != self.d:
@@ -525,3 +558,36 @@ class GB300P3MKernel:
                                                                        int(args[2]), _hptr(out)))
             return out
         raise TypeError("ConvolveHessian takes (X), (X, row, col) or (X, k, dp, dq)")
+
+    def ConvolveSpecialHessian(self, xi):
+        """AbstractKernel::ConvolveSpecialHessian (AbstractKernel.cxx:22-88), which P3MKernel
+        inherits: composed on the host, as the reference does, from ConvolveHessian(Y) and
+        ConvolveHessian(Y, r, q) with the weights beta x xi[:, r] (and their pairs), each a device
+        particle-mesh sum. Host arrays (N x PointDim)."""
+        Y, beta = self._yw()
+        Y, beta = np.asarray(Y.cpu() if _is_torch(Y) else Y), np.asarray(beta.cpu() if _is_torch(beta) else beta)
+        xi = np.ascontiguousarray(np.asarray(xi.cpu() if _is_torch(xi) else xi, dtype=np.float64))
+        d = self.d
+        if beta.shape[1] != d:
+            raise RuntimeError("ConvolveSpecialHessian needs weights with PointDim columns")
+        if xi.shape != Y.shape:
+            raise RuntimeError("Y and Xi count mismatch")
+        n = Y.shape[0]
+        kw = self._kw()
+        ha = p3m_convolve_hessian(Y, Y, beta, self.m_KernelWidth, **kw)
+        out = np.zeros((n, d))
+        for i in range(n):
+            aux = np.zeros((d, d))
+            for dim in range(d):
+                aux -= ha[i, dim] * beta[i, dim]
+            out[i] = aux @ xi[i]
+        H = np.zeros((n, d, d))
+        for r in range(d):
+            wd = np.ascontiguousarray(beta * xi[:, r:r + 1])
+            H[:, r, :] += p3m_convolve_hessian_rowcol(Y, Y, wd, self.m_KernelWidth, r, r, **kw)
+            for q in range(r + 1, d):
+                wt = np.ascontiguousarray(np.concatenate([wd, beta * xi[:, q:q + 1]], axis=1))
+                hrq = p3m_convolve_hessian_rowcol(Y, Y, wt, self.m_KernelWidth, r, q, **kw)
+                H[:, q, :] += hrq[:, :d]
+                H[:, r, :] += hrq[:, d:]
+        return out + np.einsum("irc,ic->ir", H, beta)

@@ -187,3 +187,31 @@ def convolve_hessian_rowcol(x, y, w, sigma, row, col, lo=None, hi=None, ratio: f
     grids = _splat(y, np.asarray(w, float), origin, size, s)
     p = upper_pairs(len(size)).index((min(row, col), max(row, col)))
     return _interp(x, [_conv(g, hk[p]) for g in grids], origin, size, s)
+
+
+def special_hessian(y, w, sigma, xi, lo=None, hi=None, ratio: float = 0.2, padding: float = 3.0):
+    """AbstractKernel::ConvolveSpecialHessian (AbstractKernel.cxx:22-88) composed from this P3M's
+    ConvolveHessian(Y) and ConvolveHessian(Y, r, q) with the reference's re-weightings (P3MKernel
+    inherits it): N x d for sources y, weights beta = w (N x d) and xi (N x d)."""
+    y, beta, xi = (np.asarray(a, float) for a in (y, w, xi))
+    if lo is None:
+        lo, hi = domain_of(y, y)
+    n, d = y.shape
+    ha = convolve_hessian(y, y, beta, sigma, lo, hi, ratio, padding)  # (N, dv = d, d, d)
+    out = np.zeros((n, d))
+    for i in range(n):
+        aux = np.zeros((d, d))
+        for dim in range(d):
+            aux -= ha[i, dim] * beta[i, dim]
+        out[i] = aux @ xi[i]
+    H = np.zeros((n, d, d))
+    for r in range(d):
+        wd = beta * xi[:, r:r + 1]
+        hrr = convolve_hessian_rowcol(y, y, wd, sigma, r, r, lo, hi, ratio, padding)
+        H[:, r, :] += hrr
+        for q in range(r + 1, d):
+            wt = np.concatenate([wd, beta * xi[:, q:q + 1]], axis=1)
+            hrq = convolve_hessian_rowcol(y, y, wt, sigma, r, q, lo, hi, ratio, padding)
+            H[:, q, :] += hrq[:, :d]
+            H[:, r, :] += hrq[:, d:]
+    return out + np.einsum("irc,ic->ir", H, beta)

@@ -155,3 +155,18 @@ def test_p3m_kernel_object_all_overloads(gb, K, d, mode, tol):
         k.ConvolveGradient(x, d)  # dimension out of range
     with pytest.raises(gb.GBKError):
         k.ConvolveHessian(x, 0, d)
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_p3m_special_hessian(gb, K, d):
+    from oracle import p3m
+    rng = np.random.default_rng(60 + d)
+    y, b, xi = rng.random((150, d)), rng.normal(size=(150, d)), rng.normal(size=(150, d))
+    k = gb.GB300P3MKernel(d, 0.3, context=gb.Context(mode=gb.GBK_MODE_F64))
+    k.SetSources(y)
+    k.SetWeights(b)
+    got = k.ConvolveSpecialHessian(xi)
+    ref = p3m.special_hessian(y, b, 0.3, xi)
+    assert np.linalg.norm(got - ref) <= 1e-10 * np.linalg.norm(ref)
+    ex = np.asarray(K.special_hessian(y, b, 0.3, xi)).reshape(ref.shape)
+    assert np.linalg.norm(got - ex) <= 8e-2 * np.linalg.norm(ex)

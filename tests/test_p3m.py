@@ -53,3 +53,16 @@ def test_gradient_dim_and_hessian_restatements():
     assert np.linalg.norm(h - he) <= 8e-2 * np.linalg.norm(he)
     ge = np.asarray(K.grad_dim(x, y, w, 0.3, 1)).reshape(60, 2)
     assert np.linalg.norm(g[:, :, 1] - ge) <= 8e-2 * np.linalg.norm(ge)
+
+
+def test_special_hessian_composition():
+    """AbstractKernel::ConvolveSpecialHessian composed from the P3M Hessians (as P3MKernel inherits
+    it) stays within the reference's 8e-2 of the exact special Hessian."""
+    import oracle
+    from oracle import p3m
+    K = oracle.load("port")
+    rng = np.random.default_rng(3)
+    y, b, xi = rng.random((80, 3)), rng.normal(size=(80, 3)), rng.normal(size=(80, 3))
+    sh = p3m.special_hessian(y, b, 0.3, xi)
+    ex = np.asarray(K.special_hessian(y, b, 0.3, xi)).reshape(sh.shape)
+    assert np.linalg.norm(sh - ex) <= 8e-2 * np.linalg.norm(ex)

@@ -158,7 +158,6 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     return from_rows(out, b.ny, PointDim);
   }
 
- private:
   // ExactKernel::ConvolveImageFast (ExactKernel.cxx:76-129) on the device: the image's origin,
   // spacing and size go to the C ABI; images with a non-identity direction are refused (the
   // library's pixel geometry is origin + spacing x index).
@@ -186,6 +185,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     return from_rows(out, X.rows(), PointDim);
   }
 
+ private:
   struct Buffers {
     VectorType x, y, w;
     unsigned ny, dv;

@@ -54,8 +54,9 @@ def test_reference_binding_compiles_and_reports_errors(tmp_path):
         pytest.skip("reference tree not available")
     src = tmp_path / "binding_main.cxx"
     src.write_text(
-        '#include "GB300ExactKernel.h"\n#include <cstdio>\n'
+        '#include "GB300ExactKernel.h"\n#include "GB300P3MKernel.h"\n#include <cstdio>\n'
         "template class GB300ExactKernel<double, 2>;\ntemplate class GB300ExactKernel<double, 3>;\n"
+        "template class GB300P3MKernel<double, 2>;\ntemplate class GB300P3MKernel<double, 3>;\n"
         "int main() {\n  GB300ExactKernel<double, 3> k;\n  MatrixType Y(5, 3, 0.5), W(5, 3, 1.0), X(4, 3, 0.25);\n"
         "  k.SetSources(Y); k.SetWeights(W); k.SetKernelWidth(0.3);\n"
         "  try { MatrixType V = k.Convolve(X); std::printf(\"ran %u\\n\", V.rows()); return 0; }\n"

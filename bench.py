@@ -783,6 +783,28 @@ def sweep_mixture(ns, ds, sigmas, fp64_max_n: int = 100_000, sample: int = 4096)
     return 0
 
 
+def threaded_fwd_adjoint(lib, x, y, w, sigma, a, nthreads: int):
+    """The reference's forward + adjoint with its four kernel calls split into blocks of target rows
+    run on nthreads host threads (every output row depends on its own target row only; the calls
+    release the GIL): the reference's single-threaded ExactKernel on all host cores, as its atlas
+    runs one kernel object per thread."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def split(fn, X, Y, W, A=None):
+        blocks = np.array_split(np.arange(X.shape[0]), nthreads)
+        jobs = [(np.ascontiguousarray(X[b]), None if A is None else np.ascontiguousarray(A[b])) for b in blocks]
+        with ThreadPoolExecutor(nthreads) as ex:
+            outs = list(ex.map(lambda j: fn(j[0], Y, W, sigma) if j[1] is None else fn(j[0], Y, W, sigma, j[1]),
+                               jobs))
+        return np.concatenate(outs, axis=0)
+
+    v = split(lib.convolve, x, y, w)
+    gx = split(lib.grad_alpha, x, y, w, a)
+    gw = split(lib.convolve, y, x, a)
+    gy = split(lib.grad_alpha, y, x, a, w)
+    return v, gx, gy, gw
+
+
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return 0
@@ -796,16 +818,21 @@ def run_reference_arm(args, rank, world):
         kind = "reference"
     except Exception:
         pass
+    nthreads = os.cpu_count() or 1
+    if kind == "reference":  # single-threaded per call: row blocks on every host thread
+        step = lambda xs, ys, ws, as_: threaded_fwd_adjoint(lib, xs, ys, ws, 0.1, as_, nthreads)
+    else:  # the C port threads its own loops
+        step = lambda xs, ys, ws, as_: lib.fwd_adjoint(xs, ys, ws, 0.1, as_)
     for _ in range(args.warmup if args.warmup < 1 else 1):
-        lib.fwd_adjoint(x[:256], y[:256], w[:256], 0.1, a[:256])
+        step(x[:256], y[:256], w[:256], a[:256])
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        lib.fwd_adjoint(x, y, w, 0.1, a)
+        step(x, y, w, a)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * statistics.mean(times)
     value = sample * sample / (ms / 1e3)
-    cores = 1 if kind == "reference" else int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cores = nthreads if kind == "reference" else int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

@@ -558,7 +558,7 @@ def small_kernel_bench(n: int = 4096, sigma: float = 0.2, reps: int = 50, cpu: b
 
 
 def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float = 0.1, n_check: int = 4096,
-              n_cpu: int = 20_000):
+              n_cpu: int = 20_000, spacing_ratio: float = 0.2):
     """The particle-mesh kernel (the reference's P3MKernel: grid spacing 0.2 sigma, padding 3 sigma)
     on the headline workload: N = M = 1e6 points of the 8-Gaussian mixture, sigma 0.1, Convolve
     and ConvolveGradient(X, alpha) from device arrays, timed per call with FP32 grids (f32c, the
@@ -583,8 +583,10 @@ def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float 
     Xs, As = X[:n_check].contiguous(), A[:n_check].contiguous()
     exact = {"convolve": k.Convolve(Xs).cpu().numpy(), "gradient_alpha": k.ConvolveGradient(Xs, As).cpu().numpy()}
     for mode, c in (("f32c", ctx), ("f64", ctx64)):
-        calls = (("convolve", lambda: g.p3m_convolve(X, Y, W, sigma, domain=dom, context=c)),
-                 ("gradient_alpha", lambda: g.p3m_convolve_gradient_alpha(X, Y, W, sigma, A, domain=dom, context=c)))
+        calls = (("convolve", lambda: g.p3m_convolve(X, Y, W, sigma, domain=dom, spacing_ratio=spacing_ratio,
+                                                     context=c)),
+                 ("gradient_alpha", lambda: g.p3m_convolve_gradient_alpha(X, Y, W, sigma, A, domain=dom,
+                                                                          spacing_ratio=spacing_ratio, context=c)))
         for name, fn in calls:
             for _ in range(3):
                 out = fn()
@@ -600,12 +602,14 @@ def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float 
                                "rel_l2_err_vs_exact": err}
     res["err_sample"] = f"first {n_check} targets vs the exact FP64 GPU sum over all {n} sources"
     from oracle import p3m as p3m_oracle
-    origin, size, s = p3m_oracle.grid(lo, hi, sigma)
+    origin, size, s = p3m_oracle.grid(lo, hi, sigma, spacing_ratio)
     res["grid"] = [int(v) for v in size]
+    res["spacing_ratio"] = spacing_ratio
     if cpu:
         xs, ys, ws, as_ = x[:n_cpu], y[:n_cpu], w[:n_cpu], a[:n_cpu]
-        for name, fn in (("convolve", lambda: p3m_oracle.convolve(xs, ys, ws, sigma, lo, hi)),
-                         ("gradient_alpha", lambda: p3m_oracle.convolve_gradient_alpha(xs, ys, ws, sigma, as_, lo, hi))):
+        for name, fn in (("convolve", lambda: p3m_oracle.convolve(xs, ys, ws, sigma, lo, hi, spacing_ratio)),
+                         ("gradient_alpha", lambda: p3m_oracle.convolve_gradient_alpha(xs, ys, ws, sigma, as_, lo, hi,
+                                                                                       spacing_ratio))):
             t0 = time.perf_counter()
             fn()
             dt = time.perf_counter() - t0

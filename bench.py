@@ -557,6 +557,16 @@ def small_kernel_bench(n: int = 4096, sigma: float = 0.2, reps: int = 50, cpu: b
     return res
 
 
+def p3m_grid_size(lo, hi, sigma: float, ratio: float, padding: float = 3.0):
+    """Points per axis of the particle-mesh grid (P3MKernel::DetermineGrids): the padded domain
+    length over the spacing, truncated, rounded up to a power of two."""
+    out = []
+    for l, h in zip(lo, hi):
+        n = max(int((h - l + 2 * padding * sigma) / (ratio * sigma)), 1)
+        out.append(1 << (n - 1).bit_length())
+    return out
+
+
 def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float = 0.1, n_check: int = 4096,
               n_cpu: int = 20_000, spacing_ratio: float = 0.2):
     """The particle-mesh kernel (the reference's P3MKernel: grid spacing 0.2 sigma, padding 3 sigma)
@@ -601,11 +611,10 @@ def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float 
             res[name][mode] = {"s_per_call": dt, "pairs_per_s_equivalent": float(n) * n / dt,
                                "rel_l2_err_vs_exact": err}
     res["err_sample"] = f"first {n_check} targets vs the exact FP64 GPU sum over all {n} sources"
-    from oracle import p3m as p3m_oracle
-    origin, size, s = p3m_oracle.grid(lo, hi, sigma, spacing_ratio)
-    res["grid"] = [int(v) for v in size]
+    res["grid"] = p3m_grid_size(lo, hi, sigma, spacing_ratio)
     res["spacing_ratio"] = spacing_ratio
     if cpu:
+        from oracle import p3m as p3m_oracle
         xs, ys, ws, as_ = x[:n_cpu], y[:n_cpu], w[:n_cpu], a[:n_cpu]
         for name, fn in (("convolve", lambda: p3m_oracle.convolve(xs, ys, ws, sigma, lo, hi, spacing_ratio)),
                          ("gradient_alpha", lambda: p3m_oracle.convolve_gradient_alpha(xs, ys, ws, sigma, as_, lo, hi,
@@ -642,9 +651,10 @@ def image_bench(reps: int = 5, cpu: bool = True, n: int = 128, sigma: float = 4.
     k.SetSources(Y)
     k.SetWeights(W)
     L = int(6 * sigma)
-    from oracle import image as IM
-    _, _, lo, hi, _ = IM.windows(cp, sigma, im.origin, im.spacing, im.size)
-    win_pairs = float(np.prod(hi - lo, axis=1).sum())
+    # pixels per window: int(6 sigma) per axis from the rounded index of y - 3 sigma, cropped
+    start = np.floor((cp - 3 * sigma - im.origin) / im.spacing + 0.5).astype(np.int64)
+    lo, hi = np.maximum(start, 0), np.minimum(start + L, im.size)
+    win_pairs = float(np.prod(np.maximum(hi - lo, 0), axis=1).sum())
     res = {"workload": f"{n}^3 image, {len(cp)} control points, sigma {sigma} pixels (windows of {L}^3), "
                        f"T = {T} Heun for the flow",
            "window_pairs_per_call": win_pairs, "full_pairs_per_call": float(im.pixels) * len(cp)}
@@ -679,6 +689,7 @@ def image_bench(reps: int = 5, cpu: bool = True, n: int = 128, sigma: float = 4.
         dt = timed(lambda: g.flow_image_maps(P, M, sigma, im, heun=True, fast=fast, context=c))
         res[name] = {"s_per_flow": dt, "kernel_sums": 2 * (T - 1)}
     if cpu:
+        from oracle import image as IM
         t0 = time.perf_counter()
         IM.convolve_image_fast(x, cp, mom, sigma, im.origin, im.spacing, im.size)
         dt = time.perf_counter() - t0

@@ -611,6 +611,16 @@ def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float 
             res[name][mode] = {"s_per_call": dt, "pairs_per_s_equivalent": float(n) * n / dt,
                                "rel_l2_err_vs_exact": err}
     res["err_sample"] = f"first {n_check} targets vs the exact FP64 GPU sum over all {n} sources"
+    # ConvolveHessian(X): dv x d(d+1)/2 = 18 images, FP32 grids (timing only)
+    fn = lambda: g.p3m_convolve_hessian(X, Y, W, sigma, domain=dom, spacing_ratio=spacing_ratio, context=ctx)
+    for _ in range(2):
+        fn()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fn()
+    torch.cuda.synchronize()
+    res["hessian"] = {"f32c": {"s_per_call": (time.perf_counter() - t0) / reps, "images": 3 * 6}}
     res["grid"] = p3m_grid_size(lo, hi, sigma, spacing_ratio)
     res["spacing_ratio"] = spacing_ratio
     if cpu:

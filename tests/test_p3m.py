@@ -66,3 +66,15 @@ def test_special_hessian_composition():
     sh = p3m.special_hessian(y, b, 0.3, xi)
     ex = np.asarray(K.special_hessian(y, b, 0.3, xi)).reshape(sh.shape)
     assert np.linalg.norm(sh - ex) <= 8e-2 * np.linalg.norm(ex)
+
+
+def test_bench_grid_rule_matches_the_restatement():
+    import bench
+    from oracle import p3m
+    rng = np.random.default_rng(12)
+    for _ in range(20):
+        d = int(rng.integers(2, 4))
+        lo = rng.normal(size=d)
+        hi = lo + rng.uniform(0.1, 3.0, size=d)
+        sigma, ratio = float(rng.uniform(0.03, 0.5)), float(rng.choice([0.1, 0.2, 0.3, 0.5]))
+        assert bench.p3m_grid_size(lo, hi, sigma, ratio) == [int(v) for v in p3m.grid(lo, hi, sigma, ratio)[1]]

@@ -639,6 +639,14 @@ def p3m_bench(reps: int = 5, cpu: bool = True, n: int = 1_000_000, sigma: float 
     return res
 
 
+def image_window_pairs(cp, sigma: float, origin, spacing, size) -> float:
+    """(pixel, control point) pairs of ConvolveImageFast: int(6 sigma) pixels per axis from the
+    rounded index of y - 3 sigma, cropped to the image."""
+    start = np.floor((np.asarray(cp) - 3 * sigma - np.asarray(origin)) / np.asarray(spacing) + 0.5).astype(np.int64)
+    lo, hi = np.maximum(start, 0), np.minimum(start + int(6 * sigma), np.asarray(size))
+    return float(np.prod(np.maximum(hi - lo, 0), axis=1).sum())
+
+
 def image_bench(reps: int = 5, cpu: bool = True, n: int = 128, sigma: float = 4.0, T: int = 11):
     """The image-grid path: a 128^3 image (unit spacing, origin 0), 1,000 control points on the
     cell-centred 10^3 grid of spacing 12.8, momenta N(0, 1) x 0.5, sigma 4 pixels (windows of 24^3
@@ -661,10 +669,7 @@ def image_bench(reps: int = 5, cpu: bool = True, n: int = 128, sigma: float = 4.
     k.SetSources(Y)
     k.SetWeights(W)
     L = int(6 * sigma)
-    # pixels per window: int(6 sigma) per axis from the rounded index of y - 3 sigma, cropped
-    start = np.floor((cp - 3 * sigma - im.origin) / im.spacing + 0.5).astype(np.int64)
-    lo, hi = np.maximum(start, 0), np.minimum(start + L, im.size)
-    win_pairs = float(np.prod(np.maximum(hi - lo, 0), axis=1).sum())
+    win_pairs = image_window_pairs(cp, sigma, im.origin, im.spacing, im.size)
     res = {"workload": f"{n}^3 image, {len(cp)} control points, sigma {sigma} pixels (windows of {L}^3), "
                        f"T = {T} Heun for the flow",
            "window_pairs_per_call": win_pairs, "full_pairs_per_call": float(im.pixels) * len(cp)}

@@ -100,3 +100,15 @@ def test_flow_image_maps_special_cases():
     maps, stop = IM.flow_image_maps(pos, 5 * mom, 1.5, [0.0, 0.0], [1.0, 1.0], size, bbox=box)
     assert stop == T - 2
     assert np.all(maps[: T - 2] == pts[None])
+
+
+def test_bench_window_count_matches_the_restatement():
+    """bench.py counts window pairs without the oracle; the count equals the restatement's windows."""
+    n, sigma = 40, 2.5
+    rng = np.random.default_rng(13)
+    origin, spacing = np.array([0.5, -1.0, 2.0]), np.array([1.0, 0.8, 1.2])
+    cp = origin + spacing * rng.uniform(-5, n + 5, size=(60, 3))
+    import bench
+    _, L, lo, hi, _ = IM.windows(cp, sigma, origin, spacing, [n] * 3)
+    ref = np.prod(np.maximum(hi - lo, 0), axis=1).sum()
+    assert bench.image_window_pairs(cp, sigma, origin, spacing, [n] * 3) == ref

@@ -736,6 +736,28 @@ def fp64_gpu_pairs(n: int, sigma: float):
     return {"value": n * n / (ms / 1e3), "unit": UNIT, "N": n, "ms_per_step": ms}
 
 
+def sweep_errors(port, x, y, w, a, it, jt, sigma, got, cond: bool = True):
+    """Errors of the four forward + adjoint outputs (v, gx on target rows `it`; gy, gw on source rows
+    `jt`) against the FP64 oracle: normwise max_i |err_i| / max_i |ref_i|, max abs, and (cond) the
+    condition-aware error max |err| / sum_j (1 + a_ij) |term_j| (a_ij = |x_i - y_j|^2 / sigma^2, the
+    exponent's condition number) with the plain-magnitude one, max |err| / sum_j |term_j|."""
+    xs, ys, as_, ws = (np.ascontiguousarray(t) for t in (x[it], y[jt], a[it], w[jt]))
+    v, gx, gy, gw = got
+    cases = {"v": (v[it], port.convolve(xs, y, w, sigma), lambda c: port.convolve_mag(xs, y, w, sigma, c)),
+             "gx": (gx[it], port.grad_alpha(xs, y, w, sigma, as_), lambda c: port.grad_alpha_mag(xs, y, w, sigma, as_, c)),
+             "gy": (gy[jt], port.grad_alpha(ys, x, a, sigma, ws), lambda c: port.grad_alpha_mag(ys, x, a, sigma, ws, c)),
+             "gw": (gw[jt], port.convolve(ys, x, a, sigma), lambda c: port.convolve_mag(ys, x, a, sigma, c))}
+    out = {}
+    for key, (g_, r, mag) in cases.items():
+        e = g_ - r
+        out[key] = {"normwise": float(np.linalg.norm(e, axis=1).max() / np.linalg.norm(r, axis=1).max()),
+                    "max_abs": float(np.abs(e).max())}
+        if cond:
+            out[key]["condition_aware"] = float((np.abs(e) / np.maximum(mag(True), 1e-300)).max())
+            out[key]["plain_magnitude"] = float((np.abs(e) / np.maximum(mag(False), 1e-300)).max())
+    return out
+
+
 def sweep_mixture(ns, ds, sigmas, fp64_max_n: int = 100_000, sample: int = 4096):
     """The large kernel-sum + adjoint sweep: fwd+adjoint at N = M for every (N, d, sigma) on the
     8-Gaussian mixture (seed 3), FP32C in the default order; FP64 mode timed too for N <= fp64_max_n.
@@ -774,36 +796,28 @@ def sweep_mixture(ns, ds, sigmas, fp64_max_n: int = 100_000, sample: int = 4096)
             X, Y, W, A = (torch.from_numpy(t).cuda() for t in (x, y, w, a))
             outs = [torch.empty_like(X) for _ in range(4)]
             rng = np.random.default_rng(7)
-            it = np.sort(rng.choice(n, size=min(sample, n), replace=False))
-            jt = np.sort(rng.choice(n, size=min(sample, n), replace=False))
-            xs, ys = np.ascontiguousarray(x[it]), np.ascontiguousarray(y[jt])
+            k_rows = min(sample if n <= 100_000 else 1024, n)  # bounds the FP64 oracle's time per case
+            it = np.sort(rng.choice(n, size=k_rows, replace=False))
+            jt = np.sort(rng.choice(n, size=k_rows, replace=False))
             for sigma in sigmas:
                 ms, ev = timed(ctx, d, n, X, Y, W, A, outs, sigma)
                 got = [o.cpu().numpy() for o in outs]
-                ref = {"v": port.convolve(xs, y, w, sigma), "gx": port.grad_alpha(xs, y, w, sigma, np.ascontiguousarray(a[it])),
-                       "gy": port.grad_alpha(ys, x, a, sigma, np.ascontiguousarray(w[jt])), "gw": port.convolve(ys, x, a, sigma)}
-                mag = {"v": port.convolve(xs, y, np.abs(w), sigma), "gw": port.convolve(ys, x, np.abs(a), sigma)}
-                rows = {"v": it, "gx": it, "gy": jt, "gw": jt}
-                errs = {}
-                for q, (key, r) in enumerate(ref.items()):
-                    gq = got[q][rows[key]]
-                    e = gq - r
-                    errs[key] = {"normwise": float(np.linalg.norm(e, axis=1).max() / np.linalg.norm(r, axis=1).max()),
-                                 "max_abs": float(np.abs(e).max())}
-                    if key in mag:
-                        errs[key]["condition_aware"] = float((np.abs(e) / np.maximum(mag[key], 1e-300)).max())
+                errs = sweep_errors(port, x, y, w, a, it, jt, sigma, got)
                 line = {"sweep": "mixture fwd+adjoint", "N": n, "d": d, "sigma": sigma, "ms": ms,
                         "pairs_per_s": float(n) * n / (ms / 1e3), "evaluated_fraction": ev / (2.0 * n * n),
                         "errors": errs, "error_sample": f"{len(it)} rows vs all {n} partners, FP64 oracle"}
-                if float(n) * n < 2.0 ** 30:  # below the default order's threshold: the spatial order too
-                    ctx.set_order(g.GBK_ORDER_SPATIAL)
-                    ms_s, ev_s = timed(ctx, d, n, X, Y, W, A, outs, sigma)
+                if float(n) * n < 2.0 ** 30:  # below the size rule: every order, timed and checked
+                    line["orders"] = {}
+                    for name, order in (("off", g.GBK_ORDER_OFF), ("two_float", g.GBK_ORDER_TWO_FLOAT),
+                                        ("spatial", g.GBK_ORDER_SPATIAL)):
+                        ctx.set_order(order)
+                        ms_o, ev_o = timed(ctx, d, n, X, Y, W, A, outs, sigma)
+                        got_o = [o.cpu().numpy() for o in outs]
+                        e_o = sweep_errors(port, x, y, w, a, it, jt, sigma, got_o, cond=False)
+                        line["orders"][name] = {
+                            "ms": ms_o, "evaluated_fraction": ev_o / (2.0 * n * n),
+                            "worst_normwise": max(v["normwise"] for v in e_o.values())}
                     ctx.set_order(g.GBK_ORDER_AUTO)
-                    got_s = [o.cpu().numpy() for o in outs]
-                    line["spatial_order"] = {
-                        "ms": ms_s, "pairs_per_s": float(n) * n / (ms_s / 1e3), "evaluated_fraction": ev_s / (2.0 * n * n),
-                        "normwise": {key: float(np.linalg.norm(got_s[q][rows[key]] - r, axis=1).max()
-                                                / np.linalg.norm(r, axis=1).max()) for q, (key, r) in enumerate(ref.items())}}
                 if n <= fp64_max_n:
                     ms64, _ = timed(c64, d, n, X, Y, W, A, [torch.empty_like(X) for _ in range(4)], sigma)
                     line["fp64_gpu"] = {"ms": ms64, "pairs_per_s": float(n) * n / (ms64 / 1e3)}

@@ -10,8 +10,8 @@
 // AbstractAtlas.cxx:218), lazily created on first use.
 //
 // Selecting it takes an enum value GB300Exact in KernelType.h:20-28 and one case in each
-// KernelFactory::CreateKernelObject overload (KernelFactory.cxx:100-117, 128-144, 155-171); see
-// INTEGRATION.md for the full patch.
+// KernelFactory::CreateKernelObject overload (KernelFactory.cxx:100-117, 128-144, 155-171), plus the
+// kernel-type strings of the launchers and of DeformableObjectReader.cxx:473-485.
 #pragma once
 
 #include <memory>

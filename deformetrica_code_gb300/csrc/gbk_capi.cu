@@ -43,6 +43,8 @@ int op_outputs(int op, int d, int dv) {
 }
 
 bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
+  if (variant == VARIANT_TWO_FLOAT || variant == VARIANT_SMALL_TWO_FLOAT)  // Convolve-like ops only
+    return (op == OP_CONV || op == OP_CONV_GRADA || op == OP_GRADA) && find_kernel_conv(op, mode, d, dv, variant, e);
   switch (op) {
     case OP_CONV:
     case OP_CONV_GRADA:
@@ -183,8 +185,63 @@ int gbk_ctx::choose_split(const KernelEntry &e, int d, long nx, long ny) {
   return best_s;
 }
 
+// GBK_ORDER_AUTO: caller order (AUTO_OFF), caller order with adaptive two-float coordinates
+// (AUTO_TWO_FLOAT) or the spatial order (AUTO_SPATIAL).
+//  * Large calls (nx, ny >= 4096 and nx ny >= 2^30) are always ordered: the sort costs about 1 %
+//    there when it does not help, and pruning and accuracy gain when it does.
+//  * Below that, in FP32C mode, Convolve, the alpha-gradient and their fusion run their adaptive
+//    two-float variant in caller order: each CTA whose targets spread wider than kTwoFloatWidth
+//    scaled units forms its differences from hi + lo coordinates, every other CTA runs the one-float
+//    loop, so accuracy no longer depends on the spread and narrow data pays nothing.
+//  * Other ops of at least kAutoMinPairs pairs measure the largest extent of the union of the two
+//    point sets in units of the FP32 coordinate scale (sqrt(log2 e) / sigma per input unit) and take
+//    the spatial order above kAutoCellWidth: in caller order a CTA's targets span the whole set, and
+//    rounding the centred coordinates costs ~u (|x| + |y|) on every difference, while the order's
+//    tiles are no wider than a cell of that width. The extent costs one small launch and one wait
+//    for the stream, so it is skipped while the stream is being captured; within one API call the
+//    decision for the same two point sets is reused.
+//  * Smaller calls and FP64 calls (no centring) follow the size rule alone.
+int gbk_ctx::auto_order(int op, int d, const PairArgs &a, int *choice) {
+  constexpr double kAutoMinPairs = (double)(1L << 22);
+  constexpr double kAutoCellWidth = 16.0;
+  const double pairs = (double)a.nx * (double)a.ny;
+  *choice = AUTO_OFF;
+  if (a.nx >= 4096 && a.ny >= 4096 && pairs >= (double)(1L << 30)) {
+    *choice = AUTO_SPATIAL;
+    return GBK_OK;
+  }
+  if (mode != GBK_MODE_F32C) return GBK_OK;
+  if (op == OP_CONV || op == OP_CONV_GRADA || op == OP_GRADA) {
+    *choice = AUTO_TWO_FLOAT;
+    return GBK_OK;
+  }
+  if (pairs < kAutoMinPairs || capturing()) return GBK_OK;
+  AutoOrder &m = auto_order_cache;
+  const bool same = m.epoch == call_epoch && m.sigma == a.sigma &&
+                    ((m.x == a.x && m.nx == a.nx && m.y == a.y && m.ny == a.ny) ||
+                     (m.x == a.y && m.nx == a.ny && m.y == a.x && m.ny == a.nx));
+  if (!same) {
+    double extent = 0.0;
+    if (int rc = order_extent(this, d, a.x, a.nx, a.y, a.ny, &extent)) return rc;
+    m.epoch = call_epoch;
+    m.x = a.x;
+    m.nx = a.nx;
+    m.y = a.y;
+    m.ny = a.ny;
+    m.sigma = a.sigma;
+    m.wide = !(extent * coord_scale<float>(a.sigma) <= kAutoCellWidth);  // NaN/inf extent: wide
+  }
+  if (m.wide) *choice = AUTO_SPATIAL;
+  return GBK_OK;
+}
+
 int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
   int variant = 0, ns = 0;
+  const bool unordered = !a.xperm && !a.xtiles && a.nx > 0 && a.ny > 0 && a.nx < INT_MAX && a.ny < INT_MAX;
+  int auto_choice = AUTO_OFF;
+  if (unordered && order == GBK_ORDER_AUTO)
+    if (int rc = auto_order(op, d, a, &auto_choice)) return rc;
+  if (unordered && order == GBK_ORDER_TWO_FLOAT && mode == GBK_MODE_F32C) auto_choice = AUTO_TWO_FLOAT;
   auto it = tune.find(key(op, d, dv, a.nx, a.ny));
   if (it != tune.end()) {
     variant = it->second.first;
@@ -202,6 +259,16 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
         variant = VARIANT_SMALL;
     }
   }
+  if (auto_choice == AUTO_TWO_FLOAT) {  // the op's two-float variant, else the spatial order
+    KernelEntry et;
+    const int tv = variant == VARIANT_SMALL ? VARIANT_SMALL_TWO_FLOAT : VARIANT_TWO_FLOAT;
+    if (find_kernel(op, mode, d, dv, tv, &et)) {
+      variant = tv;
+      ns = 0;  // a tuned split belongs to the tuned variant
+    } else {
+      auto_choice = order == GBK_ORDER_AUTO ? AUTO_SPATIAL : AUTO_OFF;
+    }
+  }
   KernelEntry e;
   if (!find_kernel(op, mode, d, dv, variant, &e) && !find_kernel(op, mode, d, dv, 0, &e))
     return fail(GBK_ERR_UNSUPPORTED, "no kernel for op %d, d=%d, dv=%d", op, d, dv);
@@ -209,13 +276,11 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
   if (ns <= 0) ns = choose_split(e, d, a.nx, a.ny);
   // spatial order of targets and sources (see GBK_ORDER_* in gbk.h)
   bool spatial = false, prune = false;
-  if (!a.xperm && !a.xtiles && a.nx > 0 && a.ny > 0 && a.nx < INT_MAX && a.ny < INT_MAX) {
+  if (unordered) {
     switch (order) {
       case GBK_ORDER_SPATIAL: spatial = prune = true; break;
       case GBK_ORDER_SPATIAL_NOPRUNE: spatial = true; break;
-      case GBK_ORDER_AUTO:
-        spatial = prune = a.nx >= 4096 && a.ny >= 4096 && (double)a.nx * (double)a.ny >= (double)(1L << 30);
-        break;
+      case GBK_ORDER_AUTO: spatial = prune = auto_choice == AUTO_SPATIAL; break;
       default: break;
     }
   }
@@ -409,8 +474,17 @@ int gbk_create(int device, gbk_ctx **out) {
     g_create_err = "device allocation of the pair counter failed";
     return GBK_ERR_ALLOC;
   }
+  if (cudaHostAlloc((void **)&c->host_box, 8 * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    c->release();
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    g_create_err = "pinned host allocation of the extent read-back failed";
+    return GBK_ERR_ALLOC;
+  }
   c->order_ticket = reinterpret_cast<unsigned *>(c->pair_counter + 1);
   c->nonfinite = reinterpret_cast<unsigned *>(c->pair_counter + 2);
+  noalloc_refresh_device(device);
   *out = c;
   return GBK_OK;
 }
@@ -446,7 +520,7 @@ int gbk_get_mode(const gbk_ctx *c) { return c ? c->mode : -1; }
 
 int gbk_set_order(gbk_ctx *c, int order) {
   if (!c) return GBK_ERR_ARG;
-  if (order < GBK_ORDER_AUTO || order > GBK_ORDER_SPATIAL_NOPRUNE)
+  if (order < GBK_ORDER_AUTO || order > GBK_ORDER_TWO_FLOAT)
     return c->fail(GBK_ERR_ARG, "unknown order %d", order);
   c->order = order;
   return GBK_OK;
@@ -457,6 +531,12 @@ int gbk_get_order(const gbk_ctx *c) { return c ? c->order : -1; }
 int gbk_set_alloc_limit(gbk_ctx *c, size_t bytes) {
   if (!c) return GBK_ERR_ARG;
   c->alloc_limit = bytes;
+  return GBK_OK;
+}
+
+int gbk_inject_pointer_device(gbk_ctx *c, int device) {
+  if (!c || device < -1) return GBK_ERR_ARG;
+  c->inject_pointer_device = device;
   return GBK_OK;
 }
 

@@ -22,6 +22,12 @@ namespace gbk {
 // (operand bandwidth) against ~78% for scalar FFMA, so both FP32 forms are kept.
 // ---------------------------------------------------------------------------------------------
 struct f32s {};  // tag: scalar FP32 lanes
+// Tag: packed FP32 lanes (as float) with two-float coordinates. Each centred, scaled coordinate is
+// kept as hi + lo, hi = fl32(c) and lo = fl32(c - hi), and a pair's difference is formed as
+// (x_hi - y_hi) + (x_lo - y_lo): its error is ~2u |x - y| instead of ~u (|x| + |y|), so accuracy no
+// longer depends on how far the CTA's points spread from its centre (caller order on data spread
+// wide relative to sigma). Costs 2 packed adds per coordinate per pair.
+struct f32w {};
 
 template <typename T>
 struct Lane;
@@ -49,6 +55,9 @@ struct Lane<float> {
   __device__ __forceinline__ static float get(V v, int l) { return l == 0 ? v.x : v.y; }
   __device__ __forceinline__ static V make(float a, float b) { return make_float2(a, b); }
 };
+
+template <>
+struct Lane<f32w> : Lane<float> {};
 
 template <>
 struct Lane<f32s> {
@@ -94,6 +103,8 @@ struct SrcVal<float> {
   }
 };
 template <>
+struct SrcVal<f32w> : SrcVal<float> {};
+template <>
 struct SrcVal<f32s> {
   __device__ __forceinline__ static float make(double v) { return (float)v; }
 };
@@ -117,6 +128,8 @@ struct Comp {
     sum = s;
   }
 };
+template <>
+struct Comp<f32w> : Comp<float> {};
 template <>
 struct Comp<f32s> {
   __device__ __forceinline__ static void fold(float &sum, float &comp, float run) {
@@ -145,6 +158,10 @@ __host__ __device__ inline double coord_scale<f32s>(double sigma) {
   return 1.2011224087864498 / sigma;
 }
 template <>
+__host__ __device__ inline double coord_scale<f32w>(double sigma) {
+  return 1.2011224087864498 / sigma;
+}
+template <>
 __host__ __device__ inline double coord_scale<double>(double) {
   return 1.0;
 }
@@ -156,6 +173,10 @@ __host__ __device__ inline typename Lane<T>::V exp_arg_scale(double sigma) {
 template <>
 __host__ __device__ inline float2 exp_arg_scale<float>(double sigma) {
   return float2{0.f, 0.f};  // unused: FP32 lanes work on pre-scaled coordinates
+}
+template <>
+__host__ __device__ inline float2 exp_arg_scale<f32w>(double sigma) {
+  return float2{0.f, 0.f};
 }
 
 // Squared distance (input units) beyond which the lane type's kernel value is exactly zero, with
@@ -172,8 +193,5 @@ template <>
 inline double prune_dist2<double>(double sigma) {
   return 800.0 * sigma * sigma;
 }
-
-// Bounded-iteration helpers for any cross-block wait (none of the kernel-sum kernels wait).
-constexpr unsigned long long kSpinLimit = 1ull << 26;
 
 }  // namespace gbk

@@ -39,6 +39,7 @@ struct gbk_ctx {
   int mode = 0;         // GBK_MODE_F32C / GBK_MODE_F64
   int force_split = 0;  // 0 = automatic
   size_t alloc_limit = 0;  // fault injection: buffer growth beyond this fails (0 = none)
+  int inject_pointer_device = -1;  // fault injection: device pointers reported on this GPU (-1 = none)
   long long launches = 0;
   std::string err;
 
@@ -66,6 +67,16 @@ struct gbk_ctx {
   DevBuf order_tmp;           // Morton keys and block boxes
   DevBuf order_cub;           // radix-sort scratch
   DevBuf order_src;           // source rows in sorted order
+  DevBuf order_box;           // the automatic order's extent box and its block partials
+  double *host_box = nullptr; // pinned host copy of that box (allocated by gbk_create)
+  struct AutoOrder {          // the automatic order's extent test for the point sets of this API call
+    long long epoch = -1;
+    const double *x = nullptr, *y = nullptr;
+    long nx = 0, ny = 0;
+    double sigma = 0.0;
+    bool wide = false;        // spread wider than a cell of the spatial order
+  } auto_order_cache;
+  enum { AUTO_OFF = 0, AUTO_TWO_FLOAT = 1, AUTO_SPATIAL = 2 };
   unsigned long long *pair_counter = nullptr;  // device: pairs evaluated by launch(), then a ticket
   unsigned *order_ticket = nullptr;            // device: in the pair counter's allocation
   unsigned *nonfinite = nullptr;               // device: a pruned launch's targets hold a NaN or inf
@@ -82,6 +93,7 @@ struct gbk_ctx {
   int occupancy(const gbk::KernelEntry &e, int d);
   int choose_split(const gbk::KernelEntry &e, int d, long nx, long ny);
   int launch(int op, int d, int dv, gbk::PairArgs a);
+  int auto_order(int op, int d, const gbk::PairArgs &a, int *choice);
 
   // Lets launches of one API call reuse spatial sorts of the same (unchanged) rows.
   struct OrderCacheScope {
@@ -124,10 +136,13 @@ struct gbk_ctx {
     fr(order_tmp);
     fr(order_cub);
     fr(order_src);
+    fr(order_box);
     if (pair_counter) cudaFree(pair_counter);
     pair_counter = nullptr;
     order_ticket = nullptr;
     nonfinite = nullptr;
     for (auto &b : stage) fr(b);
+    if (host_box) cudaFreeHost(host_box);
+    host_box = nullptr;
   }
 };

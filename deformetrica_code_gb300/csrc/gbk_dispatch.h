@@ -24,6 +24,11 @@ enum OpId {
 
 // Launch-shape index for problems too small to fill the GPU with the default shape.
 constexpr int VARIANT_SMALL = 8;
+// Two-float coordinates (lane tag f32w), default and small shapes: compiled for the Convolve and
+// alpha-gradient ops in FP32C mode; chosen by the automatic order for point sets spread wide relative
+// to sigma when sorting them would cost more than it saves (gbk_ctx::launch).
+constexpr int VARIANT_TWO_FLOAT = 9;
+constexpr int VARIANT_SMALL_TWO_FLOAT = 10;
 
 enum Mode { MODE_F32C = 0, MODE_F64 = 1 };
 
@@ -53,8 +58,13 @@ int num_variants(int op, int mode, int d, int dv);
 // Compiled weight-column counts for dimension d, largest first (used to chunk any dv).
 const int *supported_dv(int d, int *count);
 
+// The allocation-free kernel norm's cached scratch address for `device` (current) is looked up
+// again if it was cached (gbk_noalloc.cu); gbk_create calls it.
+void noalloc_refresh_device(int device);
+
 // Per-family lookups (one per instantiation file).
 bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e);
+bool find_kernel_conv_two_float(int op, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_deform(int op, int mode, int d, int dv, int variant, KernelEntry *e);

@@ -11,15 +11,33 @@
 #include "../../include/gbk.h"
 #include "gbk_ctx.h"
 
-inline bool is_device_pointer(const void *p) {
-  if (!p) return true;
+// Where a pointer lives for a context on GPU `device`: kHostMemory (staged through the context's
+// buffers), kThisDevice (device memory of that GPU, or managed memory) or kOtherDevice (device
+// memory of another GPU: the kernels cannot read it without peer access, so the call refuses it).
+// `injected` >= 0 reports every device allocation as memory of that GPU (fault injection, so the
+// other-GPU refusal can be tested with one GPU).
+enum PointerHome { kHostMemory = 0, kThisDevice = 1, kOtherDevice = 2 };
+
+inline PointerHome pointer_home(const void *p, int device, int injected) {
   cudaPointerAttributes at;
-  cudaError_t e = cudaPointerGetAttributes(&at, p);
-  if (e != cudaSuccess) {
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return kHostMemory;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type == cudaMemoryTypeManaged) return kThisDevice;
+  if (at.type != cudaMemoryTypeDevice) return kHostMemory;
+  const int home = injected >= 0 ? injected : at.device;
+  return home == device ? kThisDevice : kOtherDevice;
+}
+
+// Whether p is usable in place by the context's kernels (*dev), refusing device memory of
+// another GPU with GBK_ERR_ARG.
+inline int locate(gbk_ctx *c, const void *p, const char *name, bool *dev) {
+  const PointerHome h = pointer_home(p, c->device, c->inject_pointer_device);
+  *dev = h == kThisDevice;
+  if (h == kOtherDevice)
+    return c->fail(GBK_ERR_ARG, "%s: device memory of another GPU than the context's GPU %d", name, c->device);
+  return GBK_OK;
 }
 
 // Stages host arguments through the context's device buffers.
@@ -36,9 +54,20 @@ struct HostIO {
   std::vector<Out> outs;
   explicit HostIO(gbk_ctx *ctx) : c(ctx) {}
 
+  // Device memory of another GPU is refused with GBK_ERR_ARG before anything is queued.
+  bool device_resident(const void *p, const char *name) {
+    const PointerHome h = pointer_home(p, c->device, c->inject_pointer_device);
+    if (h == kOtherDevice) {
+      rc = c->fail(GBK_ERR_ARG, "%s: device memory of another GPU than the context's GPU %d", name, c->device);
+      return true;
+    }
+    return h == kThisDevice;
+  }
+
   template <typename P>
   const P *in(const P *p, size_t n, const char *name) {
-    if (rc || !p || n == 0 || is_device_pointer(p)) return p;
+    if (rc || !p || n == 0) return p;
+    if (device_resident(p, name)) return rc ? nullptr : p;
     any_host = true;
     if (slot >= gbk_ctx::kStageSlots) {
       rc = c->fail(GBK_ERR_ARG, "too many host arguments");
@@ -52,7 +81,8 @@ struct HostIO {
     return rc ? nullptr : (const P *)b.p;
   }
   double *out(double *p, size_t n, const char *name) {
-    if (rc || !p || n == 0 || is_device_pointer(p)) return p;
+    if (rc || !p || n == 0) return p;
+    if (device_resident(p, name)) return rc ? nullptr : p;
     any_host = true;
     if (slot >= gbk_ctx::kStageSlots) {
       rc = c->fail(GBK_ERR_ARG, "too many host arguments");

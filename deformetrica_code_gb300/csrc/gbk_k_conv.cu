@@ -13,7 +13,7 @@
 // per source), measured 519 ms in every CTA (normwise error 9.8e-7: the expansion loses accuracy
 // when the CTA's target box is wide) and 533 ms when restricted to CTAs whose box has a
 // half-diagonal of at most one scaled unit, so the difference form stays. FP64 uses one target per
-// thread.
+// thread. The two-float-coordinate variants are in gbk_k_conv_tf.cu.
 #include "gbk_dispatch.h"
 
 namespace gbk {
@@ -65,6 +65,8 @@ static bool by_shape(int mode, int d, int dv, int variant, KernelEntry *e) {
 }
 
 bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
+  if (variant == VARIANT_TWO_FLOAT || variant == VARIANT_SMALL_TWO_FLOAT)
+    return mode == MODE_F32C && find_kernel_conv_two_float(op, d, dv, variant, e);
   switch (op) {
     case OP_CONV: return by_shape<OpConv>(mode, d, dv, variant, e);
     case OP_CONV_GRADA: return by_shape<OpCG>(mode, d, dv, variant, e);

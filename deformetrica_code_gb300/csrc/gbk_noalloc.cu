@@ -14,7 +14,11 @@
 //    returns GBK_ERR_ARG without launching anything;
 //  * no cudaMalloc / cudaFree or other allocating routine is called;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress with
-//    that device current); make that first call before any stream capture;
+//    that device current); make that first call before any stream capture: a first call made while
+//    the context's stream is capturing returns GBK_ERR_STATE. gbk_create looks the address up again
+//    for its device if it was cached, so contexts created after a cudaDeviceReset see the new one;
+//  * device memory of another GPU than the context's is refused with GBK_ERR_ARG, as is a NaN
+//    kernel width;
 //  * all calls share the one array: calls that overlap on the GPU (two streams, two host threads)
 //    race on it, so serialise them. Nothing in the array needs to start at zero: each call writes
 //    every element it later reads.
@@ -26,6 +30,7 @@
 #include "../../include/gbk.h"
 #include "gbk_ctx.h"
 #include "gbk_dispatch.h"
+#include "gbk_hostio.h"
 #include "gbk_ops.h"
 
 namespace {
@@ -38,16 +43,22 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles
 std::mutex g_setup_mutex;
 double *g_scratch_addr[kMaxDevices] = {nullptr};
 
-// Device address of the scratch array for `device` (current); looked up once per device.
-int scratch_address(int device, double **out) {
-  if (device < 0 || device >= kMaxDevices) return GBK_ERR_UNSUPPORTED;
+// Device address of the scratch array for `device` (current); looked up once per device. The first
+// lookup may load the module holding the array, which must not happen inside a stream capture.
+int scratch_address(gbk_ctx *c, double **out) {
+  const int device = c->device;
+  if (device < 0 || device >= kMaxDevices)
+    return c->fail(GBK_ERR_UNSUPPORTED, "allocation-free kernel norm: device %d above %d", device, kMaxDevices - 1);
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_addr[device]) {
+    if (c->capturing())
+      return c->fail(GBK_ERR_STATE, "allocation-free kernel norm: the first call on GPU %d must come before "
+                     "stream capture (it looks up the scratch array's address)", device);
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       cudaGetLastError();
-      return GBK_ERR_CUDA;
+      return c->fail(GBK_ERR_CUDA, "cudaGetSymbolAddress of the scratch array: %s", cudaGetErrorString(e));
     }
     g_scratch_addr[device] = static_cast<double *>(p);
   }
@@ -55,32 +66,49 @@ int scratch_address(int device, double **out) {
   return GBK_OK;
 }
 
-bool on_device(const void *p) {
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
-}
-
 }  // namespace
+
+namespace gbk {
+// Called by gbk_create with `device` current: a cached address is looked up again, so a context
+// created after cudaDeviceReset (which unloads the module holding the array) gets the new one.
+void noalloc_refresh_device(int device) {
+  if (device < 0 || device >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch_addr[device]) return;
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) == cudaSuccess && p)
+    g_scratch_addr[device] = static_cast<double *>(p);
+  else
+    g_scratch_addr[device] = nullptr;
+  cudaGetLastError();
+}
+}  // namespace gbk
 
 extern "C" int gbk_kernel_norm_noalloc(gbk_ctx *c, int d, int dv, const double *y, const double *w,
                                        long n, double sigma, double *out) {
   using namespace gbk;
   if (!c) return GBK_ERR_ARG;
-  if (d != 2 && d != 3) return GBK_ERR_UNSUPPORTED;
-  if (dv <= 0 || n <= 0 || !y || !w || !out) return GBK_ERR_ARG;
-  if ((size_t)n * (size_t)dv > kNoAllocScratchDoubles) return GBK_ERR_ARG;  // beyond the scratch
-  if (!on_device(y) || !on_device(w) || !on_device(out)) return GBK_ERR_ARG;  // device pointers only
+  c->err.clear();
+  if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d not supported (2 or 3)", d);
+  if (dv <= 0 || n <= 0) return c->fail(GBK_ERR_ARG, "needs n > 0 points and dv > 0 weight columns");
+  if (!y || !w || !out) return c->fail(GBK_ERR_ARG, "null pointer");
+  if (!(sigma == sigma)) return c->fail(GBK_ERR_ARG, "kernel width is NaN");
+  if ((size_t)n * (size_t)dv > kNoAllocScratchDoubles)
+    return c->fail(GBK_ERR_ARG, "n * dv = %zu is above the scratch capacity of %zu doubles", (size_t)n * dv,
+                   kNoAllocScratchDoubles);
   if (cudaSetDevice(c->device) != cudaSuccess) {
     cudaGetLastError();
-    return GBK_ERR_CUDA;
+    return c->fail(GBK_ERR_CUDA, "cudaSetDevice(%d)", c->device);
+  }
+  const void *args[3] = {y, w, out};
+  const char *names[3] = {"y", "w", "out"};
+  for (int k = 0; k < 3; ++k) {  // device memory of the context's GPU only; nothing is staged
+    bool dev = false;
+    if (int rc = locate(c, args[k], names[k], &dev)) return rc;
+    if (!dev) return c->fail(GBK_ERR_ARG, "%s: host memory (this entry point takes device pointers only)", names[k]);
   }
   double *scratch = nullptr;
-  int rc = scratch_address(c->device, &scratch);
-  if (rc) return rc;
+  if (int rc = scratch_address(c, &scratch)) return rc;
 
   // scratch = [K w : n x dv][split partials : nsplit x chunk width x n]
   double *kw = scratch;
@@ -95,9 +123,12 @@ extern "C" int gbk_kernel_norm_noalloc(gbk_ctx *c, int d, int dv, const double *
         break;
       }
     KernelEntry e;
-    if (!find_kernel(OP_CONV, c->mode, d, cw, 0, &e)) return GBK_ERR_UNSUPPORTED;
+    if (!find_kernel(OP_CONV, c->mode, d, cw, 0, &e)) return c->fail(GBK_ERR_UNSUPPORTED, "no kernel for dv = %d", cw);
     // source splits: enough CTAs for every SM, at most what the free scratch holds
     int occ = 1;
+    if (e.smem > 48 * 1024 &&  // as the launch itself will: the occupancy query needs it first
+        cudaFuncSetAttribute(e.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem) != cudaSuccess)
+      cudaGetLastError();
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, e.kernel, e.block, e.smem) != cudaSuccess || occ < 1) {
       cudaGetLastError();
       occ = 1;
@@ -116,17 +147,12 @@ extern "C" int gbk_kernel_norm_noalloc(gbk_ctx *c, int d, int dv, const double *
     a.out0 = kw + c0;
     a.out0_ld = dv;
     a.partial = ns > 1 ? kw + (size_t)n * dv : nullptr;
-    cudaError_t err = e.fn(a, ns, c->stream);
-    if (err != cudaSuccess) {
-      cudaGetLastError();
-      return GBK_ERR_CUDA;
-    }
+    if (int rc = c->cuda(e.fn(a, ns, c->stream), "kernel launch")) return rc;
+    c->launches += ns > 1 ? 2 : 1;
     c0 += cw;
     rem -= cw;
   }
-  if (dot_f64(c->stream, w, kw, n * (long)dv, out, 0) != cudaSuccess) {
-    cudaGetLastError();
-    return GBK_ERR_CUDA;
-  }
+  if (int rc = c->cuda(dot_f64(c->stream, w, kw, n * (long)dv, out, 0), "FP64 dot")) return rc;
+  c->launches += 1;
   return GBK_OK;
 }

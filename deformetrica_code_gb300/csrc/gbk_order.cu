@@ -156,6 +156,62 @@ __global__ void __launch_bounds__(kThreads) box_kernel(const double *x, long n, 
   }
 }
 
+// Bounding box of the union of two point sets (x then y, one grid-stride loop over both), with the
+// same last-block reduction and self-resetting ticket as box_kernel.
+template <int D>
+__global__ void __launch_bounds__(kThreads) union_box_kernel(const double *x, long nx, const double *y, long ny,
+                                                             double *part, double *box, unsigned *ticket) {
+  __shared__ bool last;
+  double lo[D], hi[D];
+#pragma unroll
+  for (int l = 0; l < D; ++l) {
+    lo[l] = 1e300;
+    hi[l] = -1e300;
+  }
+  const long n = nx + ny;
+  for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
+    const double *p = i < nx ? x + i * D : y + (i - nx) * D;
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+      lo[l] = fmin(lo[l], p[l]);
+      hi[l] = fmax(hi[l], p[l]);
+    }
+  }
+  block_minmax<D>(lo, hi);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+      part[blockIdx.x * 2 * D + l] = lo[l];
+      part[blockIdx.x * 2 * D + D + l] = hi[l];
+    }
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+#pragma unroll
+  for (int l = 0; l < D; ++l) {
+    lo[l] = 1e300;
+    hi[l] = -1e300;
+  }
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads)
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+      lo[l] = fmin(lo[l], __ldcg(part + b * 2 * D + l));
+      hi[l] = fmax(hi[l], __ldcg(part + b * 2 * D + D + l));
+    }
+  block_minmax<D>(lo, hi);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+      box[l] = lo[l];
+      box[D + l] = hi[l];
+    }
+    *ticket = 0u;
+  }
+}
+
 // Morton key of every point, shifted right by `shift` bits (0: full key; 18: level-kMaxLevel cell).
 template <int D>
 __global__ void __launch_bounds__(kThreads) keys_kernel(const double *x, long n, const double *box, int shift,
@@ -438,6 +494,35 @@ cudaError_t unbound_boxes_if_nonfinite(cudaStream_t st, int d, const double *x, 
   const long bb = std::min<long>(std::max<long>((nvals + kThreads - 1) / kThreads, 1), 1216);
   unbound_boxes_kernel<<<(unsigned)bb, kThreads, 0, st>>>(flag, boxes, nvals, d);
   return cudaGetLastError();
+}
+
+int order_extent(gbk_ctx *c, int d, const double *x, long nx, const double *y, long ny, double *extent) {
+  *extent = 0.0;
+  if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "spatial order: dimension %d", d);
+  if (!c->host_box) return c->fail(GBK_ERR_STATE, "spatial order: no pinned read-back buffer");
+  const size_t o_box = al((size_t)kBoxBlocks * 2 * 3 * 8);
+  if (int rc = c->ensure(c->order_box, o_box + al(2 * 3 * 8), "extent scratch")) return rc;
+  double *part = (double *)c->order_box.p;
+  double *box = (double *)((char *)c->order_box.p + o_box);
+  const long n = nx + ny;
+  const int nb = (int)std::max<long>(1, std::min<long>(kBoxBlocks, (n + kThreads - 1) / kThreads));
+  if (d == 3)
+    union_box_kernel<3><<<nb, kThreads, 0, c->stream>>>(x, nx, y, ny, part, box, c->order_ticket);
+  else
+    union_box_kernel<2><<<nb, kThreads, 0, c->stream>>>(x, nx, y, ny, part, box, c->order_ticket);
+  if (int rc = c->cuda(cudaGetLastError(), "extent box")) return rc;
+  c->launches += 1;
+  if (int rc = c->cuda(cudaMemcpyAsync(c->host_box, box, 2 * d * sizeof(double), cudaMemcpyDeviceToHost, c->stream),
+                       "extent read-back"))
+    return rc;
+  if (int rc = c->cuda(cudaStreamSynchronize(c->stream), "extent read-back")) return rc;
+  double e = 0.0;
+  for (int l = 0; l < d; ++l) {
+    const double lo = c->host_box[l], hi = c->host_box[d + l];
+    if (lo <= hi) e = std::max(e, hi - lo);  // NaN coordinates are ignored by the box, as by the sort
+  }
+  *extent = e;
+  return GBK_OK;
 }
 
 int order_sort(gbk_ctx *c, int d, const double *x, long n, SortedSet *out) {

@@ -51,6 +51,10 @@ struct OrderView {
   int launches = 0;             // own kernels launched to build it
 };
 
+// Largest coordinate extent of the union of two point sets (max over axes of the union box's
+// width; 0 for empty or all-NaN sets): one box launch and a pinned read-back that waits for the stream.
+int order_extent(gbk_ctx *c, int d, const double *x, long nx, const double *y, long ny, double *extent);
+
 // Sorts n points (steps 1-3) into one of the context's two sort slots, or, inside an order-cache
 // scope of the context, returns the sort of the same rows made earlier in the same API call.
 int order_sort(gbk_ctx *c, int d, const double *x, long n, SortedSet *out);

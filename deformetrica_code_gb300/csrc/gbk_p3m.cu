@@ -552,7 +552,9 @@ static int p3m_zeros(gbk_ctx *c, int d, int dv, long nx, long ny, int k, int dp,
   if (dp < 0 || dp >= d || dq < 0 || dq >= d) return c->fail(GBK_ERR_ARG, "Invalid derivative direction");
   if (nx == 0) return GBK_OK;
   if (!out) return c->fail(GBK_ERR_ARG, "null pointer");
-  if (is_device_pointer(out)) {
+  bool dev = false;
+  if (int rc = locate(c, out, "out", &dev)) return rc;
+  if (dev) {
     if (int rc = c->cuda(cudaMemsetAsync(out, 0, (size_t)nx * sizeof(double), c->stream), "memset")) return rc;
     return c->cuda(cudaStreamSynchronize(c->stream), "sync");
   }

@@ -413,6 +413,10 @@ struct SrcLane<float> {
   typedef float2 SV;
 };
 template <>
+struct SrcLane<f32w> {
+  typedef float2 SV;
+};
+template <>
 struct SrcLane<f32s> {
   typedef float SV;
 };
@@ -429,6 +433,8 @@ struct Pack<float> {
   __device__ __forceinline__ static float2 make(double a, double b) { return make_float2((float)a, (float)b); }
 };
 template <>
+struct Pack<f32w> : Pack<float> {};
+template <>
 struct Pack<f32s> {
   __device__ __forceinline__ static float make(double a, double) { return (float)a; }
 };
@@ -437,10 +443,12 @@ struct Pack<double> {
   __device__ __forceinline__ static double make(double a, double) { return a; }
 };
 
-// Source record length, padded so that a record is a whole number of 16-byte vectors.
+// Source record: D coordinates, the op's NS extras and, for two-float coordinates, the D low
+// parts; padded so that a record is a whole number of 16-byte vectors.
 template <class Op, int D, typename T>
 struct Rec {
-  static constexpr int NJ = D + Op::NS;
+  static constexpr int LO = D + Op::NS;  // first low part (two-float coordinates only)
+  static constexpr int NJ = D + Op::NS + (std::is_same<T, f32w>::value ? D : 0);
   static constexpr int PER16 = 16 / (int)sizeof(typename SrcLane<T>::SV);
   static constexpr int NJP = (NJ + PER16 - 1) / PER16 * PER16;
 };
@@ -455,108 +463,37 @@ constexpr size_t pair_smem_bytes() {
 
 // Source chunks per visit mask (pruning): 512 bytes of shared memory.
 constexpr int kPruneWindow = 4096;
+// Adaptive two-float coordinates (lane tag f32w): a CTA whose target box is wider than this, in units
+// of the FP32 coordinate scale, uses hi + lo coordinates; the spatial order's tiles never are.
+constexpr double kTwoFloatWidth = 16.0;
 
-// FP32 mode subtracts the CTA's target bounding-box midpoint (centring); FP64 mode forms x - y
-// directly, as the reference does. UNR: unroll of the per-source loop. CSM: see pair_smem_bytes.
-// With a spatial order (a.xtiles), the CTA's targets are the sorted positions of its tile, rows
-// a.xperm[...]; sources are visited in sorted order (a.yperm) and a source chunk whose box is
-// farther than a.prune_d2 from the CTA's target box is skipped: every pair term in it is exactly
-// zero, so the sums are the same as when it is visited.
-template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int UNR, int CSM>
-__device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_idx, const int split) {
+// The pair loop of one CTA after its targets and centre are known: stage each source tile, evaluate
+// every (target, source) pair, fold the compensated sums, write the results. TWOF: two-float
+// coordinates (hi + lo parts of targets and staged sources); the record stride follows TWOF, so the
+// one-float loop of an adaptive kernel reads no low parts.
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int UNR, int CSM, bool TWOF>
+__device__ __forceinline__ void pair_body(const PairArgs &a, const int split, const long i0, const long iend,
+                                          const double *ctr, const double *s_box, unsigned *s_visit,
+                                          unsigned char *smem_raw) {
   typedef Lane<T> L;
   typedef typename L::V V;
   typedef typename SrcLane<T>::SV SV;
   constexpr int W = L::kWidth;
-  constexpr int G = R / W;  // lane groups per thread
-  constexpr int NJP = Rec<Op, D, T>::NJP;
+  constexpr int G = R / W;
+  constexpr int LO = D + Op::NS;  // first low part of a record (TWOF)
+  constexpr int NJ = D + Op::NS + (TWOF ? D : 0);
+  constexpr int PER16 = 16 / (int)sizeof(SV);
+  constexpr int NJP = (NJ + PER16 - 1) / PER16 * PER16;
   constexpr int NO = Op::NO;
-  constexpr bool CENTER = !std::is_same<T, double>::value;
-  static_assert(R % W == 0, "R must be a multiple of the lane width");
-  static_assert(TJ % MERGE == 0, "TJ must be a multiple of MERGE");
-  static_assert(BLOCK % 32 == 0 && kPruneWindow % BLOCK == 0, "visit-mask rounds need whole warps");
-
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  static_assert(NJP <= Rec<Op, D, T>::NJP, "the tile is sized for the widest record");
   SV *tile = reinterpret_cast<SV *>(smem_raw);
-  __shared__ double s_red[2 * D][BLOCK / 32];
-  __shared__ double s_ctr[D];
-  __shared__ double s_box[2 * D];
-  __shared__ unsigned s_visit[kPruneWindow / 32];
-
-  // ---- this CTA's targets: sorted positions [i0, iend) (caller order when unsorted) ----
-  long i0, iend;
-  if (a.xtiles) {
-    if (tile_idx >= (long)*a.nxtiles) return;  // beyond the tiles of this order: whole CTA
-    const int2 tl = a.xtiles[tile_idx];
-    i0 = tl.x;
-    iend = tl.y;
-  } else {
-    i0 = tile_idx * (BLOCK * R);
-    iend = i0 + BLOCK * R < a.nx ? i0 + BLOCK * R : a.nx;
-  }
   const int *const xperm = a.xperm;
   const int *const yperm = a.yperm;
   const bool prune = a.ybox != nullptr;
-
-  // ---- bounding box of the CTA's targets (FP64): centre for FP32 lanes, box for pruning ----
-  double ctr[D];
-  if (CENTER || prune) {
-    double lo[D], hi[D];
-#pragma unroll
-    for (int l = 0; l < D; ++l) {
-      lo[l] = 1e300;
-      hi[l] = -1e300;
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      long i = i0 + threadIdx.x + (long)r * BLOCK;
-      if (i < iend) {
-        const long row = xperm ? (long)xperm[i] : i;
-#pragma unroll
-        for (int l = 0; l < D; ++l) {
-          double v = a.x[row * D + l];
-          lo[l] = fmin(lo[l], v);
-          hi[l] = fmax(hi[l], v);
-        }
-      }
-    }
-#pragma unroll
-    for (int l = 0; l < D; ++l) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        lo[l] = fmin(lo[l], __shfl_xor_sync(0xffffffffu, lo[l], o));
-        hi[l] = fmax(hi[l], __shfl_xor_sync(0xffffffffu, hi[l], o));
-      }
-    }
-    if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-      for (int l = 0; l < D; ++l) {
-        s_red[l][threadIdx.x >> 5] = lo[l];
-        s_red[D + l][threadIdx.x >> 5] = hi[l];
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x < D) {
-      double mn = 1e300, mx = -1e300;
-      for (int w2 = 0; w2 < BLOCK / 32; ++w2) {
-        mn = fmin(mn, s_red[threadIdx.x][w2]);
-        mx = fmax(mx, s_red[D + threadIdx.x][w2]);
-      }
-      s_ctr[threadIdx.x] = (CENTER && mn <= mx) ? 0.5 * (mn + mx) : 0.0;
-      s_box[threadIdx.x] = mn;
-      s_box[D + threadIdx.x] = mx;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int l = 0; l < D; ++l) ctr[l] = s_ctr[l];
-  } else {
-#pragma unroll
-    for (int l = 0; l < D; ++l) ctr[l] = 0.0;
-  }
-
   const double xs = a.xscale;
   // ---- this thread's targets: centred, pre-scaled coordinates and extras, in lanes ----
   V xg[G][D];
+  V xlo[G][TWOF ? D : 1];  // low parts of two-float coordinates
   V tg[G][Op::NT > 0 ? Op::NT : 1];
 #pragma unroll
   for (int g = 0; g < G; ++g) {
@@ -572,12 +509,19 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
     }
 #pragma unroll
     for (int l = 0; l < D; ++l) xg[g][l] = Pack<T>::make(xv[0][l], xv[W - 1][l]);
+    if (TWOF) {
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+        const double h0 = (double)(float)xv[0][l], h1 = (double)(float)xv[W - 1][l];
+        xlo[g][l < (TWOF ? D : 1) ? l : 0] = Pack<T>::make(xv[0][l] - h0, xv[W - 1][l] - h1);
+      }
+    }
 #pragma unroll
     for (int k = 0; k < Op::NT; ++k) tg[g][k] = Pack<T>::make(tv[0][k], tv[W - 1][k]);
   }
 
   // running sums / compensation: registers, or shared memory after the tile (CSM)
-  V *csm = reinterpret_cast<V *>(smem_raw + (size_t)TJ * NJP * sizeof(SV));
+  V *csm = reinterpret_cast<V *>(smem_raw + (size_t)TJ * Rec<Op, D, T>::NJP * sizeof(SV));
   V acc[G][NO], sum[G][NO], cmp[G][NO];
 #pragma unroll
   for (int g = 0; g < G; ++g)
@@ -638,12 +582,16 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
 #pragma unroll
         for (int l = 0; l < D; ++l) rec[l] = (ctr[l] - a.y[j * D + l]) * xs;
         Op::load_source(a, j, rec + D);
+        if (TWOF) {
+#pragma unroll
+          for (int l = 0; l < D; ++l) rec[LO + l] = rec[l] - (double)(float)rec[l];
+        }
       } else {
 #pragma unroll
-        for (int q = 0; q < Rec<Op, D, T>::NJ; ++q) rec[q] = 0.0;  // zero weights: exact no-op
+        for (int q = 0; q < NJ; ++q) rec[q] = 0.0;  // zero weights: exact no-op
       }
 #pragma unroll
-      for (int q = Rec<Op, D, T>::NJ; q < NJP; ++q) rec[q] = 0.0;
+      for (int q = NJ; q < NJP; ++q) rec[q] = 0.0;
 #pragma unroll
       for (int q = 0; q < NJP; ++q) tile[r * NJP + q] = SrcVal<T>::make(rec[q]);
     }
@@ -666,6 +614,10 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
           V dx[D];
 #pragma unroll
           for (int l = 0; l < D; ++l) dx[l] = L::add(xg[g][l], s[l]);
+          if (TWOF) {  // (x_hi - y_hi) + (x_lo - y_lo); the staged source values are negated
+#pragma unroll
+            for (int l = 0; l < D; ++l) dx[l] = L::add(dx[l], L::add(xlo[g][l < (TWOF ? D : 1) ? l : 0], s[LO + l]));
+          }
           V r2 = L::mul(dx[0], dx[0]);
 #pragma unroll
           for (int l = 1; l < D; ++l) r2 = L::fma(dx[l], dx[l], r2);
@@ -723,6 +675,110 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
         Op::store(a, xperm ? (long)xperm[i] : i, v);
       }
     }
+  }
+}
+
+// FP32 mode subtracts the CTA's target bounding-box midpoint (centring); FP64 mode forms x - y
+// directly, as the reference does. UNR: unroll of the per-source loop. CSM: see pair_smem_bytes.
+// With a spatial order (a.xtiles), the CTA's targets are the sorted positions of its tile, rows
+// a.xperm[...]; sources are visited in sorted order (a.yperm) and a source chunk whose box is
+// farther than a.prune_d2 from the CTA's target box is skipped: every pair term in it is exactly
+// zero, so the sums are the same as when it is visited.
+template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int UNR, int CSM>
+__device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_idx, const int split) {
+  constexpr bool CENTER = !std::is_same<T, double>::value;
+  static_assert(R % Lane<T>::kWidth == 0, "R must be a multiple of the lane width");
+  static_assert(TJ % MERGE == 0, "TJ must be a multiple of MERGE");
+  static_assert(BLOCK % 32 == 0 && kPruneWindow % BLOCK == 0, "visit-mask rounds need whole warps");
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double s_red[2 * D][BLOCK / 32];
+  __shared__ double s_ctr[D];
+  __shared__ double s_box[2 * D];
+  __shared__ unsigned s_visit[kPruneWindow / 32];
+
+  // ---- this CTA's targets: sorted positions [i0, iend) (caller order when unsorted) ----
+  long i0, iend;
+  if (a.xtiles) {
+    if (tile_idx >= (long)*a.nxtiles) return;  // beyond the tiles of this order: whole CTA
+    const int2 tl = a.xtiles[tile_idx];
+    i0 = tl.x;
+    iend = tl.y;
+  } else {
+    i0 = tile_idx * (BLOCK * R);
+    iend = i0 + BLOCK * R < a.nx ? i0 + BLOCK * R : a.nx;
+  }
+  const int *const xperm = a.xperm;
+  const bool prune = a.ybox != nullptr;
+
+  // ---- bounding box of the CTA's targets (FP64): centre for FP32 lanes, box for pruning ----
+  double ctr[D];
+  if (CENTER || prune) {
+    double lo[D], hi[D];
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+      lo[l] = 1e300;
+      hi[l] = -1e300;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      long i = i0 + threadIdx.x + (long)r * BLOCK;
+      if (i < iend) {
+        const long row = xperm ? (long)xperm[i] : i;
+#pragma unroll
+        for (int l = 0; l < D; ++l) {
+          double v = a.x[row * D + l];
+          lo[l] = fmin(lo[l], v);
+          hi[l] = fmax(hi[l], v);
+        }
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < D; ++l) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        lo[l] = fmin(lo[l], __shfl_xor_sync(0xffffffffu, lo[l], o));
+        hi[l] = fmax(hi[l], __shfl_xor_sync(0xffffffffu, hi[l], o));
+      }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+        s_red[l][threadIdx.x >> 5] = lo[l];
+        s_red[D + l][threadIdx.x >> 5] = hi[l];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < D) {
+      double mn = 1e300, mx = -1e300;
+      for (int w2 = 0; w2 < BLOCK / 32; ++w2) {
+        mn = fmin(mn, s_red[threadIdx.x][w2]);
+        mx = fmax(mx, s_red[D + threadIdx.x][w2]);
+      }
+      s_ctr[threadIdx.x] = (CENTER && mn <= mx) ? 0.5 * (mn + mx) : 0.0;
+      s_box[threadIdx.x] = mn;
+      s_box[D + threadIdx.x] = mx;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int l = 0; l < D; ++l) ctr[l] = s_ctr[l];
+  } else {
+#pragma unroll
+    for (int l = 0; l < D; ++l) ctr[l] = 0.0;
+  }
+
+  if constexpr (std::is_same<T, f32w>::value) {
+    // adaptive two-float coordinates: only a CTA whose targets spread wider than kTwoFloatWidth
+    // scaled units pays for the low parts (in the spatial order no tile is that wide)
+    double width = 0.0;
+#pragma unroll
+    for (int l = 0; l < D; ++l) width = fmax(width, (s_box[D + l] - s_box[l]) * a.xscale);
+    if (!(width <= kTwoFloatWidth))
+      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, true>(a, split, i0, iend, ctr, s_box, s_visit, smem_raw);
+    else
+      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, split, i0, iend, ctr, s_box, s_visit, smem_raw);
+  } else {
+    pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, split, i0, iend, ctr, s_box, s_visit, smem_raw);
   }
 }
 

@@ -9,6 +9,7 @@
 #include "../../include/gbk.h"
 #include "gbk_ctx.h"
 #include "gbk_dispatch.h"
+#include "gbk_hostio.h"
 
 using namespace gbk;
 
@@ -65,16 +66,9 @@ int gbk_kernel_norm(gbk_ctx *c, int d, int dv, const double *y, const double *w,
   if (rc) return rc;
   // Inputs may be host pointers: gbk_convolve stages them; the reduction then needs w on the
   // device, so stage explicitly here.
-  cudaPointerAttributes at;
-  bool dev_w = cudaPointerGetAttributes(&at, w) == cudaSuccess &&
-               (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
-  cudaGetLastError();
-  bool dev_y = cudaPointerGetAttributes(&at, y) == cudaSuccess &&
-               (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
-  cudaGetLastError();
-  bool dev_out = cudaPointerGetAttributes(&at, out) == cudaSuccess &&
-                 (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
-  cudaGetLastError();
+  bool dev_w = false, dev_y = false, dev_out = false;
+  if ((rc = locate(c, w, "w", &dev_w)) || (rc = locate(c, y, "y", &dev_y)) || (rc = locate(c, out, "out", &dev_out)))
+    return rc;
   const double *dw = w, *dy = y;
   gbk_ctx::DevBuf &sw = c->stage[gbk_ctx::kStageSlots - 1];
   gbk_ctx::DevBuf &sy = c->stage[gbk_ctx::kStageSlots - 2];

@@ -86,7 +86,7 @@ class Context:
         self.mode = mode
 
     def set_order(self, order: int):
-        """GBK_ORDER_AUTO / OFF / SPATIAL / SPATIAL_NOPRUNE (include/gbk.h)."""
+        """GBK_ORDER_AUTO / OFF / SPATIAL / SPATIAL_NOPRUNE / TWO_FLOAT (include/gbk.h)."""
         self.check(self.lib.gbk_set_order(self.h, order))
 
     def get_order(self) -> int:
@@ -115,6 +115,12 @@ class Context:
         """Fault injection for tests: device-buffer growth beyond nbytes fails with GBK_ERR_ALLOC
         (0 lifts the limit)."""
         self.check(self.lib.gbk_set_alloc_limit(self.h, int(nbytes)))
+
+    def inject_pointer_device(self, device: int):
+        """Fault injection for tests: device allocations passed from now on are treated as memory
+        of GPU `device` (-1 turns it off), so the refusal of another GPU's memory can be tested on
+        one GPU."""
+        self.check(self.lib.gbk_inject_pointer_device(self.h, int(device)))
 
     def launch_count(self) -> int:
         return int(self.lib.gbk_launch_count(self.h))

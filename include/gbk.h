@@ -8,7 +8,7 @@
  *   src/support/kernels/ExactKernel.cxx             (the FP64 CPU implementation)
  *   src/support/kernels/CUDAExactKernel.cxx:41-320  (the legacy CUDA forwarding)
  *   lib/cuda_convolutions/GpuConv1D.h               (GaussGpu*Conv1D host functions)
- * and is what a new KernelFactory kernel type calls (see INTEGRATION.md).
+ * and is what a new KernelFactory kernel type calls.
  *
  * Conventions (all entry points):
  *  - Matrices are row-major double arrays: n rows x c columns, element (i, k) at p[i * c + k],
@@ -53,16 +53,31 @@ enum {
 enum { GBK_MODE_F32C = 0, GBK_MODE_F64 = 1 };
 
 /* Order in which the kernel sums visit targets and sources (gbk_set_order).
- *  AUTO: SPATIAL for calls with nx, ny >= 4096 and nx * ny >= 2^30, OFF below (where sorting
- *    costs more than a few percent of the sum).
+ *  AUTO: SPATIAL for calls with nx, ny >= 4096 and nx * ny >= 2^30. Below that, in GBK_MODE_F32C,
+ *    Convolve, the alpha-gradient and their fusion run as TWO_FLOAT; other ops of 2^22 pairs or more
+ *    measure the largest extent of the union of the two point sets and run SPATIAL when it is wider
+ *    than 16 sigma / sqrt(log2 e) = 13.3 sigma (where one-float caller order loses accuracy), else
+ *    OFF (the extent costs one small launch and one wait for the stream, and is skipped while the
+ *    stream is being captured). Smaller calls and GBK_MODE_F64 calls below the size rule are OFF.
  *  OFF: rows in caller order, every (target, source) pair evaluated.
  *  SPATIAL: targets and sources sorted along a Morton curve on the device before the sum; each CTA
  *    takes a compact tile of targets (smaller FP32 coordinate rounding after centring) and skips
  *    source chunks too far away to contribute anything but exact zeros in the precision mode.
  *    Outputs are still written in caller row order.
  *  SPATIAL_NOPRUNE: the same order with every pair evaluated (gives the same bits as SPATIAL).
+ *  TWO_FLOAT: caller order; in GBK_MODE_F32C, Convolve, the alpha-gradient and their fusion keep
+ *    the centred coordinates of every CTA whose targets spread wider than 16 units of the FP32
+ *    coordinate scale (13.3 sigma) as two floats (hi + lo), so a pair's difference is accurate to
+ *    ~2u of itself however far the points spread (about 20 % more time in such CTAs; the others
+ *    run as OFF; other ops as OFF).
  * The reference has no counterpart: ExactKernel always visits every pair in row order. */
-enum { GBK_ORDER_AUTO = 0, GBK_ORDER_OFF = 1, GBK_ORDER_SPATIAL = 2, GBK_ORDER_SPATIAL_NOPRUNE = 3 };
+enum {
+  GBK_ORDER_AUTO = 0,
+  GBK_ORDER_OFF = 1,
+  GBK_ORDER_SPATIAL = 2,
+  GBK_ORDER_SPATIAL_NOPRUNE = 3,
+  GBK_ORDER_TWO_FLOAT = 4
+};
 
 /* Gradient formula of the point-cloud and volume-mesh data terms (gbk_set_gradient_mode).
  *  REFERENCE: the reference's formulas. PointCloud::ComputeMatchGradient (PointCloud.cxx:150-198)
@@ -353,10 +368,13 @@ void gbk_registration_destroy(gbk_registration *reg);
  * must all be known in advance). No counterpart in the reference. Allocates nothing: its scratch
  * (the K w intermediate and source-split partials) is a 16 MiB __device__ array in the library,
  * held by every GPU that loads it until the process exits. y, w and `out` (one double) must be
- * device pointers; n * dv above 2^21 (2,097,152) returns GBK_ERR_ARG before any launch. Errors are
- * reported by the return code only (gbk_last_error is not updated). The first call on a device
- * looks up the array's address: make it before any stream capture. All calls share the array, so
- * calls that overlap on the GPU race: serialise them. Queued on the context's stream. */
+ * device pointers of the context's GPU (host memory, another GPU's memory and a NaN kernel width
+ * return GBK_ERR_ARG); n * dv above 2^21 (2,097,152) returns GBK_ERR_ARG before any launch;
+ * gbk_last_error describes every failure. The first call on a device looks up the array's address:
+ * make it before any stream capture (a first call on a capturing stream returns GBK_ERR_STATE).
+ * After a cudaDeviceReset, create a new context on that device before calling again: gbk_create
+ * refreshes the cached address. All calls share the array, so calls that overlap on the GPU race:
+ * serialise them. Queued on the context's stream; counted by gbk_launch_count. */
 int gbk_kernel_norm_noalloc(gbk_ctx *ctx, int d, int dv, const double *y, const double *w, long n,
                             double sigma, double *out);
 
@@ -564,6 +582,10 @@ int gbk_set_split(gbk_ctx *ctx, int nsplit);
  * beyond `bytes` fails with GBK_ERR_ALLOC as if cudaMalloc had failed (0 = no limit). The context
  * stays usable: lift the limit and the same call succeeds. */
 int gbk_set_alloc_limit(gbk_ctx *ctx, size_t bytes);
+/* Fault injection for tests: from now on every device allocation passed to the context is treated as
+ * memory of GPU `device` (-1 = off), so the refusal of another GPU's memory (GBK_ERR_ARG, nothing
+ * queued: the kernels cannot read it without peer access) can be exercised on a one-GPU machine. */
+int gbk_inject_pointer_device(gbk_ctx *ctx, int device);
 
 #ifdef __cplusplus
 }

@@ -18,4 +18,5 @@ from .kernels import (  # noqa: F401
     load,
     port_path,
     reference_path,
+    reference_root,
 )

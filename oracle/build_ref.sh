@@ -8,9 +8,10 @@
 # against the vendored, header-only Armadillo 7.700 (extra/armadillo-7.700.0.tar.xz, extracted
 # into oracle/_ref/) and the small stand-in headers in oracle/ref_shim/, with the reference's
 # RELEASE optimisation level (-O2). Nothing is copied out of the reference tree; all outputs go
-# to oracle/_ref/. Usage: oracle/build_ref.sh [REFERENCE_ROOT]  (default /root/reference).
+# to oracle/_ref/. Usage: oracle/build_ref.sh [REFERENCE_ROOT]  (default: $DEFORMETRICA_REFERENCE_DIR,
+# else the checkout location of this build's container, /root/reference).
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${DEFORMETRICA_REFERENCE_DIR:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/support/kernels" ]; then

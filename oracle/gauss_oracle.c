@@ -107,6 +107,53 @@ int oracle_grad_alpha(int d, int dv, const double *x, long nx, const double *y, 
   return 0;
 }
 
+/* Term-magnitude sums for condition-aware error measures (test denominators; no reference method).
+ * With a_ij = |x_i - y_j|^2 / sigma^2 and weight c_ij = 1 + cond * a_ij (cond = 1: the relative
+ * condition number of each term with respect to its inputs, since exp(-a) has condition a; cond = 0:
+ * the plain sum of |terms|):
+ *   oracle_convolve_mag:   out_ik = sum_j c_ij K_ij |w_jk|
+ *   oracle_grad_alpha_mag: out_il = (2 / sigma^2) sum_j c_ij K_ij (sum_k |alpha_ik| |w_jk|) |x_il - y_jl| */
+int oracle_convolve_mag(int d, int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                        double sigma, int cond, double *out) {
+  CHECK_D(d);
+  const double s2 = sigma * sigma;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < nx; ++i) {
+    double acc[16] = {0};
+    double diff[3];
+    for (long j = 0; j < ny; ++j) {
+      double k = pair_k(d, x + i * d, y + j * d, s2, diff);
+      double r2 = 0.0;
+      for (int l = 0; l < d; ++l) r2 += diff[l] * diff[l];
+      const double c = 1.0 + (cond ? r2 / s2 : 0.0);
+      for (int q = 0; q < dv; ++q) acc[q] += c * k * fabs(w[j * dv + q]);
+    }
+    for (int q = 0; q < dv; ++q) out[i * dv + q] = acc[q];
+  }
+  return 0;
+}
+
+int oracle_grad_alpha_mag(int d, int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                          double sigma, const double *alpha, int cond, double *out) {
+  CHECK_D(d);
+  const double s2 = sigma * sigma;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < nx; ++i) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    double diff[3];
+    for (long j = 0; j < ny; ++j) {
+      double k = pair_k(d, x + i * d, y + j * d, s2, diff);
+      double r2 = 0.0, ab = 0.0;
+      for (int l = 0; l < d; ++l) r2 += diff[l] * diff[l];
+      for (int q = 0; q < dv; ++q) ab += fabs(alpha[i * dv + q]) * fabs(w[j * dv + q]);
+      const double c = 1.0 + (cond ? r2 / s2 : 0.0);
+      for (int l = 0; l < d; ++l) acc[l] += c * k * ab * fabs(diff[l]);
+    }
+    for (int l = 0; l < d; ++l) out[i * d + l] = 2.0 * acc[l] / s2;
+  }
+  return 0;
+}
+
 /* ExactKernel::ConvolveGradient(X, dim), ExactKernel.cxx:294-323: sum_j (dK/dx_dim) W_j.
  * out is nx x dv. */
 int oracle_grad_dim(int d, int dv, const double *x, long nx, const double *y, const double *w,

@@ -42,8 +42,20 @@ def build_port(force: bool = False) -> str:
         return _PORT_SO
 
 
-def build_reference(reference_root: str = "/root/reference") -> str | None:
+REFERENCE_ENV = "DEFORMETRICA_REFERENCE_DIR"
+
+
+def reference_root() -> str:
+    """The reference's source tree for the recipes that read it (this package, the golden-fixture
+    script, the binding tests): the directory named by $DEFORMETRICA_REFERENCE_DIR, else the
+    checkout location of this build's container. Absent on machines without the tree."""
+    return os.environ.get(REFERENCE_ENV) or "/root/reference"
+
+
+def build_reference(reference_root: str | None = None) -> str | None:
     """Build oracle/_ref from the reference sources when they are present; else return None."""
+    if reference_root is None:
+        reference_root = globals()["reference_root"]()
     if not os.path.isdir(os.path.join(reference_root, "src", "support", "kernels")):
         return None
     with _lock:
@@ -68,6 +80,11 @@ _SIGS = {
     "oracle_hess_rowcol": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _I, _D],
     "oracle_hess_kdpdq": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _I, _I, _D],
     "oracle_special_hessian": [_I, _I, _D, _D, _L, _F, _D, _D],
+}
+# exported by the port only (test denominators, no reference method)
+_PORT_ONLY = {
+    "oracle_convolve_mag": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _D],
+    "oracle_grad_alpha_mag": [_I, _I, _D, _L, _D, _D, _L, _F, _D, _I, _D],
 }
 
 
@@ -94,6 +111,11 @@ class OracleLib:
             fn = getattr(self._lib, name)
             fn.argtypes = argt
             fn.restype = ctypes.c_int
+        for name, argt in _PORT_ONLY.items():
+            if hasattr(self._lib, name):
+                fn = getattr(self._lib, name)
+                fn.argtypes = argt
+                fn.restype = ctypes.c_int
         self._lib.oracle_last_error.restype = ctypes.c_char_p
 
     def _check(self, rc: int):
@@ -121,6 +143,24 @@ class OracleLib:
         out = np.zeros((x.shape[0], d))
         self._check(self._lib.oracle_grad_alpha(d, dv, _c(x), x.shape[0], _c(y), _c(w),
                                                 y.shape[0], sigma, _c(alpha), _c(out)))
+        return out
+
+    def convolve_mag(self, x, y, w, sigma, cond: bool = True):
+        """Sum over j of (1 + a_ij) K_ij |w_j| (cond) or K_ij |w_j|: the denominator of the
+        condition-aware (or plain-magnitude) error of each convolve element; a_ij = |x_i - y_j|^2 / sigma^2."""
+        x, y, w, d, dv = self._prep(x, y, w)
+        out = np.zeros((x.shape[0], dv))
+        self._check(self._lib.oracle_convolve_mag(d, dv, _c(x), x.shape[0], _c(y), _c(w), y.shape[0], sigma,
+                                                  int(cond), _c(out)))
+        return out
+
+    def grad_alpha_mag(self, x, y, w, sigma, alpha, cond: bool = True):
+        """The same for grad_alpha: (2/sigma^2) sum_j (1 + a_ij) K (|alpha_i|.|w_j|) |x_i - y_j|."""
+        x, y, w, d, dv = self._prep(x, y, w)
+        alpha = _f64(alpha)
+        out = np.zeros((x.shape[0], d))
+        self._check(self._lib.oracle_grad_alpha_mag(d, dv, _c(x), x.shape[0], _c(y), _c(w), y.shape[0], sigma,
+                                                    _c(alpha), int(cond), _c(out)))
         return out
 
     def grad_varlin(self, x, y, w, sigma):

@@ -1,6 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout where the reference tree is available (default /root/reference):
+Run in a checkout where the reference tree is available ($DEFORMETRICA_REFERENCE_DIR, else the
+default location oracle.reference_root() names):
 
     python tests/golden/make_golden.py [REFERENCE_ROOT]
 
@@ -85,7 +86,8 @@ def all_ops(lib, X, Y, W, Z, sigma, W3):
     return out
 
 
-def main(ref_root: str = "/root/reference"):
+def main(ref_root: str | None = None):
+    ref_root = ref_root or oracle.reference_root()
     if oracle.build_reference(ref_root) is None:
         raise SystemExit(f"reference tree not found at {ref_root}")
     ref = oracle.load("reference")
@@ -114,7 +116,7 @@ def main(ref_root: str = "/root/reference"):
     del port
 
     # 3. parallel-transport unit-test data (TestParallelTransport.cxx:19-85)
-    pt = os.path.join(ref_root, "tests", "unit_tests", "parallel-transport", "data")
+    pt = os.path.join(ref_root or oracle.reference_root(), "tests", "unit_tests", "parallel-transport", "data")
     np.savez_compressed(
         os.path.join(HERE, "parallel_transport.npz"),
         cp_regression=read_dlm(os.path.join(pt, "CPRegression.txt")),
@@ -148,14 +150,14 @@ def _formats():
     return F
 
 
-def skull_fixture(ref_root: str = "/root/reference"):
+def skull_fixture(ref_root: str | None = None):
     """Inputs and expected final state of the reference's skull registration (model.xml:
     NonOrientedPolyline, data-sigma 1, object kernel width 40, deformation kernel width 60, 6 time
     points; optimization_parameters.xml: FastGradientAscent, 10 iterations, default initial step
     1e-3 (SparseDiffeoParameters.cxx:82))."""
     F = _formats()
     from oracle.optimize import initial_control_points
-    d = os.path.join(ref_root, "tests", "functional_tests", "registration", "landmark", "2d", "skulls")
+    d = os.path.join(ref_root or oracle.reference_root(), "tests", "functional_tests", "registration", "landmark", "2d", "skulls")
     tp, tf = F.read_vtk_polydata(os.path.join(d, "data", "template.vtk"))
     gp, gf = F.read_vtk_polydata(os.path.join(d, "data", "skull_sapiens.vtk"))
     tp, gp = np.ascontiguousarray(tp[:, :2]), np.ascontiguousarray(gp[:, :2])  # a 2-D object
@@ -169,13 +171,13 @@ def skull_fixture(ref_root: str = "/root/reference"):
         **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
-def amygdala_fixture(ref_root: str = "/root/reference"):
+def amygdala_fixture(ref_root: str | None = None):
     """Inputs and expected final state of the reference's amygdala registration (model.xml:
     OrientedSurfaceMesh, data-sigma 0.1, object and deformation kernel width 10, 10 time points;
     optimization_parameters.xml: FastGradientAscent, initial step 1e-7, 10 iterations)."""
     F = _formats()
     from oracle.optimize import initial_control_points
-    d = os.path.join(ref_root, "tests", "functional_tests", "registration", "landmark", "3d", "amygdalas")
+    d = os.path.join(ref_root or oracle.reference_root(), "tests", "functional_tests", "registration", "landmark", "3d", "amygdalas")
     tp, tf_raw = F.read_vtk_polydata(os.path.join(d, "data", "decimatedAmygdala1.vtk"))
     gp, gf_raw = F.read_vtk_polydata(os.path.join(d, "data", "decimatedAmygdala2.vtk"))
     tf, gf = F.reorient_like_reader(tp, tf_raw), F.reorient_like_reader(gp, gf_raw)
@@ -189,19 +191,19 @@ def amygdala_fixture(ref_root: str = "/root/reference"):
         **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
-def volume_fixture(ref_root: str = "/root/reference"):
+def volume_fixture(ref_root: str | None = None):
     """Meshes of the reference's volume-gradient unit test (TestVolumeGradient.cxx:86-120: kernel
     width 1, forward differences of step 1e-5f, |analytic - numeric| <= 1e-5): a tetrahedral cube
     deformed towards a ball in 3-D, a triangulated square towards a disk in 2-D (the 2-D objects keep
     the first two coordinates), and the two 4-point sets of the 2-D point-cloud example."""
     F = _formats()
-    g = os.path.join(ref_root, "tests", "unit_tests", "geometries", "data")
+    g = os.path.join(ref_root or oracle.reference_root(), "tests", "unit_tests", "geometries", "data")
     out = {}
     for name, dim in (("VolumeCube", 3), ("VolumeBall", 3), ("VolumeSquare", 2), ("VolumeDisk", 2)):
         p, c = F.read_vtk_polydata(os.path.join(g, name + ".vtk"))
         out[f"{name}_pts"] = np.ascontiguousarray(p[:, :dim])
         out[f"{name}_cells"] = np.asarray(c, dtype=np.int32)
-    e = os.path.join(ref_root, "examples", "registration", "landmark", "2d", "simple_point_cloud", "data")
+    e = os.path.join(ref_root or oracle.reference_root(), "examples", "registration", "landmark", "2d", "simple_point_cloud", "data")
     for name in ("sourcePoints", "targetPoints"):
         p, _ = F.read_vtk_polydata(os.path.join(e, name + ".vtk"))
         out[f"{name}_pts"] = np.ascontiguousarray(p[:, :2])
@@ -209,7 +211,7 @@ def volume_fixture(ref_root: str = "/root/reference"):
                         fd_step=np.array(float(np.float32(1e-5))), tolerance=np.array(1e-5), **out)
 
 
-def parabola_fixture(ref_root: str = "/root/reference"):
+def parabola_fixture(ref_root: str | None = None):
     """Inputs and expected final state of the reference's parabola atlas (functional test 8,
     model.xml: DeterministicAtlas, two OrientedPolyline objects "line" and "wave", object kernel
     width 0.2, data-sigma 1, deformation kernel width 0.2, 10 time points; three subjects;
@@ -219,7 +221,7 @@ def parabola_fixture(ref_root: str = "/root/reference"):
     XmlConfigurationConverter.cxx:228), so the ratio keeps its default 1: smoothing width 0.2)."""
     F = _formats()
     from oracle.optimize import initial_control_points
-    d = os.path.join(ref_root, "tests", "functional_tests", "atlas", "landmark", "2d", "parabola")
+    d = os.path.join(ref_root or oracle.reference_root(), "tests", "functional_tests", "atlas", "landmark", "2d", "parabola")
     out = {}
     centres = []
     for i in (1, 2):
@@ -239,7 +241,7 @@ def parabola_fixture(ref_root: str = "/root/reference"):
         max_iterations=np.array(10), **out, **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
-def regression_fixture(ref_root: str = "/root/reference"):
+def regression_fixture(ref_root: str | None = None):
     """Inputs and expected final state of the reference's geodesic regression (functional test 7,
     model.xml: Regression, initial CP spacing 40, one NonOrientedPolyline object with data kernel
     width 40 and data-sigma 1, deformation kernel width 60, 5 time points from t0 = 0 to tn = 5;
@@ -250,7 +252,7 @@ def regression_fixture(ref_root: str = "/root/reference"):
     TemplateData (fixed, extrapolated, gradient)."""
     F = _formats()
     from oracle.optimize import initial_control_points
-    d = os.path.join(ref_root, "tests", "functional_tests", "regression", "landmark", "2d", "skulls")
+    d = os.path.join(ref_root or oracle.reference_root(), "tests", "functional_tests", "regression", "landmark", "2d", "skulls")
     tp, tc = F.read_vtk_polydata(os.path.join(d, "data", "template.vtk"))
     out = {"tmpl_pts": np.ascontiguousarray(tp[:, :2]), "tmpl_segs": tc}
     for k, name in enumerate(("skull_australopithecus", "skull_habilis", "skull_sapiens")):
@@ -276,7 +278,7 @@ def regression_fixture(ref_root: str = "/root/reference"):
         tolerance=np.array(1e-3), **out, **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
-def banana_fixture(ref_root: str = "/root/reference"):
+def banana_fixture(ref_root: str | None = None):
     """Inputs and expected final state of the reference's banana atlas (functional test 2,
     model.xml: DeterministicAtlas, OrientedSurfaceMesh with data kernel width 0.5 and data-sigma
     0.5, re-oriented normals, initial CP spacing 0.3, deformation kernel width 1, 20 time points;
@@ -286,7 +288,7 @@ def banana_fixture(ref_root: str = "/root/reference"):
     TemplateData), the momenta and the gradients at the final point (GradientAscent.cxx:226-236)."""
     F = _formats()
     from oracle.optimize import initial_control_points
-    d = os.path.join(ref_root, "tests", "functional_tests", "atlas", "landmark", "3d", "banana")
+    d = os.path.join(ref_root or oracle.reference_root(), "tests", "functional_tests", "atlas", "landmark", "3d", "banana")
     tp, tf_raw = F.read_vtk_polydata(os.path.join(d, "data", "template.vtk"))
     tf = F.reorient_like_reader(tp, tf_raw)
     out = {"tmpl_pts": tp, "tmpl_tris": tf}

@@ -9,7 +9,6 @@ import pytest
 from tests.conftest import ROOT
 
 PKG = os.path.join(ROOT, "deformetrica_code_gb300")
-REF = "/root/reference"
 
 
 def _build_precision_test(tmp):
@@ -36,7 +35,8 @@ def test_cpp_kernel_precision(tmp_path, mode, eps):
 
 
 def _ref_flags():
-    s = os.path.join(REF, "src", "support")
+    import oracle
+    s = os.path.join(oracle.reference_root(), "src", "support")
     arma = os.path.join(ROOT, "oracle", "_ref", "armadillo-7.700.0", "include")
     return ["-std=c++14", "-w", "-DARMA_DONT_USE_WRAPPER", "-DARMA_DONT_USE_LAPACK", "-DARMA_DONT_USE_BLAS",
             "-I" + os.path.join(ROOT, "oracle", "ref_shim"), "-I" + os.path.join(s, "kernels"),

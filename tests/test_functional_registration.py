@@ -74,7 +74,9 @@ def test_reorientation_is_consistent_and_inward(fx):
 
 
 def test_readers_match_fixture_when_reference_present(fx):
-    d = "/root/reference/tests/functional_tests/registration/landmark/3d/amygdalas"
+    import oracle
+    d = os.path.join(oracle.reference_root(), "tests", "functional_tests", "registration", "landmark", "3d",
+                     "amygdalas")
     if not os.path.isdir(d):
         pytest.skip("reference tree not present")
     from deformetrica_code_gb300.formats import read_deformation_state, read_vtk_polydata

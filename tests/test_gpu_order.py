@@ -142,6 +142,52 @@ def test_small_sigma_accuracy_improves(gb, ctx, port):
     assert err[gb.GBK_ORDER_SPATIAL][1] < err[gb.GBK_ORDER_OFF][1]
 
 
+@pytest.mark.parametrize("d", [2, 3])
+def test_two_float_coordinates(gb, ctx, port, d):
+    """GBK_ORDER_TWO_FLOAT: caller order with hi + lo coordinates for Convolve and the alpha-gradient
+    in every CTA whose targets spread wider than 16 scaled units. On the mixture at sigma = 0.02
+    (spread ~60 units) it is more accurate than one-float caller order, with and without source splits
+    and in the small launch shape; at sigma = 0.5 (spread ~2.4 units) every CTA runs the one-float
+    loop and gives the caller order's bits, as do ops without a two-float variant and the FP64 mode."""
+    rng = np.random.default_rng(40 + d)
+    sigma = 0.02
+    for nx, ny in ((6000, 9000), (700, 500)):  # the default shape; the small shape
+        X, Y = mixture(rng, nx, d), mixture(rng, ny, d)
+        W, A = rng.standard_normal((ny, d)), rng.standard_normal((nx, d))
+        ref = port.fwd_adjoint(X, Y, W, sigma, A)
+        err = {}
+        for order in (gb.GBK_ORDER_OFF, gb.GBK_ORDER_TWO_FLOAT):
+            for split in (0, 3):
+                ctx.set_split(split)
+                k = kern(gb, ctx, d, sigma, Y, W, gb.GBK_MODE_F32C, order)
+                got = k.ForwardAdjoint(X, A)
+                v = k.Convolve(X)
+                assert np.array_equal(v, got[0])  # Convolve alone = the fused pass's first output
+                err[order, split] = max(normwise_rel(g_, r_) for g_, r_ in zip(got, ref))
+        ctx.set_split(0)
+        print(d, nx, ny, "worst normwise: caller order", err[gb.GBK_ORDER_OFF, 0], "two-float",
+              err[gb.GBK_ORDER_TWO_FLOAT, 0])
+        for split in (0, 3):
+            assert err[gb.GBK_ORDER_TWO_FLOAT, split] <= 5e-7
+            assert err[gb.GBK_ORDER_TWO_FLOAT, split] < err[gb.GBK_ORDER_OFF, split]
+    X, Y = mixture(rng, 3000, d), mixture(rng, 4000, d)
+    W, A = rng.standard_normal((4000, d)), rng.standard_normal((3000, d))
+    for nx in (3000, 300):  # the default and the small shape
+        same = [kern(gb, ctx, d, 0.5, Y, W, gb.GBK_MODE_F32C, order).ForwardAdjoint(X[:nx], A[:nx])
+                for order in (gb.GBK_ORDER_OFF, gb.GBK_ORDER_TWO_FLOAT)]
+        for a_, b_ in zip(*same):
+            assert np.array_equal(a_, b_)
+    for mode in (gb.GBK_MODE_F32C, gb.GBK_MODE_F64):
+        outs = {}
+        for order in (gb.GBK_ORDER_OFF, gb.GBK_ORDER_TWO_FLOAT):
+            k = kern(gb, ctx, d, sigma, Y, W, mode, order)
+            outs[order] = (k.ConvolveGradient(X), k.ConvolveHessian(X, 0, 1)) + \
+                ((k.Convolve(X),) if mode == gb.GBK_MODE_F64 else ())
+        for a_, b_ in zip(outs[gb.GBK_ORDER_OFF], outs[gb.GBK_ORDER_TWO_FLOAT]):
+            assert np.array_equal(a_, b_)
+    ctx.set_mode(gb.GBK_MODE_F32C)
+
+
 @pytest.mark.parametrize("nx,ny,d", [(1, 1, 3), (7, 300, 3), (513, 1, 3), (1025, 777, 2), (4096, 4096, 2)])
 def test_ragged_and_degenerate(gb, ctx, port, nx, ny, d):
     rng = np.random.default_rng(nx + 17 * ny)
@@ -215,11 +261,32 @@ def test_auto_orders_large_calls_only(gb, ctx):
     # the order adds, per point set, a box and a keys kernel and (up to 16384 points) a one-CTA sort
     # (the device radix sort above that is counted as the library's), then one tiles kernel for the
     # targets and one kernel for the source boxes and copies; pruning adds the targets' non-finite
-    # scan and the conditional unbounding of the chunk boxes
+    # scan and the conditional unbounding of the chunk boxes. Below 2^30 pairs AUTO runs Convolve
+    # and the alpha-gradient in caller order (adaptive two-float variant: same launches as OFF)
+    assert launches(gb.GBK_ORDER_AUTO, 1000) == launches(gb.GBK_ORDER_OFF, 1000)
     assert launches(gb.GBK_ORDER_AUTO, 12000) == launches(gb.GBK_ORDER_OFF, 12000)
     assert launches(gb.GBK_ORDER_AUTO, 40000) == launches(gb.GBK_ORDER_OFF, 40000) + 8
     assert launches(gb.GBK_ORDER_SPATIAL, 1000) == launches(gb.GBK_ORDER_OFF, 1000) + 10
     assert launches(gb.GBK_ORDER_SPATIAL, 20000) == launches(gb.GBK_ORDER_OFF, 20000) + 8
+
+    # other ops from 2^22 pairs measure the extent of the two point sets first (one box launch):
+    # uniform points in [0, 1]^3 span 12 units of the FP32 coordinate scale at sigma 0.1 (caller
+    # order) and 60 at sigma 0.02 (the spatial order)
+    def launches_at(order, n, sigma, op="convolve"):
+        k = kern(gb, ctx, 3, sigma, rng.random((n, 3)), rng.standard_normal((n, 3)), gb.GBK_MODE_F32C, order)
+        x = rng.random((n, 3))
+        n0 = ctx.launch_count()
+        if op == "convolve":
+            k.Convolve(x)
+        else:
+            k.ConvolveGradient(x)  # varlin: no two-float variant
+        return ctx.launch_count() - n0
+
+    assert launches_at(gb.GBK_ORDER_AUTO, 20000, 0.02) == launches_at(gb.GBK_ORDER_OFF, 20000, 0.02)
+    assert launches_at(gb.GBK_ORDER_AUTO, 12000, 0.02, "varlin") == \
+        launches_at(gb.GBK_ORDER_SPATIAL, 12000, 0.02, "varlin") + 1
+    assert launches_at(gb.GBK_ORDER_AUTO, 12000, 0.1, "varlin") == launches_at(gb.GBK_ORDER_OFF, 12000, 0.1, "varlin") + 1
+    assert launches_at(gb.GBK_ORDER_AUTO, 1000, 0.02, "varlin") == launches_at(gb.GBK_ORDER_OFF, 1000, 0.02, "varlin")
 
     # forward + adjoint: x and y are sorted once each for both passes
     def fa_launches(order, n):
@@ -230,5 +297,56 @@ def test_auto_orders_large_calls_only(gb, ctx):
         return ctx.launch_count() - n0
 
     assert fa_launches(gb.GBK_ORDER_SPATIAL, 1000) == fa_launches(gb.GBK_ORDER_OFF, 1000) + 14
+    assert fa_launches(gb.GBK_ORDER_AUTO, 12000) == fa_launches(gb.GBK_ORDER_OFF, 12000)
     with pytest.raises(gb.GBKError):
         ctx.set_order(7)
+
+
+@pytest.mark.parametrize("d", [2, 3])
+@pytest.mark.parametrize("n", [10000, 30000])
+def test_default_order_meets_1e6_on_the_sweep_grid(gb, port, n, d):
+    """The large kernel-sum sweep's workload (8-Gaussian mixture, seed 3) at its two smallest sizes and
+    every kernel width, in the library's default order (GBK_ORDER_AUTO, nothing forced): each of the
+    four forward + adjoint outputs within 1e-6 of the FP64 oracle on 2048 sampled rows against all n
+    partners, both normwise (max_i |err_i| / max_i |ref_i|) and condition-aware (per element,
+    |err| / sum_j (1 + a_ij) |term_j| with a_ij = |x_i - y_j|^2 / sigma^2, the exponent's condition
+    number). At sigma = 0.02 the points span ~60 units of the FP32 coordinate scale; caller order
+    with one-float coordinates gave 1.2-1.4e-6 normwise there, so AUTO switches to two-float
+    coordinates (n = 1e4) or the spatial order (n = 3e4). The plain-magnitude error (denominator
+    sum_j |term_j|) is printed too: for a target whose nearest sources are several sigma away it is
+    bounded below by ~2u a_ij in any FP32 evaluation, whatever the order."""
+    import ctypes
+    import torch
+    import bench
+    x, y, w, a = bench.make_workload(n, n, d=d, seed=3)
+    X, Y, W, A = (torch.from_numpy(t).cuda() for t in (x, y, w, a))
+    outs = [torch.empty_like(X) for _ in range(4)]
+    c = gb.Context()
+    c.use_torch_stream()
+    assert c.get_order() == gb.GBK_ORDER_AUTO
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    rng = np.random.default_rng(7)
+    it = np.sort(rng.choice(n, size=2048, replace=False))
+    jt = np.sort(rng.choice(n, size=2048, replace=False))
+    xs, ys, as_, ws = (np.ascontiguousarray(t) for t in (x[it], y[jt], a[it], w[jt]))
+    report = []
+    for sigma in (0.02, 0.1, 0.5):
+        c.check(c.lib.gbk_forward_adjoint(c.h, d, d, p(X), n, p(Y), p(W), n, sigma, p(A), *[p(o) for o in outs]))
+        torch.cuda.synchronize()
+        v, gx, gy, gw = (o.cpu().numpy() for o in outs)
+        cases = {"v": (v[it], port.convolve(xs, y, w, sigma), lambda cd: port.convolve_mag(xs, y, w, sigma, cd)),
+                 "gx": (gx[it], port.grad_alpha(xs, y, w, sigma, as_),
+                        lambda cd: port.grad_alpha_mag(xs, y, w, sigma, as_, cd)),
+                 "gy": (gy[jt], port.grad_alpha(ys, x, a, sigma, ws),
+                        lambda cd: port.grad_alpha_mag(ys, x, a, sigma, ws, cd)),
+                 "gw": (gw[jt], port.convolve(ys, x, a, sigma), lambda cd: port.convolve_mag(ys, x, a, sigma, cd))}
+        for key, (got, r, mag) in cases.items():
+            e = np.abs(got - r)
+            nw = float(np.linalg.norm(got - r, axis=1).max() / np.linalg.norm(r, axis=1).max())
+            cond = float((e / np.maximum(mag(True), 1e-300)).max())
+            plain = float((e / np.maximum(mag(False), 1e-300)).max())
+            report.append((sigma, key, nw, cond, plain, float(e.max())))
+    print("\n".join(f"d={d} n={n} sigma={s_} {k}: normwise {nw:.2e} condition-aware {cd:.2e} "
+                    f"plain-magnitude {pl:.2e} max abs {ma:.2e}" for s_, k, nw, cd, pl, ma in report))
+    for s_, k, nw, cd, _, _ in report:
+        assert nw <= 1e-6 and cd <= 1e-6, (s_, k, nw, cd)

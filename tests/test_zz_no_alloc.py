@@ -80,3 +80,40 @@ def test_noalloc_rejects_oversize_and_host_pointers(setup):
     host = np.zeros((10, 3))
     assert lib.gbk_kernel_norm_noalloc(ctx.h, 3, 3, ctypes.c_void_p(host.ctypes.data), _p(W), 10, 0.1,
                                        _p(out)) == g._lib.GBK_ERR_ARG
+
+
+def test_noalloc_allocates_nothing_and_counts_its_launches(setup):
+    """The entry point's claim itself: after a first call (which may load the module holding the
+    scratch array), further calls leave the device's free memory unchanged, and their launches are
+    counted like every other entry point's."""
+    g, torch = setup
+    ctx = g.Context()
+    ctx.use_torch_stream()
+    lib = ctx.lib
+    rng = np.random.default_rng(33)
+    n, d, dv = 50000, 3, 3
+    Y = torch.from_numpy(rng.random((n, d))).cuda()
+    W = torch.from_numpy(rng.standard_normal((n, dv))).cuda()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    assert lib.gbk_kernel_norm_noalloc(ctx.h, d, dv, _p(Y), _p(W), n, 0.1, _p(out)) == 0
+    torch.cuda.synchronize()
+    first = float(out.item())
+    free0, _ = torch.cuda.mem_get_info()
+    n0 = ctx.launch_count()
+    for _ in range(3):
+        assert lib.gbk_kernel_norm_noalloc(ctx.h, d, dv, _p(Y), _p(W), n, 0.1, _p(out)) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert ctx.launch_count() - n0 >= 3 * 2  # pair kernel(s) + the FP64 dot, per call
+    assert float(out.item()) == first  # bitwise reproducible, scratch reused
+
+
+def test_noalloc_rejects_nan_width_with_a_message(setup):
+    g, torch = setup
+    ctx = g.Context()
+    Y = torch.zeros((100, 3), dtype=torch.float64, device="cuda")
+    W = torch.zeros((100, 3), dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    assert ctx.lib.gbk_kernel_norm_noalloc(ctx.h, 3, 3, _p(Y), _p(W), 100, float("nan"), _p(out)) == g._lib.GBK_ERR_ARG
+    assert b"NaN" in ctx.lib.gbk_last_error(ctx.h)

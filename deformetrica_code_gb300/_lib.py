@@ -128,6 +128,8 @@ SIGNATURES = {
     "gbk_inject_pointer_device": (_I, [_P, _I]),
     "gbk_image_points": (_I, [_P, _I, _P, _P, _P, _P]),
     "gbk_convolve_image_fast": (_I, [_P, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P]),
+    "gbk_convolve_gradient_image_fast": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P]),
+    "gbk_convolve_gradient_image_fast_alpha": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P, _P]),
     "gbk_flow_image_maps": (_I, [_P, _I, _L, _P, _P, _I, _D, _D, _I, _I, _P, _P, _P, _P, _P, _P]),
     "gbk_registration_create": (_I, [_P, _I, _L, _L, _P, _L, _P, _L, _P, _L, _P, _I, _D, _D, _D, _I, _I,
                                      ctypes.POINTER(_P)]),

@@ -2,7 +2,8 @@
 //
 // Drop-in beside src/support/kernels/CUDAExactKernel.h: it derives from ExactKernel because the
 // factory's base type is ExactKernel (KernelFactory.h:44), and overrides every convolution method
-// of AbstractKernel (AbstractKernel.h:120-160), so no call falls back to the CPU loops. Each method
+// of AbstractKernel (AbstractKernel.h:120-165), the image-grid ones included, so no call falls back
+// to the CPU loops. Each method
 // builds the row-major buffers the legacy CUDA path builds (vectorise_row_wise,
 // CUDAExactKernel.cxx:46-48) and makes one call into the C ABI of include/gbk.h; failures throw
 // std::runtime_error with the library's message, as the reference does for shape errors. One
@@ -164,28 +165,69 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
   virtual MatrixType ConvolveImageFast(const MatrixType &X, const typename Superclass::ImageTypePointer image) {
     Buffers b(this, X);
     if (b.dv != PointDim) throw std::runtime_error("ConvolveImageFast needs weights with PointDim columns");
-    const auto origin = image->GetOrigin();
-    const auto spacing = image->GetSpacing();
-    const auto direction = image->GetDirection();
-    const auto size = image->GetLargestPossibleRegion().GetSize();
-    double o[PointDim], s[PointDim];
-    long n[PointDim];
-    for (unsigned i = 0; i < PointDim; ++i) {
-      o[i] = origin[i];
-      s[i] = spacing[i];
-      n[i] = (long)size[i];
-      for (unsigned j = 0; j < PointDim; ++j)
-        if (direction[i][j] != (i == j ? 1.0 : 0.0))
-          throw std::runtime_error("GB300ExactKernel::ConvolveImageFast: non-identity image direction");
-    }
+    const Geometry g(image);
     std::vector<double> out((size_t)X.rows() * PointDim);
     gb300_binding::check(gbk_convolve_image_fast(gb300_binding::thread_context(), PointDim, b.x.memptr(), X.rows(),
-                                                 b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(), o, s, n,
+                                                 b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(), g.o, g.s, g.n,
                                                  out.data()));
     return from_rows(out, X.rows(), PointDim);
   }
 
+  // ExactKernel::ConvolveGradientImageFast(X, image) (ExactKernel.cxx:207-257): one dv x PointDim
+  // matrix per pixel, over the same windows.
+  virtual std::vector<MatrixType> ConvolveGradientImageFast(const MatrixType &X,
+                                                            const typename Superclass::ImageTypePointer image) {
+    Buffers b(this, X);
+    const Geometry g(image);
+    std::vector<double> out((size_t)X.rows() * b.dv * PointDim);
+    gb300_binding::check(gbk_convolve_gradient_image_fast(gb300_binding::thread_context(), PointDim, b.dv,
+                                                          b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                          this->GetKernelWidth(), g.o, g.s, g.n, out.data()));
+    std::vector<MatrixType> grad;
+    for (unsigned i = 0; i < X.rows(); ++i) {
+      MatrixType Gi(b.dv, PointDim, 0.0);
+      for (unsigned k = 0; k < b.dv; ++k)
+        for (unsigned l = 0; l < PointDim; ++l) Gi(k, l) = out[((size_t)i * b.dv + k) * PointDim + l];
+      grad.push_back(Gi);
+    }
+    return grad;
+  }
+
+  // ExactKernel::ConvolveGradientImageFast(X, alpha, image) (ExactKernel.cxx:277-290): G_p^T alpha_p.
+  virtual MatrixType ConvolveGradientImageFast(const MatrixType &X, const MatrixType &alpha,
+                                               const typename Superclass::ImageTypePointer image) {
+    Buffers b(this, X);
+    if (alpha.rows() != X.rows() || alpha.columns() != b.dv) throw std::runtime_error("alpha size mismatch");
+    const Geometry g(image);
+    VectorType a = alpha.vectorise_row_wise();
+    std::vector<double> out((size_t)X.rows() * PointDim);
+    gb300_binding::check(gbk_convolve_gradient_image_fast_alpha(
+        gb300_binding::thread_context(), PointDim, b.dv, b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+        this->GetKernelWidth(), a.memptr(), g.o, g.s, g.n, out.data()));
+    return from_rows(out, X.rows(), PointDim);
+  }
+
  private:
+  // An ITK image's origin, spacing and size for the C ABI; identity direction only.
+  struct Geometry {
+    double o[PointDim], s[PointDim];
+    long n[PointDim];
+    explicit Geometry(const typename Superclass::ImageTypePointer &image) {
+      const auto origin = image->GetOrigin();
+      const auto spacing = image->GetSpacing();
+      const auto direction = image->GetDirection();
+      const auto size = image->GetLargestPossibleRegion().GetSize();
+      for (unsigned i = 0; i < PointDim; ++i) {
+        o[i] = origin[i];
+        s[i] = spacing[i];
+        n[i] = (long)size[i];
+        for (unsigned j = 0; j < PointDim; ++j)
+          if (direction[i][j] != (i == j ? 1.0 : 0.0))
+            throw std::runtime_error("GB300ExactKernel: image with a non-identity direction");
+      }
+    }
+  };
+
   struct Buffers {
     VectorType x, y, w;
     unsigned ny, dv;

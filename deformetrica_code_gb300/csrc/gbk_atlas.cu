@@ -285,7 +285,11 @@ struct gbk_atlas {
     BatchLaunch L;
     L.op = op;
     L.dv = dv;
-    if (!find_kernel(op, c->mode, 3, dv, 0, &L.e)) return c->fail(GBK_ERR_UNSUPPORTED, "atlas: no kernel op %d dv %d", op, dv);
+    // Convolve-like stages run the adaptive two-float variant (FP32C): a CTA whose targets spread
+    // wider than 16 scaled units forms its differences from hi + lo coordinates, any other CTA runs
+    // the one-float loop; the other stages run the default variant
+    if (!find_kernel(op, c->mode, 3, dv, VARIANT_TWO_FLOAT, &L.e) && !find_kernel(op, c->mode, 3, dv, 0, &L.e))
+      return c->fail(GBK_ERR_UNSUPPORTED, "atlas: no kernel op %d dv %d", op, dv);
     const long per = (long)L.e.block * L.e.r;
     int occ = 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, L.e.kernel, L.e.block, L.e.smem) != cudaSuccess) occ = 1;
@@ -367,7 +371,7 @@ struct gbk_atlas {
   int run() {
     cudaStream_t saved = c->stream;
     c->stream = stream;
-    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
     int rc = GBK_OK;
     if (!use_graph || steps == 0) {
       rc = body();

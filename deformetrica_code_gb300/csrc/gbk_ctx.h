@@ -103,7 +103,8 @@ struct gbk_ctx {
     ~OrderCacheScope() { c->order_cache = saved; }
   };
 
-  // Holds the order policy at `o` for a scope (the registration and atlas steps use OFF).
+  // Holds the order policy at `o` for a scope (the registration, atlas and regression steps use
+  // TWO_FLOAT: caller order, adaptive two-float coordinates for the Convolve-like ops).
   struct OrderScope {
     gbk_ctx *c;
     int saved;

@@ -293,7 +293,7 @@ int gbk_geodesic_regression_create(gbk_ctx *c, int d, long ncp, int nobj, const 
       rc = ob.surf.init(c, term_kind[data_kinds[k]], d, cl, sigma_data[k], nv[k], nf, cl > 1 ? th.data() + tc_off : nullptr,
                         vt, nf_t, cl > 1 ? gh.data() + gc_off : nullptr);
       if (!rc) {
-        gbk_ctx::OrderScope offo(c, GBK_ORDER_OFF);
+        gbk_ctx::OrderScope offo(c, GBK_ORDER_TWO_FLOAT);
         rc = ob.surf.set_target(c, tgt + pt_off * d);
       }
       pt_off += vt;
@@ -349,7 +349,7 @@ int gbk_geodesic_regression_step(gbk_geodesic_regression *r, const double *cp, c
   if (!rc) rc = c->cuda(cudaMemcpyAsync(r->mom, mom, nb, cudaMemcpyDefault, r->stream), "copy mom");
   if (!rc && tmpl) rc = c->cuda(cudaMemcpyAsync(r->lm0, tmpl, mb, cudaMemcpyDefault, r->stream), "copy template");
   if (!rc) {
-    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
     rc = r->run();
   }
   if (!rc && loglik) rc = c->cuda(cudaMemcpyAsync(loglik, r->out, 5 * sizeof(double), cudaMemcpyDefault, r->stream), "copy L");
@@ -378,7 +378,7 @@ int gbk_geodesic_regression_optimize(gbk_geodesic_regression *r, double *cp, dou
   if (!cp || !mom || !tmpl || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = r->ncp * r->d, m = r->nv * r->d;
   cudaStream_t st = r->stream;
-  gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+  gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
   double *sq_dev = nullptr;
   int rc = c->cuda(cudaMalloc(&sq_dev, 4 * sizeof(double)), "cudaMalloc (optimiser)");
   if (!rc && !optimize_cp) rc = c->cuda(cudaMemcpyAsync(r->cp, cp, n * sizeof(double), cudaMemcpyDefault, st), "copy");

@@ -78,16 +78,35 @@ __device__ __forceinline__ float image_ex2(float v) {
   return r;
 }
 
-// F32 = false: FP64 as the reference (exp, no contracted multiply-adds). F32 = true (GBK_MODE_F32C):
-// offsets from the tile's centre formed in FP64 and scaled by sqrt(log2 e) / sigma, then FP32 distances,
-// K = 2^-r2 on the MUFU unit and per-pixel compensated FP32 sums (TwoSum), added up in FP64 at the end.
-template <int D, bool F32>
-__global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, const double *y, const double *w,
-                                                              const int *start, long ny, double s2, double pre,
-                                                              ImageGeom g, double *out) {
+// What a windowed image kernel accumulates per pixel p over the control points j whose window holds p:
+//  IMG_CONV: V_p = sum_j W_j K_pj (ConvolveImageFast; D weight columns);
+//  IMG_GRAD: G_p(k, l) = sum_j W_jk (x_p - y_j)_l (-2 K_pj / sigma^2) (ConvolveGradientImageFast(X, image));
+//  IMG_GRAD_ALPHA: sum_k alpha_pk G_p(k, l) (ConvolveGradientImageFast(X, alpha, image)).
+// The gradients take DV (1..3) weight columns at a time; wider weights run as column chunks.
+enum { IMG_CONV = 0, IMG_GRAD = 1, IMG_GRAD_ALPHA = 2 };
+
+struct ImageArgs {
+  const double *x, *y, *w, *alpha;
+  int w_ld, alpha_ld;  // leading dimensions of w and alpha (pointers already offset to the chunk)
+  const int *start;
+  long ny;
+  double s2, pre;
+  double *out;
+  int out_ld;   // doubles per output row
+  int acc_out;  // IMG_GRAD_ALPHA: add into out (later column chunks)
+};
+
+// F32 = false: FP64 as the reference (exp, no contracted multiply-adds, its order of operations).
+// F32 = true (GBK_MODE_F32C): offsets from the tile's centre formed in FP64 and scaled by
+// sqrt(log2 e) / sigma, then FP32 distances, K = 2^-r2 on the MUFU unit and per-pixel compensated
+// FP32 sums (TwoSum), added up in FP64 at the end (the gradients' -2 / (sigma^2 pre) applied there).
+template <int D, int DV, int KIND, bool F32>
+__global__ void __launch_bounds__(kThreads) image_fast_kernel(const ImageArgs a, const ImageGeom g) {
   typedef Tile<D> T;
-  __shared__ double s_y[F32 ? 1 : kThreads][D], s_w[F32 ? 1 : kThreads][D];
-  __shared__ float s_yf[F32 ? kThreads : 1][D], s_wf[F32 ? kThreads : 1][D];
+  constexpr int NW = KIND == IMG_CONV ? D : DV;      // weight columns staged per control point
+  constexpr int NA = KIND == IMG_CONV ? D : DV * D;  // accumulators per pixel
+  __shared__ double s_y[F32 ? 1 : kThreads][D], s_w[F32 ? 1 : kThreads][NW];
+  __shared__ float s_yf[F32 ? kThreads : 1][D], s_wf[F32 ? kThreads : 1][NW];
   __shared__ int s_start[kThreads][D];
   __shared__ int s_warp[kThreads / 32 + 1];
   const int tid = threadIdx.x;
@@ -99,24 +118,27 @@ __global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, c
   const long q[3] = {lo[0] + tid % T::X, lo[1] + (tid / T::X) % T::Y, lo[2] + tid / (T::X * T::Y)};
   const bool valid = q[0] < hi[0] && q[1] < hi[1] && (D == 2 || q[2] < hi[2]);
   const long row = q[0] + g.n[0] * (q[1] + (D == 3 ? g.n[1] * q[2] : 0));
-  double xp[D], acc[D], ctr[D];
-  float xf[D], fs[D], fc[D];
+  const double s2 = a.s2, pre = a.pre;
+  double xp[D], ctr[D], acc[NA];
+  float xf[D], fs[NA], fc[NA];
   for (int k = 0; k < D; ++k) {
-    xp[k] = valid ? x[row * D + k] : 0.0;
-    acc[k] = 0.0;
+    xp[k] = valid ? a.x[row * D + k] : 0.0;
     ctr[k] = g.origin[k] + g.spacing[k] * 0.5 * (double)(lo[k] + hi[k] - 1);
     xf[k] = (float)((xp[k] - ctr[k]) * pre);
-    fs[k] = 0.f;
-    fc[k] = 0.f;
+  }
+  for (int m = 0; m < NA; ++m) {
+    acc[m] = 0.0;
+    fs[m] = 0.f;
+    fc[m] = 0.f;
   }
   const int lane = tid & 31, warp = tid >> 5;
-  for (long c0 = 0; c0 < ny; c0 += kThreads) {
+  for (long c0 = 0; c0 < a.ny; c0 += kThreads) {
     const long j = c0 + tid;
     int st[D];
-    bool keep = j < ny;
+    bool keep = j < a.ny;
     if (keep)
       for (int k = 0; k < D; ++k) {
-        st[k] = start[j * D + k];
+        st[k] = a.start[j * D + k];
         keep = keep && (long)st[k] < hi[k] && (long)st[k] + g.L > lo[k];
       }
     // order-preserving compaction of the kept control points
@@ -131,14 +153,17 @@ __global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, c
     if (keep) {
       const int pos = base + __popc(ball & ((1u << lane) - 1u));
       for (int k = 0; k < D; ++k) {
-        if (F32) {
-          s_yf[pos][k] = (float)((y[j * D + k] - ctr[k]) * pre);
-          s_wf[pos][k] = (float)w[j * D + k];
-        } else {
-          s_y[pos][k] = y[j * D + k];
-          s_w[pos][k] = w[j * D + k];
-        }
+        if (F32)
+          s_yf[pos][k] = (float)((a.y[j * D + k] - ctr[k]) * pre);
+        else
+          s_y[pos][k] = a.y[j * D + k];
         s_start[pos][k] = st[k];
+      }
+      for (int k = 0; k < NW; ++k) {
+        if (F32)
+          s_wf[pos][k] = (float)a.w[j * a.w_ld + k];
+        else
+          s_w[pos][k] = a.w[j * a.w_ld + k];
       }
     }
     __syncthreads();
@@ -148,32 +173,51 @@ __global__ void __launch_bounds__(kThreads) image_fast_kernel(const double *x, c
         for (int k = 0; k < D; ++k) in = in && q[k] >= s_start[m][k] && q[k] < (long)s_start[m][k] + g.L;
         if (!in) continue;
         if (F32) {
-          float r2 = 0.f;
+          float r2 = 0.f, df[D];
           for (int k = 0; k < D; ++k) {
-            const float df = xf[k] - s_yf[m][k];
-            r2 = fmaf(df, df, r2);
+            df[k] = xf[k] - s_yf[m][k];
+            r2 = fmaf(df[k], df[k], r2);
           }
           const float K = image_ex2(-r2);
-          for (int k = 0; k < D; ++k) {  // TwoSum into (fs, fc)
-            const float v = s_wf[m][k] * K;
-            const float t = fs[k] + v, bp = t - fs[k];
-            fc[k] += (fs[k] - (t - bp)) + (v - bp);
-            fs[k] = t;
+          for (int c = 0; c < NA; ++c) {  // TwoSum into (fs, fc)
+            const float v = KIND == IMG_CONV ? s_wf[m][c] * K : s_wf[m][c / D] * (K * df[c % D]);
+            const float t = fs[c] + v, bp = t - fs[c];
+            fc[c] += (fs[c] - (t - bp)) + (v - bp);
+            fs[c] = t;
           }
         } else {
-          double sq = 0.0;
+          double sq = 0.0, diff[D];
           for (int k = 0; k < D; ++k) {
-            const double diff = __dsub_rn(xp[k], s_y[m][k]);
-            sq = __dadd_rn(sq, __dmul_rn(diff, diff));
+            diff[k] = __dsub_rn(xp[k], s_y[m][k]);
+            sq = __dadd_rn(sq, __dmul_rn(diff[k], diff[k]));
           }
           const double K = exp(-sq / s2);
-          for (int k = 0; k < D; ++k) acc[k] = __dadd_rn(acc[k], __dmul_rn(s_w[m][k], K));
+          if (KIND == IMG_CONV) {
+            for (int k = 0; k < D; ++k) acc[k] = __dadd_rn(acc[k], __dmul_rn(s_w[m][k], K));
+          } else {  // ExactKernel::EvaluateKernelGradient: (x - y) * (-2 K / sigma^2)
+            const double f = __ddiv_rn(__dmul_rn(-2.0, K), s2);
+            for (int k = 0; k < DV; ++k)
+              for (int l = 0; l < D; ++l)
+                acc[k * D + l] = __dadd_rn(acc[k * D + l], __dmul_rn(__dmul_rn(diff[l], f), s_w[m][k]));
+          }
         }
       }
     __syncthreads();
   }
-  if (valid)
-    for (int k = 0; k < D; ++k) out[row * D + k] = F32 ? (double)fs[k] + (double)fc[k] : acc[k];
+  if (!valid) return;
+  const double gs = -2.0 / (s2 * pre);  // F32 gradients were accumulated as K (x' - y')
+  double v[NA];
+  for (int c = 0; c < NA; ++c) v[c] = F32 ? (KIND == IMG_CONV ? 1.0 : gs) * ((double)fs[c] + (double)fc[c]) : acc[c];
+  double *o = a.out + row * (long)a.out_ld;
+  if (KIND == IMG_GRAD_ALPHA) {  // G_p^T alpha_p, summed over k in order
+    for (int l = 0; l < D; ++l) {
+      double s = 0.0;
+      for (int k = 0; k < DV; ++k) s = __dadd_rn(s, __dmul_rn(v[k * D + l], a.alpha[row * a.alpha_ld + k]));
+      o[l] = a.acc_out ? __dadd_rn(o[l], s) : s;
+    }
+  } else {
+    for (int c = 0; c < NA; ++c) o[c] = v[c];
+  }
 }
 
 template <int D>
@@ -253,27 +297,77 @@ int windows(gbk_ctx *c, const ImageGeom &g, const double *y, long per, int group
   return rc;
 }
 
-int launch_fast(gbk_ctx *c, const ImageGeom &g, const double *x, const double *y, const double *w, const int *start,
-                long ny, double sigma, double *out) {
+template <int D, int KIND, bool F32>
+void launch_image_kind(int dv, unsigned nb, cudaStream_t st, const ImageArgs &a, const ImageGeom &g) {
+  if (KIND == IMG_CONV || dv == 3)
+    image_fast_kernel<D, 3, KIND, F32><<<nb, kThreads, 0, st>>>(a, g);
+  else if (dv == 2)
+    image_fast_kernel<D, 2, KIND, F32><<<nb, kThreads, 0, st>>>(a, g);
+  else
+    image_fast_kernel<D, 1, KIND, F32><<<nb, kThreads, 0, st>>>(a, g);
+}
+
+template <int KIND>
+void launch_image_d(int d, bool f32, int dv, unsigned nb, cudaStream_t st, const ImageArgs &a, const ImageGeom &g) {
+  if (d == 3) {
+    if (f32)
+      launch_image_kind<3, KIND, true>(dv, nb, st, a, g);
+    else
+      launch_image_kind<3, KIND, false>(dv, nb, st, a, g);
+  } else {
+    if (f32)
+      launch_image_kind<2, KIND, true>(dv, nb, st, a, g);
+    else
+      launch_image_kind<2, KIND, false>(dv, nb, st, a, g);
+  }
+}
+
+// One windowed pass of `kind` over the image; the gradients run the dv weight columns as chunks of at
+// most 3 (IMG_GRAD writes its columns of each [p][k][l] row; IMG_GRAD_ALPHA adds the chunks up).
+int launch_fast(gbk_ctx *c, const ImageGeom &g, int kind, const double *x, const double *y, const double *w, int dv,
+                const double *alpha, const int *start, long ny, double sigma, double *out) {
   const long tiles = g.d == 3 ? ((g.n[0] + 7) / 8) * ((g.n[1] + 7) / 8) * ((g.n[2] + 3) / 4)
                               : ((g.n[0] + 15) / 16) * ((g.n[1] + 15) / 16);
   if (tiles > 2147483647L) return c->fail(GBK_ERR_ARG, "image too large");
-  const double s2 = sigma * sigma, pre = std::sqrt(1.4426950408889634) / sigma;  // sqrt(log2 e) / sigma
   const bool f32 = c->mode != GBK_MODE_F64;
   const unsigned nb = (unsigned)tiles;
-  if (g.d == 3) {
-    if (f32)
-      image_fast_kernel<3, true><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
-    else
-      image_fast_kernel<3, false><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
-  } else {
-    if (f32)
-      image_fast_kernel<2, true><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
-    else
-      image_fast_kernel<2, false><<<nb, kThreads, 0, c->stream>>>(x, y, w, start, ny, s2, pre, g, out);
+  ImageArgs a;
+  a.x = x;
+  a.y = y;
+  a.start = start;
+  a.ny = ny;
+  a.s2 = sigma * sigma;
+  a.pre = std::sqrt(1.4426950408889634) / sigma;  // sqrt(log2 e) / sigma
+  a.w_ld = dv;
+  a.alpha_ld = dv;
+  if (kind == IMG_CONV) {
+    a.w = w;
+    a.alpha = nullptr;
+    a.out = out;
+    a.out_ld = g.d;
+    a.acc_out = 0;
+    launch_image_d<IMG_CONV>(g.d, f32, g.d, nb, c->stream, a, g);
+    c->launches += 1;
+    return c->cuda(cudaGetLastError(), "image convolution");
   }
-  c->launches += 1;
-  return c->cuda(cudaGetLastError(), "image convolution");
+  for (int c0 = 0; c0 < dv; c0 += 3) {
+    const int cw = std::min(3, dv - c0);
+    a.w = w + c0;
+    a.alpha = alpha ? alpha + c0 : nullptr;
+    a.acc_out = c0 > 0;
+    if (kind == IMG_GRAD) {
+      a.out = out + (long)c0 * g.d;
+      a.out_ld = dv * g.d;
+      launch_image_d<IMG_GRAD>(g.d, f32, cw, nb, c->stream, a, g);
+    } else {
+      a.out = out;
+      a.out_ld = g.d;
+      launch_image_d<IMG_GRAD_ALPHA>(g.d, f32, cw, nb, c->stream, a, g);
+    }
+    c->launches += 1;
+    if (int rc = c->cuda(cudaGetLastError(), "image gradient")) return rc;
+  }
+  return GBK_OK;
 }
 
 size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -337,8 +431,59 @@ int gbk_convolve_image_fast(gbk_ctx *c, int d, const double *x, long nx, const d
   if (int rc = windows(c, g, dy, ny, 1, sigma, start, bad, bad_host)) return rc;
   if (bad_host[0] != 0x7f7f7f7f)
     return c->fail(GBK_ERR_ARG, "control point %d: its window misses the image", bad_host[0]);
-  if (int rc = launch_fast(c, g, dx, dy, dw, start, ny, sigma, dout)) return rc;
+  if (int rc = launch_fast(c, g, IMG_CONV, dx, dy, dw, d, nullptr, start, ny, sigma, dout)) return rc;
   return io.finish();
+}
+
+// ExactKernel::ConvolveGradientImageFast, both overloads: alpha == null gives the gradients
+// (nx x dv x d), else their contraction with alpha (nx x d).
+static int image_gradient(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y, const double *w,
+                          long ny, double sigma, const double *alpha, const double *origin, const double *spacing,
+                          const long *size, double *out) {
+  if (sigma < 1e-10) sigma = 1e-10;  // AbstractKernel::SetKernelWidth
+  ImageGeom g;
+  if (int rc = geom_from(c, d, origin, spacing, size, sigma, &g)) return rc;
+  if (nx != g.pixels()) return c->fail(GBK_ERR_ARG, "x has %ld rows for an image of %ld pixels", nx, g.pixels());
+  if (ny <= 0) return c->fail(GBK_ERR_ARG, "need at least one control point");
+  if (dv <= 0) return c->fail(GBK_ERR_ARG, "weights need at least one column (dv=%d)", dv);
+  if (!x || !y || !w || !out) return c->fail(GBK_ERR_ARG, "null pointer");
+  if (c->capturing()) return c->fail(GBK_ERR_STATE, "reads back the window check; not under stream capture");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  const double *da = alpha ? io.in(alpha, (size_t)nx * dv, "alpha") : nullptr;
+  double *dout = io.out(out, (size_t)nx * (alpha ? d : dv * d), "out");
+  if (io.rc) return io.rc;
+  const size_t b_start = up256((size_t)ny * d * sizeof(int));
+  if (int rc = c->ensure(c->tmp, b_start + 256, "image windows")) return rc;
+  int *start = (int *)c->tmp.p;
+  int *bad = (int *)((char *)c->tmp.p + b_start);
+  std::vector<int> bad_host;
+  if (int rc = windows(c, g, dy, ny, 1, sigma, start, bad, bad_host)) return rc;
+  if (bad_host[0] != 0x7f7f7f7f)
+    return c->fail(GBK_ERR_ARG, "control point %d: its window misses the image", bad_host[0]);
+  if (int rc = launch_fast(c, g, alpha ? IMG_GRAD_ALPHA : IMG_GRAD, dx, dy, dw, dv, da, start, ny, sigma, dout))
+    return rc;
+  return io.finish();
+}
+
+int gbk_convolve_gradient_image_fast(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                                     const double *w, long ny, double sigma, const double *origin,
+                                     const double *spacing, const long *size, double *out) {
+  GBK_IMAGE_GUARD(c);
+  GBK_RANGE();
+  return image_gradient(c, d, dv, x, nx, y, w, ny, sigma, nullptr, origin, spacing, size, out);
+}
+
+int gbk_convolve_gradient_image_fast_alpha(gbk_ctx *c, int d, int dv, const double *x, long nx, const double *y,
+                                           const double *w, long ny, double sigma, const double *alpha,
+                                           const double *origin, const double *spacing, const long *size,
+                                           double *out) {
+  GBK_IMAGE_GUARD(c);
+  GBK_RANGE();
+  if (!alpha) return c->fail(GBK_ERR_ARG, "null pointer");
+  return image_gradient(c, d, dv, x, nx, y, w, ny, sigma, alpha, origin, spacing, size, out);
 }
 
 int gbk_flow_image_maps(gbk_ctx *c, int d, long ncp, const double *pos_traj, const double *mom_traj, int T,
@@ -399,7 +544,8 @@ int gbk_flow_image_maps(gbk_ctx *c, int d, long ncp, const double *pos_traj, con
     if (fast) {
       if (bad_host[t] != 0x7f7f7f7f)
         return c->fail(GBK_ERR_ARG, "time %d, control point %d: its window misses the image", t, bad_host[t]);
-      return launch_fast(c, g, X, dpos + (size_t)t * n, dmom + (size_t)t * n, start + (size_t)t * n, ncp, sigma, V);
+      return launch_fast(c, g, IMG_CONV, X, dpos + (size_t)t * n, dmom + (size_t)t * n, d, nullptr,
+                         start + (size_t)t * n, ncp, sigma, V);
     }
     PairArgs a = pair_args(npix, ncp, sigma);
     a.x = X;

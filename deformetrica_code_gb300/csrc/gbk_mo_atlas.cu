@@ -230,7 +230,7 @@ int gbk_mo_atlas_step(gbk_mo_atlas *a, const double *cp, const double *tmpl, con
   if (!rc) rc = c->cuda(cudaMemcpyAsync(buf[2], mom, nm * sizeof(double), cudaMemcpyDefault, st), "copy");
   double terms[2] = {0, 0};
   if (!rc) {
-    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
     rc = a->evaluate(buf[0], buf[1], buf[1], buf[2], terms, grad_cp ? buf[3] : nullptr, grad_tmpl ? buf[4] : nullptr,
                      grad_mom ? buf[5] : nullptr, nullptr);
   }
@@ -262,7 +262,7 @@ int gbk_mo_atlas_optimize(gbk_mo_atlas *a, double *cp, double *tmpl, double *mom
   if (!cp || !tmpl || !mom || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = a->ncp * a->d, m = a->nv * a->d, nm = (long)a->S * n;
   cudaStream_t st = a->stream;
-  gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+  gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
   // frozen groups live in device copies; groups in the reference's order [cp] [template] momenta
   double *cp_frozen = nullptr, *tmpl_frozen = nullptr;
   int rc = GBK_OK;

@@ -243,7 +243,7 @@ int registration_create(gbk_ctx *c, int d, long ncp, int nobj, const int *kinds,
   {
     long off_t = 0;
     for (int k = 0; k < nobj && !rc; ++k) {
-      gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+      gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
       rc = r->objs[k].surf.set_target(c, r->tgt + off_t * d);
       off_t += r->objs[k].nv_t;
     }
@@ -308,7 +308,7 @@ int gbk_registration_set_point_weights(gbk_registration *r, const double *w_tmpl
   c->stream = r->stream;
   int rc = GBK_OK, clouds = 0;
   {
-    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
     long off_t = 0;
     for (RegObject &o : r->objs) {
       if (o.surf.kind == 2 && o.surf.cell == 1) {  // same buffers: a captured graph reads the new weights
@@ -341,7 +341,7 @@ int gbk_registration_step(gbk_registration *r, const double *cp, const double *m
   int rc = c->cuda(cudaMemcpyAsync(r->cp, cp, nb, cudaMemcpyDefault, r->stream), "copy cp");
   if (!rc) rc = c->cuda(cudaMemcpyAsync(r->mom, mom, nb, cudaMemcpyDefault, r->stream), "copy mom");
   if (!rc) {
-    gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+    gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
     rc = r->run();
   }
   if (!rc && loglik) rc = c->cuda(cudaMemcpyAsync(loglik, r->out, 5 * sizeof(double), cudaMemcpyDefault, r->stream), "copy L");
@@ -390,7 +390,7 @@ int gbk_registration_optimize(gbk_registration *r, double *cp, double *mom, int 
   if (!cp || !mom || !history || !iterations) return c->fail(GBK_ERR_ARG, "null pointer");
   const long n = r->ncp * r->d;
   const size_t nb = (size_t)n * sizeof(double);
-  gbk_ctx::OrderScope off(c, GBK_ORDER_OFF);
+  gbk_ctx::OrderScope off(c, GBK_ORDER_TWO_FLOAT);
   cudaStream_t st = r->stream;
   double *sq_dev = nullptr;
   int rc = c->cuda(cudaMalloc(&sq_dev, 4 * sizeof(double)), "cudaMalloc (optimiser)");

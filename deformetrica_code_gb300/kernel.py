@@ -383,6 +383,38 @@ class GB300ExactKernel:
                    self.m_KernelWidth, _hptr(origin), _hptr(spacing), _hptr(size), _ptr(out))
         return out
 
+    def ConvolveGradientImageFast(self, X, *args):
+        """ExactKernel::ConvolveGradientImageFast, both overloads (ExactKernel.cxx:207-290):
+        (X, image) -> (pixels x dv x d) kernel gradients summed over the control points' windows,
+        (X, alpha, image) -> (pixels x d) their contraction G_p^T alpha_p. The same windows as
+        ConvolveImageFast; any weight column count."""
+        X = _check(X, "X", self.d)
+        Y, W = self._yw()
+        if len(args) == 1:
+            alpha, image = None, args[0]
+        elif len(args) == 2:
+            alpha, image = _check(args[0], "alpha", W.shape[1]), args[1]
+        else:
+            raise TypeError("ConvolveGradientImageFast(X, image) or (X, alpha, image)")
+        origin, spacing, size = image.arrays(self.d)
+        if X.shape[0] != int(np.prod(size)):
+            raise ValueError(f"X has {X.shape[0]} rows for an image of {int(np.prod(size))} pixels")
+        if alpha is not None and alpha.shape[0] != X.shape[0]:
+            raise RuntimeError("X and alpha count mismatch")
+        dv = W.shape[1]
+        if alpha is None:
+            out = _empty_like(X, (X.shape[0], dv, self.d))
+            self.ctx.bind_stream(X, Y, W)
+            self._call(self.ctx.lib.gbk_convolve_gradient_image_fast, self.d, dv, _ptr(X), X.shape[0], _ptr(Y),
+                       _ptr(W), Y.shape[0], self.m_KernelWidth, _hptr(origin), _hptr(spacing), _hptr(size), _ptr(out))
+        else:
+            out = _empty_like(X, (X.shape[0], self.d))
+            self.ctx.bind_stream(X, Y, W, alpha)
+            self._call(self.ctx.lib.gbk_convolve_gradient_image_fast_alpha, self.d, dv, _ptr(X), X.shape[0], _ptr(Y),
+                       _ptr(W), Y.shape[0], self.m_KernelWidth, _ptr(alpha), _hptr(origin), _hptr(spacing),
+                       _hptr(size), _ptr(out))
+        return out
+
     def ForwardAdjoint(self, X, alpha):
         """Convolve plus the gradients of sum_i alpha_i . (K W)_i w.r.t. X, Y and W."""
         X = _check(X, "X", self.d)

@@ -123,7 +123,9 @@ void *gbk_get_stream(const gbk_ctx *ctx);
 int gbk_set_mode(gbk_ctx *ctx, int mode);
 int gbk_get_mode(const gbk_ctx *ctx);
 /* Sets the GBK_ORDER_* policy of later kernel-sum calls (default GBK_ORDER_AUTO). The
- * registration and atlas steps always use GBK_ORDER_OFF. No counterpart in the reference. */
+ * registration, atlas and regression steps always use GBK_ORDER_TWO_FLOAT (no sort inside their graphs;
+ * the adaptive two-float variant keeps their accuracy on points spread wide relative to sigma). No
+ * counterpart in the reference. */
 int gbk_set_order(gbk_ctx *ctx, int order);
 int gbk_get_order(const gbk_ctx *ctx);
 /* Sets the GBK_GRADIENT_* formula of later point-cloud and volume-mesh data terms (default
@@ -434,6 +436,20 @@ int gbk_image_points(gbk_ctx *ctx, int d, const double *origin, const double *sp
 int gbk_convolve_image_fast(gbk_ctx *ctx, int d, const double *x, long nx, const double *y, const double *w, long ny,
                             double sigma, const double *origin, const double *spacing, const long *size,
                             double *out);
+/* ExactKernel::ConvolveGradientImageFast(X, image) (src/support/kernels/ExactKernel.cxx:207-257): the
+ * same windows; out (nx x dv x d, row p = the dv x d matrix G_p) with G_p(k, l) = sum over the control
+ * points y_j whose window holds pixel p of w_jk (x_p - y_j)_l (-2 K(x_p, y_j) / sigma^2)
+ * (EvaluateKernelGradient, ExactKernel.h:98-110); w is ny x dv, any dv >= 1. Errors as
+ * gbk_convolve_image_fast. The reference's image adjoint calls it (AdjointEquationsIntegrator.cxx:196). */
+int gbk_convolve_gradient_image_fast(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                                     const double *w, long ny, double sigma, const double *origin,
+                                     const double *spacing, const long *size, double *out);
+/* ExactKernel::ConvolveGradientImageFast(X, alpha, image) (ExactKernel.cxx:277-290): out (nx x d),
+ * row p = G_p^T alpha_p with G_p as above and alpha nx x dv (AdjointEquationsIntegrator.cxx:389, 401). */
+int gbk_convolve_gradient_image_fast_alpha(gbk_ctx *ctx, int d, int dv, const double *x, long nx, const double *y,
+                                           const double *w, long ny, double sigma, const double *alpha,
+                                           const double *origin, const double *spacing, const long *size,
+                                           double *out);
 /* The backward integration of the image maps (Diffeos.cxx:725-770, non-regression branch): all T
  * maps (T x prod(size) x d) start as the image points; unless |mom_traj[0]| < 1e-20, from
  * t = T-1 down, maps[t-1] = maps[t] - dt V(maps[t]; pos[t], mom[t]) (Heun: the average of both

@@ -1,8 +1,9 @@
 """FP64 numpy restatement of the reference's image-grid kernel path (TEST INFRASTRUCTURE ONLY: the
-oracle of gbk_convolve_image_fast and gbk_flow_image_maps). The reference's code needs ITK images;
-ITK is not available here, so the index rounding and region cropping are restated from ITK's
-documented behaviour and parity with the reference's binary is unpinned (the reference has no test
-of this path either).
+oracle of gbk_convolve_image_fast, gbk_convolve_gradient_image_fast(_alpha) and gbk_flow_image_maps).
+The reference's code needs ITK images; ITK is not available here, so the index rounding and region
+cropping are restated from ITK's documented behaviour. The three ExactKernel methods are pinned
+against the reference's own compiled code run through ITK stand-ins with that behaviour
+(oracle/ref_shim/, tests/golden/image_fast.npz); the reference has no test of this path.
 
 * image points (GridFunctions::ImageToPoints, src/support/utilities/GridFunctions.cxx:41-60): one
   row per pixel in ITK iteration order (first index fastest), the physical point origin +
@@ -14,6 +15,10 @@ of this path either).
   V[p] += W[j] K(X[p], y_j), K = exp(-|X[p] - y_j|^2 / sigma^2), X the rows of the (deformed) image
   points. A region that misses the image cannot be cropped and the reference's ITK region iterator
   throws: here a ValueError;
+* ExactKernel::ConvolveGradientImageFast(X, image) (ExactKernel.cxx:207-257): the same windows; every
+  pixel p of control point j's region gets G[p][k][l] += g_l W[j][k] with g = (X[p] - y_j) (-2 K / sigma^2)
+  (EvaluateKernelGradient, ExactKernel.h:98-110); and ConvolveGradientImageFast(X, alpha, image)
+  (:277-290): out[p][l] = sum_k G[p][k][l] alpha[p][k];
 * Diffeos image maps (src/core/model_tools/deformations/Diffeos.cxx:725-770, the non-regression
   branch): maps[t] = image points for all t; if |mom[0]|_F < 1e-20 nothing moves; else backward
   from t = T-1: dY = conv(maps[t]; pos[t], mom[t]), maps[t-1] = maps[t] - dt dY, with Heun
@@ -73,6 +78,42 @@ def convolve_image_fast(x, y, w, sigma, origin, spacing, size):
         K = np.exp(-sq / s2)
         V[rows] += w[j, :d] * K[:, None]
     return V
+
+
+def convolve_gradient_image_fast(x, y, w, sigma, origin, spacing, size, alpha=None):
+    """ExactKernel::ConvolveGradientImageFast: (prod(size) x dv x d) gradients, or with `alpha`
+    (prod(size) x dv) their contraction (prod(size) x d)."""
+    x, y, w = np.asarray(x, float), np.asarray(y, float), np.asarray(w, float)
+    size = [int(s) for s in size]
+    d = len(size)
+    if x.shape[0] != int(np.prod(size)):
+        raise ValueError("one row of x per pixel")
+    if y.shape[0] != w.shape[0]:
+        raise ValueError("Sources and weights count mismatch")
+    _, _, lo, hi, ok = windows(y, sigma, origin, spacing, size)
+    if not ok.all():
+        raise ValueError(f"control point {int(np.argmin(ok))}: its region misses the image")
+    strides = np.cumprod([1] + size[:-1])
+    s2 = sigma * sigma
+    G = np.zeros((x.shape[0], w.shape[1], d))
+    for j in range(y.shape[0]):
+        axes = [np.arange(lo[j, k], hi[j, k]) for k in range(d)]
+        grid = np.meshgrid(*axes, indexing="ij")
+        rows = sum(g.ravel() * strides[k] for k, g in enumerate(grid))
+        diff = x[rows] - y[j]
+        sq = np.zeros(rows.shape[0])
+        for k in range(d):
+            sq += diff[:, k] * diff[:, k]
+        f = (-2.0 * np.exp(-sq / s2)) / s2
+        g = diff * f[:, None]
+        G[rows] += w[j][None, :, None] * g[:, None, :]
+    if alpha is None:
+        return G
+    alpha = np.asarray(alpha, float)
+    out = np.zeros((x.shape[0], d))
+    for k in range(w.shape[1]):  # sum over k in order, as the reference's G^T alpha
+        out += G[:, k, :] * alpha[:, k:k + 1]
+    return out
 
 
 def _exact_convolve(x, y, w, sigma):

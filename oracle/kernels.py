@@ -81,6 +81,10 @@ _SIGS = {
     "oracle_hess_kdpdq": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _I, _I, _D],
     "oracle_special_hessian": [_I, _I, _D, _D, _L, _F, _D, _D],
 }
+# exported by the reference library only: the image-grid methods through the ITK stand-ins
+_REF_ONLY = {
+    "oracle_ref_image_fast": [_I, _I, _I, _D, _L, _D, _D, _L, _F, _D, _D, _D, ctypes.POINTER(ctypes.c_long), _D],
+}
 # exported by the port only (test denominators, no reference method)
 _PORT_ONLY = {
     "oracle_convolve_mag": [_I, _I, _D, _L, _D, _D, _L, _F, _I, _D],
@@ -111,7 +115,7 @@ class OracleLib:
             fn = getattr(self._lib, name)
             fn.argtypes = argt
             fn.restype = ctypes.c_int
-        for name, argt in _PORT_ONLY.items():
+        for name, argt in {**_PORT_ONLY, **_REF_ONLY}.items():
             if hasattr(self._lib, name):
                 fn = getattr(self._lib, name)
                 fn.argtypes = argt
@@ -211,6 +215,22 @@ class OracleLib:
         out = np.zeros((y.shape[0], d))
         self._check(self._lib.oracle_special_hessian(d, dv, _c(y), _c(w), y.shape[0], sigma,
                                                      _c(xi), _c(out)))
+        return out
+
+    def image_fast(self, kind: int, x, y, w, sigma, origin, spacing, size, alpha=None):
+        """The reference's own image-grid methods (reference library only): kind 0 ConvolveImageFast
+        (nx x d), 1 ConvolveGradientImageFast(X, image) (nx x dv x d), 2 ConvolveGradientImageFast(X,
+        alpha, image) (nx x d); identity direction."""
+        x, y, w, d, dv = self._prep(x, y, w)
+        nx = x.shape[0]
+        a = _f64(alpha) if alpha is not None else np.zeros((nx, dv))
+        o, sp = _f64(origin), _f64(spacing)
+        sz = np.ascontiguousarray(size, dtype=np.int64)
+        shape = {0: (nx, d), 1: (nx, dv, d), 2: (nx, d)}[kind]
+        out = np.zeros(shape)
+        self._check(self._lib.oracle_ref_image_fast(d, kind, dv, _c(x), nx, _c(y), _c(w), y.shape[0], sigma, _c(a),
+                                                    _c(o), _c(sp), sz.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                                                    _c(out)))
         return out
 
     # Source-side adjoint by symmetry of K (see oracle_fwd_adjoint in gauss_oracle.c).

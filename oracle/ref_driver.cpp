@@ -12,6 +12,7 @@
 // oracle_last_error()), -2 for a dimension outside {2, 3}.
 
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -142,6 +143,28 @@ int special_hessian_d(int dv, const double *y, const double *w, long ny, double 
   });
 }
 
+// ExactKernel::ConvolveImageFast (kind 0, out nx x D), ConvolveGradientImageFast(X, image) (kind 1,
+// out nx x dv x D) and ConvolveGradientImageFast(X, alpha, image) (kind 2, out nx x D) on an image of
+// the given origin, spacing and size (identity direction), through the ITK stand-ins of ref_shim/.
+template <unsigned D>
+int image_fast_d(int kind, int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                 double sigma, const double *alpha, const double *origin, const double *spacing,
+                 const long *size, double *out) {
+  return guarded([&] {
+    Setup<D> s(y, w, ny, dv, sigma);
+    auto image = std::make_shared<itk::Image<double, D>>(origin, spacing, size);
+    const MatrixType X = from_rows(x, nx, D);
+    if (kind == 0) {
+      to_rows(s.k.ConvolveImageFast(X, image), out);
+    } else if (kind == 1) {
+      const std::vector<MatrixType> g = s.k.ConvolveGradientImageFast(X, image);
+      for (long i = 0; i < nx; ++i) to_rows(g[(size_t)i], out + i * dv * D);
+    } else {
+      to_rows(s.k.ConvolveGradientImageFast(X, from_rows(alpha, nx, dv), image), out);
+    }
+  });
+}
+
 }  // namespace
 
 #define DISPATCH(fn, ...)                         \
@@ -198,6 +221,13 @@ int oracle_hess_kdpdq(int d, int dv, const double *x, long nx, const double *y, 
 int oracle_special_hessian(int d, int dv, const double *y, const double *w, long ny, double sigma,
                            const double *xi, double *out) {
   DISPATCH(special_hessian, dv, y, w, ny, sigma, xi, out);
+}
+
+// The image-grid methods (reference library only; the port has no counterpart).
+int oracle_ref_image_fast(int d, int kind, int dv, const double *x, long nx, const double *y, const double *w,
+                          long ny, double sigma, const double *alpha, const double *origin, const double *spacing,
+                          const long *size, double *out) {
+  DISPATCH(image_fast, kind, dv, x, nx, y, w, ny, sigma, alpha, origin, spacing, size, out);
 }
 
 }  // extern "C"

@@ -138,6 +138,8 @@ def main(ref_root: str | None = None):
     regression_fixture(ref_root)
     # 8. functional test 2: a banana surface atlas estimated by GradientAscent
     banana_fixture(ref_root)
+    # 9. the image-grid methods of ExactKernel through the ITK stand-ins of oracle/ref_shim
+    image_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
 
 
@@ -314,3 +316,44 @@ def banana_fixture(ref_root: str | None = None):
 
 if __name__ == "__main__":
     main(*(sys.argv[1:2]))
+
+
+def image_cases():
+    """Seeded image-grid cases (deformed image points, control points over the image and past its
+    edges so windows are cropped, dv = d and dv = 4 weights): name -> arrays."""
+    rng = np.random.default_rng(11)
+    cases = {}
+    for name, size, origin, spacing, sigma, ny, dv in (
+            ("d2", [23, 17], [0.5, -1.0], [1.0, 1.5], 2.2, 11, 2),
+            ("d2w4", [16, 21], [-2.0, 0.25], [0.75, 1.0], 1.7, 9, 4),
+            ("d3", [11, 9, 8], [0.0, 0.5, -0.5], [1.0, 1.2, 0.8], 1.45, 10, 3),
+            ("d3w4", [9, 10, 7], [1.0, -1.0, 0.0], [1.1, 0.9, 1.0], 1.2, 8, 4)):
+        d = len(size)
+        from oracle import image as im
+        n = int(np.prod(size))
+        x = im.image_points(origin, spacing, size) + 0.15 * rng.standard_normal((n, d))
+        lo = np.asarray(origin)
+        hi = lo + np.asarray(spacing) * (np.asarray(size) - 1)
+        y = rng.uniform(lo - 1.5, hi + 1.5, (ny, d))
+        cases[name] = dict(x=x, y=y, w=rng.standard_normal((ny, dv)), alpha=rng.standard_normal((n, dv)),
+                           sigma=np.array(sigma), origin=np.asarray(origin, float),
+                           spacing=np.asarray(spacing, float), size=np.asarray(size, np.int64))
+    return cases
+
+
+def image_fixture(ref_root: str | None = None):
+    """ExactKernel::ConvolveImageFast (dv = d cases) and both ConvolveGradientImageFast overloads
+    (ExactKernel.cxx:76-129, 207-290), computed by the reference's own compiled code on the ITK
+    stand-ins of oracle/ref_shim: tests/golden/image_fast.npz."""
+    oracle.build_reference(ref_root)
+    ref = oracle.load("reference")
+    res = {}
+    for name, c in image_cases().items():
+        for k, v in c.items():
+            res[f"{name}_{k}"] = v
+        args = (c["x"], c["y"], c["w"], float(c["sigma"]), c["origin"], c["spacing"], c["size"])
+        if c["w"].shape[1] == c["x"].shape[1]:
+            res[f"{name}_convolve"] = ref.image_fast(0, *args)
+        res[f"{name}_gradient"] = ref.image_fast(1, *args)
+        res[f"{name}_gradient_alpha"] = ref.image_fast(2, *args, alpha=c["alpha"])
+    np.savez_compressed(os.path.join(HERE, "image_fast.npz"), **res)

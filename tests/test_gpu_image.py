@@ -1,6 +1,7 @@
-"""GPU image-grid path (gbk_image_points, gbk_convolve_image_fast, gbk_flow_image_maps) against the
-oracle's restatement of ExactKernel::ConvolveImageFast and Diffeos' image-map integration
-(oracle/image.py). In GBK_MODE_F64 the windowed sums follow the reference's arithmetic and order of
+"""GPU image-grid path (gbk_image_points, gbk_convolve_image_fast, gbk_convolve_gradient_image_fast(_alpha),
+gbk_flow_image_maps) against the oracle's restatement of ExactKernel::ConvolveImageFast,
+ConvolveGradientImageFast and Diffeos' image-map integration (oracle/image.py), and against the
+reference's own ExactKernel image methods (golden vectors, tests/golden/image_fast.npz). In GBK_MODE_F64 the windowed sums follow the reference's arithmetic and order of
 additions per pixel and differ from the oracle only through exp (1e-13 normwise); GBK_MODE_F32C
 evaluates them in FP32 with compensated sums (1e-6)."""
 import numpy as np
@@ -139,3 +140,61 @@ def test_flow_image_maps_box_and_zero_momenta(gb):
     maps, stop = gb.flow_image_maps(pos, 0.0 * mom, sigma, im, context=ctx)
     assert stop is None
     np.testing.assert_array_equal(maps, np.repeat(im.points()[None], pos.shape[0], axis=0))
+
+
+GOLDEN_CASES = ("d2", "d2w4", "d3", "d3w4")
+
+
+@pytest.fixture(scope="module")
+def image_golden():
+    import os
+    from tests.conftest import GOLDEN
+    return dict(np.load(os.path.join(GOLDEN, "image_fast.npz")))
+
+
+def _golden_case(image_golden, name):
+    return {k[len(name) + 1:]: v for k, v in image_golden.items() if k.startswith(name + "_")}
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("mode,tol", [("F64", 1e-12), ("F32C", 1e-6)])
+def test_image_methods_match_the_reference(gb, image_golden, name, mode, tol):
+    """ConvolveImageFast and both ConvolveGradientImageFast overloads against the reference's own
+    compiled ExactKernel (golden vectors; dv = 4 runs as two column chunks): FP64 to the exp's rounding,
+    FP32C normwise within 1e-6; host and device arrays give the same bits."""
+    import torch
+    g = _golden_case(image_golden, name)
+    d = g["x"].shape[1]
+    im = gb.ImageGrid(g["origin"], g["spacing"], g["size"])
+    k = gb.GB300ExactKernel(d, float(g["sigma"]), mode=getattr(gb, f"GBK_MODE_{mode}"))
+    k.SetSources(g["y"])
+    k.SetWeights(g["w"])
+    got = {"gradient": k.ConvolveGradientImageFast(g["x"], im),
+           "gradient_alpha": k.ConvolveGradientImageFast(g["x"], g["alpha"], im)}
+    if "convolve" in g:
+        got["convolve"] = k.ConvolveImageFast(g["x"], im)
+    for key, v in got.items():
+        r = g[key].reshape(v.shape[0], -1)
+        e = np.linalg.norm(v.reshape(v.shape[0], -1) - r, axis=1).max() / np.linalg.norm(r, axis=1).max()
+        assert e <= tol, (key, e)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    kd = gb.GB300ExactKernel(d, float(g["sigma"]), context=k.ctx)
+    kd.SetSources(dev(g["y"]))
+    kd.SetWeights(dev(g["w"]))
+    np.testing.assert_array_equal(kd.ConvolveGradientImageFast(dev(g["x"]), dev(g["alpha"]), im).cpu().numpy(),
+                                  got["gradient_alpha"])
+    np.testing.assert_array_equal(kd.ConvolveGradientImageFast(dev(g["x"]), im).cpu().numpy(), got["gradient"])
+
+
+def test_image_gradient_errors(gb):
+    size, origin, spacing, pos, mom = _case(2)
+    im = gb.ImageGrid(origin, spacing, size)
+    k = gb.GB300ExactKernel(2, 1.5)
+    k.SetSources(pos[0] + 1e3)  # every window misses the image
+    k.SetWeights(mom[0])
+    x = im.points()
+    with pytest.raises(gb.GBKError, match="misses the image"):
+        k.ConvolveGradientImageFast(x, im)
+    k.SetSources(pos[0])
+    with pytest.raises(RuntimeError, match="count mismatch"):
+        k.ConvolveGradientImageFast(x, np.zeros((7, 2)), im)

@@ -1,7 +1,9 @@
 """The image-grid oracle (oracle/image.py): pixel order, the windowed sum of
 ExactKernel::ConvolveImageFast against a pair-by-pair restatement, its truncation against the exact
-sum, the rounding of the window start, and the image-map flow's special cases. No reference test
-pins this path (it needs ITK)."""
+sum, the rounding of the window start, and the image-map flow's special cases. The reference has no
+test of this path (it needs ITK); ConvolveImageFast and both ConvolveGradientImageFast overloads are
+pinned against the reference's own compiled code run on ITK stand-ins with ITK's documented index,
+crop and iteration behaviour (tests/golden/image_fast.npz, tests/golden/make_golden.py)."""
 import numpy as np
 import pytest
 
@@ -112,3 +114,49 @@ def test_bench_window_count_matches_the_restatement():
     _, L, lo, hi, _ = IM.windows(cp, sigma, origin, spacing, [n] * 3)
     ref = np.prod(np.maximum(hi - lo, 0), axis=1).sum()
     assert bench.image_window_pairs(cp, sigma, origin, spacing, [n] * 3) == ref
+
+
+GOLDEN_CASES = ("d2", "d2w4", "d3", "d3w4")
+
+
+@pytest.fixture(scope="module")
+def image_golden():
+    import os
+    from tests.conftest import GOLDEN
+    return dict(np.load(os.path.join(GOLDEN, "image_fast.npz")))
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_restatement_matches_the_reference_image_methods(image_golden, name):
+    """ConvolveImageFast and both ConvolveGradientImageFast overloads of the reference (golden
+    vectors from its compiled ExactKernel) against the restatement, to FP64 rounding."""
+    g = {k[len(name) + 1:]: v for k, v in image_golden.items() if k.startswith(name + "_")}
+    args = (g["x"], g["y"], g["w"], float(g["sigma"]), g["origin"], g["spacing"], [int(v) for v in g["size"]])
+    if "convolve" in g:
+        v = IM.convolve_image_fast(*args)
+        assert np.abs(v - g["convolve"]).max() <= 1e-14 * np.abs(g["convolve"]).max()
+    G = IM.convolve_gradient_image_fast(*args)
+    assert G.shape == g["gradient"].shape
+    assert np.abs(G - g["gradient"]).max() <= 1e-14 * np.abs(g["gradient"]).max()
+    assert (g["gradient"] == 0).any() and (g["gradient"] != 0).mean() > 0.5  # cropped and covered pixels
+    H = IM.convolve_gradient_image_fast(*args, alpha=g["alpha"])
+    assert np.abs(H - g["gradient_alpha"]).max() <= 1e-14 * np.abs(g["gradient_alpha"]).max()
+
+
+def test_image_gradient_is_the_derivative_of_the_windowed_sum():
+    """Inside every window, d/dx_p of sum_j W_jk K(x_p, y_j) is the gradient's row (finite
+    differences on one pixel's coordinates; the windows do not move with x)."""
+    rng = np.random.default_rng(3)
+    size, origin, spacing, sigma = [12, 10], [0.0, 0.0], [1.0, 1.0], 1.6
+    x = IM.image_points(origin, spacing, size)
+    y = rng.uniform([2, 2], [9, 7], (5, 2))
+    w = rng.standard_normal((5, 2))
+    G = IM.convolve_gradient_image_fast(x, y, w, sigma, origin, spacing, size)
+    p, eps = 47, 1e-6
+    for l in range(2):
+        xp, xm = x.copy(), x.copy()
+        xp[p, l] += eps
+        xm[p, l] -= eps
+        fd = (IM.convolve_image_fast(xp, y, w, sigma, origin, spacing, size)[p]
+              - IM.convolve_image_fast(xm, y, w, sigma, origin, spacing, size)[p]) / (2 * eps)
+        np.testing.assert_allclose(G[p, :, l], fd, rtol=1e-6, atol=1e-9)

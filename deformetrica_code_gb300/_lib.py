@@ -26,6 +26,9 @@ GBK_ORDER_OFF = 1
 GBK_ORDER_SPATIAL = 2
 GBK_ORDER_SPATIAL_NOPRUNE = 3
 GBK_ORDER_TWO_FLOAT = 4
+GBK_STAGING_AUTO = 0
+GBK_STAGING_LOADS = 1
+GBK_STAGING_BULK = 2
 GBK_GRADIENT_REFERENCE = 0
 GBK_GRADIENT_EXACT = 1
 GBK_ESTIMATOR_FAST_GRADIENT_ASCENT = 0
@@ -126,6 +129,9 @@ SIGNATURES = {
     "gbk_p3m_convolve_hessian_kdpdq": (_I, [_P, _I, _I, _L, _L, _I, _I, _I, _P]),
     "gbk_set_alloc_limit": (_I, [_P, ctypes.c_size_t]),
     "gbk_inject_pointer_device": (_I, [_P, _I]),
+    "gbk_set_staging": (_I, [_P, _I]),
+    "gbk_get_staging": (_I, [_P]),
+    "gbk_last_launch": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "gbk_image_points": (_I, [_P, _I, _P, _P, _P, _P]),
     "gbk_convolve_image_fast": (_I, [_P, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P]),
     "gbk_convolve_gradient_image_fast": (_I, [_P, _I, _I, _P, _L, _P, _P, _L, _D, _P, _P, _P, _P]),

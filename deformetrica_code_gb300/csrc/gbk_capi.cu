@@ -45,6 +45,8 @@ int op_outputs(int op, int d, int dv) {
 bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
   if (variant == VARIANT_TWO_FLOAT || variant == VARIANT_SMALL_TWO_FLOAT)  // Convolve-like ops only
     return (op == OP_CONV || op == OP_CONV_GRADA || op == OP_GRADA) && find_kernel_conv(op, mode, d, dv, variant, e);
+  if (variant == VARIANT_BULK)
+    return mode == MODE_F32C && find_kernel_conv_bulk(op, d, dv, e);
   switch (op) {
     case OP_CONV:
     case OP_CONV_GRADA:
@@ -269,11 +271,6 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
       auto_choice = order == GBK_ORDER_AUTO ? AUTO_SPATIAL : AUTO_OFF;
     }
   }
-  KernelEntry e;
-  if (!find_kernel(op, mode, d, dv, variant, &e) && !find_kernel(op, mode, d, dv, 0, &e))
-    return fail(GBK_ERR_UNSUPPORTED, "no kernel for op %d, d=%d, dv=%d", op, d, dv);
-  if (force_split > 0) ns = force_split;
-  if (ns <= 0) ns = choose_split(e, d, a.nx, a.ny);
   // spatial order of targets and sources (see GBK_ORDER_* in gbk.h)
   bool spatial = false, prune = false;
   if (unordered) {
@@ -284,6 +281,17 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
       default: break;
     }
   }
+  // bulk asynchronous staging of the sorted source copies (GBK_STAGING_*): the spatial order's
+  // default-shape Convolve-like launches
+  if (spatial && variant == 0 && (staging == GBK_STAGING_BULK || (staging == GBK_STAGING_AUTO && kBulkByDefault))) {
+    KernelEntry eb;
+    if (find_kernel(op, mode, d, dv, VARIANT_BULK, &eb)) variant = VARIANT_BULK;
+  }
+  KernelEntry e;
+  if (!find_kernel(op, mode, d, dv, variant, &e) && !find_kernel(op, mode, d, dv, 0, &e))
+    return fail(GBK_ERR_UNSUPPORTED, "no kernel for op %d, d=%d, dv=%d", op, d, dv);
+  if (force_split > 0) ns = force_split;
+  if (ns <= 0) ns = choose_split(e, d, a.nx, a.ny);
   if (spatial) {
     // sorted copies of the source rows the op reads (y, the weight columns, the special Hessian's
     // xi); OpAdjointCP's source extras share arrays with its targets, so it gathers while staging
@@ -343,6 +351,11 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     }
   }
   a.pair_count = pair_counter;
+  a.status = status;
+  // the bulk copies read whole chunks of the sorted copies, which order_sources pads to whole chunks
+  a.bulk = spatial && variant == VARIANT_BULK && op != OP_ADJCP && op != OP_SPECIAL && a.w_ld == dv ? 1 : 0;
+  last_variant = variant;
+  last_nsplit = ns;
   if (ns > 1) {
     // launch_pairs rounds the split count; size the buffer for the requested count
     int rc = ensure(partial, (size_t)ns * e.no * std::max(a.nx, 1L) * sizeof(double), "split partials");
@@ -465,8 +478,8 @@ int gbk_create(int device, gbk_ctx **out) {
   }
   c->stream = c->own_stream;
   // pair counter and the spatial order's self-resetting ticket
-  if (cudaMalloc(&c->pair_counter, 3 * sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMemset(c->pair_counter, 0, 3 * sizeof(unsigned long long)) != cudaSuccess) {
+  if (cudaMalloc(&c->pair_counter, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(c->pair_counter, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     c->release();
     cudaStreamDestroy(c->own_stream);
@@ -484,6 +497,7 @@ int gbk_create(int device, gbk_ctx **out) {
   }
   c->order_ticket = reinterpret_cast<unsigned *>(c->pair_counter + 1);
   c->nonfinite = reinterpret_cast<unsigned *>(c->pair_counter + 2);
+  c->status = reinterpret_cast<unsigned *>(c->pair_counter + 3);
   noalloc_refresh_device(device);
   *out = c;
   return GBK_OK;
@@ -563,7 +577,31 @@ int gbk_get_estimator(const gbk_ctx *c) { return c ? c->estimator : -1; }
 int gbk_synchronize(gbk_ctx *c) {
   GBK_GUARD(c);
   GBK_RANGE();
-  return c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  if (int rc = c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize")) return rc;
+  unsigned st = 0;
+  if (int rc = c->cuda(cudaMemcpy(&st, c->status, sizeof st, cudaMemcpyDeviceToHost), "status read")) return rc;
+  if (st) {
+    cudaMemset(c->status, 0, sizeof st);
+    return c->fail(GBK_ERR_TIMEOUT, "a bounded device-side wait gave up in a kernel sum since the last check; "
+                   "its outputs are not valid");
+  }
+  return GBK_OK;
+}
+
+int gbk_set_staging(gbk_ctx *c, int staging) {
+  if (!c) return GBK_ERR_ARG;
+  if (staging < GBK_STAGING_AUTO || staging > GBK_STAGING_BULK) return c->fail(GBK_ERR_ARG, "unknown staging %d", staging);
+  c->staging = staging;
+  return GBK_OK;
+}
+
+int gbk_get_staging(const gbk_ctx *c) { return c ? c->staging : -1; }
+
+int gbk_last_launch(const gbk_ctx *c, int *variant, int *nsplit) {
+  if (!c) return GBK_ERR_ARG;
+  if (variant) *variant = c->last_variant;
+  if (nsplit) *nsplit = c->last_nsplit;
+  return GBK_OK;
 }
 
 long long gbk_launch_count(const gbk_ctx *c) { return c ? c->launches : 0; }

@@ -28,6 +28,11 @@ struct f32s {};  // tag: scalar FP32 lanes
 // longer depends on how far the CTA's points spread from its centre (caller order on data spread
 // wide relative to sigma). Costs 2 packed adds per coordinate per pair.
 struct f32w {};
+// Tag: packed FP32 lanes (as float) whose source tiles are staged by bulk asynchronous copies
+// (cp.async.bulk into a double-buffered shared area, completion tracked by mbarriers) when the
+// launch's sources are the library's own chunk-padded sorted copies (PairArgs::bulk); otherwise the
+// kernel stages with ordinary loads. Same arithmetic, same bits as float.
+struct f32b {};
 
 template <typename T>
 struct Lane;
@@ -58,6 +63,8 @@ struct Lane<float> {
 
 template <>
 struct Lane<f32w> : Lane<float> {};
+template <>
+struct Lane<f32b> : Lane<float> {};
 
 template <>
 struct Lane<f32s> {
@@ -105,6 +112,8 @@ struct SrcVal<float> {
 template <>
 struct SrcVal<f32w> : SrcVal<float> {};
 template <>
+struct SrcVal<f32b> : SrcVal<float> {};
+template <>
 struct SrcVal<f32s> {
   __device__ __forceinline__ static float make(double v) { return (float)v; }
 };
@@ -130,6 +139,8 @@ struct Comp {
 };
 template <>
 struct Comp<f32w> : Comp<float> {};
+template <>
+struct Comp<f32b> : Comp<float> {};
 template <>
 struct Comp<f32s> {
   __device__ __forceinline__ static void fold(float &sum, float &comp, float run) {
@@ -162,6 +173,10 @@ __host__ __device__ inline double coord_scale<f32w>(double sigma) {
   return 1.2011224087864498 / sigma;
 }
 template <>
+__host__ __device__ inline double coord_scale<f32b>(double sigma) {
+  return 1.2011224087864498 / sigma;
+}
+template <>
 __host__ __device__ inline double coord_scale<double>(double) {
   return 1.0;
 }
@@ -178,6 +193,10 @@ template <>
 __host__ __device__ inline float2 exp_arg_scale<f32w>(double sigma) {
   return float2{0.f, 0.f};
 }
+template <>
+__host__ __device__ inline float2 exp_arg_scale<f32b>(double sigma) {
+  return float2{0.f, 0.f};
+}
 
 // Squared distance (input units) beyond which the lane type's kernel value is exactly zero, with
 // margin. FP32 lanes evaluate ex2.approx.ftz(-r2) on coordinates scaled by coord_scale: for
@@ -192,6 +211,49 @@ inline double prune_dist2(double sigma) {
 template <>
 inline double prune_dist2<double>(double sigma) {
   return 800.0 * sigma * sigma;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bulk asynchronous copies global -> shared (cp.async.bulk) completed on an mbarrier in shared
+// memory. Addresses must be 16-byte aligned and sizes multiples of 16 bytes; an mbarrier phase
+// takes at most 2^20 - 1 bytes of transactions.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+// makes the initialised barriers visible to the asynchronous proxy
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// one arrival that also announces `bytes` of transactions for the current phase
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for the phase of `parity` to complete for at most ~2^31 SM clock cycles (about one second);
+// false if it did not.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > (1LL << 31)) return false;
+  return true;
+}
+// orders this thread's earlier generic-proxy accesses of shared memory before later asynchronous
+// copies into it (the buffer being refilled was read by ordinary loads)
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
 }
 
 }  // namespace gbk

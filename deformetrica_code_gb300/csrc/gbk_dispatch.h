@@ -29,6 +29,9 @@ constexpr int VARIANT_SMALL = 8;
 // to sigma when sorting them would cost more than it saves (gbk_ctx::launch).
 constexpr int VARIANT_TWO_FLOAT = 9;
 constexpr int VARIANT_SMALL_TWO_FLOAT = 10;
+// Bulk asynchronous staging of the source tiles (lane tag f32b), default shape: compiled for the
+// Convolve and alpha-gradient ops in FP32C mode, for the spatial order's sorted source copies.
+constexpr int VARIANT_BULK = 11;
 
 enum Mode { MODE_F32C = 0, MODE_F64 = 1 };
 
@@ -65,6 +68,7 @@ void noalloc_refresh_device(int device);
 // Per-family lookups (one per instantiation file).
 bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_conv_two_float(int op, int d, int dv, int variant, KernelEntry *e);
+bool find_kernel_conv_bulk(int op, int d, int dv, KernelEntry *e);
 bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_deform(int op, int mode, int d, int dv, int variant, KernelEntry *e);

@@ -586,8 +586,11 @@ int order_sources(gbk_ctx *c, int d, const double *y, const SortedSet &s, int ch
   const long n = s.n, nchunks = (n + chunk - 1) / chunk;
   if (int rc = c->ensure(c->order_keep[1], al((size_t)nchunks * 2 * d * 8), "source boxes")) return rc;
   SourceCopies sc = want;
+  // every copy is padded to whole chunks, so a chunk can be fetched whole (bulk staging); the rows
+  // past n are never used
+  const size_t npad = (size_t)nchunks * chunk;
   size_t copy_bytes = 0;
-  for (int k = 0; k < sc.na; ++k) copy_bytes += al((size_t)n * sc.cols[k] * sizeof(double));
+  for (int k = 0; k < sc.na; ++k) copy_bytes += al(npad * sc.cols[k] * sizeof(double));
   if (copy_bytes)
     if (int rc = c->ensure(c->order_src, copy_bytes, "sorted source copies")) return rc;
   char *cb = (char *)c->order_src.p;
@@ -595,7 +598,7 @@ int order_sources(gbk_ctx *c, int d, const double *y, const SortedSet &s, int ch
     sc.dst[k] = nullptr;
     if (k < sc.na) {
       sc.dst[k] = (double *)cb;
-      cb += al((size_t)n * sc.cols[k] * sizeof(double));
+      cb += al(npad * sc.cols[k] * sizeof(double));
     }
   }
   double *boxes = (double *)c->order_keep[1].p;

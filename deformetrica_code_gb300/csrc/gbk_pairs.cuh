@@ -64,6 +64,11 @@ struct PairArgs {
   double prune_d2;     // a source chunk whose box is farther than this (squared) from the CTA's
                        // target box contributes exact zeros only (set by launch_pairs)
   unsigned long long *pair_count;  // if set, += (target, source) pairs this launch evaluated
+  // bulk staging (lane tag f32b): 1 when y and w are the library's sorted copies, contiguous
+  // (w_ld = the op's weight columns), padded to whole TJ-record chunks and 16-byte aligned, so every
+  // chunk can be fetched whole by cp.async.bulk; 0 stages with ordinary loads
+  int bulk;
+  unsigned *status;  // device word: bit 0 set when a bounded wait of the launch gave up (null: none)
 };
 
 __device__ __forceinline__ void put(double *p, int acc, double v) {
@@ -417,6 +422,10 @@ struct SrcLane<f32w> {
   typedef float2 SV;
 };
 template <>
+struct SrcLane<f32b> {
+  typedef float2 SV;
+};
+template <>
 struct SrcLane<f32s> {
   typedef float SV;
 };
@@ -434,6 +443,8 @@ struct Pack<float> {
 };
 template <>
 struct Pack<f32w> : Pack<float> {};
+template <>
+struct Pack<f32b> : Pack<float> {};
 template <>
 struct Pack<f32s> {
   __device__ __forceinline__ static float make(double a, double) { return (float)a; }
@@ -458,7 +469,33 @@ struct Rec {
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int CSM>
 constexpr size_t pair_smem_bytes() {
   return (size_t)TJ * Rec<Op, D, T>::NJP * sizeof(typename SrcLane<T>::SV) +
-         (size_t)CSM * (R / Lane<T>::kWidth) * Op::NO * BLOCK * sizeof(typename Lane<T>::V);
+         (size_t)CSM * (R / Lane<T>::kWidth) * Op::NO * BLOCK * sizeof(typename Lane<T>::V) +
+         (std::is_same<T, f32b>::value ? (size_t)2 * TJ * (D + Op::NS) * sizeof(double) : 0);
+}
+
+// Bulk staging state of a CTA (lane tag f32b): the two buffers' mbarriers, the parity each waits for
+// next, and the elected thread's verdict on the last wait. One instance per kernel, kept across the
+// target tiles a CTA loops over.
+struct BulkState {
+  unsigned long long bar[2];
+  unsigned parity[2];
+  unsigned ok;
+};
+__device__ __forceinline__ BulkState &bulk_state() {
+  __shared__ BulkState s;
+  return s;
+}
+// Called by every thread of a bulk-staging kernel before its first tile.
+__device__ __forceinline__ void bulk_init() {
+  BulkState &st = bulk_state();
+  if (threadIdx.x == 0) {
+    mbar_init(&st.bar[0], 1);
+    mbar_init(&st.bar[1], 1);
+    st.parity[0] = st.parity[1] = 0;
+    st.ok = 1;
+    mbar_fence_init();
+  }
+  __syncthreads();
 }
 
 // Source chunks per visit mask (pruning): 512 bytes of shared memory.
@@ -542,61 +579,33 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const int split, co
   if (je > a.ny) je = a.ny;
   long visited = 0;  // sources of the visited chunks
 
-  for (long jt = jb; jt < je; jt += TJ) {
-    if (prune) {
-      // Visit mask of the next kPruneWindow source chunks, one distance test per chunk for the
-      // whole CTA (FP64, spread over the threads), then one shared-memory bit per chunk.
-      const long q = (jt - jb) / TJ;
-      const int wq = (int)(q % kPruneWindow);
-      if (wq == 0) {
-        __syncthreads();  // every thread is done with the previous window's mask
+  // Visit mask of the kPruneWindow source chunks from jt: one distance test per chunk for the whole
+  // CTA (FP64, spread over the threads), then one shared-memory bit per chunk. Collective.
+  auto make_mask = [&](const long jt) {
+    __syncthreads();  // every thread is done with the previous window's mask
 #pragma unroll 4
-        for (int r = 0; r < kPruneWindow / BLOCK; ++r) {
-          const long jc = jt + (long)(r * BLOCK + threadIdx.x) * TJ;  // first source of the chunk
-          bool visit = false;
-          if (jc < je) {
-            const double *cb = a.ybox + (jc / TJ) * (2 * D);
-            double d2 = 0.0;
+    for (int r = 0; r < kPruneWindow / BLOCK; ++r) {
+      const long jc = jt + (long)(r * BLOCK + threadIdx.x) * TJ;  // first source of the chunk
+      bool visit = false;
+      if (jc < je) {
+        const double *cb = a.ybox + (jc / TJ) * (2 * D);
+        double d2 = 0.0;
 #pragma unroll
-            for (int l = 0; l < D; ++l) {
-              const double gap = fmax(0.0, fmax(cb[l] - s_box[D + l], s_box[l] - cb[D + l]));
-              d2 += gap * gap;
-            }
-            visit = !(d2 > a.prune_d2);
-          }
-          const unsigned bits = __ballot_sync(0xffffffffu, visit);
-          if ((threadIdx.x & 31) == 0) s_visit[(r * BLOCK + threadIdx.x) >> 5] = bits;
+        for (int l = 0; l < D; ++l) {
+          const double gap = fmax(0.0, fmax(cb[l] - s_box[D + l], s_box[l] - cb[D + l]));
+          d2 += gap * gap;
         }
-        __syncthreads();
+        visit = !(d2 > a.prune_d2);
       }
-      if (!((s_visit[wq >> 5] >> (wq & 31)) & 1u)) continue;  // same decision in every thread
-    }
-    const int cnt = (int)((je - jt) < TJ ? (je - jt) : TJ);
-    visited += cnt;
-    // ---- stage TJ source records: -(y - c) * xscale and extras, broadcast to the lane type ----
-    for (int r = threadIdx.x; r < TJ; r += BLOCK) {
-      double rec[NJP];
-      if (r < cnt) {
-        long j = jt + r;
-        if (yperm) j = yperm[j];
-#pragma unroll
-        for (int l = 0; l < D; ++l) rec[l] = (ctr[l] - a.y[j * D + l]) * xs;
-        Op::load_source(a, j, rec + D);
-        if (TWOF) {
-#pragma unroll
-          for (int l = 0; l < D; ++l) rec[LO + l] = rec[l] - (double)(float)rec[l];
-        }
-      } else {
-#pragma unroll
-        for (int q = 0; q < NJ; ++q) rec[q] = 0.0;  // zero weights: exact no-op
-      }
-#pragma unroll
-      for (int q = NJ; q < NJP; ++q) rec[q] = 0.0;
-#pragma unroll
-      for (int q = 0; q < NJP; ++q) tile[r * NJP + q] = SrcVal<T>::make(rec[q]);
+      const unsigned bits = __ballot_sync(0xffffffffu, visit);
+      if ((threadIdx.x & 31) == 0) s_visit[(r * BLOCK + threadIdx.x) >> 5] = bits;
     }
     __syncthreads();
+  };
 
+  // Every pair of the staged tile's first cnt sources with the thread's targets, folded into the
+  // compensated sums run by run.
+  auto compute_tile = [&](const int cnt) {
     const int nrun = (cnt + MERGE - 1) / MERGE;
     for (int run = 0; run < nrun; ++run) {
       const SV *rp = tile + run * MERGE * NJP;
@@ -647,9 +656,129 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const int split, co
           acc[g][o] = L::zero();
         }
     }
+  };
+
+  if constexpr (std::is_same<T, f32b>::value) {
+    if (a.bulk) {  // bulk asynchronous staging of the library's chunk-padded sorted source copies
+      static_assert(!TWOF && NJ == D + Op::NS, "bulk staging stages coordinates and weights only");
+      BulkState &st = bulk_state();
+      double *raw = reinterpret_cast<double *>(smem_raw + (size_t)TJ * Rec<Op, D, T>::NJP * sizeof(SV) +
+                                               (size_t)CSM * G * NO * BLOCK * sizeof(V));
+      constexpr unsigned kBytesY = TJ * D * sizeof(double), kBytesW = TJ * Op::NS * sizeof(double);
+      const long nch = (je - jb + TJ - 1) / TJ;  // chunks of this split
+      long cur_window = -1;
+      // first visited chunk >= q of this split, or nch (collective: may build a window's mask)
+      auto next_visited = [&](long q) -> long {
+        while (q < nch) {
+          if (!prune) return q;
+          const long wbase = q - q % kPruneWindow;
+          if (wbase != cur_window) {
+            make_mask(jb + wbase * TJ);
+            cur_window = wbase;
+          }
+          const int wq = (int)(q - wbase);
+          for (int w = wq >> 5; w < kPruneWindow / 32; ++w) {
+            unsigned bits = s_visit[w];
+            if (w == (wq >> 5)) bits &= ~0u << (wq & 31);
+            if (bits) {
+              const long c = wbase + w * 32 + (__ffs(bits) - 1);
+              return c < nch ? c : nch;
+            }
+          }
+          q = wbase + kPruneWindow;
+        }
+        return nch;
+      };
+      // the elected thread fetches chunk q (coordinates, then weights) into buffer b
+      auto issue = [&](const long q, const int b) {
+        double *ry = raw + (size_t)b * TJ * (D + Op::NS);
+        const long jt = jb + q * TJ;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&st.bar[b], kBytesY + kBytesW);
+        bulk_copy_g2s(ry, a.y + jt * D, kBytesY, &st.bar[b]);
+        bulk_copy_g2s(ry + TJ * D, a.w + jt * Op::NS, kBytesW, &st.bar[b]);
+      };
+      unsigned par[2] = {st.parity[0], st.parity[1]};
+      long q = next_visited(0);
+      int b = 0;
+      if (threadIdx.x == 0 && q < nch) issue(q, 0);
+      while (q < nch) {
+        const long jt = jb + q * TJ;
+        const int cnt = (int)((je - jt) < TJ ? (je - jt) : TJ);
+        visited += cnt;
+        if (threadIdx.x == 0) st.ok = mbar_wait_bounded(&st.bar[b], par[b]) ? 1u : 0u;
+        __syncthreads();
+        if (!st.ok) {  // the copy never completed: report it; the CTA stops (pair_kernel checks st.ok)
+          if (threadIdx.x == 0 && a.status) atomicOr(a.status, 1u);
+          return;
+        }
+        par[b] ^= 1u;
+        const double *ry = raw + (size_t)b * TJ * (D + Op::NS), *rw = ry + TJ * D;
+        for (int r = threadIdx.x; r < TJ; r += BLOCK) {
+          double rec[NJP];
+#pragma unroll
+          for (int l = 0; l < D; ++l) rec[l] = r < cnt ? (ctr[l] - ry[r * D + l]) * xs : 0.0;
+#pragma unroll
+          for (int k = 0; k < Op::NS; ++k) rec[D + k] = r < cnt ? rw[r * Op::NS + k] : 0.0;
+#pragma unroll
+          for (int k = NJ; k < NJP; ++k) rec[k] = 0.0;
+#pragma unroll
+          for (int k = 0; k < NJP; ++k) tile[r * NJP + k] = SrcVal<T>::make(rec[k]);
+        }
+        const long nq = next_visited(q + 1);
+        __syncthreads();  // the tile is staged and buffer b consumed
+        if (threadIdx.x == 0 && nq < nch) issue(nq, b ^ 1);  // overlaps the tile's pair work
+        compute_tile(cnt);
+        __syncthreads();
+        q = nq;
+        b ^= 1;
+      }
+      if (threadIdx.x == 0) {
+        st.parity[0] = par[0];
+        st.parity[1] = par[1];
+      }
+      goto sums_done;
+    }
+  }
+
+  for (long jt = jb; jt < je; jt += TJ) {
+    if (prune) {
+      const long q = (jt - jb) / TJ;
+      const int wq = (int)(q % kPruneWindow);
+      if (wq == 0) make_mask(jt);
+      if (!((s_visit[wq >> 5] >> (wq & 31)) & 1u)) continue;  // same decision in every thread
+    }
+    const int cnt = (int)((je - jt) < TJ ? (je - jt) : TJ);
+    visited += cnt;
+    // ---- stage TJ source records: -(y - c) * xscale and extras, broadcast to the lane type ----
+    for (int r = threadIdx.x; r < TJ; r += BLOCK) {
+      double rec[NJP];
+      if (r < cnt) {
+        long j = jt + r;
+        if (yperm) j = yperm[j];
+#pragma unroll
+        for (int l = 0; l < D; ++l) rec[l] = (ctr[l] - a.y[j * D + l]) * xs;
+        Op::load_source(a, j, rec + D);
+        if (TWOF) {
+#pragma unroll
+          for (int l = 0; l < D; ++l) rec[LO + l] = rec[l] - (double)(float)rec[l];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < NJ; ++q) rec[q] = 0.0;  // zero weights: exact no-op
+      }
+#pragma unroll
+      for (int q = NJ; q < NJP; ++q) rec[q] = 0.0;
+#pragma unroll
+      for (int q = 0; q < NJP; ++q) tile[r * NJP + q] = SrcVal<T>::make(rec[q]);
+    }
+    __syncthreads();
+
+    compute_tile(cnt);
     __syncthreads();
   }
 
+sums_done:
   if (a.pair_count && threadIdx.x == 0 && visited > 0)
     atomicAdd(a.pair_count, (unsigned long long)(iend - i0) * (unsigned long long)visited);
 
@@ -787,9 +916,17 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
   const long nt = a.xtiles ? (long)*a.nxtiles : (long)gridDim.x;
+  if constexpr (std::is_same<T, f32b>::value) {
+    if ((long)blockIdx.x >= nt) return;  // no tile for this CTA (whole CTA)
+    bulk_init();
+  }
   for (long t = blockIdx.x; t < nt; t += gridDim.x) {
     if (t != (long)blockIdx.x) __syncthreads();  // the previous tile is done with shared memory
     pair_block<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM>(a, t, (int)blockIdx.y);
+    if constexpr (std::is_same<T, f32b>::value) {
+      __syncthreads();
+      if (!bulk_state().ok) return;  // a bounded wait gave up (reported in a.status)
+    }
   }
 }
 
@@ -801,6 +938,7 @@ template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int 
 __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel_batched(const PairArgs *args, const int4 *items) {
   const int4 it = items[blockIdx.x];
   const PairArgs a = args[it.x];
+  if constexpr (std::is_same<T, f32b>::value) bulk_init();
   pair_block<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM>(a, (long)it.y, it.z);
 }
 

@@ -116,6 +116,16 @@ class Context:
         (0 lifts the limit)."""
         self.check(self.lib.gbk_set_alloc_limit(self.h, int(nbytes)))
 
+    def set_staging(self, staging: int):
+        """GBK_STAGING_AUTO / LOADS / BULK: how the spatial order stages source tiles (include/gbk.h)."""
+        self.check(self.lib.gbk_set_staging(self.h, staging))
+
+    def last_launch(self) -> tuple[int, int]:
+        """(compiled variant, source splits) of the context's last kernel-sum launch."""
+        v, n = ctypes.c_int(), ctypes.c_int()
+        self.check(self.lib.gbk_last_launch(self.h, ctypes.byref(v), ctypes.byref(n)))
+        return v.value, n.value
+
     def inject_pointer_device(self, device: int):
         """Fault injection for tests: device allocations passed from now on are treated as memory
         of GPU `device` (-1 turns it off), so the refusal of another GPU's memory can be tested on

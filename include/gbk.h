@@ -46,7 +46,7 @@ enum {
   GBK_ERR_UNSUPPORTED = 2, /* dimension or dv combination not supported */
   GBK_ERR_CUDA = 3,        /* a CUDA runtime call failed */
   GBK_ERR_ALLOC = 4,       /* device memory allocation failed */
-  GBK_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  GBK_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up (reported by gbk_synchronize) */
   GBK_ERR_STATE = 6        /* call not allowed in the current state (e.g. during capture) */
 };
 
@@ -122,6 +122,23 @@ int gbk_set_stream(gbk_ctx *ctx, void *stream);
 void *gbk_get_stream(const gbk_ctx *ctx);
 int gbk_set_mode(gbk_ctx *ctx, int mode);
 int gbk_get_mode(const gbk_ctx *ctx);
+
+/* How the spatial order's Convolve-like kernel sums stage each chunk of TJ sorted sources into shared
+ * memory (gbk_set_staging; no counterpart in the reference, whose legacy CUDA kernel loads each
+ * source tile with every thread, GpuConv1D.cu:35-84):
+ *  AUTO: BULK (measured on GB300 at N = M = 1e6, d = 3: 3 % faster at sigma = 0.1, 4 % at 0.02);
+ *  LOADS: every thread loads and converts its records with ordinary global loads;
+ *  BULK: one thread fetches the next visited chunk's coordinates and weights with cp.async.bulk into
+ *    the other half of a double buffer (completion on an mbarrier) while the CTA computes the
+ *    current one, then every thread converts from shared memory. Same results, bit for bit. A wait
+ *    that does not complete within about a second stops the CTA and is reported by gbk_synchronize
+ *    as GBK_ERR_TIMEOUT. */
+enum { GBK_STAGING_AUTO = 0, GBK_STAGING_LOADS = 1, GBK_STAGING_BULK = 2 };
+int gbk_set_staging(gbk_ctx *ctx, int staging);
+int gbk_get_staging(const gbk_ctx *ctx);
+/* The compiled variant (launch shape) and source-split count of the context's last kernel-sum launch
+ * (-1, 0 before any); for reports and the autotuner's tests. */
+int gbk_last_launch(const gbk_ctx *ctx, int *variant, int *nsplit);
 /* Sets the GBK_ORDER_* policy of later kernel-sum calls (default GBK_ORDER_AUTO). The
  * registration, atlas and regression steps always use GBK_ORDER_TWO_FLOAT (no sort inside their graphs;
  * the adaptive two-float variant keeps their accuracy on points spread wide relative to sigma). No
@@ -136,7 +153,8 @@ int gbk_get_gradient_mode(const gbk_ctx *ctx);
  * GradientAscent the optimisers' tau, freeze-counter and aux outputs are not set. */
 int gbk_set_estimator(gbk_ctx *ctx, int estimator);
 int gbk_get_estimator(const gbk_ctx *ctx);
-/* Waits for all work queued on the context's stream. */
+/* Waits for all work queued on the context's stream. Returns GBK_ERR_TIMEOUT (and clears the report)
+ * when a kernel sum's bounded device-side wait gave up since the last call (see GBK_STAGING_BULK). */
 int gbk_synchronize(gbk_ctx *ctx);
 /* Number of the library's own kernels launched on this context so far. */
 long long gbk_launch_count(const gbk_ctx *ctx);

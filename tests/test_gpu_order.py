@@ -350,3 +350,52 @@ def test_default_order_meets_1e6_on_the_sweep_grid(gb, port, n, d):
                     f"plain-magnitude {pl:.2e} max abs {ma:.2e}" for s_, k, nw, cd, pl, ma in report))
     for s_, k, nw, cd, _, _ in report:
         assert nw <= 1e-6 and cd <= 1e-6, (s_, k, nw, cd)
+
+
+@pytest.mark.parametrize("d,dv", [(3, 3), (2, 2), (3, 6)])
+def test_bulk_staging_is_bit_exact(gb, ctx, d, dv):
+    """GBK_STAGING_BULK (cp.async.bulk into a double-buffered shared area, mbarrier completion)
+    stages the same source records as ordinary loads: the spatial order's results are bitwise equal,
+    pruned and unpruned, with and without source splits, for a source count that is not a multiple of
+    the chunk; the launch reports the bulk variant, and no bounded wait gives up."""
+    rng = np.random.default_rng(70 + d + dv)
+    nx, ny = 20000, 30001  # enough work for the default launch shape (the small one has no bulk variant)
+    X, Y = mixture(rng, nx, d), mixture(rng, ny, d)
+    W, A = rng.standard_normal((ny, dv)), rng.standard_normal((nx, dv))
+    for order in (gb.GBK_ORDER_SPATIAL, gb.GBK_ORDER_SPATIAL_NOPRUNE):
+        for split in (0, 3):
+            ctx.set_split(split)
+            got = {}
+            for staging in (gb.GBK_STAGING_LOADS, gb.GBK_STAGING_BULK):
+                ctx.set_staging(staging)
+                k = kern(gb, ctx, d, 0.03, Y, W, gb.GBK_MODE_F32C, order)
+                got[staging] = (k.Convolve(X),) + k.ConvolveAndGradient(X, A) + k.ForwardAdjoint(X, A)
+                variant, _ = ctx.last_launch()
+                assert (variant == 11) == (staging == gb.GBK_STAGING_BULK)
+                ctx.synchronize()
+            for a_, b_ in zip(got[gb.GBK_STAGING_LOADS], got[gb.GBK_STAGING_BULK]):
+                assert np.array_equal(a_, b_)
+    ctx.set_split(0)
+    ctx.set_staging(gb.GBK_STAGING_AUTO)
+
+
+def test_bulk_staging_across_prune_windows(gb, ctx):
+    """More than 4096 source chunks (two visit-mask windows) at a small width, where most chunks are
+    pruned: the bulk path's look-ahead to the next visited chunk crosses the window boundary."""
+    import torch
+    rng = np.random.default_rng(77)
+    X, Y = mixture(rng, 3000, 3), mixture(rng, 1_100_000, 3)
+    W = rng.standard_normal((1_100_000, 3))
+    dev = lambda a: torch.from_numpy(a).cuda()
+    Xd, Yd, Wd = dev(X), dev(Y), dev(W)
+    got = {}
+    for staging in (gb.GBK_STAGING_LOADS, gb.GBK_STAGING_BULK):
+        ctx.set_staging(staging)
+        k = kern(gb, ctx, 3, 0.01, Yd, Wd, gb.GBK_MODE_F32C, gb.GBK_ORDER_SPATIAL)
+        p0 = ctx.evaluated_pairs()
+        got[staging] = k.Convolve(Xd).cpu().numpy()
+        got[staging, "pairs"] = ctx.evaluated_pairs() - p0
+        ctx.synchronize()
+    assert np.array_equal(got[gb.GBK_STAGING_LOADS], got[gb.GBK_STAGING_BULK])
+    assert got[gb.GBK_STAGING_LOADS, "pairs"] == got[gb.GBK_STAGING_BULK, "pairs"] < 0.5 * 3000 * 1_100_000
+    ctx.set_staging(gb.GBK_STAGING_AUTO)

@@ -83,6 +83,8 @@ SIGNATURES = {
     "gbk_kernel_norm": (_I, [_P, _I, _I, _P, _P, _L, _D, _P]),
     "gbk_kernel_norm_noalloc": (_I, [_P, _I, _I, _P, _P, _L, _D, _P]),
     "gbk_autotune": (_I, [_P, _I, _I, _I, _L, _L, _D]),
+    "gbk_autotune_data": (_I, [_P, _I, _I, _I, _P, _L, _P, _P, _L, _D, _P, ctypes.POINTER(_I), ctypes.POINTER(_I),
+                               ctypes.POINTER(_D)]),
     "gbk_tune_save": (_I, [_P, ctypes.c_char_p]),
     "gbk_tune_load": (_I, [_P, ctypes.c_char_p]),
     "gbk_set_split": (_I, [_P, _I]),

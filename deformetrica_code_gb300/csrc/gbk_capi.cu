@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -59,12 +60,6 @@ bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
     case OP_ADJCP: return find_kernel_deform(op, mode, d, dv, variant, e);
   }
   return false;
-}
-
-int num_variants(int op, int mode, int d, int dv) {
-  bool hot_op = op == OP_CONV || op == OP_CONV_GRADA || op == OP_GRADA;
-  bool hot_shape = (d == 3 && dv == 3) || (d == 2 && dv == 2);
-  return (mode == MODE_F32C && hot_op && hot_shape) ? 4 : 1;
 }
 
 const int *supported_dv(int d, int *count) {
@@ -144,8 +139,8 @@ static int bucket(long n) {
   return b;
 }
 
-gbk_ctx::TuneKey gbk_ctx::key(int op, int d, int dv, long nx, long ny) const {
-  return TuneKey{op, mode, d, dv, bucket(nx), bucket(ny)};
+gbk_ctx::TuneKey gbk_ctx::key(int op, int d, int dv, long nx, long ny, int path) const {
+  return TuneKey{op, mode, d, dv, bucket(nx), bucket(ny), path};
 }
 
 int gbk_ctx::occupancy(const KernelEntry &e, int) {
@@ -237,55 +232,83 @@ int gbk_ctx::auto_order(int op, int d, const PairArgs &a, int *choice) {
   return GBK_OK;
 }
 
-int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
-  int variant = 0, ns = 0;
+// The path a kernel-sum launch takes and its default launch shape: the order (caller order, or the
+// spatial order with or without pruning), the coordinate form (two-float variants in caller order
+// below the size rule) and the staging (bulk copies in the spatial order), then the small shape
+// when the default one cannot fill the GPU. Waits for the stream only where the automatic order
+// measures the point sets' extent (gbk_ctx::auto_order).
+int gbk_ctx::plan(int op, int d, int dv, const PairArgs &a, LaunchPlan *p) {
+  *p = LaunchPlan();
   const bool unordered = !a.xperm && !a.xtiles && a.nx > 0 && a.ny > 0 && a.nx < INT_MAX && a.ny < INT_MAX;
-  int auto_choice = AUTO_OFF;
+  int choice = AUTO_OFF;
   if (unordered && order == GBK_ORDER_AUTO)
-    if (int rc = auto_order(op, d, a, &auto_choice)) return rc;
-  if (unordered && order == GBK_ORDER_TWO_FLOAT && mode == GBK_MODE_F32C) auto_choice = AUTO_TWO_FLOAT;
-  auto it = tune.find(key(op, d, dv, a.nx, a.ny));
-  if (it != tune.end()) {
-    variant = it->second.first;
-    ns = it->second.second;
-  } else {
-    // Too little work for the default shape to fill the GPU (e.g. control points x control
-    // points): use the small shape (fewer targets per CTA, shorter source tiles, more splits).
-    KernelEntry e0;
-    if (find_kernel(op, mode, d, dv, 0, &e0)) {
-      long per_cta = (long)e0.block * e0.r;
-      long itiles = (a.nx + per_cta - 1) / per_cta;
-      long max_split = std::max(1L, a.ny / (2L * e0.tj));
-      KernelEntry es;
-      if (itiles * max_split < 2L * num_sms && find_kernel(op, mode, d, dv, VARIANT_SMALL, &es))
-        variant = VARIANT_SMALL;
-    }
-  }
-  if (auto_choice == AUTO_TWO_FLOAT) {  // the op's two-float variant, else the spatial order
-    KernelEntry et;
-    const int tv = variant == VARIANT_SMALL ? VARIANT_SMALL_TWO_FLOAT : VARIANT_TWO_FLOAT;
-    if (find_kernel(op, mode, d, dv, tv, &et)) {
-      variant = tv;
-      ns = 0;  // a tuned split belongs to the tuned variant
-    } else {
-      auto_choice = order == GBK_ORDER_AUTO ? AUTO_SPATIAL : AUTO_OFF;
-    }
-  }
-  // spatial order of targets and sources (see GBK_ORDER_* in gbk.h)
-  bool spatial = false, prune = false;
+    if (int rc = auto_order(op, d, a, &choice)) return rc;
+  if (unordered && order == GBK_ORDER_TWO_FLOAT && mode == GBK_MODE_F32C) choice = AUTO_TWO_FLOAT;
+  KernelEntry et;
+  if (choice == AUTO_TWO_FLOAT && !find_kernel(op, mode, d, dv, VARIANT_TWO_FLOAT, &et))
+    choice = order == GBK_ORDER_AUTO ? AUTO_SPATIAL : AUTO_OFF;  // no two-float variant for this op
   if (unordered) {
     switch (order) {
-      case GBK_ORDER_SPATIAL: spatial = prune = true; break;
-      case GBK_ORDER_SPATIAL_NOPRUNE: spatial = true; break;
-      case GBK_ORDER_AUTO: spatial = prune = auto_choice == AUTO_SPATIAL; break;
+      case GBK_ORDER_SPATIAL: p->spatial = p->prune = true; break;
+      case GBK_ORDER_SPATIAL_NOPRUNE: p->spatial = true; break;
+      case GBK_ORDER_AUTO: p->spatial = p->prune = choice == AUTO_SPATIAL; break;
       default: break;
     }
   }
-  // bulk asynchronous staging of the sorted source copies (GBK_STAGING_*): the spatial order's
-  // default-shape Convolve-like launches
-  if (spatial && variant == 0 && (staging == GBK_STAGING_BULK || (staging == GBK_STAGING_AUTO && kBulkByDefault))) {
+  p->path = p->spatial ? PATH_SPATIAL : (choice == AUTO_TWO_FLOAT ? PATH_TWO_FLOAT : PATH_PLAIN);
+  // Too little work for the default shape to fill the GPU (e.g. control points x control points):
+  // the small shape (fewer targets per CTA, shorter source tiles, more splits).
+  bool small = false;
+  KernelEntry e0, es;
+  if (find_kernel(op, mode, d, dv, 0, &e0)) {
+    const long per_cta = (long)e0.block * e0.r;
+    const long itiles = (a.nx + per_cta - 1) / per_cta;
+    const long max_split = std::max(1L, a.ny / (2L * e0.tj));
+    small = itiles * max_split < 2L * num_sms && find_kernel(op, mode, d, dv, VARIANT_SMALL, &es);
+  }
+  if (p->path == PATH_TWO_FLOAT) {
+    p->variant = small ? VARIANT_SMALL_TWO_FLOAT : VARIANT_TWO_FLOAT;
+  } else {
+    p->variant = small ? VARIANT_SMALL : 0;
     KernelEntry eb;
-    if (find_kernel(op, mode, d, dv, VARIANT_BULK, &eb)) variant = VARIANT_BULK;
+    if (p->spatial && !small && (staging == GBK_STAGING_BULK || (staging == GBK_STAGING_AUTO && kBulkByDefault)) &&
+        find_kernel(op, mode, d, dv, VARIANT_BULK, &eb))
+      p->variant = VARIANT_BULK;
+  }
+  return GBK_OK;
+}
+
+// Compiled variants a launch on `path` may take: the same arithmetic as the path's default, so a
+// tuned choice never changes the accuracy (two-float variants stay two-float), and bulk staging only
+// where the sources are the spatial order's copies (and the staging policy allows it).
+std::vector<int> gbk_ctx::family(int path, int op, int d, int dv) const {
+  std::vector<int> cand;
+  if (path == PATH_TWO_FLOAT) {
+    cand = {VARIANT_TWO_FLOAT, VARIANT_SMALL_TWO_FLOAT};
+  } else {
+    if (path == PATH_SPATIAL && staging != GBK_STAGING_LOADS) cand.push_back(VARIANT_BULK);
+    for (int v = 0; v < kNumShapeVariants; ++v) cand.push_back(v);
+    cand.push_back(VARIANT_SMALL);
+  }
+  std::vector<int> out;
+  KernelEntry e;
+  for (int v : cand)
+    if (find_kernel(op, mode, d, dv, v, &e)) out.push_back(v);
+  return out;
+}
+
+int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
+  LaunchPlan pl;
+  if (int rc = plan(op, d, dv, a, &pl)) return rc;
+  int variant = pl.variant, ns = 0;
+  const bool spatial = pl.spatial, prune = pl.prune;
+  auto it = tune.find(key(op, d, dv, a.nx, a.ny, pl.path));
+  if (it != tune.end()) {
+    const std::vector<int> fam = family(pl.path, op, d, dv);
+    if (std::find(fam.begin(), fam.end(), it->second.first) != fam.end()) {
+      variant = it->second.first;
+      ns = it->second.second;
+    }
   }
   KernelEntry e;
   if (!find_kernel(op, mode, d, dv, variant, &e) && !find_kernel(op, mode, d, dv, 0, &e))
@@ -499,6 +522,8 @@ int gbk_create(int device, gbk_ctx **out) {
   c->nonfinite = reinterpret_cast<unsigned *>(c->pair_counter + 2);
   c->status = reinterpret_cast<unsigned *>(c->pair_counter + 3);
   noalloc_refresh_device(device);
+  if (const char *tf = getenv("GBK_TUNE_FILE"))  // a tuned table saved by gbk_tune_save
+    if (*tf) gbk_tune_load(c, tf);
   *out = c;
   return GBK_OK;
 }

@@ -12,6 +12,7 @@
 #include <string>
 #include <tuple>
 #include <utility>
+#include <vector>
 
 #include "gbk_dispatch.h"
 
@@ -89,15 +90,29 @@ struct gbk_ctx {
   // N = M = 1e5 (bitwise identical results).
   static constexpr bool kBulkByDefault = true;
 
-  typedef std::tuple<int, int, int, int, int, int> TuneKey;  // op, mode, d, dv, log2 nx, log2 ny
-  std::map<TuneKey, std::pair<int, int>> tune;                // -> (variant, nsplit)
+  // op, mode, d, dv, log2 nx, log2 ny, path (PATH_*)
+  typedef std::tuple<int, int, int, int, int, int, int> TuneKey;
+  std::map<TuneKey, std::pair<int, int>> tune;  // -> (variant, nsplit; nsplit 0 = the heuristic's)
+  // The path of a kernel-sum launch: caller order with one-float or two-float coordinates, or the
+  // spatial order. The tuning table is kept per path.
+  enum { PATH_PLAIN = 0, PATH_TWO_FLOAT = 1, PATH_SPATIAL = 2 };
+  struct LaunchPlan {
+    int path = PATH_PLAIN;
+    int variant = 0;
+    bool spatial = false, prune = false;
+  };
+  // Shape variants 0 .. kNumShapeVariants - 1 (default, 2-way unroll, 4 targets per thread, scalar
+  // lanes, 128-thread CTAs) where compiled (gbk_k_conv*.cu)
+  static constexpr int kNumShapeVariants = 5;
   std::map<const void *, int> occ_cache;
 
   int fail(int code, const char *fmt, ...);
   int cuda(cudaError_t e, const char *what);
   bool capturing() const;
   int ensure(DevBuf &b, size_t bytes, const char *what);
-  TuneKey key(int op, int d, int dv, long nx, long ny) const;
+  TuneKey key(int op, int d, int dv, long nx, long ny, int path) const;
+  int plan(int op, int d, int dv, const gbk::PairArgs &a, LaunchPlan *p);
+  std::vector<int> family(int path, int op, int d, int dv) const;
   int occupancy(const gbk::KernelEntry &e, int d);
   int choose_split(const gbk::KernelEntry &e, int d, long nx, long ny);
   int launch(int op, int d, int dv, gbk::PairArgs a);

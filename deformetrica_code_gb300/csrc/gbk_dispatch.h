@@ -24,9 +24,9 @@ enum OpId {
 
 // Launch-shape index for problems too small to fill the GPU with the default shape.
 constexpr int VARIANT_SMALL = 8;
-// Two-float coordinates (lane tag f32w), default and small shapes: compiled for the Convolve and
-// alpha-gradient ops in FP32C mode; chosen by the automatic order for point sets spread wide relative
-// to sigma when sorting them would cost more than it saves (gbk_ctx::launch).
+// Adaptive two-float coordinates (lane tag f32w), default and small shapes: compiled for the Convolve
+// and alpha-gradient ops in FP32C mode; the automatic order's caller-order path below its size rule
+// (gbk_ctx::plan).
 constexpr int VARIANT_TWO_FLOAT = 9;
 constexpr int VARIANT_SMALL_TWO_FLOAT = 10;
 // Bulk asynchronous staging of the source tiles (lane tag f32b), default shape: compiled for the
@@ -56,7 +56,6 @@ int op_outputs(int op, int d, int dv);
 // Fills *e and returns true when the combination is compiled. dv must be one of the compiled
 // column counts (see supported_dv); the host splits other counts into chunks.
 bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e);
-int num_variants(int op, int mode, int d, int dv);
 
 // Compiled weight-column counts for dimension d, largest first (used to chunk any dv).
 const int *supported_dv(int d, int *count);
@@ -69,6 +68,7 @@ void noalloc_refresh_device(int device);
 bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_conv_two_float(int op, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_conv_bulk(int op, int d, int dv, KernelEntry *e);
+bool find_kernel_conv_shape(int op, int d, int dv, int variant, KernelEntry *e);  // variants 1..4, FP32C
 bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_deform(int op, int mode, int d, int dv, int variant, KernelEntry *e);

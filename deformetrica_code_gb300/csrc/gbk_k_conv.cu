@@ -1,10 +1,9 @@
 // Instantiations: Convolve, fused Convolve + alpha-gradient, alpha-gradient.
 //
-// FP32-compensated variants (BLOCK threads, R targets per thread, TJ sources per tile, MERGE
-// sources per compensated run, MINB CTAs per SM for the register allocator, UNR unroll of the
-// source loop): the hot (d, dv) = (3, 3) and (2, 2) shapes carry several variants for the
-// autotuner; other shapes carry the default one. Fused pass at N = M = 1e6 on GB300: default
-// 564 ms; 2-way unroll 578 ms; 4 targets per thread at 2 CTAs/SM 603 ms; scalar FP32 lanes 568 ms;
+// FP32-compensated default (BLOCK threads, R targets per thread, TJ sources per tile, MERGE sources
+// per compensated run, MINB CTAs per SM for the register allocator, UNR unroll of the source loop)
+// and small shapes; the other shapes the autotuner chooses from are in gbk_k_conv_var.cu. Fused pass
+// at N = M = 1e6 on GB300: default 564 ms; 2-way unroll 578 ms; 4 targets per thread at 2 CTAs/SM 603 ms; scalar FP32 lanes 568 ms;
 // compensation terms in shared memory 605-636 ms (removed). Longer plain-FP32 runs before each
 // compensated fold are faster but less accurate (spatial order, 1e6: MERGE 64 534 ms, normwise
 // 1.9e-7; 128: 524 ms, 2.7e-7; 256: 519 ms, 4.0e-7), so every variant keeps runs of 64 and the
@@ -18,31 +17,32 @@
 
 namespace gbk {
 
+template <int D, int DV>
+using OpCG = OpConvGradAlpha<D, DV, true>;
+template <int D, int DV>
+using OpGA = OpConvGradAlpha<D, DV, false>;
+
+template <template <int, int> class OP>
+constexpr int op_of() {
+  return std::is_same<OP<3, 3>, OpConv<3, 3>>::value ? OP_CONV
+         : std::is_same<OP<3, 3>, OpCG<3, 3>>::value ? OP_CONV_GRADA
+                                                      : OP_GRADA;
+}
+
 template <template <int, int> class OP, int D, int DV>
 static bool pick_conv_like(int mode, int variant, KernelEntry *e) {
   typedef OP<D, DV> O;
   if (mode == MODE_F64) {
     if (variant == VARIANT_SMALL) return set_entry<O, double, D, 64, 1, 32, 32, 8>(e);
+    if (variant != 0) return false;
     return set_entry<O, double, D, 128, 1, 128, 128>(e);
   }
   if (variant == VARIANT_SMALL) return set_entry<O, float, D, 64, 2, 32, 32, 8>(e);
-  constexpr bool hot = (D == 3 && DV == 3) || (D == 2 && DV == 2);
-  if constexpr (hot) {
-    switch (variant) {
-      case 1: return set_entry<O, float, D, 256, 2, 256, 64, 3, 2>(e);   // 2-way unroll
-      case 2: return set_entry<O, float, D, 256, 4, 256, 64, 2, 2>(e);   // 4 targets / thread
-      case 3: return set_entry<O, f32s, D, 256, 2, 256, 64, 3, 4>(e);    // scalar FP32 lanes
-      default: break;
-    }
-  }
+  if (variant != 0) return find_kernel_conv_shape(op_of<OP>(), D, DV, variant, e);
   // default: one float2 lane pair per thread, 4-way unrolled source loop, 3 CTAs of 256 per SM
   return set_entry<O, float, D, 256, 2, 256, 64, 3, 4>(e);
 }
 
-template <int D, int DV>
-using OpCG = OpConvGradAlpha<D, DV, true>;
-template <int D, int DV>
-using OpGA = OpConvGradAlpha<D, DV, false>;
 
 template <template <int, int> class OP>
 static bool by_shape(int mode, int d, int dv, int variant, KernelEntry *e) {

@@ -6,6 +6,7 @@ namespace gbk {
 template <int D>
 static bool pick_adjcp(int mode, int variant, KernelEntry *e) {
   typedef OpAdjointCP<D> O;
+  if (variant != 0 && variant != VARIANT_SMALL) return false;  // the default and the small shape only
   if (mode == MODE_F64) {
     if (variant == VARIANT_SMALL) return set_entry<O, double, D, 64, 1, 32, 32, 4>(e);
     return set_entry<O, double, D, 128, 1, 64, 64, 2>(e);

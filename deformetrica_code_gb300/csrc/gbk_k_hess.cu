@@ -10,6 +10,7 @@ static bool pick_one(int mode, int variant, KernelEntry *e) {
     if (mode == MODE_F64) return set_entry<O, double, D, 64, 1, 32, 32, 8>(e);
     return set_entry<O, float, D, 64, 2, 32, 32, 8>(e);
   }
+  if (variant != 0) return false;  // the default and the small shape only
   if (mode == MODE_F64) return set_entry<O, double, D, 128, 1, 128, 128>(e);
   return set_entry<O, float, D, 256, 2, 256, 64, 2, 4>(e);
 }

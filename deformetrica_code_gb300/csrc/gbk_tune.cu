@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <tuple>
 #include <vector>
 
 #include "../../include/gbk.h"
@@ -97,119 +98,193 @@ int gbk_kernel_norm(gbk_ctx *c, int d, int dv, const double *y, const double *w,
   return GBK_OK;
 }
 
-int gbk_autotune(gbk_ctx *c, int op, int d, int dv, long nx, long ny, double sigma) {
-  if (!c) return GBK_ERR_ARG;
-  c->err.clear();
-  if (op < 0 || op >= OP_COUNT) return c->fail(GBK_ERR_ARG, "unknown op %d", op);
-  if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d", d);
-  if (nx <= 0 || ny <= 0) return c->fail(GBK_ERR_ARG, "autotune needs nx, ny > 0");
-  if (op == OP_SPECIAL) {
-    dv = d;
-    ny = nx;
-  }
-  KernelEntry e0;
-  if (!find_kernel(op, c->mode, d, dv, 0, &e0)) return c->fail(GBK_ERR_UNSUPPORTED, "op %d d=%d dv=%d", op, d, dv);
-  if (c->capturing()) return c->fail(GBK_ERR_STATE, "autotune during stream capture");
-  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
+}  // extern "C"
 
-  const long nin = std::max(nx, ny);
-  size_t sz_x = (size_t)nin * d, sz_w = (size_t)nin * 6, sz_o = (size_t)nx * dv * d * d + (size_t)nx * 16;
-  std::vector<double *> bufs;
-  auto alloc = [&](size_t n) -> double * {
-    double *p = nullptr;
-    if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) {
-      cudaGetLastError();
-      return nullptr;
-    }
-    bufs.push_back(p);
-    return p;
-  };
-  auto cleanup = [&]() {
-    cudaStreamSynchronize(c->stream);
-    for (double *p : bufs) cudaFree(p);
-    cudaGetLastError();
-  };
-  double *X = alloc(sz_x), *Y = alloc(sz_x), *Wt = alloc(sz_w), *A = alloc(sz_w), *O0 = alloc(sz_o), *O1 = alloc((size_t)nx * d);
-  if (!X || !Y || !Wt || !A || !O0 || !O1) {
-    cleanup();
-    return c->fail(GBK_ERR_ALLOC, "autotune buffers");
-  }
-  fill_uniform_kernel<<<(unsigned)((sz_x + 255) / 256), 256, 0, c->stream>>>(X, (long)sz_x, 1, 0.0, 1.0);
-  fill_uniform_kernel<<<(unsigned)((sz_x + 255) / 256), 256, 0, c->stream>>>(Y, (long)sz_x, 2, 0.0, 1.0);
-  fill_uniform_kernel<<<(unsigned)((sz_w + 255) / 256), 256, 0, c->stream>>>(Wt, (long)sz_w, 3, -1.0, 1.0);
-  fill_uniform_kernel<<<(unsigned)((sz_w + 255) / 256), 256, 0, c->stream>>>(A, (long)sz_w, 4, -1.0, 1.0);
+namespace {
 
-  PairArgs a;
-  memset(&a, 0, sizeof a);
-  a.x = X;
-  a.nx = nx;
-  a.y = (op == OP_SPECIAL) ? X : Y;
-  a.ny = ny;
-  a.w = Wt;
-  a.w_ld = dv;
-  a.ta = (op == OP_SPECIAL) ? Wt : A;
-  a.ta_ld = dv;
-  a.tb = A;
-  a.tb_ld = d;
-  a.sb = A;
-  a.sb_ld = d;
-  a.sigma = sigma < 1e-10 ? 1e-10 : sigma;
-  a.out0 = O0;
-  a.out0_ld = op_outputs(op, d, dv) + 8;
-  a.out1 = O1;
-  a.out1_ld = d;
-  a.nsplit = 1;
-
+// Times every compiled variant of the launch's path (gbk_ctx::family) with a range of source-split
+// counts through gbk_ctx::launch itself (the same order policy, sorts, staging and split reduction
+// as the call being tuned) and keeps the fastest (variant, split) for the call's size bucket and
+// path. `a` holds valid device arrays. The spatial order's sorts are made once (order cache).
+int tune_core(gbk_ctx *c, int op, int d, int dv, PairArgs a, int *best_variant, int *best_split, float *best_ms_out) {
+  gbk_ctx::OrderCacheScope cache(c);
+  gbk_ctx::LaunchPlan pl;
+  if (int rc = c->plan(op, d, dv, a, &pl)) return rc;
+  const auto k = c->key(op, d, dv, a.nx, a.ny, pl.path);
+  const std::vector<int> fam = c->family(pl.path, op, d, dv);
+  if (fam.empty()) return c->fail(GBK_ERR_UNSUPPORTED, "op %d d=%d dv=%d", op, d, dv);
   cudaEvent_t e_start, e_stop;
-  cudaEventCreate(&e_start);
-  cudaEventCreate(&e_stop);
-  const auto k = c->key(op, d, dv, nx, ny);
+  if (cudaEventCreate(&e_start) != cudaSuccess || cudaEventCreate(&e_stop) != cudaSuccess) {
+    cudaGetLastError();
+    return c->fail(GBK_ERR_CUDA, "cudaEventCreate");
+  }
   const int saved_force = c->force_split;
   c->force_split = 0;
+  const auto saved = c->tune.find(k) != c->tune.end() ? c->tune[k] : std::pair<int, int>{-1, -1};
   float best_ms = 1e30f;
-  std::pair<int, int> best{0, 1};
+  std::pair<int, int> best{pl.variant, 0};
   int rc = GBK_OK;
-  const int nv = num_variants(op, c->mode, d, dv);
-  for (int v = 0; v < nv && !rc; ++v) {
+  for (int v : fam) {
     KernelEntry e;
     if (!find_kernel(op, c->mode, d, dv, v, &e)) continue;
+    const long max_split = std::max(1L, a.ny / (2L * e.tj));
     std::vector<int> cands = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32};
-    c->tune.erase(k);
-    int heur = c->choose_split(e, d, nx, ny);
-    cands.push_back(heur);
+    cands.push_back(c->choose_split(e, d, a.nx, a.ny));
     std::sort(cands.begin(), cands.end());
     cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
-    long max_split = std::max(1L, ny / (2L * e.tj));
+    bool warm = false;
     for (int ns : cands) {
-      if (ns > max_split) continue;
+      if (ns > max_split && ns != 1) continue;
       c->tune[k] = {v, ns};
-      rc = c->launch(op, d, dv, a);  // warm-up
-      if (rc) break;
+      if (!warm) {  // first launch of the variant: module load, buffer growth, sorts
+        if ((rc = c->launch(op, d, dv, a))) break;
+        warm = true;
+      }
       cudaEventRecord(e_start, c->stream);
-      const int reps = 3;
-      for (int r = 0; r < reps && !rc; ++r) rc = c->launch(op, d, dv, a);
+      if ((rc = c->launch(op, d, dv, a))) break;
       cudaEventRecord(e_stop, c->stream);
-      if (rc) break;
       cudaEventSynchronize(e_stop);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e_start, e_stop);
-      ms /= reps;
+      if (ms < 20.f) {  // short launches: the best of three
+        for (int r = 0; r < 2 && !rc; ++r) {
+          cudaEventRecord(e_start, c->stream);
+          rc = c->launch(op, d, dv, a);
+          cudaEventRecord(e_stop, c->stream);
+          cudaEventSynchronize(e_stop);
+          float m2 = 0.f;
+          cudaEventElapsedTime(&m2, e_start, e_stop);
+          ms = std::min(ms, m2);
+        }
+        if (rc) break;
+      }
       if (ms < best_ms) {
         best_ms = ms;
         best = {v, ns};
       }
     }
+    if (rc) break;
   }
   c->force_split = saved_force;
   cudaEventDestroy(e_start);
   cudaEventDestroy(e_stop);
-  cleanup();
   if (rc) {
-    c->tune.erase(k);
+    if (saved.first >= 0)
+      c->tune[k] = saved;
+    else
+      c->tune.erase(k);
     return rc;
   }
   c->tune[k] = best;
+  if (best_variant) *best_variant = best.first;
+  if (best_split) *best_split = best.second;
+  if (best_ms_out) *best_ms_out = best_ms;
   return GBK_OK;
+}
+
+bool tunable_op(int op) { return op >= OP_CONV && op <= OP_HESSRC; }
+
+// device scratch of one tuning call (freed on every exit)
+struct TuneBuffers {
+  std::vector<double *> bufs;
+  double *get(size_t n) {
+    double *p = nullptr;
+    if (cudaMalloc(&p, std::max(n, (size_t)1) * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    bufs.push_back(p);
+    return p;
+  }
+  ~TuneBuffers() {
+    cudaDeviceSynchronize();
+    for (double *p : bufs) cudaFree(p);
+    cudaGetLastError();
+  }
+};
+
+PairArgs tune_args(int op, int d, int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                   double sigma, const double *alpha, double *o0, double *o1) {
+  PairArgs a;
+  memset(&a, 0, sizeof a);
+  a.x = x;
+  a.nx = nx;
+  a.y = y;
+  a.ny = ny;
+  a.w = w;
+  a.w_ld = dv;
+  a.ta = alpha;
+  a.ta_ld = dv;
+  a.sigma = sigma < 1e-10 ? 1e-10 : sigma;
+  a.out0 = o0;
+  a.out0_ld = op_outputs(op, d, dv);
+  a.out1 = o1;
+  a.out1_ld = d;
+  a.nsplit = 1;
+  if (op == OP_GRADDIM) a.p0 = 0;
+  if (op == OP_HESSRC) a.p0 = a.p1 = 0;
+  return a;
+}
+
+int tune_checks(gbk_ctx *c, int op, int d, int dv, long nx, long ny) {
+  if (op < 0 || op >= OP_COUNT || !tunable_op(op))
+    return c->fail(GBK_ERR_ARG, "op %d cannot be tuned (Convolve, the gradients and the Hessians can)", op);
+  if (d != 2 && d != 3) return c->fail(GBK_ERR_UNSUPPORTED, "dimension %d", d);
+  int cnt;
+  const int *sup = supported_dv(d, &cnt);
+  if (std::find(sup, sup + cnt, dv) == sup + cnt)
+    return c->fail(GBK_ERR_UNSUPPORTED, "dv = %d is not a compiled column width (tune each column chunk)", dv);
+  if (nx <= 0 || ny <= 0) return c->fail(GBK_ERR_ARG, "autotune needs nx, ny > 0");
+  if (c->capturing()) return c->fail(GBK_ERR_STATE, "autotune during stream capture");
+  if (cudaSetDevice(c->device) != cudaSuccess) return c->fail(GBK_ERR_CUDA, "cudaSetDevice");
+  return GBK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbk_autotune(gbk_ctx *c, int op, int d, int dv, long nx, long ny, double sigma) {
+  if (!c) return GBK_ERR_ARG;
+  c->err.clear();
+  ++c->call_epoch;
+  if (int rc = tune_checks(c, op, d, dv, nx, ny)) return rc;
+  TuneBuffers tb;
+  const long nin = std::max(nx, ny);
+  const size_t sz_x = (size_t)nin * d, sz_w = (size_t)nin * dv;
+  double *X = tb.get(sz_x), *Y = tb.get(sz_x), *Wt = tb.get(sz_w), *A = tb.get(sz_w);
+  double *O0 = tb.get((size_t)nx * op_outputs(op, d, dv)), *O1 = tb.get((size_t)nx * d);
+  if (!X || !Y || !Wt || !A || !O0 || !O1) return c->fail(GBK_ERR_ALLOC, "autotune buffers");
+  fill_uniform_kernel<<<(unsigned)((sz_x + 255) / 256), 256, 0, c->stream>>>(X, (long)sz_x, 1, 0.0, 1.0);
+  fill_uniform_kernel<<<(unsigned)((sz_x + 255) / 256), 256, 0, c->stream>>>(Y, (long)sz_x, 2, 0.0, 1.0);
+  fill_uniform_kernel<<<(unsigned)((sz_w + 255) / 256), 256, 0, c->stream>>>(Wt, (long)sz_w, 3, -1.0, 1.0);
+  fill_uniform_kernel<<<(unsigned)((sz_w + 255) / 256), 256, 0, c->stream>>>(A, (long)sz_w, 4, -1.0, 1.0);
+  if (int rc = c->cuda(cudaGetLastError(), "autotune inputs")) return rc;
+  return tune_core(c, op, d, dv, tune_args(op, d, dv, X, nx, Y, Wt, ny, sigma, A, O0, O1), nullptr, nullptr, nullptr);
+}
+
+int gbk_autotune_data(gbk_ctx *c, int op, int d, int dv, const double *x, long nx, const double *y, const double *w,
+                      long ny, double sigma, const double *alpha, int *variant, int *nsplit, double *ms) {
+  if (!c) return GBK_ERR_ARG;
+  c->err.clear();
+  ++c->call_epoch;
+  if (int rc = tune_checks(c, op, d, dv, nx, ny)) return rc;
+  if (!x || !y || !w || ((op == OP_CONV_GRADA || op == OP_GRADA) && !alpha)) return c->fail(GBK_ERR_ARG, "null pointer");
+  HostIO io(c);
+  const double *dx = io.in(x, (size_t)nx * d, "x");
+  const double *dy = io.in(y, (size_t)ny * d, "y");
+  const double *dw = io.in(w, (size_t)ny * dv, "w");
+  const double *da = alpha ? io.in(alpha, (size_t)nx * dv, "alpha") : nullptr;
+  if (io.rc) return io.rc;
+  TuneBuffers tb;
+  double *O0 = tb.get((size_t)nx * op_outputs(op, d, dv)), *O1 = tb.get((size_t)nx * d);
+  if (!O0 || !O1) return c->fail(GBK_ERR_ALLOC, "autotune buffers");
+  float best_ms = 0.f;
+  int rc = tune_core(c, op, d, dv, tune_args(op, d, dv, dx, nx, dy, dw, ny, sigma, da, O0, O1), variant, nsplit,
+                     &best_ms);
+  if (!rc && ms) *ms = best_ms;
+  if (!rc) rc = io.finish();
+  return rc;
 }
 
 int gbk_tune_save(const gbk_ctx *c, const char *path) {
@@ -217,10 +292,12 @@ int gbk_tune_save(const gbk_ctx *c, const char *path) {
   FILE *f = fopen(path, "w");
   if (!f) return GBK_ERR_ARG;
   for (const auto &kv : c->tune) {
-    int op, mode, d, dv, bx, by;
-    std::tie(op, mode, d, dv, bx, by) = kv.first;
-    fprintf(f, "{\"op\": %d, \"mode\": %d, \"d\": %d, \"dv\": %d, \"bx\": %d, \"by\": %d, \"variant\": %d, \"nsplit\": %d}\n",
-            op, mode, d, dv, bx, by, kv.second.first, kv.second.second);
+    int op, mode, d, dv, bx, by, path;
+    std::tie(op, mode, d, dv, bx, by, path) = kv.first;
+    fprintf(f,
+            "{\"op\": %d, \"mode\": %d, \"d\": %d, \"dv\": %d, \"bx\": %d, \"by\": %d, \"path\": %d, "
+            "\"variant\": %d, \"nsplit\": %d}\n",
+            op, mode, d, dv, bx, by, path, kv.second.first, kv.second.second);
   }
   fclose(f);
   return GBK_OK;
@@ -231,14 +308,25 @@ int gbk_tune_load(gbk_ctx *c, const char *path) {
   FILE *f = fopen(path, "r");
   if (!f) return c->fail(GBK_ERR_ARG, "cannot open %s", path);
   char line[512];
+  int bad = 0;
   while (fgets(line, sizeof line, f)) {
-    int op, mode, d, dv, bx, by, v, ns;
-    if (sscanf(line, "{\"op\": %d, \"mode\": %d, \"d\": %d, \"dv\": %d, \"bx\": %d, \"by\": %d, \"variant\": %d, \"nsplit\": %d}",
-               &op, &mode, &d, &dv, &bx, &by, &v, &ns) == 8) {
-      if (v < 0 || (v >= num_variants(op, mode, d, dv) && v != VARIANT_SMALL) || ns < 0) continue;  // nsplit 0 = automatic
-      c->tune[gbk_ctx::TuneKey{op, mode, d, dv, bx, by}] = {v, ns};
+    int op, mode, d, dv, bx, by, path, v, ns;
+    if (sscanf(line,
+               "{\"op\": %d, \"mode\": %d, \"d\": %d, \"dv\": %d, \"bx\": %d, \"by\": %d, \"path\": %d, "
+               "\"variant\": %d, \"nsplit\": %d}",
+               &op, &mode, &d, &dv, &bx, &by, &path, &v, &ns) != 9) {
+      ++bad;
+      continue;
     }
+    KernelEntry e;
+    // entries for variants this build does not compile, or malformed, are skipped
+    if (op < 0 || op >= OP_COUNT || path < 0 || path > 2 || ns < 0 || !find_kernel(op, mode, d, dv, v, &e)) {
+      ++bad;
+      continue;
+    }
+    c->tune[gbk_ctx::TuneKey{op, mode, d, dv, bx, by, path}] = {v, ns};
   }
+  (void)bad;
   fclose(f);
   return GBK_OK;
 }

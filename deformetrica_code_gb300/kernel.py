@@ -160,7 +160,24 @@ class Context:
         self.check(self.lib.gbk_synchronize(self.h))
 
     def autotune(self, op: str, d: int, dv: int, nx: int, ny: int, sigma: float):
+        """Tunes `op` (a key of _lib.OPS) for calls of this size on synthetic inputs (gbk_autotune)."""
         self.check(self.lib.gbk_autotune(self.h, _lib.OPS[op], d, dv, nx, ny, sigma))
+
+    def autotune_data(self, op: str, x, y, w, sigma: float, alpha=None):
+        """Tunes `op` on these arrays through the path their call takes (gbk_autotune_data); returns
+        (variant, nsplit, ms per launch) of the choice."""
+        x = _check(x, "x")
+        y = _check(y, "y", x.shape[1])
+        w = _check(w, "w")
+        if alpha is not None:
+            alpha = _check(alpha, "alpha", w.shape[1])
+        v, n, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        if any(_is_torch(a) and a.is_cuda for a in (x, y, w, alpha) if a is not None):
+            self.use_torch_stream()
+        self.check(self.lib.gbk_autotune_data(self.h, _lib.OPS[op], x.shape[1], w.shape[1], _ptr(x), x.shape[0],
+                                              _ptr(y), _ptr(w), y.shape[0], sigma, _ptr(alpha), ctypes.byref(v),
+                                              ctypes.byref(n), ctypes.byref(ms)))
+        return v.value, n.value, ms.value
 
     def tune_save(self, path: str):
         self.check(self.lib.gbk_tune_save(self.h, path.encode()))

@@ -604,10 +604,29 @@ void gbk_atlas_destroy(gbk_atlas *atlas);
 
 /* ---- tuning ------------------------------------------------------------------------------ */
 
-/* Times the compiled variants and source-split factors of `op` for this shape on synthetic data
- * and keeps the fastest for calls whose (nx, ny) fall in the same size bucket. */
+/* The autotuner (no counterpart in the reference). A kernel-sum launch takes one of three paths --
+ * caller order with one-float coordinates, caller order with adaptive two-float coordinates (the
+ * automatic order below its size rule), or the spatial order -- and each path has a family of
+ * compiled launch shapes with the same arithmetic (default, 2-way unroll, 4 targets per thread,
+ * scalar lanes, 128-thread CTAs, the small shape, two-float default / small, bulk staging), so a
+ * tuned choice changes the speed, never the accuracy. The tuning table maps (op, precision, d, dv,
+ * log2 nx, log2 ny, path) to (shape, source splits); a call whose key is in the table uses it. A
+ * context created while the environment variable GBK_TUNE_FILE names a file saved by gbk_tune_save
+ * starts with that table. op is a GBK_OP_* up to GBK_OP_HESSIAN_ROWCOL (Convolve, the fused Convolve +
+ * alpha-gradient, the alpha-gradient, varlin, ConvolveGradient(X, dim), the Hessians); dv one
+ * compiled column width.
+ *
+ * Times every shape of the path such a call takes (with the context's order and staging policy)
+ * with a range of split counts on synthetic uniform inputs of that size, and keeps the fastest. */
 int gbk_autotune(gbk_ctx *ctx, int op, int d, int dv, long nx, long ny, double sigma);
-/* Saves / loads the tuned table as JSON lines. */
+/* The same on the caller's own arrays (host or device; alpha nx x dv for the alpha-gradient ops,
+ * else may be NULL), through exactly the path the call with these arrays takes (sorts and pruning
+ * included). variant, nsplit and ms (optional) receive the choice and its time per launch. */
+int gbk_autotune_data(gbk_ctx *ctx, int op, int d, int dv, const double *x, long nx, const double *y,
+                      const double *w, long ny, double sigma, const double *alpha, int *variant, int *nsplit,
+                      double *ms);
+/* Saves / loads the tuned table as JSON lines (entries for shapes this build does not compile are
+ * skipped on load). */
 int gbk_tune_save(const gbk_ctx *ctx, const char *path);
 int gbk_tune_load(gbk_ctx *ctx, const char *path);
 /* Forces the number of source splits (0 = automatic) -- for tests and tuning. */

@@ -35,9 +35,34 @@ METRIC = "kernel pairs/s fwd+adjoint"
 UNIT = "pairs/s"
 FLOPS_PER_PAIR_PASS = 26  # FP32 flops per pair of one fused Convolve + alpha-gradient pass (FMA = 2)
 LANE_OPS_PER_PAIR_PASS = 16  # FP32 lane instructions per pair of that pass (FMA = 1)
-# DRAM bytes (read + write) of one fused pass at N = M = 1e6 from one ncu capture of this kernel
-# (profiles/pair_kernel_fused_N1e6_traffic.md); None for other sizes.
+# DRAM bytes (read + write) of one fused pass at N = M = 1e6, d = 3, sigma = 0.1 (the headline kernel),
+# from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); a constant, not measured per run.
 TRAFFIC_1E6 = 384661248 + 313689600
+TRAFFIC_SOURCE = ("constant from one ncu capture of the fused pass at N = M = 1e6, d = 3, sigma = 0.1 "
+                  "(dram__bytes_read.sum + dram__bytes_write.sum); not measured in this run")
+# Algorithmic FP32 lane instructions per pair (FMA = 1) of each kernel-sum operation at d = dv = 3, in
+# gbk_evaluated_pairs_by_op order: Convolve 9, fused Convolve + alpha-gradient 16, alpha-gradient 13,
+# varlin 18, ConvolveGradient(X, dim) 10, ConvolveHessian(X) 36, ConvolveHessian(X, r, c) 14, the
+# special Hessian 23, the fused control-point adjoint update 40. Two-float CTAs and compensation
+# folds are not counted.
+OP_NAMES = ("convolve", "convolve_gradient_alpha", "gradient_alpha", "gradient_varlin", "gradient_dim",
+            "hessian", "hessian_rowcol", "special_hessian", "adjoint_cp")
+LANE_OPS_BY_OP = (9, 16, 13, 18, 10, 36, 14, 23, 40)
+
+
+def pair_work(ctx, before, after, iters: int, s_per_iter: float, sm_mhz: float = 2070.0):
+    """Evaluated pairs per iteration by operation (from gbk_evaluated_pairs_by_op counts taken
+    around `iters` iterations), pairs/s, and the FP32 lane fraction at the nominal SM clock."""
+    per = [(b - a) / iters for a, b in zip(before, after)]
+    pairs = sum(per)
+    lane_ops = sum(f * p for f, p in zip(LANE_OPS_BY_OP, per))
+    peak_lanes = SMS * FP32_LANES * sm_mhz * 1e6
+    return {"evaluated_pairs_per_iter": pairs,
+            "by_op": {n: p for n, p in zip(OP_NAMES, per) if p},
+            "pairs_per_s": pairs / s_per_iter,
+            "fp32_lane_frac": lane_ops / s_per_iter / peak_lanes,
+            "lane_frac_basis": f"sum over ops of pairs x algorithmic lane ops (d = dv = 3 counts) / "
+                               f"({SMS} SMs x {FP32_LANES} lanes x {sm_mhz:.0f} MHz)"}
 SMS = 152
 FP32_LANES = 128
 
@@ -111,8 +136,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(sample: int, kind_pref: str = "port"):
-    """Times the FP64 oracle's forward+adjoint on a bounded sample (sample x sample pairs)."""
+def _omp_threads(n: int | None):
+    """Sets the OpenMP thread count of the oracle's C port (its loops are OpenMP); returns the old one."""
+    try:
+        gomp = ctypes.CDLL("libgomp.so.1")
+        old = gomp.omp_get_max_threads()
+        if n is not None:
+            gomp.omp_set_num_threads(int(n))
+        return old
+    except OSError:
+        return None
+
+
+def cpu_baseline(sample: int, kind_pref: str = "port", single_sample: int = 8192):
+    """Times the FP64 CPU implementation's forward + adjoint on a bounded sample (sample x sample
+    pairs) on all host cores, and on one core (single_sample x single_sample), as the reference's
+    ExactKernel runs per call."""
     import oracle
     kind = "port"
     lib = None
@@ -131,36 +170,44 @@ def cpu_baseline(sample: int, kind_pref: str = "port"):
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     if kind == "reference":
         cores = 1  # the reference's ExactKernel is single-threaded per call
-    return {"value": sample * sample / dt, "unit": UNIT, "cores": cores,
-            "kind": "reference" if kind == "reference" else "port",
-            "sample": f"fwd+adjoint of {sample}x{sample} pairs (d=3, sigma=0.1), FP64, {dt:.2f} s"}
+    res = {"value": sample * sample / dt, "unit": UNIT, "cores": cores,
+           "kind": "reference" if kind == "reference" else "port",
+           "sample": f"fwd+adjoint of {sample}x{sample} pairs (d=3, sigma=0.1), FP64, {dt:.2f} s"}
+    if kind == "port" and single_sample > 0:
+        old = _omp_threads(1)
+        try:
+            xs, ys, ws, as_ = make_workload(single_sample, single_sample, seed=34)
+            t0 = time.perf_counter()
+            lib.fwd_adjoint(xs, ys, ws, 0.1, as_)
+            d1 = time.perf_counter() - t0
+        finally:
+            _omp_threads(old)
+        res["single_thread"] = {"value": single_sample * single_sample / d1, "unit": UNIT, "cores": 1,
+                                "sample": f"fwd+adjoint of {single_sample}x{single_sample} pairs, FP64, {d1:.2f} s"}
+    return res
 
 
-def accuracy(x, y, w, a, sigma, v, gx, gy, gw, sample: int = 2048, seed: int = 7):
-    """Errors of the GPU outputs against the FP64 oracle: `sample` targets against all sources
-    (v, gx) and `sample` sources against all targets (gy, gw). Normwise relative error
-    max_i |err_i| / max_i |ref_i| for each output; for v also the condition-aware error
-    max |err| / (K |w|)."""
+def accuracy(x, y, w, a, sigma, v, gx, gy, gw, sample: int = 2048, cond_sample: int = 512, seed: int = 7):
+    """Errors of the four GPU outputs against the FP64 oracle: v and gx on `sample` target rows against
+    all sources, gy and gw on `sample` source rows against all targets. Per output: normwise
+    max_i |err_i| / max_i |ref_i| and max abs error; on the first `cond_sample` of those rows the
+    condition-aware error max |err| / sum_j (1 + a_ij) |term_j| (a_ij = |x_i - y_j|^2 / sigma^2, the
+    exponent's condition number) and the plain-magnitude one, max |err| / sum_j |term_j|."""
     import oracle
     port = oracle.load("port")
     rng = np.random.default_rng(seed)
     it = np.sort(rng.choice(x.shape[0], size=min(sample, x.shape[0]), replace=False))
     jt = np.sort(rng.choice(y.shape[0], size=min(sample, y.shape[0]), replace=False))
-    xs, ys = np.ascontiguousarray(x[it]), np.ascontiguousarray(y[jt])
-    rv = port.convolve(xs, y, w, sigma)
-    mag = port.convolve(xs, y, np.abs(w), sigma)
-    rgx = port.grad_alpha(xs, y, w, sigma, np.ascontiguousarray(a[it]))
-    rgw = port.convolve(ys, x, a, sigma)
-    rgy = port.grad_alpha(ys, x, a, sigma, np.ascontiguousarray(w[jt]))
-
-    def nrm(got, ref):
-        e = np.linalg.norm(got - ref, axis=1).max()
-        return float(e / np.linalg.norm(ref, axis=1).max())
-
-    return {"v": nrm(v[it], rv), "gx": nrm(gx[it], rgx), "gy": nrm(gy[jt], rgy), "gw": nrm(gw[jt], rgw),
-            "v_condition_aware": float((np.abs(v[it] - rv) / mag).max()),
-            "sample": f"{len(it)} targets x {y.shape[0]} sources and {len(jt)} sources x {x.shape[0]} targets vs FP64 oracle",
-            "measure": "normwise max_i|err_i|/max_i|ref_i|"}
+    out = sweep_errors(port, x, y, w, a, it, jt, sigma, (v, gx, gy, gw), cond=False)
+    ic = np.sort(rng.choice(it, size=min(cond_sample, len(it)), replace=False))
+    jc = np.sort(rng.choice(jt, size=min(cond_sample, len(jt)), replace=False))
+    cond = sweep_errors(port, x, y, w, a, ic, jc, sigma, (v, gx, gy, gw), cond=True)
+    for key in out:
+        out[key]["condition_aware"] = cond[key]["condition_aware"]
+        out[key]["plain_magnitude"] = cond[key]["plain_magnitude"]
+    out["sample"] = (f"{len(it)} targets x {y.shape[0]} sources and {len(jt)} sources x {x.shape[0]} targets "
+                     f"(condition-aware: {len(ic)} + {len(jc)} of those rows) vs the FP64 oracle")
+    return out
 
 
 def registration_workload():
@@ -193,6 +240,7 @@ def registration_bench(steps: int, cpu: bool = True):
         reg = Registration(cp.shape[0], tp, tf, gp, gf, context=ctx, **kw)
         for _ in range(3):  # eager, capture, first replay
             ll, gcp, gm = reg.step(cp, mom)
+        c0 = ctx.evaluated_pairs_by_op()
         ts = []
         for _ in range(nsteps):
             t0 = time.perf_counter()
@@ -200,6 +248,8 @@ def registration_bench(steps: int, cpu: bool = True):
             ts.append(time.perf_counter() - t0)
         res[name] = {"s_per_iter": statistics.mean(ts), "loglik": float(ll[0]),
                      "kernels_per_iter": reg.graph_launches()}
+        if name == "f32c":
+            res[name].update(pair_work(ctx, c0, ctx.evaluated_pairs_by_op(), nsteps, statistics.mean(ts)))
         if name == "f64":
             v = np.random.default_rng(9).standard_normal(mom.shape)
             eps = 1e-3
@@ -253,6 +303,7 @@ def atlas_bench(steps: int, cpu: bool = True):
     atlas = Atlas(cp, tp, tf, targets, context=ctx, **kw)
     for _ in range(3):
         ll, gm, gc, gt = atlas.step(mom)
+    c0 = ctx.evaluated_pairs_by_op()
     ts = []
     for _ in range(steps):
         t0 = time.perf_counter()
@@ -263,6 +314,7 @@ def atlas_bench(steps: int, cpu: bool = True):
                        f"2000 CP, T=11, currents", "f32c": {"s_per_iter": statistics.mean(ts),
                                                             "loglik": float(ll[0]),
                                                             "kernels_per_iter": atlas.graph_launches()}}
+    res["f32c"].update(pair_work(ctx, c0, ctx.evaluated_pairs_by_op(), steps, statistics.mean(ts)))
     atlas.close()
     if cpu:
         import oracle
@@ -996,6 +1048,7 @@ def main():
             one_side()
             e.record(stream)
         torch.cuda.synchronize()
+    launch_cfg = ctx.last_launch()  # the fused pass's compiled variant and source splits
     ev_pass = (ctx.evaluated_pairs() - ev1) / len(kev)  # pairs one fused pass evaluated
     ev_step = (ev1 - ev0) / args.steps  # both passes of a step
     kernel_ms = statistics.mean(s.elapsed_time(e) for s, e in kev)
@@ -1057,7 +1110,10 @@ def main():
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
                          "frac": achieved / peak_tflops,
                          "traffic": TRAFFIC_1E6 if n == 1_000_000 else None,
-                         "kernel": "pair_kernel<OpConvGradAlpha<3,3,true>, float2 lanes> (one fused pass)",
+                         "traffic_source": TRAFFIC_SOURCE,
+                         "kernel": "pair_kernel<OpConvGradAlpha<3,3,true>, float2 lanes, bulk-staged source tiles>"
+                                   " (one fused pass)",
+                         "launch_config": {"variant": launch_cfg[0], "nsplit": launch_cfg[1]},
                          "fp32_lane_frac": LANE_OPS_PER_PAIR_PASS * ev_pass / (kernel_ms / 1e3)
                          / (SMS * FP32_LANES * sm_mhz * 1e6),
                          "evaluated_pairs_per_pass": ev_pass,

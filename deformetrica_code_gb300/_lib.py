@@ -61,6 +61,7 @@ SIGNATURES = {
     "gbk_set_mode": (_I, [_P, _I]),
     "gbk_get_mode": (_I, [_P]),
     "gbk_evaluated_pairs": (ctypes.c_longlong, [_P]),
+    "gbk_evaluated_pairs_by_op": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), _I]),
     "gbk_set_order": (_I, [_P, _I]),
     "gbk_get_order": (_I, [_P]),
     "gbk_set_gradient_mode": (_I, [_P, _I]),

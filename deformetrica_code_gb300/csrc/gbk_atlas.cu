@@ -320,6 +320,7 @@ struct gbk_atlas {
       a.partial = nullptr;  // patched in upload()
       // coordinate pre-scale of the lane type (the single-problem launcher sets it itself)
       a.xscale = c->mode == MODE_F64 ? coord_scale<double>(a.sigma) : coord_scale<float>(a.sigma);
+      a.pair_count = c->pair_counter_of(op);  // evaluated pairs, by operation (gbk_evaluated_pairs_by_op)
       if (nsplit > 1) partial_per_subject = std::max(partial_per_subject, (size_t)nsplit * L.e.no * a.nx);
       for (long t = 0; t < itiles; ++t)
         for (int sp = 0; sp < nsplit; ++sp) items.push_back({s, (int)t, sp, std::min(jc, a.ny - (long)sp * jc)});

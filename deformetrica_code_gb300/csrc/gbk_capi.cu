@@ -46,8 +46,8 @@ int op_outputs(int op, int d, int dv) {
 bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
   if (variant == VARIANT_TWO_FLOAT || variant == VARIANT_SMALL_TWO_FLOAT)  // Convolve-like ops only
     return (op == OP_CONV || op == OP_CONV_GRADA || op == OP_GRADA) && find_kernel_conv(op, mode, d, dv, variant, e);
-  if (variant == VARIANT_BULK)
-    return mode == MODE_F32C && find_kernel_conv_bulk(op, d, dv, e);
+  if (variant == VARIANT_BULK || variant == VARIANT_BULK_128)
+    return mode == MODE_F32C && find_kernel_conv_bulk(op, d, dv, variant, e);
   switch (op) {
     case OP_CONV:
     case OP_CONV_GRADA:
@@ -127,6 +127,14 @@ int gbk_ctx::ensure(DevBuf &b, size_t bytes, const char *what) {
   b.p = p;
   b.cap = want;
   return GBK_OK;
+}
+
+// Zeroed counters for `n` target tiles (grow-only; the kernels reset every counter they use).
+int gbk_ctx::ensure_tickets(long n) {
+  const size_t bytes = (size_t)std::max(n, 1L) * sizeof(unsigned);
+  if (tickets.cap >= bytes) return GBK_OK;
+  if (int rc = ensure(tickets, bytes, "split tickets")) return rc;
+  return cuda(cudaMemsetAsync(tickets.p, 0, tickets.cap, stream), "ticket reset");
 }
 
 // Tuning-table key: operation, precision, shape and size buckets (powers of two).
@@ -286,7 +294,10 @@ std::vector<int> gbk_ctx::family(int path, int op, int d, int dv) const {
   if (path == PATH_TWO_FLOAT) {
     cand = {VARIANT_TWO_FLOAT, VARIANT_SMALL_TWO_FLOAT};
   } else {
-    if (path == PATH_SPATIAL && staging != GBK_STAGING_LOADS) cand.push_back(VARIANT_BULK);
+    if (path == PATH_SPATIAL && staging != GBK_STAGING_LOADS) {
+      cand.push_back(VARIANT_BULK);
+      cand.push_back(VARIANT_BULK_128);
+    }
     for (int v = 0; v < kNumShapeVariants; ++v) cand.push_back(v);
     cand.push_back(VARIANT_SMALL);
   }
@@ -300,6 +311,7 @@ std::vector<int> gbk_ctx::family(int path, int op, int d, int dv) const {
 int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
   LaunchPlan pl;
   if (int rc = plan(op, d, dv, a, &pl)) return rc;
+  long ticket_tiles = 0;  // target tiles of the launch (the fused split reduction's tickets)
   int variant = pl.variant, ns = 0;
   const bool spatial = pl.spatial, prune = pl.prune;
   auto it = tune.find(key(op, d, dv, a.nx, a.ny, pl.path));
@@ -347,6 +359,7 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     a.xtiles = tv.tiles;
     a.nxtiles = tv.ntiles;
     a.xtile_bound = tv.grid;
+    ticket_tiles = tv.tile_bound;
     a.ybox = prune ? sv.boxes : nullptr;
     if (prune) {
       // the reference's sums are NaN or infinite wherever a target coordinate or extra is, however
@@ -373,10 +386,10 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
       }
     }
   }
-  a.pair_count = pair_counter;
+  a.pair_count = pair_counter_of(op);
   a.status = status;
   // the bulk copies read whole chunks of the sorted copies, which order_sources pads to whole chunks
-  a.bulk = spatial && variant == VARIANT_BULK && op != OP_ADJCP && op != OP_SPECIAL && a.w_ld == dv ? 1 : 0;
+  a.bulk = spatial && (variant == VARIANT_BULK || variant == VARIANT_BULK_128) && op != OP_ADJCP && op != OP_SPECIAL && a.w_ld == dv ? 1 : 0;
   last_variant = variant;
   last_nsplit = ns;
   if (ns > 1) {
@@ -384,10 +397,14 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     int rc = ensure(partial, (size_t)ns * e.no * std::max(a.nx, 1L) * sizeof(double), "split partials");
     if (rc) return rc;
     a.partial = (double *)partial.p;
+    // the last split CTA of each target tile reduces the tile (no separate reduction launch)
+    if (!spatial) ticket_tiles = (a.nx + (long)e.block * e.r - 1) / ((long)e.block * e.r);
+    if ((rc = ensure_tickets(ticket_tiles))) return rc;
+    a.tickets = (unsigned *)tickets.p;
   }
   int rc = cuda(e.fn(a, ns, stream), "kernel launch");
   if (rc) return rc;
-  launches += (ns > 1) ? 2 : 1;
+  launches += 1;
   return GBK_OK;
 }
 
@@ -501,8 +518,8 @@ int gbk_create(int device, gbk_ctx **out) {
   }
   c->stream = c->own_stream;
   // pair counter and the spatial order's self-resetting ticket
-  if (cudaMalloc(&c->pair_counter, 4 * sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMemset(c->pair_counter, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+  if (cudaMalloc(&c->pair_counter, gbk_ctx::kCounterWords * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(c->pair_counter, 0, gbk_ctx::kCounterWords * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     c->release();
     cudaStreamDestroy(c->own_stream);
@@ -607,6 +624,7 @@ int gbk_synchronize(gbk_ctx *c) {
   if (int rc = c->cuda(cudaMemcpy(&st, c->status, sizeof st, cudaMemcpyDeviceToHost), "status read")) return rc;
   if (st) {
     cudaMemset(c->status, 0, sizeof st);
+    if (c->tickets.p) cudaMemset(c->tickets.p, 0, c->tickets.cap);  // a stopped CTA left its tile's count
     return c->fail(GBK_ERR_TIMEOUT, "a bounded device-side wait gave up in a kernel sum since the last check; "
                    "its outputs are not valid");
   }
@@ -631,19 +649,27 @@ int gbk_last_launch(const gbk_ctx *c, int *variant, int *nsplit) {
 
 long long gbk_launch_count(const gbk_ctx *c) { return c ? c->launches : 0; }
 
-long long gbk_evaluated_pairs(gbk_ctx *c) {
-  if (!c || !c->pair_counter) return -1;
+int gbk_evaluated_pairs_by_op(gbk_ctx *c, long long *counts, int n) {
+  if (!c || !c->pair_counter || !counts || n < 0) return GBK_ERR_ARG;
   if (cudaSetDevice(c->device) != cudaSuccess) {
     cudaGetLastError();
-    return -1;
+    return c->fail(GBK_ERR_CUDA, "cudaSetDevice(%d)", c->device);
   }
-  unsigned long long v = 0;
-  if (cudaMemcpyAsync(&v, c->pair_counter, sizeof v, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
-      cudaStreamSynchronize(c->stream) != cudaSuccess) {
-    cudaGetLastError();
-    return -1;
-  }
-  return (long long)v;
+  unsigned long long v[OP_COUNT] = {0};
+  if (int rc = c->cuda(cudaMemcpyAsync(v, c->pair_counter_of(0), sizeof v, cudaMemcpyDeviceToHost, c->stream),
+                       "pair counters"))
+    return rc;
+  if (int rc = c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize")) return rc;
+  for (int k = 0; k < n; ++k) counts[k] = k < OP_COUNT ? (long long)v[k] : 0;
+  return GBK_OK;
+}
+
+long long gbk_evaluated_pairs(gbk_ctx *c) {
+  long long v[OP_COUNT];
+  if (gbk_evaluated_pairs_by_op(c, v, OP_COUNT) != GBK_OK) return -1;
+  long long t = 0;
+  for (long long x : v) t += x;
+  return t;
 }
 
 int gbk_set_split(gbk_ctx *c, int nsplit) {

@@ -45,6 +45,7 @@ struct gbk_ctx {
   std::string err;
 
   DevBuf partial;             // source-split partial sums
+  DevBuf tickets;             // per target tile: split CTAs done (the fused split reduction)
   DevBuf stage[kStageSlots];  // host-argument staging
   DevBuf reduce;              // FP64 reductions and small temporaries
   DevBuf tmp;                 // op temporaries (e.g. K w for the kernel norm)
@@ -78,7 +79,11 @@ struct gbk_ctx {
     bool wide = false;        // spread wider than a cell of the spatial order
   } auto_order_cache;
   enum { AUTO_OFF = 0, AUTO_TWO_FLOAT = 1, AUTO_SPATIAL = 2 };
-  unsigned long long *pair_counter = nullptr;  // device: pairs evaluated by launch(), then a ticket
+  // device, one allocation: [0] unused, [1] the spatial order's ticket, [2] the non-finite flag,
+  // [3] the status word, [4 + op] pairs evaluated by the kernel sums of operation op
+  unsigned long long *pair_counter = nullptr;
+  static constexpr int kCounterWords = 4 + gbk::OP_COUNT;
+  unsigned long long *pair_counter_of(int op) const { return pair_counter ? pair_counter + 4 + op : nullptr; }
   unsigned *order_ticket = nullptr;            // device: in the pair counter's allocation
   unsigned *nonfinite = nullptr;               // device: a pruned launch's targets hold a NaN or inf
   unsigned *status = nullptr;                  // device: bit 0 = a bounded wait gave up (gbk_synchronize)
@@ -116,6 +121,7 @@ struct gbk_ctx {
   int occupancy(const gbk::KernelEntry &e, int d);
   int choose_split(const gbk::KernelEntry &e, int d, long nx, long ny);
   int launch(int op, int d, int dv, gbk::PairArgs a);
+  int ensure_tickets(long n);
   int auto_order(int op, int d, const gbk::PairArgs &a, int *choice);
 
   // Lets launches of one API call reuse spatial sorts of the same (unchanged) rows.
@@ -148,6 +154,7 @@ struct gbk_ctx {
       b.cap = 0;
     };
     fr(partial);
+    fr(tickets);
     fr(reduce);
     fr(tmp);
     fr(order_keep[0]);

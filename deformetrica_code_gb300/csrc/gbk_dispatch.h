@@ -32,6 +32,7 @@ constexpr int VARIANT_SMALL_TWO_FLOAT = 10;
 // Bulk asynchronous staging of the source tiles (lane tag f32b), default shape: compiled for the
 // Convolve and alpha-gradient ops in FP32C mode, for the spatial order's sorted source copies.
 constexpr int VARIANT_BULK = 11;
+constexpr int VARIANT_BULK_128 = 12;  // the same with 128-thread CTAs and 128-source chunks
 
 enum Mode { MODE_F32C = 0, MODE_F64 = 1 };
 
@@ -67,7 +68,7 @@ void noalloc_refresh_device(int device);
 // Per-family lookups (one per instantiation file).
 bool find_kernel_conv(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_conv_two_float(int op, int d, int dv, int variant, KernelEntry *e);
-bool find_kernel_conv_bulk(int op, int d, int dv, KernelEntry *e);
+bool find_kernel_conv_bulk(int op, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_conv_shape(int op, int d, int dv, int variant, KernelEntry *e);  // variants 1..4, FP32C
 bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry *e);

@@ -69,6 +69,9 @@ struct PairArgs {
   // chunk can be fetched whole by cp.async.bulk; 0 stages with ordinary loads
   int bulk;
   unsigned *status;  // device word: bit 0 set when a bounded wait of the launch gave up (null: none)
+  // with nsplit > 1: one zeroed counter per target tile (index as the CTAs' tile index); the last split
+  // CTA of a tile reduces the partials itself and resets it. Null: a split_reduce_kernel launch does.
+  unsigned *tickets;
 };
 
 __device__ __forceinline__ void put(double *p, int acc, double v) {
@@ -509,7 +512,8 @@ constexpr double kTwoFloatWidth = 16.0;
 // coordinates (hi + lo parts of targets and staged sources); the record stride follows TWOF, so the
 // one-float loop of an adaptive kernel reads no low parts.
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int UNR, int CSM, bool TWOF>
-__device__ __forceinline__ void pair_body(const PairArgs &a, const int split, const long i0, const long iend,
+__device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx, const int split, const long i0,
+                                          const long iend,
                                           const double *ctr, const double *s_box, unsigned *s_visit,
                                           unsigned char *smem_raw) {
   typedef Lane<T> L;
@@ -805,6 +809,35 @@ sums_done:
       }
     }
   }
+  if (a.nsplit > 1 && a.tickets) {
+    // Fused split reduction: the last of the tile's nsplit CTAs to finish (a ticket per tile, counted
+    // with one atomic per CTA after its partials are fenced) sums the partials in split order, as
+    // split_reduce_kernel does, and resets the ticket for the next launch. No CTA waits for another.
+    __shared__ unsigned s_last;
+    __syncthreads();  // every thread's partials are written
+    if (threadIdx.x == 0) {
+      __threadfence();
+      s_last = atomicAdd(a.tickets + tile_idx, 1u) == (unsigned)(a.nsplit - 1);
+    }
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      for (int r = 0; r < R; ++r) {
+        const long i = i0 + threadIdx.x + (long)r * BLOCK;
+        if (i >= iend) continue;
+        double v[NO];
+#pragma unroll
+        for (int o = 0; o < NO; ++o) v[o] = 0.0;
+        for (int s2 = 0; s2 < a.nsplit; ++s2) {
+          const double *p = a.partial + (long)s2 * NO * a.nx;
+#pragma unroll
+          for (int o = 0; o < NO; ++o) v[o] += __ldcg(p + (long)o * a.nx + i);
+        }
+        Op::store(a, xperm ? (long)xperm[i] : i, v);
+      }
+      if (threadIdx.x == 0) a.tickets[tile_idx] = 0u;
+    }
+  }
 }
 
 // FP32 mode subtracts the CTA's target bounding-box midpoint (centring); FP64 mode forms x - y
@@ -903,11 +936,14 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
 #pragma unroll
     for (int l = 0; l < D; ++l) width = fmax(width, (s_box[D + l] - s_box[l]) * a.xscale);
     if (!(width <= kTwoFloatWidth))
-      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, true>(a, split, i0, iend, ctr, s_box, s_visit, smem_raw);
+      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, true>(a, tile_idx, split, i0, iend, ctr, s_box, s_visit,
+                                                                 smem_raw);
     else
-      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, split, i0, iend, ctr, s_box, s_visit, smem_raw);
+      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, tile_idx, split, i0, iend, ctr, s_box, s_visit,
+                                                                 smem_raw);
   } else {
-    pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, split, i0, iend, ctr, s_box, s_visit, smem_raw);
+    pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, tile_idx, split, i0, iend, ctr, s_box, s_visit,
+                                                                 smem_raw);
   }
 }
 
@@ -1029,7 +1065,7 @@ cudaError_t launch_pairs(PairArgs a, int nsplit, cudaStream_t st) {
   dim3 grid((unsigned)tiles, (unsigned)nsplit);
   kern<<<grid, BLOCK, smem, st>>>(a);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || nsplit == 1) return e;
+  if (e != cudaSuccess || nsplit == 1 || a.tickets) return e;
   split_reduce_kernel<Op><<<(unsigned)((a.nx + 255) / 256), 256, 0, st>>>(a);
   return cudaGetLastError();
 }

@@ -142,6 +142,12 @@ class Context:
             raise GBKError(3, "gbk_evaluated_pairs failed")
         return v
 
+    def evaluated_pairs_by_op(self) -> list[int]:
+        """Pairs evaluated so far per operation (gbk_evaluated_pairs_by_op order); waits."""
+        counts = (ctypes.c_longlong * 9)()
+        self.check(self.lib.gbk_evaluated_pairs_by_op(self.h, counts, 9))
+        return [int(v) for v in counts]
+
     def bind_stream(self, *arrays):
         """Queue on torch's current stream when any argument is a CUDA tensor."""
         if any(_is_torch(a) and a.is_cuda for a in arrays if a is not None):

@@ -159,9 +159,13 @@ int gbk_synchronize(gbk_ctx *ctx);
 /* Number of the library's own kernels launched on this context so far. */
 long long gbk_launch_count(const gbk_ctx *ctx);
 /* (target, source) pairs the kernel sums of this context have evaluated so far (pairs in source
- * chunks skipped by GBK_ORDER_SPATIAL are not counted; the registration and atlas steps are not
- * counted). Waits for the context's stream; -1 on error. No counterpart in the reference. */
+ * chunks skipped by GBK_ORDER_SPATIAL are not counted; the registration, atlas and regression steps
+ * on this context are, graph replays included). Waits for the context's stream; -1 on error. No
+ * counterpart in the reference. */
 long long gbk_evaluated_pairs(gbk_ctx *ctx);
+/* The same per operation: counts[op] for op = 0 .. n-1 (GBK_OP_* order; 9 operations, the last the
+ * fused control-point adjoint update), including the batched atlas launches. Waits for the stream. */
+int gbk_evaluated_pairs_by_op(gbk_ctx *ctx, long long *counts, int n);
 
 /* ---- kernel sums (AbstractKernel surface) ------------------------------------------------ */
 

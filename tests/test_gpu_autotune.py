@@ -19,7 +19,7 @@ from tests.conftest import normwise_rel
 pytestmark = pytest.mark.gpu
 
 TWO_FLOAT_FAMILY = {9, 10}
-SPATIAL_FAMILY = {11, 0, 1, 2, 3, 4, 8}
+SPATIAL_FAMILY = {11, 12, 0, 1, 2, 3, 4, 8}
 
 
 @pytest.fixture(scope="module")

@@ -379,6 +379,31 @@ def test_bulk_staging_is_bit_exact(gb, ctx, d, dv):
     ctx.set_staging(gb.GBK_STAGING_AUTO)
 
 
+def test_bulk_staging_128_thread_shape(gb, tmp_path):
+    """The bulk-staged 128-thread shape (12, a tuner choice) against the load-staged one (4) with the
+    same split count, set through a tuning table: the same bits."""
+    import numpy as np
+    rng = np.random.default_rng(81)
+    nx, ny, d = 20000, 30001, 3
+    X, Y = mixture(rng, nx, d), mixture(rng, ny, d)
+    W, A = rng.standard_normal((ny, d)), rng.standard_normal((nx, d))
+    b = lambda n: int(np.log2(n))
+    got = {}
+    for variant in (4, 12):
+        path = str(tmp_path / f"t{variant}.jsonl")
+        with open(path, "w") as f:
+            f.write('{"op": 1, "mode": 0, "d": 3, "dv": 3, "bx": %d, "by": %d, "path": 2, "variant": %d, "nsplit": 3}\n'
+                    % (b(nx), b(ny), variant))
+        c = gb.Context()
+        c.tune_load(path)
+        k = kern(gb, c, d, 0.03, Y, W, gb.GBK_MODE_F32C, gb.GBK_ORDER_SPATIAL)
+        got[variant] = k.ConvolveAndGradient(X, A)
+        assert c.last_launch() == (variant, 3)
+        c.synchronize()
+    for a_, b_ in zip(got[4], got[12]):
+        assert np.array_equal(a_, b_)
+
+
 def test_bulk_staging_across_prune_windows(gb, ctx):
     """More than 4096 source chunks (two visit-mask windows) at a small width, where most chunks are
     pruned: the bulk path's look-ahead to the next visited chunk crosses the window boundary."""

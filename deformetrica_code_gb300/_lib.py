@@ -133,6 +133,11 @@ SIGNATURES = {
     "gbk_set_alloc_limit": (_I, [_P, ctypes.c_size_t]),
     "gbk_inject_pointer_device": (_I, [_P, _I]),
     "gbk_set_staging": (_I, [_P, _I]),
+    "gbk_buffer_create": (_I, [_P, ctypes.POINTER(_P)]),
+    "gbk_buffer_upload": (_I, [_P, _P, _P, ctypes.c_size_t]),
+    "gbk_buffer_data": (_P, [_P]),
+    "gbk_buffer_uploads": (ctypes.c_longlong, [_P]),
+    "gbk_buffer_destroy": (None, [_P]),
     "gbk_get_staging": (_I, [_P]),
     "gbk_last_launch": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "gbk_image_points": (_I, [_P, _I, _P, _P, _P, _P]),

@@ -15,6 +15,7 @@
 // kernel-type strings of the launchers and of DeformableObjectReader.cxx:473-485.
 #pragma once
 
+#include <cstdlib>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -25,6 +26,9 @@
 
 namespace gb300_binding {
 
+// The library context of the calling thread, created on first use on the GPU named by the
+// environment variable GBK_DEVICE (default 0) in the precision named by GBK_MODE ("f64" for the FP64
+// mode, anything else the default compensated FP32).
 inline gbk_ctx *thread_context() {
   struct Holder {
     gbk_ctx *c = nullptr;
@@ -34,7 +38,12 @@ inline gbk_ctx *thread_context() {
   };
   static thread_local Holder h;
   if (!h.c) {
-    if (gbk_create(0, &h.c) != GBK_OK) throw std::runtime_error(std::string("gbk_create: ") + gbk_last_error(nullptr));
+    const char *dev = std::getenv("GBK_DEVICE");
+    const char *mode = std::getenv("GBK_MODE");
+    if (gbk_create(dev ? std::atoi(dev) : 0, &h.c) != GBK_OK)
+      throw std::runtime_error(std::string("gbk_create: ") + gbk_last_error(nullptr));
+    if (mode && std::string(mode) == "f64" && gbk_set_mode(h.c, GBK_MODE_F64) != GBK_OK)
+      throw std::runtime_error(gbk_last_error(h.c));
   }
   return h.c;
 }
@@ -51,17 +60,25 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
   typedef ExactKernel<ScalarType, PointDim> Superclass;
 
   GB300ExactKernel() : Superclass() {}
+  // a copy uploads its own device copies on first use
   GB300ExactKernel(const GB300ExactKernel &o) : Superclass(o) {}
   GB300ExactKernel(const MatrixType &X, double h) : Superclass(X, h) {}
   GB300ExactKernel(const MatrixType &X, const MatrixType &W, double h) : Superclass(X, W, h) {}
   virtual GB300ExactKernel *Clone() const { return new GB300ExactKernel(*this); }
-  virtual ~GB300ExactKernel() {}
+  virtual ~GB300ExactKernel() {
+    gbk_buffer_destroy(m_DeviceSources);
+    gbk_buffer_destroy(m_DeviceWeights);
+  }
+
+  // Uploads of the sources so far (for tests: SetSources, SetWeights or SetKernelWidth mark the object
+  // modified and the next call uploads again; calls in between reuse the device copies).
+  long long SourceUploads() const { return m_DeviceSources ? gbk_buffer_uploads(m_DeviceSources) : 0; }
 
   virtual MatrixType Convolve(const MatrixType &X) {
     Buffers b(this, X);
     std::vector<double> out((size_t)X.rows() * b.dv);
     gb300_binding::check(gbk_convolve(gb300_binding::thread_context(), PointDim, b.dv, b.x.memptr(), X.rows(),
-                                      b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(), out.data()));
+                                      b.y, b.w, b.ny, this->GetKernelWidth(), out.data()));
     return from_rows(out, X.rows(), b.dv);
   }
 
@@ -69,7 +86,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     Buffers b(this, X);
     std::vector<double> out((size_t)X.rows() * b.dv * PointDim);
     gb300_binding::check(gbk_convolve_gradient(gb300_binding::thread_context(), PointDim, b.dv, b.x.memptr(),
-                                               X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                               X.rows(), b.y, b.w, b.ny,
                                                this->GetKernelWidth(), out.data()));
     std::vector<MatrixType> g;
     for (unsigned i = 0; i < X.rows(); ++i) {
@@ -86,7 +103,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     VectorType a = alpha.vectorise_row_wise();
     std::vector<double> out((size_t)X.rows() * PointDim);
     gb300_binding::check(gbk_convolve_gradient_alpha(gb300_binding::thread_context(), PointDim, b.dv,
-                                                     b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                     b.x.memptr(), X.rows(), b.y, b.w, b.ny,
                                                      this->GetKernelWidth(), a.memptr(), out.data()));
     return from_rows(out, X.rows(), PointDim);
   }
@@ -95,7 +112,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     Buffers b(this, X);
     std::vector<double> out(b.ny);
     gb300_binding::check(gbk_convolve_gradient_kdp(gb300_binding::thread_context(), PointDim, b.dv,
-                                                   b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                   b.x.memptr(), X.rows(), b.y, b.w, b.ny,
                                                    this->GetKernelWidth(), (int)k, (int)dp, out.data()));
     return VectorType(out);
   }
@@ -104,7 +121,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     Buffers b(this, X);
     std::vector<double> out((size_t)X.rows() * b.dv);
     gb300_binding::check(gbk_convolve_gradient_dim(gb300_binding::thread_context(), PointDim, b.dv,
-                                                   b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                   b.x.memptr(), X.rows(), b.y, b.w, b.ny,
                                                    this->GetKernelWidth(), (int)dim, out.data()));
     return from_rows(out, X.rows(), b.dv);
   }
@@ -114,7 +131,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     const unsigned D = PointDim;
     std::vector<double> out((size_t)X.rows() * b.dv * D * D);
     gb300_binding::check(gbk_convolve_hessian(gb300_binding::thread_context(), D, b.dv, b.x.memptr(), X.rows(),
-                                              b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(),
+                                              b.y, b.w, b.ny, this->GetKernelWidth(),
                                               out.data()));
     std::vector<std::vector<MatrixType> > h;
     for (unsigned i = 0; i < X.rows(); ++i) {
@@ -134,7 +151,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     Buffers b(this, X);
     std::vector<double> out(X.rows());
     gb300_binding::check(gbk_convolve_hessian_kdpdq(gb300_binding::thread_context(), PointDim, b.dv,
-                                                    b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                    b.x.memptr(), X.rows(), b.y, b.w, b.ny,
                                                     this->GetKernelWidth(), (int)k, (int)dp, (int)dq, out.data()));
     return VectorType(out);
   }
@@ -143,7 +160,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     Buffers b(this, X);
     std::vector<double> out((size_t)X.rows() * b.dv);
     gb300_binding::check(gbk_convolve_hessian_rowcol(gb300_binding::thread_context(), PointDim, b.dv,
-                                                     b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                     b.x.memptr(), X.rows(), b.y, b.w, b.ny,
                                                      this->GetKernelWidth(), (int)row, (int)col, out.data()));
     return from_rows(out, X.rows(), b.dv);
   }
@@ -153,8 +170,8 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     if (xi.rows() != b.ny) throw std::runtime_error("Y and Xi count mismatch");
     VectorType x = xi.vectorise_row_wise();
     std::vector<double> out((size_t)b.ny * PointDim);
-    gb300_binding::check(gbk_convolve_special_hessian(gb300_binding::thread_context(), PointDim, b.y.memptr(),
-                                                      b.w.memptr(), b.ny, this->GetKernelWidth(), x.memptr(),
+    gb300_binding::check(gbk_convolve_special_hessian(gb300_binding::thread_context(), PointDim, b.y,
+                                                      b.w, b.ny, this->GetKernelWidth(), x.memptr(),
                                                       out.data()));
     return from_rows(out, b.ny, PointDim);
   }
@@ -168,7 +185,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     const Geometry g(image);
     std::vector<double> out((size_t)X.rows() * PointDim);
     gb300_binding::check(gbk_convolve_image_fast(gb300_binding::thread_context(), PointDim, b.x.memptr(), X.rows(),
-                                                 b.y.memptr(), b.w.memptr(), b.ny, this->GetKernelWidth(), g.o, g.s, g.n,
+                                                 b.y, b.w, b.ny, this->GetKernelWidth(), g.o, g.s, g.n,
                                                  out.data()));
     return from_rows(out, X.rows(), PointDim);
   }
@@ -181,7 +198,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     const Geometry g(image);
     std::vector<double> out((size_t)X.rows() * b.dv * PointDim);
     gb300_binding::check(gbk_convolve_gradient_image_fast(gb300_binding::thread_context(), PointDim, b.dv,
-                                                          b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+                                                          b.x.memptr(), X.rows(), b.y, b.w, b.ny,
                                                           this->GetKernelWidth(), g.o, g.s, g.n, out.data()));
     std::vector<MatrixType> grad;
     for (unsigned i = 0; i < X.rows(); ++i) {
@@ -202,7 +219,7 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     VectorType a = alpha.vectorise_row_wise();
     std::vector<double> out((size_t)X.rows() * PointDim);
     gb300_binding::check(gbk_convolve_gradient_image_fast_alpha(
-        gb300_binding::thread_context(), PointDim, b.dv, b.x.memptr(), X.rows(), b.y.memptr(), b.w.memptr(), b.ny,
+        gb300_binding::thread_context(), PointDim, b.dv, b.x.memptr(), X.rows(), b.y, b.w, b.ny,
         this->GetKernelWidth(), a.memptr(), g.o, g.s, g.n, out.data()));
     return from_rows(out, X.rows(), PointDim);
   }
@@ -228,20 +245,37 @@ class GB300ExactKernel : public ExactKernel<ScalarType, PointDim> {
     }
   };
 
+  // The call's targets as a row-major host array and the device copies of the sources and weights,
+  // uploaded only when the object is modified (m_Modified, AbstractKernel.h:172-185: SetSources,
+  // SetWeights and SetKernelWidth set it; as for the reference's P3MKernel, matrices changed in
+  // place through GetSources() / GetWeights() are not seen until one of those is called).
   struct Buffers {
-    VectorType x, y, w;
+    VectorType x;
+    const double *y = nullptr, *w = nullptr;
     unsigned ny, dv;
     Buffers(GB300ExactKernel *k, const MatrixType &X) {
       MatrixType &Y = k->GetSources();
       MatrixType &W = k->GetWeights();
       if (Y.rows() != W.rows()) throw std::runtime_error("Sources and weights count mismatch");
       x = X.vectorise_row_wise();
-      y = Y.vectorise_row_wise();
-      w = W.vectorise_row_wise();
       ny = Y.rows();
       dv = W.columns();
+      gbk_ctx *c = gb300_binding::thread_context();
+      if (!k->m_DeviceSources) gb300_binding::check(gbk_buffer_create(c, &k->m_DeviceSources));
+      if (!k->m_DeviceWeights) gb300_binding::check(gbk_buffer_create(c, &k->m_DeviceWeights));
+      if (k->IsModified() || gbk_buffer_uploads(k->m_DeviceSources) == 0) {
+        VectorType yv = Y.vectorise_row_wise(), wv = W.vectorise_row_wise();
+        gb300_binding::check(gbk_buffer_upload(c, k->m_DeviceSources, yv.memptr(), (size_t)ny * PointDim));
+        gb300_binding::check(gbk_buffer_upload(c, k->m_DeviceWeights, wv.memptr(), (size_t)ny * dv));
+        k->UnsetModified();
+      }
+      y = gbk_buffer_data(k->m_DeviceSources);
+      w = gbk_buffer_data(k->m_DeviceWeights);
     }
   };
+
+  gbk_buffer *m_DeviceSources = nullptr;
+  gbk_buffer *m_DeviceWeights = nullptr;
 
   static MatrixType from_rows(const std::vector<double> &v, unsigned rows, unsigned cols) {
     MatrixType M(rows, cols, 0.0);

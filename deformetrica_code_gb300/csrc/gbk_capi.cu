@@ -672,6 +672,68 @@ long long gbk_evaluated_pairs(gbk_ctx *c) {
   return t;
 }
 
+// A device array the library owns for a caller that keeps no device memory of its own (the C++
+// binding's per-object copies of the sources and weights).
+struct gbk_buffer {
+  int device = 0;
+  double *p = nullptr;
+  size_t cap = 0;  // doubles
+  long long uploads = 0;
+};
+
+int gbk_buffer_create(gbk_ctx *c, gbk_buffer **out) {
+  if (!c || !out) return GBK_ERR_ARG;
+  *out = new gbk_buffer();
+  (*out)->device = c->device;
+  return GBK_OK;
+}
+
+int gbk_buffer_upload(gbk_ctx *c, gbk_buffer *b, const double *host, size_t count) {
+  GBK_GUARD(c);
+  GBK_RANGE();
+  if (!b || (count && !host)) return c->fail(GBK_ERR_ARG, "null pointer");
+  if (b->device != c->device) return c->fail(GBK_ERR_ARG, "buffer of GPU %d, context on GPU %d", b->device, c->device);
+  if (c->capturing()) return c->fail(GBK_ERR_STATE, "buffer upload while the stream is being captured");
+  if (count > b->cap) {
+    if (c->alloc_limit && count * sizeof(double) > c->alloc_limit)
+      return c->fail(GBK_ERR_ALLOC, "buffer of %zu bytes refused (injected allocation limit)", count * sizeof(double));
+    if (b->p) {
+      if (int rc = c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize")) return rc;
+      cudaFree(b->p);
+      b->p = nullptr;
+      b->cap = 0;
+    }
+    if (int rc = c->cuda(cudaMalloc(&b->p, count * sizeof(double)), "buffer allocation")) return rc;
+    b->cap = count;
+  }
+  if (count) {
+    if (int rc = c->cuda(cudaMemcpyAsync(b->p, host, count * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+                         "buffer upload"))
+      return rc;
+    if (int rc = c->cuda(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize")) return rc;
+  }
+  ++b->uploads;
+  return GBK_OK;
+}
+
+const double *gbk_buffer_data(const gbk_buffer *b) { return b ? b->p : nullptr; }
+
+long long gbk_buffer_uploads(const gbk_buffer *b) { return b ? b->uploads : -1; }
+
+void gbk_buffer_destroy(gbk_buffer *b) {
+  if (!b) return;
+  if (b->p) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(b->device);
+    cudaDeviceSynchronize();
+    cudaFree(b->p);
+    cudaSetDevice(cur);
+    cudaGetLastError();
+  }
+  delete b;
+}
+
 int gbk_set_split(gbk_ctx *c, int nsplit) {
   if (!c || nsplit < 0) return GBK_ERR_ARG;
   c->force_split = nsplit;

@@ -606,6 +606,23 @@ int gbk_atlas_optimize(gbk_atlas *atlas, double *cp, double *tmpl, double *mom, 
                        int *iterations, double *info);
 void gbk_atlas_destroy(gbk_atlas *atlas);
 
+/* ---- library-owned device arrays ------------------------------------------------------------ *
+ * For callers that keep no device memory themselves but call repeatedly with the same inputs: the
+ * C++ reference binding uploads a kernel object's sources and weights once and again only after
+ * SetSources / SetWeights / SetKernelWidth set the object's m_Modified flag (AbstractKernel.h:85-115,
+ * 172-185), where the legacy CUDA path copied them on every call (CUDAExactKernel.cxx:46-48).
+ * gbk_buffer_data's device pointer can be passed to every entry point in place of a host array. */
+typedef struct gbk_buffer gbk_buffer;
+int gbk_buffer_create(gbk_ctx *ctx, gbk_buffer **out);
+/* Copies `count` doubles from host memory into the buffer (growing it on the context's GPU) and
+ * waits for the copy. Not while the context's stream is being captured. */
+int gbk_buffer_upload(gbk_ctx *ctx, gbk_buffer *buf, const double *host, size_t count);
+const double *gbk_buffer_data(const gbk_buffer *buf);
+/* Number of uploads into the buffer so far (-1 for NULL). */
+long long gbk_buffer_uploads(const gbk_buffer *buf);
+/* Frees the device array (waits for the buffer's GPU) and the handle. */
+void gbk_buffer_destroy(gbk_buffer *buf);
+
 /* ---- tuning ------------------------------------------------------------------------------ */
 
 /* The autotuner (no counterpart in the reference). A kernel-sum launch takes one of three paths --

@@ -77,3 +77,39 @@ def test_reference_binding_compiles_and_reports_errors(tmp_path):
         assert res.returncode == 0 and "ran 4" in res.stdout
     else:
         assert res.returncode == 3 and "runtime_error" in res.stdout, res.stdout + res.stderr
+
+
+def _build_binding_test(tmp):
+    import oracle
+    oracle.build_port()
+    obj = os.path.join(tmp, "gauss_oracle.o")
+    subprocess.check_call(["gcc", "-O2", "-fopenmp", "-std=c11", "-c", os.path.join(ROOT, "oracle", "gauss_oracle.c"),
+                           "-o", obj])
+    exe = os.path.join(tmp, "test_binding")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "tests", "cpp", "binding_standin"),
+                           "-I", os.path.join(ROOT, "oracle", "ref_shim"), "-I", os.path.join(ROOT, "include"),
+                           "-I", os.path.join(PKG, "cpp", "reference_binding"),
+                           os.path.join(ROOT, "tests", "cpp", "test_binding.cpp"), obj, "-L", PKG, "-lgbkernel",
+                           "-Wl,-rpath," + PKG, "-fopenmp", "-o", exe])
+    return exe
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,eps,eps_cancel", [("f64", 1e-10, 1e-10), ("f32c", 1e-5, 1e-4)])
+def test_reference_binding_runs_on_the_gpu(tmp_path, mode, eps, eps_cancel):
+    """GB300ExactKernel (the reference binding) on the GPU, over a stand-in of the reference's base
+    class: every override against the FP64 oracle (the reference's element-wise criterion; in FP32C
+    the Hessian-type outputs, cancellations of larger terms, at 1e-4), sources uploaded once per
+    modification, the image methods equal to direct C-ABI calls, shape errors thrown."""
+    exe = _build_binding_test(str(tmp_path))
+    env = dict(os.environ, GBK_MODE=mode)
+    res = subprocess.run([exe, str(eps), str(eps_cancel)], capture_output=True, text=True, env=env, timeout=300)
+    print(res.stdout)
+    assert res.returncode == 0, res.stdout + res.stderr
+
+
+def test_reference_binding_compiles_against_the_standin():
+    """The same program compiles on any host (no GPU needed to build it)."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        assert os.path.exists(_build_binding_test(tmp))

@@ -3,6 +3,7 @@
 #
 # Compiles, in place and unmodified, the reference sources
 #   src/support/kernels/ExactKernel.cxx, src/support/kernels/AbstractKernel.cxx,
+#   src/support/kernels/P3MKernel.cxx,
 #   src/support/linear_algebra/Armadillo{Matrix,Vector}Wrapper.cxx, MatrixListWrapper.cxx,
 #   src/support/utilities/SimpleTimer.cxx
 # against the vendored, header-only Armadillo 7.700 (extra/armadillo-7.700.0.tar.xz, extracted
@@ -28,7 +29,7 @@ CXXFLAGS=(-std=c++14 -O2 -fPIC -w
   -DARMA_DONT_USE_WRAPPER -DARMA_DONT_USE_LAPACK -DARMA_DONT_USE_BLAS -DARMA_DONT_USE_HDF5
   -I"$HERE/ref_shim" -I"$S/kernels" -I"$S/linear_algebra" -I"$S/utilities" -I"$S/fast_math"
   -I"$ARMA/include")
-SRCS=("$HERE/ref_driver.cpp" "$S/kernels/ExactKernel.cxx" "$S/kernels/AbstractKernel.cxx"
+SRCS=("$HERE/ref_driver.cpp" "$S/kernels/ExactKernel.cxx" "$S/kernels/AbstractKernel.cxx" "$S/kernels/P3MKernel.cxx"
   "$S/linear_algebra/ArmadilloMatrixWrapper.cxx" "$S/linear_algebra/ArmadilloVectorWrapper.cxx"
   "$S/linear_algebra/MatrixListWrapper.cxx" "$S/utilities/SimpleTimer.cxx")
 OBJS=()

@@ -84,6 +84,7 @@ _SIGS = {
 # exported by the reference library only: the image-grid methods through the ITK stand-ins
 _REF_ONLY = {
     "oracle_ref_image_fast": [_I, _I, _I, _D, _L, _D, _D, _L, _F, _D, _D, _D, ctypes.POINTER(ctypes.c_long), _D],
+    "oracle_ref_p3m": [_I, _I, _I, _D, _L, _D, _D, _L, _F, _D, _D, _D, _F, _F, _I, _I, _I, _D],
 }
 # exported by the port only (test denominators, no reference method)
 _PORT_ONLY = {
@@ -231,6 +232,27 @@ class OracleLib:
         self._check(self._lib.oracle_ref_image_fast(d, kind, dv, _c(x), nx, _c(y), _c(w), y.shape[0], sigma, _c(a),
                                                     _c(o), _c(sp), sz.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
                                                     _c(out)))
+        return out
+
+    P3M_KINDS = {"convolve": 0, "gradient": 1, "gradient_alpha": 2, "gradient_dim": 3, "hessian": 4,
+                 "hessian_rowcol": 5, "special_hessian": 6, "gradient_kdp": 7, "hessian_kdpdq": 8}
+
+    def p3m(self, method: str, x, y, w, sigma, lo, hi, ratio: float = 0.2, padding: float = 3.0, alpha=None,
+            args=(0, 0, 0)):
+        """The reference's own P3MKernel<double, d> (reference library only), with data domain [lo, hi],
+        working spacing ratio and padding factor, through the ITK stand-ins (direct DFTs). method: a key
+        of P3M_KINDS; alpha is the alpha of ConvolveGradient(X, alpha) or the xi of
+        ConvolveSpecialHessian (which ignores x); args are dim / (row, col) / (k, dp) / (k, dp, dq)."""
+        kind = self.P3M_KINDS[method]
+        x, y, w, d, dv = self._prep(x, y, w)
+        nx, ny = x.shape[0], y.shape[0]
+        a = _f64(alpha) if alpha is not None else np.zeros((max(nx, ny), max(dv, d)))
+        shape = {0: (nx, dv), 1: (nx, dv, d), 2: (nx, d), 3: (nx, dv), 4: (nx, dv, d, d), 5: (nx, dv),
+                 6: (ny, d), 7: (nx,), 8: (nx,)}[kind]
+        out = np.zeros(shape)
+        a0, a1, a2 = (list(args) + [0, 0, 0])[:3]
+        self._check(self._lib.oracle_ref_p3m(d, kind, dv, _c(x), nx, _c(y), _c(w), ny, sigma, _c(a),
+                                             _c(_f64(lo)), _c(_f64(hi)), ratio, padding, a0, a1, a2, _c(out)))
         return out
 
     # Source-side adjoint by symmetry of K (see oracle_fwd_adjoint in gauss_oracle.c).

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "ExactKernel.h"
+#include "P3MKernel.h"
 
 namespace {
 
@@ -165,6 +166,68 @@ int image_fast_d(int kind, int dv, const double *x, long nx, const double *y, co
   });
 }
 
+// P3MKernel<double, D> (src/support/kernels/P3MKernel.cxx) with its grid parameters: the data domain
+// [lo, hi] (the D x 2 matrix SetDataDomain takes), the working spacing ratio and the padding factor,
+// through the ITK stand-ins of ref_shim/ (direct DFTs in place of VNL's FFT). kind selects the method:
+//  0 Convolve(X)                      out nx x dv
+//  1 ConvolveGradient(X)              out nx x dv x D
+//  2 ConvolveGradient(X, alpha)       out nx x D
+//  3 ConvolveGradient(X, dim = arg0)  out nx x dv
+//  4 ConvolveHessian(X)               out nx x dv x D x D
+//  5 ConvolveHessian(X, arg0, arg1)   out nx x dv
+//  6 ConvolveSpecialHessian(xi = alpha) (AbstractKernel's, over the P3M Hessians; X ignored) out ny x D
+//  7 ConvolveGradient(X, arg0, arg1)  out nx (the reference's stub)
+//  8 ConvolveHessian(X, arg0, arg1, arg2) out nx (the reference's stub)
+template <unsigned D>
+int p3m_d(int kind, int dv, const double *x, long nx, const double *y, const double *w, long ny, double sigma,
+          const double *alpha, const double *lo, const double *hi, double ratio, double padding, int arg0,
+          int arg1, int arg2, double *out) {
+  return guarded([&] {
+    P3MKernel<double, D> k;
+    MatrixType dom(D, 2, 0.0);
+    for (unsigned i = 0; i < D; ++i) {
+      dom(i, 0) = lo[i];
+      dom(i, 1) = hi[i];
+    }
+    k.SetDataDomain(dom);
+    k.SetWorkingSpacingRatio(ratio);
+    k.SetPaddingFactor(padding);
+    k.SetKernelWidth(sigma);
+    k.SetSources(from_rows(y, ny, D));
+    k.SetWeights(from_rows(w, ny, dv));
+    const MatrixType X = kind == 6 ? MatrixType() : from_rows(x, nx, D);
+    switch (kind) {
+      case 0: to_rows(k.Convolve(X), out); break;
+      case 1: {
+        const std::vector<MatrixType> g = k.ConvolveGradient(X);
+        for (long i = 0; i < nx; ++i) to_rows(g[(size_t)i], out + i * dv * D);
+        break;
+      }
+      case 2: to_rows(k.ConvolveGradient(X, from_rows(alpha, nx, dv)), out); break;
+      case 3: to_rows(k.ConvolveGradient(X, (unsigned)arg0), out); break;
+      case 4: {
+        const std::vector<std::vector<MatrixType>> h = k.ConvolveHessian(X);
+        for (long i = 0; i < nx; ++i)
+          for (int c = 0; c < dv; ++c) to_rows(h[(size_t)i][(size_t)c], out + (i * dv + c) * D * D);
+        break;
+      }
+      case 5: to_rows(k.ConvolveHessian(X, (unsigned)arg0, (unsigned)arg1), out); break;
+      case 6: to_rows(k.ConvolveSpecialHessian(from_rows(alpha, ny, D)), out); break;
+      case 7: {
+        const VectorType v = k.ConvolveGradient(X, (unsigned)arg0, (unsigned)arg1);
+        for (long i = 0; i < nx; ++i) out[i] = v[(unsigned)i];
+        break;
+      }
+      case 8: {
+        const VectorType v = k.ConvolveHessian(X, (unsigned)arg0, (unsigned)arg1, (unsigned)arg2);
+        for (long i = 0; i < nx; ++i) out[i] = v[(unsigned)i];
+        break;
+      }
+      default: throw std::runtime_error("unknown P3M method");
+    }
+  });
+}
+
 }  // namespace
 
 #define DISPATCH(fn, ...)                         \
@@ -228,6 +291,13 @@ int oracle_ref_image_fast(int d, int kind, int dv, const double *x, long nx, con
                           long ny, double sigma, const double *alpha, const double *origin, const double *spacing,
                           const long *size, double *out) {
   DISPATCH(image_fast, kind, dv, x, nx, y, w, ny, sigma, alpha, origin, spacing, size, out);
+}
+
+// P3MKernel's methods (reference library only; see p3m_d for kind and the argument meaning).
+int oracle_ref_p3m(int d, int kind, int dv, const double *x, long nx, const double *y, const double *w, long ny,
+                   double sigma, const double *alpha, const double *lo, const double *hi, double ratio,
+                   double padding, int arg0, int arg1, int arg2, double *out) {
+  DISPATCH(p3m, kind, dv, x, nx, y, w, ny, sigma, alpha, lo, hi, ratio, padding, arg0, arg1, arg2, out);
 }
 
 }  // extern "C"

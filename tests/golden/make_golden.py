@@ -20,6 +20,10 @@ sources by oracle/build_ref.sh) and records its outputs:
 * ``skull_registration.npz`` -- functional test 5 (registration/landmark/2d/skulls: a 2-D
   NonOrientedPolyline registration): the two polylines (x, y of the VTK points, 2-point LINES
   cells), the initial control points and the final FastGradientAscent state.
+* ``p3m_reference.npz`` -- every method of the reference's P3MKernel<double, d>
+  (src/support/kernels/P3MKernel.cxx) on seeded 2-D and 3-D cases (32^d and 64^d grids, one with
+  points outside the data domain), compiled from the reference's source against the ITK stand-ins
+  of oracle/ref_shim (direct discrete Fourier transforms in place of VNL's FFT).
 * ``amygdala_registration.npz`` -- functional test 6 of the reference
   (tests/functional_tests/configure.ini [Test6], registration/landmark/3d/amygdalas): the two
   meshes as the reference reads them (VTK float points, triangles re-oriented by its normals
@@ -140,6 +144,8 @@ def main(ref_root: str | None = None):
     banana_fixture(ref_root)
     # 9. the image-grid methods of ExactKernel through the ITK stand-ins of oracle/ref_shim
     image_fixture(ref_root)
+    # 10. every P3MKernel method through the same stand-ins (direct DFTs in place of VNL's FFT)
+    p3m_fixture(ref_root)
     print("wrote", sorted(os.listdir(HERE)))
 
 
@@ -314,8 +320,6 @@ def banana_fixture(ref_root: str | None = None):
         **{f"state_{k}": np.asarray(v) for k, v in st.items()})
 
 
-if __name__ == "__main__":
-    main(*(sys.argv[1:2]))
 
 
 def image_cases():
@@ -357,3 +361,55 @@ def image_fixture(ref_root: str | None = None):
         res[f"{name}_gradient"] = ref.image_fast(1, *args)
         res[f"{name}_gradient_alpha"] = ref.image_fast(2, *args, alpha=c["alpha"])
     np.savez_compressed(os.path.join(HERE, "image_fast.npz"), **res)
+
+
+def p3m_cases():
+    """Seeded P3M cases: name -> arrays (targets x, sources y, weights w, alpha, the special
+    Hessian's sources / momenta / xi, the data domain lo/hi, sigma, spacing ratio, padding)."""
+    rng = np.random.default_rng(17)
+    cases = {}
+    for name, d, nx, ny, dv, sigma, ratio, padding, span, dom in (
+            ("d2", 2, 160, 190, 2, 0.2, 0.2, 3.0, (0.0, 1.0), None),
+            ("d2out", 2, 150, 170, 3, 0.1, 0.2, 3.0, (-0.5, 1.5), (0.2, 0.8)),
+            ("d3", 3, 90, 110, 3, 0.3, 0.5, 3.0, (0.0, 1.0), None),
+            ("d3dv2", 3, 80, 100, 2, 0.25, 0.4, 2.0, (0.0, 1.0), None)):
+        x, y = rng.uniform(*span, (nx, d)), rng.uniform(*span, (ny, d))
+        if dom is None:
+            both = np.concatenate([x, y])
+            lo, hi = both.min(axis=0), both.max(axis=0)
+        else:
+            lo, hi = np.full(d, dom[0]), np.full(d, dom[1])
+        ys = rng.uniform(*span, (ny, d))
+        cases[name] = dict(x=x, y=y, w=rng.standard_normal((ny, dv)), alpha=rng.standard_normal((nx, dv)),
+                           ys=ys, beta=rng.standard_normal((ny, d)), xi=rng.standard_normal((ny, d)),
+                           lo=lo, hi=hi, ys_lo=ys.min(axis=0), ys_hi=ys.max(axis=0), sigma=np.array(sigma),
+                           ratio=np.array(ratio), padding=np.array(padding))
+    return cases
+
+
+def p3m_fixture(ref_root: str | None = None):
+    """Every P3MKernel method (P3MKernel.cxx:1245-1729, and AbstractKernel::ConvolveSpecialHessian over
+    its Hessians) computed by the reference's own compiled code: tests/golden/p3m_reference.npz."""
+    oracle.build_reference(ref_root)
+    ref = oracle.load("reference")
+    res = {}
+    for name, c in p3m_cases().items():
+        for k, v in c.items():
+            res[f"{name}_{k}"] = v
+        d = c["x"].shape[1]
+        common = dict(lo=c["lo"], hi=c["hi"], ratio=float(c["ratio"]), padding=float(c["padding"]))
+        xyws = (c["x"], c["y"], c["w"], float(c["sigma"]))
+        res[f"{name}_convolve"] = ref.p3m("convolve", *xyws, **common)
+        res[f"{name}_gradient"] = ref.p3m("gradient", *xyws, **common)
+        res[f"{name}_gradient_alpha"] = ref.p3m("gradient_alpha", *xyws, alpha=c["alpha"], **common)
+        res[f"{name}_gradient_dim"] = ref.p3m("gradient_dim", *xyws, args=(d - 1,), **common)
+        res[f"{name}_hessian"] = ref.p3m("hessian", *xyws, **common)
+        res[f"{name}_hessian_rowcol"] = ref.p3m("hessian_rowcol", *xyws, args=(d - 1, 0), **common)
+        res[f"{name}_special_hessian"] = ref.p3m(
+            "special_hessian", c["ys"], c["ys"], c["beta"], float(c["sigma"]), c["ys_lo"], c["ys_hi"],
+            float(c["ratio"]), float(c["padding"]), alpha=c["xi"])
+    np.savez_compressed(os.path.join(HERE, "p3m_reference.npz"), **res)
+
+
+if __name__ == "__main__":
+    main(*(sys.argv[1:2]))

@@ -1,6 +1,7 @@
-"""GPU particle-mesh kernel (gbk_p3m_*, the reference's P3MKernel with cuFFT) against its FP64
-restatement (oracle/p3m.py) and against the exact kernel sums (the reference's P3M tolerance,
-8e-2). Parity with the reference's own P3M binary is unpinned: it needs ITK/FFTW."""
+"""GPU particle-mesh kernel (gbk_p3m_*, the reference's P3MKernel with cuFFT) against the reference's
+own P3MKernel (golden vectors made by its source compiled on ITK stand-ins,
+tests/golden/p3m_reference.npz), against its FP64 restatement (oracle/p3m.py) and against the exact
+kernel sums (the reference's P3M tolerance, 8e-2)."""
 import numpy as np
 import pytest
 
@@ -170,3 +171,37 @@ def test_p3m_special_hessian(gb, K, d):
     assert np.linalg.norm(got - ref) <= 1e-10 * np.linalg.norm(ref)
     ex = np.asarray(K.special_hessian(y, b, 0.3, xi)).reshape(ref.shape)
     assert np.linalg.norm(got - ex) <= 8e-2 * np.linalg.norm(ex)
+
+
+@pytest.mark.parametrize("mode,tol", [("F64", 1e-10), ("F32C", 1e-5)])
+@pytest.mark.parametrize("name", ["d2", "d2out", "d3", "d3dv2"])
+def test_p3m_matches_the_reference_p3m(gb, name, mode, tol):
+    """Every P3MKernel overload on the device against the reference's own outputs (FP64 grids to
+    1e-10, FP32 grids to 1e-5 normwise), through the C ABI (kernel.p3m_*) and the kernel object
+    (GB300P3MKernel, including the inherited ConvolveSpecialHessian)."""
+    from deformetrica_code_gb300 import kernel as KM
+    from tests.test_p3m import p3m_case
+    c = p3m_case(name)
+    x, y, w, sigma = c["x"], c["y"], c["w"], float(c["sigma"])
+    d = x.shape[1]
+    ctx = gb.Context(mode=getattr(gb, f"GBK_MODE_{mode}"))
+    kw = dict(domain=(c["lo"], c["hi"]), spacing_ratio=float(c["ratio"]), padding_factor=float(c["padding"]),
+              context=ctx)
+    got = {
+        "convolve": KM.p3m_convolve(x, y, w, sigma, **kw),
+        "gradient": KM.p3m_convolve_gradient(x, y, w, sigma, **kw),
+        "gradient_alpha": KM.p3m_convolve_gradient_alpha(x, y, w, sigma, c["alpha"], **kw),
+        "gradient_dim": KM.p3m_convolve_gradient_dim(x, y, w, sigma, d - 1, **kw),
+        "hessian": KM.p3m_convolve_hessian(x, y, w, sigma, **kw),
+        "hessian_rowcol": KM.p3m_convolve_hessian_rowcol(x, y, w, sigma, d - 1, 0, **kw),
+    }
+    k = gb.GB300P3MKernel(d, sigma, context=ctx, working_spacing_ratio=float(c["ratio"]),
+                          padding_factor=float(c["padding"]))
+    k.SetSources(c["ys"])
+    k.SetWeights(c["beta"])
+    k.SetDataDomain(c["ys_lo"], c["ys_hi"])
+    got["special_hessian"] = k.ConvolveSpecialHessian(c["xi"])
+    for key, val in got.items():
+        ref = c[key]
+        assert val.shape == ref.shape, key
+        assert np.linalg.norm(val - ref) <= tol * np.linalg.norm(ref), (key, np.linalg.norm(val - ref) / np.linalg.norm(ref))

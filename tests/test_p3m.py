@@ -1,6 +1,10 @@
-"""The particle-mesh (P3M) oracle (oracle/p3m.py, a restatement of the reference's P3MKernel,
-whose own build needs ITK/FFTW): the grid rule and the approximation error against the exact
-kernel, within the 8e-2 the reference's tests accept for P3M. No GPU."""
+"""The particle-mesh (P3M) oracle (oracle/p3m.py, a restatement of the reference's P3MKernel): the
+grid rule, the approximation error against the exact kernel (within the 8e-2 the reference's tests
+accept for P3M), and every method against the reference's own P3MKernel compiled from its source on
+ITK stand-ins (direct DFTs in place of VNL's FFT; tests/golden/p3m_reference.npz, made by
+tests/golden/make_golden.py). No GPU."""
+import os
+
 import numpy as np
 import pytest
 
@@ -78,3 +82,57 @@ def test_bench_grid_rule_matches_the_restatement():
         hi = lo + rng.uniform(0.1, 3.0, size=d)
         sigma, ratio = float(rng.uniform(0.03, 0.5)), float(rng.choice([0.1, 0.2, 0.3, 0.5]))
         assert bench.p3m_grid_size(lo, hi, sigma, ratio) == [int(v) for v in p3m.grid(lo, hi, sigma, ratio)[1]]
+
+
+P3M_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "p3m_reference.npz")
+P3M_CASES = ("d2", "d2out", "d3", "d3dv2")
+
+
+def p3m_case(name):
+    z = np.load(P3M_GOLDEN)
+    return {k[len(name) + 1:]: z[k] for k in z.files if k.startswith(name + "_")}
+
+
+def p3m_restated(c):
+    """Every P3MKernel method of the restatement on one golden case (keys as in the fixture)."""
+    from oracle import p3m
+    x, y, w, sigma = c["x"], c["y"], c["w"], float(c["sigma"])
+    d = x.shape[1]
+    kw = dict(lo=c["lo"], hi=c["hi"], ratio=float(c["ratio"]), padding=float(c["padding"]))
+    return {
+        "convolve": p3m.convolve(x, y, w, sigma, **kw),
+        "gradient": p3m.convolve_gradient(x, y, w, sigma, **kw),
+        "gradient_alpha": p3m.convolve_gradient_alpha(x, y, w, sigma, c["alpha"], **kw),
+        "gradient_dim": p3m.convolve_gradient_dim(x, y, w, sigma, d - 1, **kw),
+        "hessian": p3m.convolve_hessian(x, y, w, sigma, **kw),
+        "hessian_rowcol": p3m.convolve_hessian_rowcol(x, y, w, sigma, d - 1, 0, **kw),
+        "special_hessian": p3m.special_hessian(c["ys"], c["beta"], sigma, c["xi"], c["ys_lo"], c["ys_hi"],
+                                               float(c["ratio"]), float(c["padding"])),
+    }
+
+
+@pytest.mark.parametrize("name", P3M_CASES)
+def test_restatement_matches_the_reference_p3m(name):
+    """The FP64 restatement reproduces the reference's P3MKernel (every overload, the special Hessian
+    composed over its Hessians, points outside the data domain) to rounding: the two differ only in
+    the order of the transform sums."""
+    c = p3m_case(name)
+    for key, got in p3m_restated(c).items():
+        ref = c[key]
+        assert got.shape == ref.shape, key
+        assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref), key
+    if name == "d2out":  # targets off the grid get nothing, in the reference as in the restatement
+        assert np.count_nonzero(np.all(c["convolve"] == 0, axis=1)) > 0
+
+
+def test_reference_p3m_library_matches_its_golden_vectors():
+    """Where the reference tree is present, its P3MKernel built on the stand-ins still gives the
+    committed vectors (the fixture is current)."""
+    import oracle
+    if oracle.build_reference() is None:
+        pytest.skip("reference tree absent")
+    ref = oracle.load("reference")
+    c = p3m_case("d3dv2")
+    got = ref.p3m("gradient_alpha", c["x"], c["y"], c["w"], float(c["sigma"]), c["lo"], c["hi"],
+                  float(c["ratio"]), float(c["padding"]), alpha=c["alpha"])
+    assert np.array_equal(got, c["gradient_alpha"])

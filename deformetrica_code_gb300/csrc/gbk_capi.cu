@@ -308,6 +308,22 @@ std::vector<int> gbk_ctx::family(int path, int op, int d, int dv) const {
   return out;
 }
 
+// Packed coordinates for the small FP32 shapes (PairArgs::xp / yp): per coordinate of x (the first
+// nxd values) and y, the float pair (hi, lo) of v * s with hi = fl32(v s) and lo = fl32(v s - hi), lo = 0
+// where hi is not finite (so an infinite coordinate stays infinite, as when the kernel converts it).
+__global__ void pack_scaled_kernel(const double *x, long nxd, const double *y, long nyd, double s, float2 *xp,
+                                   float2 *yp) {
+  for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nxd + nyd; k += (long)gridDim.x * blockDim.x) {
+    const double v = (k < nxd ? x[k] : y[k - nxd]) * s;
+    const float hi = (float)v;
+    const float lo = isfinite(hi) ? (float)(v - (double)hi) : 0.f;
+    if (k < nxd)
+      xp[k] = make_float2(hi, lo);
+    else
+      yp[k - nxd] = make_float2(hi, lo);
+  }
+}
+
 int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
   LaunchPlan pl;
   if (int rc = plan(op, d, dv, a, &pl)) return rc;
@@ -385,6 +401,21 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
         a.sb_ld = d;
       }
     }
+  }
+  if (e.packable && !spatial && !a.xperm && !a.yperm && !a.xtiles && a.nx > 0 && a.ny > 0 && mode == MODE_F32C) {
+    // the small shapes centre in FP32 from coordinates packed once per launch (see packable)
+    const bool same = a.x == a.y && a.nx == a.ny;
+    const long nxd = a.nx * d, nyd = same ? 0 : a.ny * d;
+    if (int rc = ensure(packed, (size_t)(nxd + nyd) * sizeof(float2), "packed coordinates")) return rc;
+    float2 *xp = (float2 *)packed.p;
+    const long tot = nxd + nyd;
+    const unsigned blocks = (unsigned)std::min<long>((tot + 255) / 256, 4L * num_sms);
+    pack_scaled_kernel<<<blocks, 256, 0, stream>>>(a.x, nxd, a.y, nyd, coord_scale<float>(a.sigma), xp,
+                                                   same ? xp : xp + nxd);
+    if (int rc = cuda(cudaGetLastError(), "coordinate packing")) return rc;
+    launches += 1;
+    a.xp = xp;
+    a.yp = same ? xp : xp + nxd;
   }
   a.pair_count = pair_counter_of(op);
   a.status = status;

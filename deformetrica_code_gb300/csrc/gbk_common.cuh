@@ -108,6 +108,7 @@ struct SrcVal<float> {
     float f = (float)v;
     return make_float2(f, f);
   }
+  __device__ __forceinline__ static float2 make(float f) { return make_float2(f, f); }
 };
 template <>
 struct SrcVal<f32w> : SrcVal<float> {};
@@ -116,6 +117,7 @@ struct SrcVal<f32b> : SrcVal<float> {};
 template <>
 struct SrcVal<f32s> {
   __device__ __forceinline__ static float make(double v) { return (float)v; }
+  __device__ __forceinline__ static float make(float v) { return v; }
 };
 template <>
 struct SrcVal<double> {

@@ -49,6 +49,7 @@ struct gbk_ctx {
   DevBuf stage[kStageSlots];  // host-argument staging
   DevBuf reduce;              // FP64 reductions and small temporaries
   DevBuf tmp;                 // op temporaries (e.g. K w for the kernel norm)
+  DevBuf packed;              // packed coordinates of the small FP32 shapes (PairArgs::xp / yp)
   int order = 0;              // GBK_ORDER_* (0 = automatic)
   int gradient_mode = 0;      // GBK_GRADIENT_* of the point-cloud and volume data terms
   int estimator = 0;          // GBK_ESTIMATOR_* of the *_optimize calls
@@ -157,6 +158,7 @@ struct gbk_ctx {
     fr(tickets);
     fr(reduce);
     fr(tmp);
+    fr(packed);
     fr(order_keep[0]);
     fr(order_keep[1]);
     for (auto &ss : sort_slot) {

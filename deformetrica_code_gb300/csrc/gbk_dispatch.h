@@ -49,6 +49,7 @@ struct KernelEntry {
   int tj;     // sources per shared-memory tile
   int no;     // accumulators per target (partial-buffer width)
   int smem;   // dynamic shared memory bytes per CTA
+  bool packable;  // reads packed coordinates in caller order (PairArgs::xp / yp; see packable)
 };
 
 // Accumulators per target of an op (the partial buffer holds nsplit * no * nx doubles).
@@ -91,6 +92,7 @@ inline bool set_entry(KernelEntry *e) {
   e->tj = TJ;
   e->no = OpT::NO;
   e->smem = (int)pair_smem_bytes<OpT, T, D, BLOCK, R, TJ, CSM>();
+  e->packable = packable<T, BLOCK>();
   return true;
 }
 }  // namespace gbk

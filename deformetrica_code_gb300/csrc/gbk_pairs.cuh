@@ -72,6 +72,11 @@ struct PairArgs {
   // with nsplit > 1: one zeroed counter per target tile (index as the CTAs' tile index); the last split
   // CTA of a tile reduces the partials itself and resets it. Null: a split_reduce_kernel launch does.
   unsigned *tickets;
+  // packed coordinates (caller order, small FP32 shapes; see packable): per coordinate the float pair
+  // (hi, lo) of x * xscale, hi = fl32(x * xscale), lo = fl32(x * xscale - hi) (lo = 0 where hi is not
+  // finite), written once per launch by pack_scaled_kernel. Null: the kernel converts a.x / a.y.
+  const float2 *xp;
+  const float2 *yp;
 };
 
 __device__ __forceinline__ void put(double *p, int acc, double v) {
@@ -443,6 +448,7 @@ struct Pack;
 template <>
 struct Pack<float> {
   __device__ __forceinline__ static float2 make(double a, double b) { return make_float2((float)a, (float)b); }
+  __device__ __forceinline__ static float2 make(float a, float b) { return make_float2(a, b); }
 };
 template <>
 struct Pack<f32w> : Pack<float> {};
@@ -451,11 +457,36 @@ struct Pack<f32b> : Pack<float> {};
 template <>
 struct Pack<f32s> {
   __device__ __forceinline__ static float make(double a, double) { return (float)a; }
+  __device__ __forceinline__ static float make(float a, float) { return a; }
 };
 template <>
 struct Pack<double> {
   __device__ __forceinline__ static double make(double a, double) { return a; }
 };
+
+// Launch shapes that read packed coordinates (PairArgs::xp / yp) in caller order: the small FP32 shapes.
+// Their CTAs own few targets and short source ranges, so converting coordinates from FP64 in every
+// CTA (the bounding box, the centring and the scaling, repeated for every target tile and source
+// split) costs more than their pair work on a GPU whose FP64 rate is ~1/64 of FP32; with packed
+// coordinates a CTA centres in FP32 only.
+template <typename T, int BLOCK>
+__host__ __device__ constexpr bool packable() {
+  return BLOCK <= 64 && (std::is_same<T, float>::value || std::is_same<T, f32w>::value ||
+                         std::is_same<T, f32s>::value);
+}
+
+// The centred coordinate q = p - c of a packed coordinate p = hi + lo and a float centre c, in FP32:
+// hi - c exactly as a + e (Knuth's TwoSum), then qh = fl(a + fl(e + lo)) -- q rounded once up to the
+// rounding of the small term -- and ql = fl((a - qh) + fl(e + lo)), the low part for two-float
+// coordinates (qh + ql = q to ~2^-48 |q|).
+__device__ __forceinline__ void centre_packed(float2 p, float c, float &qh, float &ql) {
+  const float a = __fsub_rn(p.x, c);
+  const float bb = __fsub_rn(a, p.x);
+  const float e = __fadd_rn(__fsub_rn(p.x, __fsub_rn(a, bb)), __fsub_rn(-c, bb));
+  const float t = __fadd_rn(e, p.y);
+  qh = __fadd_rn(a, t);
+  ql = __fadd_rn(__fsub_rn(a, qh), t);
+}
 
 // Source record: D coordinates, the op's NS extras and, for two-float coordinates, the D low
 // parts; padded so that a record is a whole number of 16-byte vectors.
@@ -514,8 +545,8 @@ constexpr double kTwoFloatWidth = 16.0;
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int UNR, int CSM, bool TWOF>
 __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx, const int split, const long i0,
                                           const long iend,
-                                          const double *ctr, const double *s_box, unsigned *s_visit,
-                                          unsigned char *smem_raw) {
+                                          const double *ctr, const float *ctrf, const double *s_box,
+                                          unsigned *s_visit, unsigned char *smem_raw) {
   typedef Lane<T> L;
   typedef typename L::V V;
   typedef typename SrcLane<T>::SV SV;
@@ -532,12 +563,39 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx
   const int *const yperm = a.yperm;
   const bool prune = a.ybox != nullptr;
   const double xs = a.xscale;
+  constexpr bool PK = packable<T, BLOCK>();
+  const bool packed = PK && a.xp != nullptr;  // caller order: no permutation, no pruning
   // ---- this thread's targets: centred, pre-scaled coordinates and extras, in lanes ----
   V xg[G][D];
   V xlo[G][TWOF ? D : 1];  // low parts of two-float coordinates
   V tg[G][Op::NT > 0 ? Op::NT : 1];
+  if constexpr (PK) {
+    if (packed) {
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        float qh[W][D], ql[W][D];
+        double tv[W][Op::NT > 0 ? Op::NT : 1];
+#pragma unroll
+        for (int w2 = 0; w2 < W; ++w2) {
+          long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
+          const long ic = i < iend ? i : (iend - 1);  // out-of-range lanes compute a copy, never stored
+#pragma unroll
+          for (int l = 0; l < D; ++l) centre_packed(a.xp[ic * D + l], ctrf[l], qh[w2][l], ql[w2][l]);
+          Op::load_target(a, ic, tv[w2]);
+        }
+#pragma unroll
+        for (int l = 0; l < D; ++l) {
+          xg[g][l] = Pack<T>::make(qh[0][l], qh[W - 1][l]);
+          if (TWOF) xlo[g][l < (TWOF ? D : 1) ? l : 0] = Pack<T>::make(ql[0][l], ql[W - 1][l]);
+        }
+#pragma unroll
+        for (int k = 0; k < Op::NT; ++k) tg[g][k] = Pack<T>::make(tv[0][k], tv[W - 1][k]);
+      }
+    }
+  }
 #pragma unroll
   for (int g = 0; g < G; ++g) {
+    if (packed) break;
     double xv[W][D], tv[W][Op::NT > 0 ? Op::NT : 1];
 #pragma unroll
     for (int w2 = 0; w2 < W; ++w2) {
@@ -754,6 +812,35 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx
     }
     const int cnt = (int)((je - jt) < TJ ? (je - jt) : TJ);
     visited += cnt;
+    if constexpr (PK) {
+      if (packed) {  // -(y' - c) from the packed coordinates in FP32, extras converted from FP64
+        for (int r = threadIdx.x; r < TJ; r += BLOCK) {
+          SV rv[NJP];
+#pragma unroll
+          for (int q = 0; q < NJP; ++q) rv[q] = SrcVal<T>::make(0.f);  // padding and empty slots: exact no-ops
+          if (r < cnt) {
+            const long j = jt + r;
+            double ex[Op::NS > 0 ? Op::NS : 1];
+            Op::load_source(a, j, ex);
+#pragma unroll
+            for (int l = 0; l < D; ++l) {
+              float qh, ql;
+              centre_packed(a.yp[j * D + l], ctrf[l], qh, ql);
+              rv[l] = SrcVal<T>::make(-qh);
+              if (TWOF) rv[LO + l < NJP ? LO + l : 0] = SrcVal<T>::make(-ql);
+            }
+#pragma unroll
+            for (int k = 0; k < Op::NS; ++k) rv[D + k] = SrcVal<T>::make(ex[k]);
+          }
+#pragma unroll
+          for (int q = 0; q < NJP; ++q) tile[r * NJP + q] = rv[q];
+        }
+        __syncthreads();
+        compute_tile(cnt);
+        __syncthreads();
+        continue;
+      }
+    }
     // ---- stage TJ source records: -(y - c) * xscale and extras, broadcast to the lane type ----
     for (int r = threadIdx.x; r < TJ; r += BLOCK) {
       double rec[NJP];
@@ -822,16 +909,30 @@ sums_done:
     __syncthreads();
     if (s_last) {
       __threadfence();
+      // SB splits' partials are loaded before they are added (in split order, as the separate
+      // reduction adds them), so a CTA waits for one round of L2 loads per SB splits, not per split.
+      constexpr int SB_VALS = BLOCK <= 64 ? 24 : 12;  // small shapes have registers to spare here
+      constexpr int SB = NO >= SB_VALS ? 1 : SB_VALS / NO;
       for (int r = 0; r < R; ++r) {
         const long i = i0 + threadIdx.x + (long)r * BLOCK;
         if (i >= iend) continue;
         double v[NO];
 #pragma unroll
         for (int o = 0; o < NO; ++o) v[o] = 0.0;
-        for (int s2 = 0; s2 < a.nsplit; ++s2) {
-          const double *p = a.partial + (long)s2 * NO * a.nx;
+        for (int s0 = 0; s0 < a.nsplit; s0 += SB) {
+          double buf[SB][NO];
 #pragma unroll
-          for (int o = 0; o < NO; ++o) v[o] += __ldcg(p + (long)o * a.nx + i);
+          for (int k = 0; k < SB; ++k) {
+            const double *p = a.partial + (long)(s0 + k < a.nsplit ? s0 + k : s0) * NO * a.nx;
+#pragma unroll
+            for (int o = 0; o < NO; ++o) buf[k][o] = __ldcg(p + (long)o * a.nx + i);
+          }
+#pragma unroll
+          for (int k = 0; k < SB; ++k)
+            if (s0 + k < a.nsplit) {
+#pragma unroll
+              for (int o = 0; o < NO; ++o) v[o] += buf[k][o];
+            }
         }
         Op::store(a, xperm ? (long)xperm[i] : i, v);
       }
@@ -858,6 +959,10 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
   __shared__ double s_ctr[D];
   __shared__ double s_box[2 * D];
   __shared__ unsigned s_visit[kPruneWindow / 32];
+  constexpr bool PK = packable<T, BLOCK>();
+  __shared__ float s_redf[PK ? 2 * D : 1][BLOCK / 32];
+  __shared__ float s_ctrf[D];
+  __shared__ float s_widf;
 
   // ---- this CTA's targets: sorted positions [i0, iend) (caller order when unsorted) ----
   long i0, iend;
@@ -872,10 +977,72 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
   }
   const int *const xperm = a.xperm;
   const bool prune = a.ybox != nullptr;
+  const bool packed = PK && a.xp != nullptr;
 
   // ---- bounding box of the CTA's targets (FP64): centre for FP32 lanes, box for pruning ----
   double ctr[D];
-  if (CENTER || prune) {
+  float ctrf[D];
+  if constexpr (PK) {
+    if (packed) {
+      // Packed coordinates (caller order, no pruning): the box of the high parts in FP32 (scaled units),
+      // its midpoint as the CTA's float centre; NaN coordinates are ignored by fminf / fmaxf.
+      float lo[D], hi[D];
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+        lo[l] = 3.0e38f;
+        hi[l] = -3.0e38f;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const long i = i0 + threadIdx.x + (long)r * BLOCK;
+        if (i < iend) {
+#pragma unroll
+          for (int l = 0; l < D; ++l) {
+            const float v = a.xp[i * D + l].x;
+            lo[l] = fminf(lo[l], v);
+            hi[l] = fmaxf(hi[l], v);
+          }
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          lo[l] = fminf(lo[l], __shfl_xor_sync(0xffffffffu, lo[l], o));
+          hi[l] = fmaxf(hi[l], __shfl_xor_sync(0xffffffffu, hi[l], o));
+        }
+      }
+      if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int l = 0; l < D; ++l) {
+          s_redf[l][threadIdx.x >> 5] = lo[l];
+          s_redf[D + l][threadIdx.x >> 5] = hi[l];
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float wid = 0.f;
+        for (int l = 0; l < D; ++l) {
+          float mn = 3.0e38f, mx = -3.0e38f;
+          for (int w2 = 0; w2 < BLOCK / 32; ++w2) {
+            mn = fminf(mn, s_redf[l][w2]);
+            mx = fmaxf(mx, s_redf[D + l][w2]);
+          }
+          s_ctrf[l] = mn <= mx ? 0.5f * mn + 0.5f * mx : 0.f;
+          wid = fmaxf(wid, mx - mn);  // an infinite spread makes the CTA wide, as the FP64 box does
+        }
+        s_widf = wid;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+        ctrf[l] = s_ctrf[l];
+        ctr[l] = 0.0;
+      }
+    }
+  }
+  if (packed) {
+  } else if (CENTER || prune) {
     double lo[D], hi[D];
 #pragma unroll
     for (int l = 0; l < D; ++l) {
@@ -923,27 +1090,37 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
     }
     __syncthreads();
 #pragma unroll
-    for (int l = 0; l < D; ++l) ctr[l] = s_ctr[l];
+    for (int l = 0; l < D; ++l) {
+      ctr[l] = s_ctr[l];
+      ctrf[l] = 0.f;
+    }
   } else {
 #pragma unroll
-    for (int l = 0; l < D; ++l) ctr[l] = 0.0;
+    for (int l = 0; l < D; ++l) {
+      ctr[l] = 0.0;
+      ctrf[l] = 0.f;
+    }
   }
 
   if constexpr (std::is_same<T, f32w>::value) {
     // adaptive two-float coordinates: only a CTA whose targets spread wider than kTwoFloatWidth
     // scaled units pays for the low parts (in the spatial order no tile is that wide)
     double width = 0.0;
+    if (packed) {
+      width = (double)s_widf;
+    } else {
 #pragma unroll
-    for (int l = 0; l < D; ++l) width = fmax(width, (s_box[D + l] - s_box[l]) * a.xscale);
+      for (int l = 0; l < D; ++l) width = fmax(width, (s_box[D + l] - s_box[l]) * a.xscale);
+    }
     if (!(width <= kTwoFloatWidth))
-      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, true>(a, tile_idx, split, i0, iend, ctr, s_box, s_visit,
-                                                                 smem_raw);
+      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, true>(a, tile_idx, split, i0, iend, ctr, ctrf, s_box,
+                                                                 s_visit, smem_raw);
     else
-      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, tile_idx, split, i0, iend, ctr, s_box, s_visit,
-                                                                 smem_raw);
+      pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, tile_idx, split, i0, iend, ctr, ctrf, s_box,
+                                                                 s_visit, smem_raw);
   } else {
-    pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, tile_idx, split, i0, iend, ctr, s_box, s_visit,
-                                                                 smem_raw);
+    pair_body<Op, T, D, BLOCK, R, TJ, MERGE, UNR, CSM, false>(a, tile_idx, split, i0, iend, ctr, ctrf, s_box,
+                                                                 s_visit, smem_raw);
   }
 }
 

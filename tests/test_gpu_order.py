@@ -262,11 +262,13 @@ def test_auto_orders_large_calls_only(gb, ctx):
     # (the device radix sort above that is counted as the library's), then one tiles kernel for the
     # targets and one kernel for the source boxes and copies; pruning adds the targets' non-finite
     # scan and the conditional unbounding of the chunk boxes. Below 2^30 pairs AUTO runs Convolve
-    # and the alpha-gradient in caller order (adaptive two-float variant: same launches as OFF)
-    assert launches(gb.GBK_ORDER_AUTO, 1000) == launches(gb.GBK_ORDER_OFF, 1000)
+    # and the alpha-gradient in caller order (adaptive two-float variant: same launches as OFF). The
+    # small shape packs the coordinates once per launch in caller order (one launch), not in the
+    # spatial order.
+    assert launches(gb.GBK_ORDER_AUTO, 1000) == launches(gb.GBK_ORDER_OFF, 1000) == 2
     assert launches(gb.GBK_ORDER_AUTO, 12000) == launches(gb.GBK_ORDER_OFF, 12000)
     assert launches(gb.GBK_ORDER_AUTO, 40000) == launches(gb.GBK_ORDER_OFF, 40000) + 8
-    assert launches(gb.GBK_ORDER_SPATIAL, 1000) == launches(gb.GBK_ORDER_OFF, 1000) + 10
+    assert launches(gb.GBK_ORDER_SPATIAL, 1000) == launches(gb.GBK_ORDER_OFF, 1000) + 10 - 1
     assert launches(gb.GBK_ORDER_SPATIAL, 20000) == launches(gb.GBK_ORDER_OFF, 20000) + 8
 
     # other ops from 2^22 pairs measure the extent of the two point sets first (one box launch):
@@ -296,7 +298,8 @@ def test_auto_orders_large_calls_only(gb, ctx):
         k.ForwardAdjoint(x, al)
         return ctx.launch_count() - n0
 
-    assert fa_launches(gb.GBK_ORDER_SPATIAL, 1000) == fa_launches(gb.GBK_ORDER_OFF, 1000) + 14
+    # (caller order packs the coordinates for each of the two small-shape passes)
+    assert fa_launches(gb.GBK_ORDER_SPATIAL, 1000) == fa_launches(gb.GBK_ORDER_OFF, 1000) + 14 - 2
     assert fa_launches(gb.GBK_ORDER_AUTO, 12000) == fa_launches(gb.GBK_ORDER_OFF, 12000)
     with pytest.raises(gb.GBKError):
         ctx.set_order(7)
@@ -424,3 +427,28 @@ def test_bulk_staging_across_prune_windows(gb, ctx):
     assert np.array_equal(got[gb.GBK_STAGING_LOADS], got[gb.GBK_STAGING_BULK])
     assert got[gb.GBK_STAGING_LOADS, "pairs"] == got[gb.GBK_STAGING_BULK, "pairs"] < 0.5 * 3000 * 1_100_000
     ctx.set_staging(gb.GBK_STAGING_AUTO)
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_small_shape_packed_coordinates_far_from_the_origin(gb, ctx, port, d):
+    """Problems too small for the default launch shape run the small shape, which centres
+    coordinates packed once per launch (hi + lo floats of the scaled coordinates) in FP32 with an
+    exact TwoSum: accuracy must not depend on how far the points sit from the origin. Every output
+    of the fused forward + adjoint and the ops without a fused form stay within FP32C tolerance of
+    the FP64 oracle with the data moved 1e3 and 1e5 units away, in caller order and two-float."""
+    rng = np.random.default_rng(90 + d)
+    X0, Y0 = mixture(rng, 700, d), mixture(rng, 500, d)
+    W, A = rng.standard_normal((500, d)), rng.standard_normal((700, d))
+    sigma = 0.1
+    for offset in (0.0, 1e3, 1e5):
+        X, Y = X0 + offset, Y0 + offset
+        ref = port.fwd_adjoint(X, Y, W, sigma, A)
+        ref_varlin = port.grad_varlin(X, Y, W, sigma)
+        for order in (gb.GBK_ORDER_OFF, gb.GBK_ORDER_TWO_FLOAT):
+            k = kern(gb, ctx, d, sigma, Y, W, gb.GBK_MODE_F32C, order)
+            got = k.ForwardAdjoint(X, A)
+            for g_, r_ in zip(got, ref):
+                assert normwise_rel(g_, r_) <= 5e-7, (offset, order)
+            assert normwise_rel(np.asarray(k.ConvolveGradient(X)).reshape(ref_varlin.shape), ref_varlin) <= 5e-7
+            assert ctx.last_launch()[0] == 8, ctx.last_launch()  # varlin ran the small shape (variant 8)
+    ctx.set_order(gb.GBK_ORDER_AUTO)

@@ -48,6 +48,8 @@ bool find_kernel(int op, int mode, int d, int dv, int variant, KernelEntry *e) {
     return (op == OP_CONV || op == OP_CONV_GRADA || op == OP_GRADA) && find_kernel_conv(op, mode, d, dv, variant, e);
   if (variant == VARIANT_BULK || variant == VARIANT_BULK_128)
     return mode == MODE_F32C && find_kernel_conv_bulk(op, d, dv, variant, e);
+  if (variant == VARIANT_WARP || variant == VARIANT_WARP_TWO_FLOAT)
+    return mode == MODE_F32C && find_kernel_warp(op, d, dv, variant, e);
   switch (op) {
     case OP_CONV:
     case OP_CONV_GRADA:
@@ -165,10 +167,18 @@ int gbk_ctx::occupancy(const KernelEntry &e, int) {
   return blocks;
 }
 
-// Source splits: enough CTAs to fill every SM with a small tail, each split >= 2 source tiles.
+// Source splits: enough CTAs to fill every SM with a small tail, each split >= 2 source tiles. A
+// warp-split kernel (e.ks > 0) aims at two CTAs per SM, each of its warps keeping >= one tile.
 int gbk_ctx::choose_split(const KernelEntry &e, int d, long nx, long ny) {
   if (force_split > 0) return force_split;
-  long per_cta = (long)e.block * e.r;
+  if (e.ks > 0) {
+    const long itiles = std::max(1L, (nx + e.tile - 1) / e.tile);
+    long cap = std::max(1L, ny / ((long)e.ks * e.tj));
+    cap = std::min(cap, 64L);
+    cap = std::min(cap, std::max(1L, (long)((512L << 20) / (8L * e.no * std::max(nx, 1L)))));
+    return (int)std::max(1L, std::min(cap, (2L * num_sms + itiles - 1) / itiles));
+  }
+  long per_cta = (long)e.tile;
   long itiles = (nx + per_cta - 1) / per_cta;
   long slots = (long)num_sms * occupancy(e, d);
   long max_split = std::max(1L, ny / (2L * e.tj));
@@ -269,12 +279,19 @@ int gbk_ctx::plan(int op, int d, int dv, const PairArgs &a, LaunchPlan *p) {
   bool small = false;
   KernelEntry e0, es;
   if (find_kernel(op, mode, d, dv, 0, &e0)) {
-    const long per_cta = (long)e0.block * e0.r;
+    const long per_cta = (long)e0.tile;
     const long itiles = (a.nx + per_cta - 1) / per_cta;
     const long max_split = std::max(1L, a.ny / (2L * e0.tj));
     small = itiles * max_split < 2L * num_sms && find_kernel(op, mode, d, dv, VARIANT_SMALL, &es);
   }
-  if (p->path == PATH_TWO_FLOAT) {
+  // too small for the default shape, in caller order: the warp-split kernel where it is compiled
+  KernelEntry ew;
+  const bool warp = small && !p->spatial && unordered && mode == MODE_F32C &&
+                    find_kernel(op, mode, d, dv, p->path == PATH_TWO_FLOAT ? VARIANT_WARP_TWO_FLOAT : VARIANT_WARP,
+                                &ew);
+  if (warp) {
+    p->variant = p->path == PATH_TWO_FLOAT ? VARIANT_WARP_TWO_FLOAT : VARIANT_WARP;
+  } else if (p->path == PATH_TWO_FLOAT) {
     p->variant = small ? VARIANT_SMALL_TWO_FLOAT : VARIANT_TWO_FLOAT;
   } else {
     p->variant = small ? VARIANT_SMALL : 0;
@@ -292,7 +309,7 @@ int gbk_ctx::plan(int op, int d, int dv, const PairArgs &a, LaunchPlan *p) {
 std::vector<int> gbk_ctx::family(int path, int op, int d, int dv) const {
   std::vector<int> cand;
   if (path == PATH_TWO_FLOAT) {
-    cand = {VARIANT_TWO_FLOAT, VARIANT_SMALL_TWO_FLOAT};
+    cand = {VARIANT_TWO_FLOAT, VARIANT_SMALL_TWO_FLOAT, VARIANT_WARP_TWO_FLOAT};
   } else {
     if (path == PATH_SPATIAL && staging != GBK_STAGING_LOADS) {
       cand.push_back(VARIANT_BULK);
@@ -300,6 +317,7 @@ std::vector<int> gbk_ctx::family(int path, int op, int d, int dv) const {
     }
     for (int v = 0; v < kNumShapeVariants; ++v) cand.push_back(v);
     cand.push_back(VARIANT_SMALL);
+    if (path == PATH_PLAIN) cand.push_back(VARIANT_WARP);  // caller order only (packed coordinates)
   }
   std::vector<int> out;
   KernelEntry e;
@@ -341,6 +359,14 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
   KernelEntry e;
   if (!find_kernel(op, mode, d, dv, variant, &e) && !find_kernel(op, mode, d, dv, 0, &e))
     return fail(GBK_ERR_UNSUPPORTED, "no kernel for op %d, d=%d, dv=%d", op, d, dv);
+  // packed coordinates need caller order and points on both sides; a warp-split kernel needs them
+  const bool can_pack = !spatial && !a.xperm && !a.yperm && !a.xtiles && a.nx > 0 && a.ny > 0 && mode == MODE_F32C;
+  if (e.ks > 0 && !can_pack) {
+    variant = find_kernel(op, mode, d, dv, VARIANT_SMALL, &e) ? VARIANT_SMALL : 0;
+    if (variant == 0 && !find_kernel(op, mode, d, dv, 0, &e))
+      return fail(GBK_ERR_UNSUPPORTED, "no kernel for op %d, d=%d, dv=%d", op, d, dv);
+    ns = 0;
+  }
   if (force_split > 0) ns = force_split;
   if (ns <= 0) ns = choose_split(e, d, a.nx, a.ny);
   if (spatial) {
@@ -368,7 +394,7 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     OrderView tv, sv;
     if (int rc = order_sort(this, d, a.x, a.nx, &xs)) return rc;
     if (int rc = order_sort(this, d, a.y, a.ny, &ys)) return rc;
-    if (int rc = order_targets(this, d, xs, e.block * e.r, a.sigma, &tv)) return rc;
+    if (int rc = order_targets(this, d, xs, e.tile, a.sigma, &tv)) return rc;
     if (int rc = order_sources(this, d, a.y, ys, e.tj, want, &sv)) return rc;
     launches += xs.launches + ys.launches;
     a.xperm = tv.perm;
@@ -402,7 +428,7 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
       }
     }
   }
-  if (e.packable && !spatial && !a.xperm && !a.yperm && !a.xtiles && a.nx > 0 && a.ny > 0 && mode == MODE_F32C) {
+  if (e.packable && can_pack) {
     // the small shapes centre in FP32 from coordinates packed once per launch (see packable)
     const bool same = a.x == a.y && a.nx == a.ny;
     const long nxd = a.nx * d, nyd = same ? 0 : a.ny * d;
@@ -429,7 +455,7 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     if (rc) return rc;
     a.partial = (double *)partial.p;
     // the last split CTA of each target tile reduces the tile (no separate reduction launch)
-    if (!spatial) ticket_tiles = (a.nx + (long)e.block * e.r - 1) / ((long)e.block * e.r);
+    if (!spatial) ticket_tiles = (a.nx + (long)e.tile - 1) / (long)e.tile;
     if ((rc = ensure_tickets(ticket_tiles))) return rc;
     a.tickets = (unsigned *)tickets.p;
   }

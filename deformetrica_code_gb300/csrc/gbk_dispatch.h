@@ -33,6 +33,11 @@ constexpr int VARIANT_SMALL_TWO_FLOAT = 10;
 // Convolve and alpha-gradient ops in FP32C mode, for the spatial order's sorted source copies.
 constexpr int VARIANT_BULK = 11;
 constexpr int VARIANT_BULK_128 = 12;  // the same with 128-thread CTAs and 128-source chunks
+// Warp-split kernels (gbk_pairs_warp.cuh) for problems too small to fill the GPU, caller order with
+// packed coordinates: one-float (Convolve-like ops and the fused control-point adjoint update) and
+// adaptive two-float (Convolve-like ops), FP32C.
+constexpr int VARIANT_WARP = 13;
+constexpr int VARIANT_WARP_TWO_FLOAT = 14;
 
 enum Mode { MODE_F32C = 0, MODE_F64 = 1 };
 
@@ -50,6 +55,8 @@ struct KernelEntry {
   int no;     // accumulators per target (partial-buffer width)
   int smem;   // dynamic shared memory bytes per CTA
   bool packable;  // reads packed coordinates in caller order (PairArgs::xp / yp; see packable)
+  int tile;       // targets per CTA
+  int ks;         // warps of a CTA dividing its sources (warp-split kernels), 0 otherwise
 };
 
 // Accumulators per target of an op (the partial buffer holds nsplit * no * nx doubles).
@@ -74,6 +81,7 @@ bool find_kernel_conv_shape(int op, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_grad(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_hess(int op, int mode, int d, int dv, int variant, KernelEntry *e);
 bool find_kernel_deform(int op, int mode, int d, int dv, int variant, KernelEntry *e);
+bool find_kernel_warp(int op, int d, int dv, int variant, KernelEntry *e);  // VARIANT_WARP*, FP32C
 
 }  // namespace gbk
 
@@ -93,6 +101,8 @@ inline bool set_entry(KernelEntry *e) {
   e->no = OpT::NO;
   e->smem = (int)pair_smem_bytes<OpT, T, D, BLOCK, R, TJ, CSM>();
   e->packable = packable<T, BLOCK>();
+  e->tile = BLOCK * R;
+  e->ks = 0;
   return true;
 }
 }  // namespace gbk

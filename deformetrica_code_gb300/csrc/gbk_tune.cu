@@ -127,7 +127,7 @@ int tune_core(gbk_ctx *c, int op, int d, int dv, PairArgs a, int *best_variant, 
   for (int v : fam) {
     KernelEntry e;
     if (!find_kernel(op, c->mode, d, dv, v, &e)) continue;
-    const long max_split = std::max(1L, a.ny / (2L * e.tj));
+    const long max_split = std::max(1L, a.ny / ((e.ks > 0 ? (long)e.ks : 2L) * e.tj));
     std::vector<int> cands = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32};
     cands.push_back(c->choose_split(e, d, a.nx, a.ny));
     std::sort(cands.begin(), cands.end());

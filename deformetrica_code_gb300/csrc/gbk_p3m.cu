@@ -33,6 +33,7 @@ struct P3MGrid {
   long n[3] = {1, 1, 1};
   double origin[3] = {0, 0, 0};
   double s = 1.0;
+  double inv_s = 1.0;  // 1 / s (FP32 grids: continuous indices by multiplication)
   long cells() const { return n[0] * n[1] * (d == 3 ? n[2] : 1); }
   long ccells() const { return n[0] * (d == 3 ? n[1] * (n[2] / 2 + 1) : (n[1] / 2 + 1)); }
 };
@@ -127,28 +128,37 @@ __global__ void p3m_kernel_images(P3MGrid g, double sigma, G *img, long cells) {
 
 // multilinear corners of one point, slot b = corner b in the reference's order (first dimension
 // slowest): linear index, weight, `use` (inside the grid and weight > 0) and `interior` (no index
-// <= 0, the splat's border rule). Fixed slots keep the arrays in registers.
-template <int D>
+// <= 0, the splat's border rule). Fixed slots keep the arrays in registers. The continuous index
+// (p - origin) / s is formed in FP64 (the reference's division on FP64 grids, a multiplication by
+// the reciprocal spacing on FP32 grids); the fractions and weights are in the grid's precision G,
+// so FP32 grids weigh and sum in FP32: GB300's FP64 rate is ~1/64 of its FP32 rate, and FP64
+// weights and sums dominated these kernels while the FP32 grid values carry ~1e-7 relative anyway.
+template <int D, typename G>
 struct P3MCorners {
   long l[1 << D];
-  double w[1 << D];
+  G w[1 << D];
   bool use[1 << D], interior[1 << D];
 };
 
-template <int D>
-__device__ inline void p3m_corners(const double *p, const P3MGrid &g, P3MCorners<D> &cs) {
+template <int D, typename G>
+__device__ inline void p3m_corners(const double *p, const P3MGrid &g, P3MCorners<D, G> &cs) {
   long i1[D];
-  double f[D], h[D];
+  G f[D], h[D];
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    const double c = (p[k] - g.origin[k]) / g.s;
-    i1[k] = (long)floor(c);
-    f[k] = c - i1[k];
-    h[k] = (i1[k] + 1) - c;
+    double c;
+    if constexpr (std::is_same<G, double>::value)
+      c = (p[k] - g.origin[k]) / g.s;
+    else
+      c = (p[k] - g.origin[k]) * g.inv_s;
+    const double fl = floor(c);
+    i1[k] = (long)fl;
+    f[k] = (G)(c - fl);
+    h[k] = (G)((fl + 1.0) - c);
   }
 #pragma unroll
   for (int b = 0; b < (1 << D); ++b) {
-    double wt = 1.0;
+    G wt = (G)1;
     bool in = true, inner = true;
     long l = 0;
 #pragma unroll
@@ -162,7 +172,7 @@ __device__ inline void p3m_corners(const double *p, const P3MGrid &g, P3MCorners
     }
     cs.l[b] = l;
     cs.w[b] = wt;
-    cs.use[b] = in && wt > 0;
+    cs.use[b] = in && wt > (G)0;
     cs.interior[b] = inner;
   }
 }
@@ -171,12 +181,13 @@ template <int D, typename G>
 __global__ void p3m_splat(const double *y, const double *wts, long ny, int dv, P3MGrid g, G *grids, long cells) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ny) return;
-  P3MCorners<D> cs;
-  p3m_corners<D>(y + i * D, g, cs);
+  P3MCorners<D, G> cs;
+  p3m_corners<D, G>(y + i * D, g, cs);
+  for (int k = 0; k < dv; ++k) {
+    const G wk = (G)wts[i * dv + k];
 #pragma unroll
-  for (int c = 0; c < (1 << D); ++c) {
-    if (!cs.use[c] || !cs.interior[c]) continue;
-    for (int k = 0; k < dv; ++k) atomicAdd(grids + (long)k * cells + cs.l[c], (G)(cs.w[c] * wts[i * dv + k]));
+    for (int c = 0; c < (1 << D); ++c)
+      if (cs.use[c] && cs.interior[c]) atomicAdd(grids + (long)k * cells + cs.l[c], cs.w[c] * wk);
   }
 }
 
@@ -198,21 +209,21 @@ __global__ void p3m_multiply(const C *spec, const C *kspec, int nimg, int per_gr
 
 // values at the targets: mode 0 the nimg images; mode 2 contracted with alpha (images ordered
 // p + D k, out nx x D); mode 3 the symmetric Hessians (images ordered q + D(D+1)/2 k, q the upper
-// entry, out nx x dv x D x D)
+// entry, out nx x dv x D x D). Sums in the grid's precision G.
 template <int D, typename G>
 __global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, long cells, P3MGrid g, int mode,
                            const double *alpha, int dv, double *out) {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nx) return;
-  P3MCorners<D> cs;
-  p3m_corners<D>(x + i * D, g, cs);
+  P3MCorners<D, G> cs;
+  p3m_corners<D, G>(x + i * D, g, cs);
   if (mode == 0) {
     for (int q = 0; q < nimg; ++q) {
-      double v = 0.0;
+      G v = (G)0;
 #pragma unroll
       for (int c = 0; c < (1 << D); ++c)
         if (cs.use[c]) v += cs.w[c] * imgs[(long)q * cells + cs.l[c]];
-      out[i * nimg + q] = v;
+      out[i * nimg + q] = (double)v;
     }
   } else if (mode == 3) {
     constexpr int H = D * (D + 1) / 2;
@@ -220,23 +231,23 @@ __global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, lo
       int q = 0;
       for (int r = 0; r < D; ++r)
         for (int cc = r; cc < D; ++cc, ++q) {
-          double v = 0.0;
+          G v = (G)0;
 #pragma unroll
           for (int c = 0; c < (1 << D); ++c)
             if (cs.use[c]) v += cs.w[c] * imgs[(long)(q + H * k) * cells + cs.l[c]];
-          out[((i * dv + k) * D + r) * D + cc] = v;
-          out[((i * dv + k) * D + cc) * D + r] = v;
+          out[((i * dv + k) * D + r) * D + cc] = (double)v;
+          out[((i * dv + k) * D + cc) * D + r] = (double)v;
         }
     }
   } else {
-    double r[D];
+    G r[D];
 #pragma unroll
-    for (int p = 0; p < D; ++p) r[p] = 0.0;
+    for (int p = 0; p < D; ++p) r[p] = (G)0;
     for (int k = 0; k < dv; ++k) {
-      const double a = alpha[i * dv + k];
+      const G a = (G)alpha[i * dv + k];
 #pragma unroll
       for (int p = 0; p < D; ++p) {
-        double v = 0.0;
+        G v = (G)0;
 #pragma unroll
         for (int c = 0; c < (1 << D); ++c)
           if (cs.use[c]) v += cs.w[c] * imgs[(long)(p + D * k) * cells + cs.l[c]];
@@ -244,7 +255,7 @@ __global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, lo
       }
     }
 #pragma unroll
-    for (int p = 0; p < D; ++p) out[i * D + p] = r[p];
+    for (int p = 0; p < D; ++p) out[i * D + p] = (double)r[p];
   }
 }
 
@@ -471,6 +482,7 @@ int p3m_run(gbk_ctx *c, int mode, int p0, int p1, int d, int dv, const double *x
   P3MGrid g;
   g.d = d;
   g.s = ratio * sigma;
+  g.inv_s = 1.0 / g.s;
   for (int k = 0; k < d; ++k) {
     const double length = box[d + k] - box[k];
     const double nd = (length + 2 * padding * sigma) / g.s;

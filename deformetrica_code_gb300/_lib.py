@@ -9,7 +9,8 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libgbkernel.so")
+# $GBK_LIBRARY selects another build of the same library (e.g. the bounds-checked one)
+LIB_PATH = os.environ.get("GBK_LIBRARY") or os.path.join(HERE, "libgbkernel.so")
 
 GBK_OK = 0
 GBK_ERR_ARG = 1
@@ -18,6 +19,7 @@ GBK_ERR_CUDA = 3
 GBK_ERR_ALLOC = 4
 GBK_ERR_TIMEOUT = 5
 GBK_ERR_STATE = 6
+GBK_ERR_BOUNDS = 7
 
 GBK_MODE_F32C = 0
 GBK_MODE_F64 = 1

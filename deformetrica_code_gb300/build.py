@@ -19,6 +19,10 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbkernel.so")
+# the bounds-checked build (-DGBK_BOUNDS_CHECK=1: every target / source index of the kernel sums
+# checked, a failure reported as GBK_ERR_BOUNDS by gbk_synchronize); for tests, not the default
+CHECKED_BUILD_DIR = os.path.join(HERE, "_build_checked")
+CHECKED_LIB = os.path.join(HERE, "libgbkernel_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
@@ -40,15 +44,19 @@ def _deps() -> list[str]:
             + glob.glob(os.path.join(INCLUDE, "*.h")))
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+def up_to_date(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(p) <= t for p in _deps())
 
 
-def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> str:
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, jobs: int | None = None, bounds_check: bool = False) -> str:
+    """Builds libgbkernel.so, or with bounds_check=True libgbkernel_checked.so; returns its path."""
+    LIB = CHECKED_LIB if bounds_check else globals()["LIB"]
+    BUILD_DIR = CHECKED_BUILD_DIR if bounds_check else globals()["BUILD_DIR"]
+    flags = NVCC_FLAGS + (["-DGBK_BOUNDS_CHECK=1"] if bounds_check else [])
+    if not force and up_to_date(LIB):
         return LIB
     nvcc = _nvcc()
     os.makedirs(BUILD_DIR, exist_ok=True)
@@ -60,7 +68,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         if (not force and os.path.exists(obj) and os.path.getmtime(obj) >= newest_header
                 and os.path.getmtime(obj) >= os.path.getmtime(src)):
             return obj
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj + ".tmp"]
+        cmd = [nvcc, *ARCH, *flags, "-c", src, "-o", obj + ".tmp"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{res.stderr[-4000:]}")
@@ -84,4 +92,5 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    import sys
+    print(build(verbose=True, bounds_check="--bounds-check" in sys.argv[1:]))

@@ -682,6 +682,9 @@ int gbk_synchronize(gbk_ctx *c) {
   if (st) {
     cudaMemset(c->status, 0, sizeof st);
     if (c->tickets.p) cudaMemset(c->tickets.p, 0, c->tickets.cap);  // a stopped CTA left its tile's count
+    if (st & 2u)
+      return c->fail(GBK_ERR_BOUNDS, "an index check of the bounds-checked build failed in a kernel sum since "
+                     "the last check (the index was clamped); its outputs are not valid");
     return c->fail(GBK_ERR_TIMEOUT, "a bounded device-side wait gave up in a kernel sum since the last check; "
                    "its outputs are not valid");
   }

@@ -16,6 +16,27 @@
 namespace gbk {
 
 // ---------------------------------------------------------------------------------------------
+// Index checks of a bounds-checked build (-DGBK_BOUNDS_CHECK=1; compiled out otherwise): an index
+// outside [0, n) sets bit 1 of the launch's status word (gbk_synchronize reports GBK_ERR_BOUNDS) and
+// is clamped into the array, so a checked kernel never reads or writes outside its arrays.
+// ---------------------------------------------------------------------------------------------
+#ifndef GBK_BOUNDS_CHECK
+#define GBK_BOUNDS_CHECK 0
+#endif
+__device__ __forceinline__ long checked_index(long i, long n, unsigned *status) {
+#if GBK_BOUNDS_CHECK
+  if (i < 0 || i >= n) {
+    if (status) atomicOr(status, 2u);
+    return i < 0 || n <= 0 ? 0 : n - 1;
+  }
+#else
+  (void)n;
+  (void)status;
+#endif
+  return i;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Lane types: Lane<float> carries two targets (float2, packed FFMA2), Lane<f32s> one target in
 // scalar FP32, Lane<double> one target in FP64. Packed FFMA2 halves issue slots, but with three
 // distinct register operands per instruction it measured ~68% of the FP32 lane peak on GB300

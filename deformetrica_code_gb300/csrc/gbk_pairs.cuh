@@ -578,7 +578,8 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx
 #pragma unroll
         for (int w2 = 0; w2 < W; ++w2) {
           long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
-          const long ic = i < iend ? i : (iend - 1);  // out-of-range lanes compute a copy, never stored
+          // out-of-range lanes compute a copy, never stored
+          const long ic = checked_index(i < iend ? i : (iend - 1), a.nx, a.status);
 #pragma unroll
           for (int l = 0; l < D; ++l) centre_packed(a.xp[ic * D + l], ctrf[l], qh[w2][l], ql[w2][l]);
           Op::load_target(a, ic, tv[w2]);
@@ -600,8 +601,8 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx
 #pragma unroll
     for (int w2 = 0; w2 < W; ++w2) {
       long i = i0 + threadIdx.x + (long)(g * W + w2) * BLOCK;
-      long ic = i < iend ? i : (iend - 1);  // out-of-range lanes compute a copy, never stored
-      if (xperm) ic = xperm[ic];
+      long ic = checked_index(i < iend ? i : (iend - 1), a.nx, a.status);  // out-of-range lanes: a copy
+      if (xperm) ic = checked_index(xperm[ic], a.nx, a.status);
 #pragma unroll
       for (int l = 0; l < D; ++l) xv[w2][l] = (a.x[ic * D + l] - ctr[l]) * xs;
       Op::load_target(a, ic, tv[w2]);
@@ -754,7 +755,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx
       // the elected thread fetches chunk q (coordinates, then weights) into buffer b
       auto issue = [&](const long q, const int b) {
         double *ry = raw + (size_t)b * TJ * (D + Op::NS);
-        const long jt = jb + q * TJ;
+        const long jt = checked_index(jb + q * TJ, a.ny, a.status);
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&st.bar[b], kBytesY + kBytesW);
         bulk_copy_g2s(ry, a.y + jt * D, kBytesY, &st.bar[b]);
@@ -819,7 +820,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx
 #pragma unroll
           for (int q = 0; q < NJP; ++q) rv[q] = SrcVal<T>::make(0.f);  // padding and empty slots: exact no-ops
           if (r < cnt) {
-            const long j = jt + r;
+            const long j = checked_index(jt + r, a.ny, a.status);
             double ex[Op::NS > 0 ? Op::NS : 1];
             Op::load_source(a, j, ex);
 #pragma unroll
@@ -845,8 +846,8 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, const long tile_idx
     for (int r = threadIdx.x; r < TJ; r += BLOCK) {
       double rec[NJP];
       if (r < cnt) {
-        long j = jt + r;
-        if (yperm) j = yperm[j];
+        long j = checked_index(jt + r, a.ny, a.status);
+        if (yperm) j = checked_index(yperm[j], a.ny, a.status);
 #pragma unroll
         for (int l = 0; l < D; ++l) rec[l] = (ctr[l] - a.y[j * D + l]) * xs;
         Op::load_source(a, j, rec + D);
@@ -892,7 +893,7 @@ sums_done:
 #pragma unroll
         for (int o = 0; o < NO; ++o) p[(long)o * a.nx + i] = v[o];
       } else {
-        Op::store(a, xperm ? (long)xperm[i] : i, v);
+        Op::store(a, checked_index(xperm ? (long)xperm[i] : i, a.nx, a.status), v);
       }
     }
   }
@@ -934,7 +935,7 @@ sums_done:
               for (int o = 0; o < NO; ++o) v[o] += buf[k][o];
             }
         }
-        Op::store(a, xperm ? (long)xperm[i] : i, v);
+        Op::store(a, checked_index(xperm ? (long)xperm[i] : i, a.nx, a.status), v);
       }
       if (threadIdx.x == 0) a.tickets[tile_idx] = 0u;
     }
@@ -998,7 +999,7 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
         if (i < iend) {
 #pragma unroll
           for (int l = 0; l < D; ++l) {
-            const float v = a.xp[i * D + l].x;
+            const float v = a.xp[checked_index(i, a.nx, a.status) * D + l].x;
             lo[l] = fminf(lo[l], v);
             hi[l] = fmaxf(hi[l], v);
           }
@@ -1053,7 +1054,7 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
     for (int r = 0; r < R; ++r) {
       long i = i0 + threadIdx.x + (long)r * BLOCK;
       if (i < iend) {
-        const long row = xperm ? (long)xperm[i] : i;
+        const long row = checked_index(xperm ? (long)xperm[checked_index(i, a.nx, a.status)] : i, a.nx, a.status);
 #pragma unroll
         for (int l = 0; l < D; ++l) {
           double v = a.x[row * D + l];

@@ -59,7 +59,8 @@ __device__ __forceinline__ void warp_body(const PairArgs &a, const long i0, cons
 #pragma unroll
     for (int w2 = 0; w2 < W; ++w2) {
       const long i = i0 + lane + (long)(g * W + w2) * 32;
-      const long ic = i < iend ? i : (iend - 1);  // out-of-range lanes compute a copy, never stored
+      // out-of-range lanes compute a copy, never stored
+      const long ic = checked_index(i < iend ? i : (iend - 1), a.nx, a.status);
 #pragma unroll
       for (int l = 0; l < D; ++l) centre_packed(a.xp[ic * D + l], c[l], qh[w2][l], ql[w2][l]);
       Op::load_target(a, ic, tv[w2]);
@@ -88,7 +89,7 @@ __device__ __forceinline__ void warp_body(const PairArgs &a, const long i0, cons
 #pragma unroll
       for (int q = 0; q < NJP; ++q) rv[q] = SrcVal<T>::make(0.f);
       if (lane < cnt) {
-        const long j = jt + lane;
+        const long j = checked_index(jt + lane, a.ny, a.status);
         double ex[Op::NS > 0 ? Op::NS : 1];
         Op::load_source(a, j, ex);
 #pragma unroll
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(32 * KS, MINB) pair_kernel_warp(const PairArgs
     for (int r = 0; r < R; ++r) {
       const long i = i0 + lane + (long)r * 32;
       if (i < iend) {
-        const float v = a.xp[i * D + l].x;
+        const float v = a.xp[checked_index(i, a.nx, a.status) * D + l].x;
         lo = fminf(lo, v);
         hi = fmaxf(hi, v);
       }

@@ -47,7 +47,8 @@ enum {
   GBK_ERR_CUDA = 3,        /* a CUDA runtime call failed */
   GBK_ERR_ALLOC = 4,       /* device memory allocation failed */
   GBK_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up (reported by gbk_synchronize) */
-  GBK_ERR_STATE = 6        /* call not allowed in the current state (e.g. during capture) */
+  GBK_ERR_STATE = 6,       /* call not allowed in the current state (e.g. during capture) */
+  GBK_ERR_BOUNDS = 7       /* an index check of a bounds-checked build failed (reported by gbk_synchronize) */
 };
 
 enum { GBK_MODE_F32C = 0, GBK_MODE_F64 = 1 };
@@ -154,7 +155,10 @@ int gbk_get_gradient_mode(const gbk_ctx *ctx);
 int gbk_set_estimator(gbk_ctx *ctx, int estimator);
 int gbk_get_estimator(const gbk_ctx *ctx);
 /* Waits for all work queued on the context's stream. Returns GBK_ERR_TIMEOUT (and clears the report)
- * when a kernel sum's bounded device-side wait gave up since the last call (see GBK_STAGING_BULK). */
+ * when a kernel sum's bounded device-side wait gave up since the last call (see GBK_STAGING_BULK), and
+ * GBK_ERR_BOUNDS when, in a library built with bounds checks (GBK_BOUNDS_CHECK=1: build.py
+ * build(bounds_check=True), libgbkernel_checked.so), a kernel sum met a target or source index
+ * outside its arrays (the index was clamped and the outputs are not valid). */
 int gbk_synchronize(gbk_ctx *ctx);
 /* Number of the library's own kernels launched on this context so far. */
 long long gbk_launch_count(const gbk_ctx *ctx);

@@ -138,18 +138,20 @@ int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *m
     a.w_ld = d;
     a.ta = mt;
     a.ta_ld = d;
-    a.out0 = s.va;  // dPos = K p
+    // dPos = K p, dMom = G^T p, and the explicit Euler step fused into the stores:
+    // pos[t+1] = pos[t] + dt dPos ; mom[t+1] = mom[t] - dt dMom (Diffeos.cxx:631-632); with nearly zero
+    // momenta pos stays cp0 and mom[t+1] = mom[t] (zeroed below) (:601-613)
+    a.out0 = pos + (t + 1) * n;
     a.out0_ld = d;
-    a.out1 = s.vb;  // dMom = G^T p
+    a.base0 = pt;
+    a.step0 = dt;
+    a.flag_out0 = cp0;
+    a.out1 = mom + (t + 1) * n;
     a.out1_ld = d;
+    a.base1 = mt;
+    a.step1 = -dt;
+    a.flag = s.flag;
     if ((rc = c->launch(OP_CONV_GRADA, d, d, a))) return rc;
-    // pos[t+1] = pos[t] + dt dPos ; mom[t+1] = mom[t] - dt dMom (Diffeos.cxx:631-632);
-    // with nearly zero momenta: pos stays cp0 and mom[t+1] = 0 (:601-613)
-    if ((rc = c->cuda(lincomb(st, pos + (t + 1) * n, pt, dt, s.va, 0, nullptr, n, s.flag, cp0), "euler")))
-      return rc;
-    if ((rc = c->cuda(lincomb(st, mom + (t + 1) * n, mt, -dt, s.vb, 0, nullptr, n, s.flag, nullptr), "euler")))
-      return rc;
-    c->launches += 2;
   }
   // nearly zero momenta: the reference leaves mom[t >= 1] at their initial zeros (:601-613)
   zero_if_flag_kernel<<<blocks_for((T - 1) * n), 256, 0, st>>>(mom + n, (T - 1) * n, s.flag);
@@ -180,17 +182,20 @@ int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mo
     if ((rc = c->launch(OP_CONV, d, d, a))) return rc;
     if ((rc = c->cuda(lincomb(st, lt1, lt, dt, s.vc, 0, nullptr, m, s.flag, nullptr), "euler"))) return rc;
     c->launches += 1;
-    if (heun) {
+    if (heun) {  // the Heun corrector fused into the store: lt1 = lt + dt/2 vc + dt/2 K(lt1) p (in place)
       PairArgs b = pair_args(nlm, ncp, sigma);
       b.x = lt1;
       b.y = pos + (t + 1) * n;
       b.w = mom + (t + 1) * n;
       b.w_ld = d;
-      b.out0 = s.vd;
+      b.out0 = lt1;
       b.out0_ld = d;
+      b.base0 = lt;
+      b.aux0 = s.vc;
+      b.aux_c0 = 0.5 * dt;
+      b.step0 = 0.5 * dt;
+      b.flag = s.flag;
       if ((rc = c->launch(OP_CONV, d, d, b))) return rc;
-      if ((rc = c->cuda(lincomb(st, lt1, lt, 0.5 * dt, s.vc, 0.5 * dt, s.vd, m, s.flag, nullptr), "heun"))) return rc;
-      c->launches += 1;
     }
   }
   return GBK_OK;
@@ -256,16 +261,25 @@ int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, con
       b.y = pos + (t - 1) * n;
       b.w = mom + (t - 1) * n;
       b.w_ld = d;
-      b.out1 = s.vd;
-      b.out1_ld = d;
-      if ((rc = c->launch(OP_GRADA, d, d, b))) return rc;
-      if (jump_here) {  // and the cursor moves back in this branch only (:123-128)
+      if (!jump_here) {  // the Heun corrector fused into the store: th1 = th_t + dt/2 vc + dt/2 vd (in place)
+        b.out1 = th1;
+        b.out1_ld = d;
+        b.base1 = theta + t * m;
+        b.aux1 = s.vc;
+        b.aux_c1 = 0.5 * dt;
+        b.step1 = 0.5 * dt;
+        if ((rc = c->launch(OP_GRADA, d, d, b))) return rc;
+      } else {
+        b.out1 = s.vd;
+        b.out1_ld = d;
+        if ((rc = c->launch(OP_GRADA, d, d, b))) return rc;
+        // and the cursor moves back in this branch only (:123-128)
         if ((rc = c->cuda(lincomb(st, s.vd, s.vd, 1.0, jumps->grads[si], 0.0, nullptr, m), "jump"))) return rc;
         c->launches += 1;
         si = si > 0 ? si - 1 : 0;
+        if ((rc = c->cuda(lincomb(st, th1, theta + t * m, 0.5 * dt, s.vc, 0.5 * dt, s.vd, m), "heun"))) return rc;
+        c->launches += 1;
       }
-      if ((rc = c->cuda(lincomb(st, th1, theta + t * m, 0.5 * dt, s.vc, 0.5 * dt, s.vd, m), "heun"))) return rc;
-      c->launches += 1;
     }
     for (int k = 0; k < (own_index ? jumps->n : 0); ++k)
       if (jumps->times[k] == t - 1) {

@@ -77,6 +77,18 @@ struct PairArgs {
   // finite), written once per launch by pack_scaled_kernel. Null: the kernel converts a.x / a.y.
   const float2 *xp;
   const float2 *yp;
+  // Fused explicit-Euler / Heun update of an output (the deformation loops; Convolve and the
+  // alpha-gradients): with base0 set, the first output's element becomes
+  //   out0 = base0 + aux_c0 * aux0 + step0 * v   (aux0 optional; lincomb_kernel's order of additions)
+  // and, while *flag != 0 (momenta below the reference's threshold), out0 = flag_out0 (or base0 when
+  // null); likewise the second output with base1 ... . base, aux and flag_out have the output's
+  // layout. An output may be the launch's own targets or target extras: a CTA writes a target row
+  // only after every CTA of its tile has read it (its own prologue, or the last split of the tile).
+  const double *base0, *aux0, *flag_out0;
+  double step0, aux_c0;
+  const double *base1, *aux1, *flag_out1;
+  double step1, aux_c1;
+  const int *flag;
 };
 
 __device__ __forceinline__ void put(double *p, int acc, double v) {
@@ -84,6 +96,27 @@ __device__ __forceinline__ void put(double *p, int acc, double v) {
     *p += v;
   else
     *p = v;
+}
+
+// Stores element `off` of the first (which = 0) or second output: the plain store (put) or the
+// fused update of PairArgs::base0 / base1.
+__device__ __forceinline__ void put_out(const PairArgs &a, int which, long off, double v) {
+  double *out = which ? a.out1 : a.out0;
+  const double *base = which ? a.base1 : a.base0;
+  if (!base) {
+    put(out + off, which ? a.acc1 : a.acc0, v);
+    return;
+  }
+  if (a.flag && *a.flag) {
+    const double *fo = which ? a.flag_out1 : a.flag_out0;
+    out[off] = fo ? fo[off] : base[off];
+    return;
+  }
+  const double *aux = which ? a.aux1 : a.aux0;
+  double r = base[off];
+  if (aux) r += (which ? a.aux_c1 : a.aux_c0) * aux[off];
+  r += (which ? a.step1 : a.step0) * v;
+  out[off] = r;
 }
 
 // =============================================================================================
@@ -111,7 +144,7 @@ struct OpConv {
   }
   __device__ static void store(const PairArgs &a, long i, const double *v) {
 #pragma unroll
-    for (int k = 0; k < DV; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, v[k]);
+    for (int k = 0; k < DV; ++k) put_out(a, 0, i * a.out0_ld + k, v[k]);
   }
 };
 
@@ -150,11 +183,11 @@ struct OpConvGradAlpha {
     constexpr int G0 = CONV ? DV : 0;
     if (CONV && a.out0) {
 #pragma unroll
-      for (int k = 0; k < DV; ++k) put(a.out0 + i * a.out0_ld + k, a.acc0, v[k]);
+      for (int k = 0; k < DV; ++k) put_out(a, 0, i * a.out0_ld + k, v[k]);
     }
     const double f = -2.0 / (a.sigma * a.sigma * a.xscale);  // dx was accumulated pre-scaled
 #pragma unroll
-    for (int l = 0; l < D; ++l) put(a.out1 + i * a.out1_ld + l, a.acc1, v[G0 + l] * f);
+    for (int l = 0; l < D; ++l) put_out(a, 1, i * a.out1_ld + l, v[G0 + l] * f);
   }
 };
 

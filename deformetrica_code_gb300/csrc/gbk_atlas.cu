@@ -41,6 +41,7 @@ unsigned nb(long n, int bs = 256) { return (unsigned)std::max(1L, (n + bs - 1) /
 __global__ void lincomb_batched_kernel(int S, long n, double *out, long so, const double *base, long sb,
                                        double c1, const double *v1, long s1, double c2, const double *v2,
                                        long s2, const int *flag, const double *flag_value, long sf) {
+  pdl_entry();
   long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (long)S * n) return;
   const long s = k / n, i = k % n;
@@ -56,6 +57,7 @@ __global__ void lincomb_batched_kernel(int S, long n, double *out, long so, cons
 
 // flag[s] = (|p_s|_F < 1e-20), one CTA per subject
 __global__ void __launch_bounds__(256) norm_flag_batched_kernel(const double *p, long n, long stride, int *flag) {
+  pdl_entry();
   __shared__ double sh[256];
   const double *q = p + (long)blockIdx.x * stride;
   double acc = 0.0;
@@ -70,6 +72,7 @@ __global__ void __launch_bounds__(256) norm_flag_batched_kernel(const double *p,
 }
 
 __global__ void zero_flagged_kernel(int S, long n, double *p, long stride, const int *flag) {
+  pdl_entry();
   long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (long)S * n) return;
   const long s = k / n;
@@ -79,6 +82,7 @@ __global__ void zero_flagged_kernel(int S, long n, double *p, long stride, const
 // out[s] = sum_i a[s][i] b[s][i] in FP64, one CTA per subject, fixed order
 __global__ void __launch_bounds__(256) dot_batched_kernel(const double *a, long sa, const double *b, long sbb,
                                                           long n, double *out, int out_stride) {
+  pdl_entry();
   __shared__ double sh[256];
   const double *x = a + (long)blockIdx.x * sa, *y = b + (long)blockIdx.x * sbb;
   double acc = 0.0;
@@ -95,6 +99,7 @@ __global__ void __launch_bounds__(256) dot_batched_kernel(const double *a, long 
 // per-subject log-likelihood terms and totals (subject order)
 __global__ void loglik_kernel(int S, const double *norm_t, const double *ss, const double *st, const double *kpp,
                               double inv2s2, double *match, double *out) {
+  pdl_entry();
   if (threadIdx.x != 0) return;
   double tot = 0.0, data = 0.0, reg = 0.0;
   for (int s = 0; s < S; ++s) {
@@ -114,6 +119,7 @@ __global__ void loglik_kernel(int S, const double *norm_t, const double *ss, con
 // out[i] = sum_s (c1 a[s][i] + c2 b[s][i]) in subject order
 __global__ void sum_subjects_kernel(int S, long n, double *out, const double *a, long sa, double c1, const double *b,
                                     long sbb, double c2) {
+  pdl_entry();
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double r = 0.0;
@@ -127,6 +133,7 @@ __global__ void sum_subjects_kernel(int S, long n, double *out, const double *a,
 // template faces of every subject's deformed template: centres, normals (+ varifold tensors)
 __global__ void face_batched_kernel(int S, const double *pts, long spts, const int *tris, long nf, int kind,
                                     double *c, double *n, double *mn, double *w) {
+  pdl_entry();
   long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (long)S * nf) return;
   const long s = k / nf, f = k % nf;
@@ -170,6 +177,7 @@ __device__ inline void sym6(const double *m, const double *x, double *y) {
 __global__ void face_grad_batched_kernel(long total, int kind, int dw, const double *n, const double *mn,
                                          const double *kts, const double *ktt, const double *gs, const double *gt,
                                          double *kt, double *gk) {
+  pdl_entry();
   long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= total) return;
   if (kind == 0) {
@@ -201,6 +209,7 @@ __global__ void face_grad_batched_kernel(long total, int kind, int dw, const dou
 __global__ void vertex_gather_batched_kernel(int S, long nv, long nf, const double *pts, long spts, const int *tris,
                                              const int *ptr, const int *fc, const double *kt, const double *gk,
                                              double *out, long sout, double scale) {
+  pdl_entry();
   long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= (long)S * nv) return;
   const long s = k / nv, v = k % nv;
@@ -567,66 +576,68 @@ int gbk_atlas::body() {
   int rc;
   auto ok = [&](cudaError_t e, const char *what) { return c->cuda(e, what); };
   // trajectories start at the shared control points / template and each subject's momenta
-  lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, pos, sT_n, cp, 0, 0, nullptr, 0, 0, nullptr, 0,
-                                                           nullptr, nullptr, 0);
-  lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, momt, sT_n, mom, n, 0, nullptr, 0, 0, nullptr, 0,
-                                                           nullptr, nullptr, 0);
-  lincomb_batched_kernel<<<nb((long)S * m), 256, 0, st>>>(S, m, lm, sT_m, lm0, 0, 0, nullptr, 0, 0, nullptr, 0,
-                                                           nullptr, nullptr, 0);
-  norm_flag_batched_kernel<<<S, 256, 0, st>>>(mom, n, n, flag);
+  // (launch errors of the element-wise kernels are read back with cudaGetLastError after each stage)
+  (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, pos, sT_n, cp, 0, 0, nullptr, 0, 0,
+                    nullptr, 0, nullptr, nullptr, 0);
+  (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, momt, sT_n, mom, n, 0, nullptr, 0, 0,
+                    nullptr, 0, nullptr, nullptr, 0);
+  (void)gbk::launch(lincomb_batched_kernel, nb((long)S * m), 256, 0, st, S, m, lm, sT_m, lm0, 0, 0, nullptr, 0, 0,
+                    nullptr, 0, nullptr, nullptr, 0);
+  (void)gbk::launch(norm_flag_batched_kernel, S, 256, 0, st, mom, n, n, flag);
   c->launches += 4;
   if ((rc = ok(cudaGetLastError(), "init"))) return rc;
   // shooting (Diffeos.cxx:589-660)
   for (int t = 0; t + 1 < T; ++t) {
     if ((rc = run_launch(L++))) return rc;
     const double *dpos = t == 0 ? kp : va, *dmom = t == 0 ? greg : vb;
-    lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, pos + (t + 1) * n, sT_n, pos + t * n, sT_n, dt, dpos,
-                                                             sr, 0, nullptr, 0, flag, cp, 0);
-    lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, momt + (t + 1) * n, sT_n, momt + t * n, sT_n, -dt,
-                                                             dmom, sr, 0, nullptr, 0, flag, nullptr, 0);
+    (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, pos + (t + 1) * n, sT_n, pos + t * n,
+                      sT_n, dt, dpos, sr, 0, nullptr, 0, flag, cp, 0);
+    (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, momt + (t + 1) * n, sT_n, momt + t * n,
+                      sT_n, -dt, dmom, sr, 0, nullptr, 0, flag, nullptr, 0);
     c->launches += 2;
   }
-  zero_flagged_kernel<<<nb((long)S * (T - 1) * n), 256, 0, st>>>(S, (T - 1) * n, momt + n, sT_n, flag);
+  (void)gbk::launch(zero_flagged_kernel, nb((long)S * (T - 1) * n), 256, 0, st, S, (T - 1) * n, momt + n, sT_n, flag);
   c->launches += 1;
   // flow (Diffeos.cxx:661-712)
   for (int t = 0; t + 1 < T; ++t) {
     if ((rc = run_launch(L++))) return rc;
-    lincomb_batched_kernel<<<nb((long)S * m), 256, 0, st>>>(S, m, lm + (t + 1) * m, sT_m, lm + t * m, sT_m, dt, vc, sr,
-                                                             0, nullptr, 0, flag, nullptr, 0);
+    (void)gbk::launch(lincomb_batched_kernel, nb((long)S * m), 256, 0, st, S, m, lm + (t + 1) * m, sT_m, lm + t * m,
+                      sT_m, dt, vc, sr, 0, nullptr, 0, flag, nullptr, 0);
     c->launches += 1;
     if (heun) {
       if ((rc = run_launch(L++))) return rc;
-      lincomb_batched_kernel<<<nb((long)S * m), 256, 0, st>>>(S, m, lm + (t + 1) * m, sT_m, lm + t * m, sT_m,
-                                                               0.5 * dt, vc, sr, 0.5 * dt, vd, sr, flag, nullptr, 0);
+      (void)gbk::launch(lincomb_batched_kernel, nb((long)S * m), 256, 0, st, S, m, lm + (t + 1) * m, sT_m, lm + t * m,
+                        sT_m, 0.5 * dt, vc, sr, 0.5 * dt, vd, sr, flag, nullptr, 0);
       c->launches += 1;
     }
   }
   // data term on the deformed templates
   const double *lmT = lm + (T - 1) * m;
-  face_batched_kernel<<<nb((long)S * nf), 256, 0, st>>>(S, lmT, sT_m, tris, nf, kind, cs, ns, mns, ws);
+  (void)gbk::launch(face_batched_kernel, nb((long)S * nf), 256, 0, st, S, lmT, sT_m, tris, nf, kind, cs, ns, mns, ws);
   c->launches += 1;
   if ((rc = run_launch(L++))) return rc;  // self
   if ((rc = run_launch(L++))) return rc;  // cross
   const double *alpha = kind ? ws : ns;
-  dot_batched_kernel<<<S, 256, 0, st>>>(alpha, nf * dw, kts, nf * dw, nf * dw, dot_ss, 1);
-  dot_batched_kernel<<<S, 256, 0, st>>>(alpha, nf * dw, ktt, nf * dw, nf * dw, dot_st, 1);
-  dot_batched_kernel<<<S, 256, 0, st>>>(kp, sr, mom, n, n, kpp, 1);
-  loglik_kernel<<<1, 32, 0, st>>>(S, norm_t, dot_ss, dot_st, kpp, 0.5 / data_sigma2, match, out);
-  face_grad_batched_kernel<<<nb((long)S * nf), 256, 0, st>>>((long)S * nf, kind, dw, ns, mns, kts, ktt, gs, gt, kt, gk);
-  vertex_gather_batched_kernel<<<nb((long)S * nv), 256, 0, st>>>(S, nv, nf, lmT, sT_m, tris, csr_ptr, csr_fc, kt, gk,
-                                                                  theta + (T - 1) * m, sT_m, 0.5 / data_sigma2);
+  (void)gbk::launch(dot_batched_kernel, S, 256, 0, st, alpha, nf * dw, kts, nf * dw, nf * dw, dot_ss, 1);
+  (void)gbk::launch(dot_batched_kernel, S, 256, 0, st, alpha, nf * dw, ktt, nf * dw, nf * dw, dot_st, 1);
+  (void)gbk::launch(dot_batched_kernel, S, 256, 0, st, kp, sr, mom, n, n, kpp, 1);
+  (void)gbk::launch(loglik_kernel, 1, 32, 0, st, S, norm_t, dot_ss, dot_st, kpp, 0.5 / data_sigma2, match, out);
+  (void)gbk::launch(face_grad_batched_kernel, nb((long)S * nf), 256, 0, st, (long)S * nf, kind, dw, ns, mns, kts, ktt,
+                    gs, gt, kt, gk);
+  (void)gbk::launch(vertex_gather_batched_kernel, nb((long)S * nv), 256, 0, st, S, nv, nf, lmT, sT_m, tris, csr_ptr,
+                    csr_fc, kt, gk, theta + (T - 1) * m, sT_m, 0.5 / data_sigma2);
   c->launches += 6;
   if ((rc = ok(cudaGetLastError(), "data term"))) return rc;
   // landmark adjoint (AdjointEquationsIntegrator.cxx:59-136)
   for (int t = T - 1; t > 0; --t) {
     if ((rc = run_launch(L++))) return rc;
-    lincomb_batched_kernel<<<nb((long)S * m), 256, 0, st>>>(S, m, theta + (t - 1) * m, sT_m, theta + t * m, sT_m, dt,
-                                                             vc, sr, 0, nullptr, 0, nullptr, nullptr, 0);
+    (void)gbk::launch(lincomb_batched_kernel, nb((long)S * m), 256, 0, st, S, m, theta + (t - 1) * m, sT_m,
+                      theta + t * m, sT_m, dt, vc, sr, 0, nullptr, 0, nullptr, nullptr, 0);
     c->launches += 1;
     if (heun) {
       if ((rc = run_launch(L++))) return rc;
-      lincomb_batched_kernel<<<nb((long)S * m), 256, 0, st>>>(S, m, theta + (t - 1) * m, sT_m, theta + t * m, sT_m,
-                                                               0.5 * dt, vc, sr, 0.5 * dt, vd, sr, nullptr, nullptr, 0);
+      (void)gbk::launch(lincomb_batched_kernel, nb((long)S * m), 256, 0, st, S, m, theta + (t - 1) * m, sT_m,
+                        theta + t * m, sT_m, 0.5 * dt, vc, sr, 0.5 * dt, vd, sr, nullptr, nullptr, 0);
       c->launches += 1;
     }
   }
@@ -636,28 +647,28 @@ int gbk_atlas::body() {
   for (int t = T - 1; t > 0; --t) {
     if ((rc = run_launch(L++))) return rc;
     if ((rc = run_launch(L++))) return rc;
-    lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, xp + (t - 1) * n, sT_n, xp + t * n, sT_n, dt, va, sr,
-                                                             0, nullptr, 0, nullptr, nullptr, 0);
-    lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, xm + (t - 1) * n, sT_n, xm + t * n, sT_n, dt, vb, sr,
-                                                             0, nullptr, 0, nullptr, nullptr, 0);
+    (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, xp + (t - 1) * n, sT_n, xp + t * n,
+                      sT_n, dt, va, sr, 0, nullptr, 0, nullptr, nullptr, 0);
+    (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, xm + (t - 1) * n, sT_n, xm + t * n,
+                      sT_n, dt, vb, sr, 0, nullptr, 0, nullptr, nullptr, 0);
     c->launches += 2;
     if (heun) {
       if ((rc = run_launch(L++))) return rc;
       if ((rc = run_launch(L++))) return rc;
-      lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, xp + (t - 1) * n, sT_n, xp + t * n, sT_n, 0.5 * dt,
-                                                               va, sr, 0.5 * dt, vc, sr, nullptr, nullptr, 0);
-      lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, xm + (t - 1) * n, sT_n, xm + t * n, sT_n, 0.5 * dt,
-                                                               vb, sr, 0.5 * dt, vd, sr, nullptr, nullptr, 0);
+      (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, xp + (t - 1) * n, sT_n, xp + t * n,
+                        sT_n, 0.5 * dt, va, sr, 0.5 * dt, vc, sr, nullptr, nullptr, 0);
+      (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, xm + (t - 1) * n, sT_n, xm + t * n,
+                        sT_n, 0.5 * dt, vb, sr, 0.5 * dt, vd, sr, nullptr, nullptr, 0);
       c->launches += 2;
     }
   }
   // gradients: dL/dp_s = -xi_mom_s(0) - K p_s ; dL/dcp = sum_s (-xi_pos_s(0) - G_s) ;
   // template: sum_s -theta_s(0)
-  lincomb_batched_kernel<<<nb((long)S * n), 256, 0, st>>>(S, n, gmom, n, nullptr, 0, -1.0, xm, sT_n, -1.0, kp, sr,
-                                                           nullptr, nullptr, 0);
-  sum_subjects_kernel<<<nb(n), 256, 0, st>>>(S, n, gcp, xp, sT_n, -1.0, greg, sr, -1.0);
-  sum_subjects_kernel<<<nb(m), 256, 0, st>>>(S, m, smoothing > 0 ? gtmpl_l2 : gtmpl, theta, sT_m, -1.0, nullptr, 0,
-                                              0.0);
+  (void)gbk::launch(lincomb_batched_kernel, nb((long)S * n), 256, 0, st, S, n, gmom, n, nullptr, 0, -1.0, xm, sT_n,
+                    -1.0, kp, sr, nullptr, nullptr, 0);
+  (void)gbk::launch(sum_subjects_kernel, nb(n), 256, 0, st, S, n, gcp, xp, sT_n, -1.0, greg, sr, -1.0);
+  (void)gbk::launch(sum_subjects_kernel, nb(m), 256, 0, st, S, m, smoothing > 0 ? gtmpl_l2 : gtmpl, theta, sT_m, -1.0,
+                    nullptr, 0, 0.0);
   c->launches += 3;
   if (L != launches.size()) return c->fail(GBK_ERR_STATE, "atlas: launch order mismatch");
   if ((rc = ok(cudaGetLastError(), "atlas gradients"))) return rc;

@@ -331,6 +331,7 @@ std::vector<int> gbk_ctx::family(int path, int op, int d, int dv) const {
 // where hi is not finite (so an infinite coordinate stays infinite, as when the kernel converts it).
 __global__ void pack_scaled_kernel(const double *x, long nxd, const double *y, long nyd, double s, float2 *xp,
                                    float2 *yp) {
+  pdl_entry();
   for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nxd + nyd; k += (long)gridDim.x * blockDim.x) {
     const double v = (k < nxd ? x[k] : y[k - nxd]) * s;
     const float hi = (float)v;
@@ -436,9 +437,10 @@ int gbk_ctx::launch(int op, int d, int dv, PairArgs a) {
     float2 *xp = (float2 *)packed.p;
     const long tot = nxd + nyd;
     const unsigned blocks = (unsigned)std::min<long>((tot + 255) / 256, 4L * num_sms);
-    pack_scaled_kernel<<<blocks, 256, 0, stream>>>(a.x, nxd, a.y, nyd, coord_scale<float>(a.sigma), xp,
-                                                   same ? xp : xp + nxd);
-    if (int rc = cuda(cudaGetLastError(), "coordinate packing")) return rc;
+    if (int rc = cuda(gbk::launch(pack_scaled_kernel, blocks, 256, 0, stream, a.x, nxd, a.y, nyd,
+                                  coord_scale<float>(a.sigma), xp, same ? xp : xp + nxd),
+                      "coordinate packing"))
+      return rc;
     launches += 1;
     a.xp = xp;
     a.yp = same ? xp : xp + nxd;

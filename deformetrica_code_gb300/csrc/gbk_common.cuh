@@ -12,8 +12,52 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
+
+#include <utility>
 
 namespace gbk {
+
+// ---------------------------------------------------------------------------------------------
+// Programmatic dependent launch. A kernel launched through launch() below may be placed on the
+// SMs while the previous kernel of its stream is still running, so its launch latency and CTA
+// placement overlap the predecessor's tail; this matters for the deformation loops' hundreds of
+// small dependent launches inside one CUDA graph. Every kernel of the library begins with
+// pdl_entry(): griddepcontrol.wait blocks until the predecessor grid has completed and its memory
+// is visible, so nothing is read or written earlier than in plain stream order, and then
+// griddepcontrol.launch_dependents lets the next kernel be placed. Launched without the attribute
+// (<<<>>>, or GBK_PDL=0 in the environment), both instructions do nothing.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Programmatic launches are on unless GBK_PDL=0 (read once per process).
+inline bool pdl_enabled() {
+  static const bool on = [] {
+    const char *e = getenv("GBK_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+// kern<<<grid, block, smem, st>>>(args...) with programmatic stream serialisation allowed.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                          Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // ---------------------------------------------------------------------------------------------
 // Index checks of a bounds-checked build (-DGBK_BOUNDS_CHECK=1; compiled out otherwise): an index

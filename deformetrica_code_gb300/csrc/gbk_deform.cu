@@ -34,6 +34,7 @@ namespace gbk {
 __global__ void lincomb_kernel(double *out, const double *base, double c1, const double *v1,
                                double c2, const double *v2, long n, const int *flag,
                                const double *flag_value) {
+  pdl_entry();
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (flag && *flag) {
@@ -48,6 +49,7 @@ __global__ void lincomb_kernel(double *out, const double *base, double c1, const
 
 __global__ void __launch_bounds__(1024) norm_flag_kernel(const double *p, long n, double thresh,
                                                          int *flag) {
+  pdl_entry();
   __shared__ double s[1024];
   double acc = 0.0;
   for (long i = threadIdx.x; i < n; i += blockDim.x) acc = fma(p[i], p[i], acc);
@@ -62,6 +64,7 @@ __global__ void __launch_bounds__(1024) norm_flag_kernel(const double *p, long n
 
 __global__ void __launch_bounds__(1024) dot_kernel(const double *a, const double *b, long n,
                                                    double *out, int accumulate) {
+  pdl_entry();
   __shared__ double s[1024];
   double acc = 0.0;
   for (long i = threadIdx.x; i < n; i += blockDim.x) acc = fma(a[i], b[i], acc);
@@ -76,6 +79,7 @@ __global__ void __launch_bounds__(1024) dot_kernel(const double *a, const double
 
 __global__ void scalar_combine_kernel(double *out, const double *a, double alpha, const double *b,
                                       double beta, const double *c, double gamma) {
+  pdl_entry();
   double r = 0.0;
   if (a) r += alpha * *a;
   if (b) r += beta * *b;
@@ -84,6 +88,7 @@ __global__ void scalar_combine_kernel(double *out, const double *a, double alpha
 }
 
 __global__ void zero_if_flag_kernel(double *p, long n, const int *flag) {
+  pdl_entry();
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && *flag) p[i] = 0.0;
 }
@@ -93,25 +98,21 @@ static unsigned blocks_for(long n, int bs = 256) { return (unsigned)std::max(1L,
 cudaError_t lincomb(cudaStream_t st, double *out, const double *base, double c1, const double *v1,
                     double c2, const double *v2, long n, const int *flag, const double *flag_value) {
   if (n <= 0) return cudaSuccess;
-  lincomb_kernel<<<blocks_for(n), 256, 0, st>>>(out, base, c1, v1, c2, v2, n, flag, flag_value);
-  return cudaGetLastError();
+  return launch(lincomb_kernel, blocks_for(n), 256, 0, st, out, base, c1, v1, c2, v2, n, flag, flag_value);
 }
 
 cudaError_t small_norm_flag(cudaStream_t st, const double *p, long n, double thresh, int *flag) {
-  norm_flag_kernel<<<1, 1024, 0, st>>>(p, n, thresh, flag);
-  return cudaGetLastError();
+  return launch(norm_flag_kernel, 1, 1024, 0, st, p, n, thresh, flag);
 }
 
 cudaError_t dot_f64(cudaStream_t st, const double *a, const double *b, long n, double *out,
                     int accumulate) {
-  dot_kernel<<<1, 1024, 0, st>>>(a, b, n, out, accumulate);
-  return cudaGetLastError();
+  return launch(dot_kernel, 1, 1024, 0, st, a, b, n, out, accumulate);
 }
 
 cudaError_t scalar_combine(cudaStream_t st, double *out, const double *a, double alpha,
                            const double *b, double beta, const double *c, double gamma) {
-  scalar_combine_kernel<<<1, 1, 0, st>>>(out, a, alpha, b, beta, c, gamma);
-  return cudaGetLastError();
+  return launch(scalar_combine_kernel, 1, 1, 0, st, out, a, alpha, b, beta, c, gamma);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -154,9 +155,9 @@ int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *m
     if ((rc = c->launch(OP_CONV_GRADA, d, d, a))) return rc;
   }
   // nearly zero momenta: the reference leaves mom[t >= 1] at their initial zeros (:601-613)
-  zero_if_flag_kernel<<<blocks_for((T - 1) * n), 256, 0, st>>>(mom + n, (T - 1) * n, s.flag);
   c->launches += 1;
-  return c->cuda(cudaGetLastError(), "zero_if_flag_kernel");
+  return c->cuda(launch(zero_if_flag_kernel, blocks_for((T - 1) * n), 256, 0, st, mom + n, (T - 1) * n, s.flag),
+                 "zero_if_flag_kernel");
 }
 
 int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,

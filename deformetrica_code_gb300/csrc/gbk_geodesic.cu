@@ -35,6 +35,7 @@ namespace {
 // L_data = sum over (observation, object) in order of -(0.5 match) / sigma2, and the sum of matches
 __global__ void regression_data_kernel(const double *match, const double *sigma2, int n, double *l_data,
                                        double *match_sum) {
+  pdl_entry();
   double acc = 0.0, m = 0.0;
   for (int k = 0; k < n; ++k) {
     acc -= 0.5 * match[k] / sigma2[k];
@@ -88,8 +89,10 @@ struct gbk_geodesic_regression {
                                    gobs + (long)o * m + ob.off * d, 0.5 / ob.sigma2, 0)))
           return rc;
       }
-    regression_data_kernel<<<1, 1, 0, st>>>(out + 8, sigma2, nobs * nobj, out + 1, out + 3);
-    if ((rc = c->cuda(cudaGetLastError(), "data terms"))) return rc;
+    if ((rc = c->cuda(gbk::launch(regression_data_kernel, 1, 1, 0, st, out + 8, sigma2, nobs * nobj, out + 1,
+                                  out + 3),
+                      "data terms")))
+      return rc;
     PairArgs a = pair_args(ncp, ncp, sigma_def);
     a.x = cp;
     a.y = cp;

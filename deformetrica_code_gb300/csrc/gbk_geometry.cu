@@ -41,6 +41,7 @@ static unsigned nblk(long n, int bs = 256) { return (unsigned)std::max(1L, (n + 
 template <int D, int CELL>
 __global__ void cell_kernel(const double *pts, const int *cells, long nf, int kind, double *c, double *n,
                             double *mn, double *w) {
+  pdl_entry();
   constexpr int NM = D * (D + 1) / 2;
   long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
@@ -110,6 +111,7 @@ __device__ inline void sym_mul(const double *m, const double *x, double *y) {
 template <int D, int CELL>
 __global__ void cell_grad_kernel(long nf, int kind, const double *n, const double *mn, const double *kts,
                                  const double *ktt, const double *gs, const double *gt, double *kt, double *gk) {
+  pdl_entry();
   constexpr int NM = D * (D + 1) / 2;
   long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
@@ -152,6 +154,7 @@ template <int D, int CELL>
 __global__ void vertex_gather_kernel(long nv, const double *pts, const int *cells, const int *ptr, const int *fc,
                                      const double *kt, const double *gk, double *grad, double scale,
                                      int accumulate) {
+  pdl_entry();
   long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   double g[D];
@@ -185,6 +188,7 @@ __global__ void vertex_gather_kernel(long nv, const double *pts, const int *cell
 // the determinant's sign into sg when it is given.
 template <int D, int CELL>
 __global__ void measure_kernel(const double *pts, const int *cells, long nf, double *c, double *w, double *sg) {
+  pdl_entry();
   long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   if constexpr (CELL == 1) {
@@ -225,6 +229,7 @@ __global__ void measure_kernel(const double *pts, const int *cells, long nf, dou
 template <int D, int CELL>
 __global__ void measure_grad_kernel(long nf, int exact, const double *kts, const double *ktt, const double *gs,
                                     const double *gt, const double *sg, double *kt, double *gk) {
+  pdl_entry();
   long f = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   if constexpr (CELL == 1) {
@@ -272,6 +277,7 @@ template <int D, int CELL>
 __global__ void measure_gather_kernel(long nv, const double *pts, const int *cells, const int *ptr, const int *fc,
                                       const double *kt, const double *gk, double *grad, double scale,
                                       int accumulate) {
+  pdl_entry();
   long v = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   double g[D];
@@ -298,39 +304,41 @@ __global__ void measure_gather_kernel(long nv, const double *pts, const int *cel
 }
 
 __global__ void fill_kernel(double *p, long n, double v) {
+  pdl_entry();
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
 }
 
 static cudaError_t fill_ones(cudaStream_t st, double *p, long n) {
-  fill_kernel<<<nblk(n), 256, 0, st>>>(p, n, 1.0);
-  return cudaGetLastError();
+  return launch(fill_kernel, nblk(n), 256, 0, st, p, n, 1.0);
 }
 
-// launches one of the measure kernels for the term's (d, cell)
+// launches one of the measure kernels for the term's (d, cell); a launch error is left for
+// cudaGetLastError
 #define GBK_MEASURE_DISPATCH(T, KERNEL, GRID, ST, ...)                     \
   do {                                                                     \
     if ((T).cell == 1) {                                                   \
       if ((T).d == 2)                                                      \
-        KERNEL<2, 1><<<(GRID), 256, 0, (ST)>>>(__VA_ARGS__);               \
+        (void)launch(KERNEL<2, 1>, (GRID), 256, 0, (ST), __VA_ARGS__);     \
       else                                                                 \
-        KERNEL<3, 1><<<(GRID), 256, 0, (ST)>>>(__VA_ARGS__);               \
+        (void)launch(KERNEL<3, 1>, (GRID), 256, 0, (ST), __VA_ARGS__);     \
     } else if ((T).d == 2) {                                               \
-      KERNEL<2, 3><<<(GRID), 256, 0, (ST)>>>(__VA_ARGS__);                 \
+      (void)launch(KERNEL<2, 3>, (GRID), 256, 0, (ST), __VA_ARGS__);       \
     } else {                                                               \
-      KERNEL<3, 4><<<(GRID), 256, 0, (ST)>>>(__VA_ARGS__);                 \
+      (void)launch(KERNEL<3, 4>, (GRID), 256, 0, (ST), __VA_ARGS__);       \
     }                                                                      \
   } while (0)
 
-// launches one of the cell kernels for the term's (d, cell)
+// launches one of the cell kernels for the term's (d, cell); a launch error is left for
+// cudaGetLastError
 #define GBK_CELL_DISPATCH(T, KERNEL, GRID, ST, ...)                       \
   do {                                                                     \
     if ((T).cell == 3)                                                     \
-      KERNEL<3, 3><<<(GRID), 256, 0, (ST)>>>(__VA_ARGS__);                 \
+      (void)launch(KERNEL<3, 3>, (GRID), 256, 0, (ST), __VA_ARGS__);       \
     else if ((T).d == 2)                                                   \
-      KERNEL<2, 2><<<(GRID), 256, 0, (ST)>>>(__VA_ARGS__);                 \
+      (void)launch(KERNEL<2, 2>, (GRID), 256, 0, (ST), __VA_ARGS__);       \
     else                                                                   \
-      KERNEL<3, 2><<<(GRID), 256, 0, (ST)>>>(__VA_ARGS__);                 \
+      (void)launch(KERNEL<3, 2>, (GRID), 256, 0, (ST), __VA_ARGS__);       \
   } while (0)
 
 // ---------------------------------------------------------------------------------------------

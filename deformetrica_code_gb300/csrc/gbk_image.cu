@@ -58,6 +58,7 @@ unsigned blocks_for(long n, int bs = kThreads) { return (unsigned)std::max(1L, (
 template <int D>
 __global__ void image_windows_kernel(const double *y, long n, long per, double sigma, ImageGeom g, int *start,
                                      int *bad) {
+  pdl_entry();
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   bool ok = g.L > 0;
@@ -102,6 +103,7 @@ struct ImageArgs {
 // FP32 sums (TwoSum), added up in FP64 at the end (the gradients' -2 / (sigma^2 pre) applied there).
 template <int D, int DV, int KIND, bool F32>
 __global__ void __launch_bounds__(kThreads) image_fast_kernel(const ImageArgs a, const ImageGeom g) {
+  pdl_entry();
   typedef Tile<D> T;
   constexpr int NW = KIND == IMG_CONV ? D : DV;      // weight columns staged per control point
   constexpr int NA = KIND == IMG_CONV ? D : DV * D;  // accumulators per pixel
@@ -222,6 +224,7 @@ __global__ void __launch_bounds__(kThreads) image_fast_kernel(const ImageArgs a,
 
 template <int D>
 __global__ void image_points_kernel(ImageGeom g, double *out) {
+  pdl_entry();
   const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= g.pixels()) return;
   long rem = r;
@@ -234,6 +237,7 @@ __global__ void image_points_kernel(ImageGeom g, double *out) {
 
 // out = base - dt a (Euler), or base - (a + b) h (Heun), rounded as written
 __global__ void back_step_kernel(double *out, const double *base, const double *a, const double *b, double f, long n) {
+  pdl_entry();
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double s = b ? __dadd_rn(a[i], b[i]) : a[i];
@@ -243,6 +247,7 @@ __global__ void back_step_kernel(double *out, const double *base, const double *
 // flag = 1 when a column of the n x D rows leaves [bbox[k][0], bbox[k][1]] (one CTA)
 template <int D>
 __global__ void out_of_box_kernel(const double *p, long n, const double *bbox, int *flag) {
+  pdl_entry();
   __shared__ int s_out;
   if (threadIdx.x == 0) s_out = 0;
   __syncthreads();

@@ -107,6 +107,7 @@ __device__ void block_minmax(double *lo, double *hi) {
 template <int D>
 __global__ void __launch_bounds__(kThreads) box_kernel(const double *x, long n, double *part, double *box,
                                                        unsigned *ticket) {
+  pdl_entry();
   __shared__ bool last;
   double lo[D], hi[D];
 #pragma unroll
@@ -161,6 +162,7 @@ __global__ void __launch_bounds__(kThreads) box_kernel(const double *x, long n, 
 template <int D>
 __global__ void __launch_bounds__(kThreads) union_box_kernel(const double *x, long nx, const double *y, long ny,
                                                              double *part, double *box, unsigned *ticket) {
+  pdl_entry();
   __shared__ bool last;
   double lo[D], hi[D];
 #pragma unroll
@@ -216,6 +218,7 @@ __global__ void __launch_bounds__(kThreads) union_box_kernel(const double *x, lo
 template <int D>
 __global__ void __launch_bounds__(kThreads) keys_kernel(const double *x, long n, const double *box, int shift,
                                                         unsigned *keys, int *rows) {
+  pdl_entry();
   const long i = blockIdx.x * (long)kThreads + threadIdx.x;
   if (i >= n) return;
   double ext = 0.0;
@@ -274,6 +277,7 @@ __device__ bool tile_at(const unsigned *keys, long n, long p, int shift, int til
 template <int D>
 __global__ void __launch_bounds__(kThreads) tiles_kernel(const unsigned *keys, long n, int key_bits, const double *box,
                                                          double cell_scale, int tile, int2 *tiles, int *ntiles) {
+  pdl_entry();
   const long p = blockIdx.x * (long)kThreads + threadIdx.x;
   if (p >= n) return;
   const int shift = key_bits - D * cell_level<D>(box, cell_scale);  // 0 < shift <= key_bits
@@ -296,6 +300,7 @@ struct SmallSort {
 template <int ITEMS>
 __global__ void __launch_bounds__(kSmallThreads, 1)
     small_sort_kernel(const unsigned *cell_keys, int n, unsigned *sorted_keys, int *perm) {
+  pdl_entry();
   typedef typename SmallSort<ITEMS>::Sort Sort;
   extern __shared__ __align__(16) unsigned char small_smem[];
   const int t = threadIdx.x;
@@ -322,6 +327,7 @@ __global__ void __launch_bounds__(kSmallThreads, 1)
 template <int D>
 __global__ void source_pack_kernel(const double *y, const int *perm, long n, int chunk, double *boxes,
                                    SourceCopies sc) {
+  pdl_entry();
   __shared__ double s[2 * D][kThreads / 32];
   const long c = blockIdx.x;
   double lo[D], hi[D];
@@ -462,6 +468,7 @@ int sort_into(gbk_ctx *c, gbk_ctx::SortSlot &s, const double *x, long n, SortedS
 __global__ void __launch_bounds__(kThreads) nonfinite_kernel(int d, const double *x, long n, const double *a, int lda,
                                                              const double *b, int ldb, const double *e, int lde,
                                                              unsigned *flag) {
+  pdl_entry();
   bool bad = false;
   for (long i = blockIdx.x * (long)kThreads + threadIdx.x; i < n; i += (long)gridDim.x * kThreads) {
     for (int k = 0; k < d; ++k) bad = bad || !isfinite(x[i * d + k]);
@@ -477,6 +484,7 @@ __global__ void __launch_bounds__(kThreads) nonfinite_kernel(int d, const double
 
 // boxes: lo[d], hi[d] per chunk -> (-inf, +inf) when *flag
 __global__ void unbound_boxes_kernel(const unsigned *flag, double *boxes, long nvals, int d) {
+  pdl_entry();
   if (!*flag) return;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nvals; i += (long)gridDim.x * blockDim.x)
     boxes[i] = (i % (2 * d)) < d ? -INFINITY : INFINITY;

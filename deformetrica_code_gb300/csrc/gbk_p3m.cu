@@ -95,6 +95,7 @@ inline int p3m_kernels(int d) { return 1 + d + d * (d + 1) / 2; }
 // Kernel images in inverse-FFT-shifted layout: slot j holds the value at grid index (j + n/2) mod n.
 template <int D, typename G>
 __global__ void p3m_kernel_images(P3MGrid g, double sigma, G *img, long cells) {
+  gbk::pdl_entry();
   long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= cells) return;
   long slot[3], ind[3];
@@ -182,6 +183,7 @@ __device__ inline void p3m_corners(const double *p, const P3MGrid &g, P3MCorners
 // with one atomic per weight. Padded slots receive zeros.
 template <int D, typename G>
 __global__ void p3m_splat(const double *y, const double *wts, long ny, int dv, int dvp, P3MGrid g, G *grids) {
+  gbk::pdl_entry();
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ny) return;
   P3MCorners<D, G> cs;
@@ -218,6 +220,7 @@ __global__ void p3m_splat(const double *y, const double *wts, long ny, int dv, i
 template <typename C, typename G>
 __global__ void p3m_multiply(const C *spec, const C *kspec, int nimg, int per_grid, int kernel0, long ccells, G scale,
                              C *out) {
+  gbk::pdl_entry();
   long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= ccells) return;
   for (int m = 0; m < nimg; ++m) {
@@ -236,6 +239,7 @@ __global__ void p3m_multiply(const C *spec, const C *kspec, int nimg, int per_gr
 // grids, so the transforms and the interpolation's images stay contiguous).
 template <typename G>
 __global__ void p3m_deinterleave(const G *in, long cells, int dv, int dvp, G *out) {
+  gbk::pdl_entry();
   const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= cells) return;
   for (int k = 0; k < dv; ++k) out[(long)k * cells + j] = in[j * dvp + k];
@@ -247,6 +251,7 @@ __global__ void p3m_deinterleave(const G *in, long cells, int dv, int dvp, G *ou
 template <int D, typename G>
 __global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, long cells, P3MGrid g, int mode,
                            const double *alpha, int dv, double *out) {
+  gbk::pdl_entry();
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nx) return;
   P3MCorners<D, G> cs;
@@ -296,6 +301,7 @@ __global__ void p3m_interp(const double *x, long nx, const G *imgs, int nimg, lo
 // bounding box of x and y: one CTA, FP64
 template <int D>
 __global__ void p3m_box(const double *x, long nx, const double *y, long ny, double *box) {
+  gbk::pdl_entry();
   __shared__ double s_lo[D][256], s_hi[D][256];
   double lo[D], hi[D];
   for (int k = 0; k < D; ++k) {

@@ -1162,6 +1162,7 @@ __device__ __forceinline__ void pair_block(const PairArgs &a, const long tile_id
 // built (their count is known on the device only; the grid is sized for the usual count).
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
+  pdl_entry();
   const long nt = a.xtiles ? (long)*a.nxtiles : (long)gridDim.x;
   if constexpr (std::is_same<T, f32b>::value) {
     if ((long)blockIdx.x >= nt) return;  // no tile for this CTA (whole CTA)
@@ -1183,6 +1184,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel(const PairArgs a) {
 // every field of args, including j_chunk, nsplit, partial and xscale (coord_scale of the lane type).
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
 __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel_batched(const PairArgs *args, const int4 *items) {
+  pdl_entry();
   const int4 it = items[blockIdx.x];
   const PairArgs a = args[it.x];
   if constexpr (std::is_same<T, f32b>::value) bulk_init();
@@ -1192,6 +1194,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) pair_kernel_batched(const PairArg
 // Sums the per-split FP64 partials in split order and applies the op's store.
 template <class Op>
 __global__ void split_reduce_kernel(const PairArgs a) {
+  pdl_entry();
   constexpr int NO = Op::NO;
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nx) return;
@@ -1215,6 +1218,7 @@ struct LaunchCfg {
 // Batched split reduction: thread over (problem, target) items ritems[b] = (problem, first target).
 template <class Op>
 __global__ void split_reduce_batched_kernel(const PairArgs *args, const int2 *ritems) {
+  pdl_entry();
   constexpr int NO = Op::NO;
   const int2 it = ritems[blockIdx.x];
   const PairArgs &a = args[it.x];
@@ -1241,11 +1245,9 @@ cudaError_t launch_pairs_batched(const PairArgs *args, const int4 *items, int ni
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  kern<<<(unsigned)nitems, BLOCK, smem, st>>>(args, items);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch(kern, (unsigned)nitems, BLOCK, smem, st, args, items);
   if (e != cudaSuccess || nritems <= 0) return e;
-  split_reduce_batched_kernel<Op><<<(unsigned)nritems, 256, 0, st>>>(args, ritems);
-  return cudaGetLastError();
+  return launch(split_reduce_batched_kernel<Op>, (unsigned)nritems, 256, 0, st, args, ritems);
 }
 
 template <class Op, typename T, int D, int BLOCK, int R, int TJ, int MERGE, int MINB, int UNR, int CSM>
@@ -1274,11 +1276,9 @@ cudaError_t launch_pairs(PairArgs a, int nsplit, cudaStream_t st) {
   a.prune_d2 = prune_dist2<T>(a.sigma);
   const long tiles = a.xtiles ? a.xtile_bound : (a.nx + (long)BLOCK * R - 1) / ((long)BLOCK * R);
   dim3 grid((unsigned)tiles, (unsigned)nsplit);
-  kern<<<grid, BLOCK, smem, st>>>(a);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch(kern, grid, BLOCK, smem, st, a);
   if (e != cudaSuccess || nsplit == 1 || a.tickets) return e;
-  split_reduce_kernel<Op><<<(unsigned)((a.nx + 255) / 256), 256, 0, st>>>(a);
-  return cudaGetLastError();
+  return launch(split_reduce_kernel<Op>, (unsigned)((a.nx + 255) / 256), 256, 0, st, a);
 }
 
 }  // namespace gbk

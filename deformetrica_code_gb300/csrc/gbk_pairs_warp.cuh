@@ -161,6 +161,7 @@ __device__ __forceinline__ void warp_body(const PairArgs &a, const long i0, cons
 
 template <class Op, typename T, int D, int KS, int R, int MERGE, int UNR, int MINB>
 __global__ void __launch_bounds__(32 * KS, MINB) pair_kernel_warp(const PairArgs a) {
+  pdl_entry();
   typedef WarpShape<Op, T, D, KS, R, MERGE, UNR> S;
   constexpr int NO = Op::NO;
   constexpr int TILE = S::TILE;
@@ -293,8 +294,7 @@ cudaError_t launch_pairs_warp(PairArgs a, int nsplit, cudaStream_t st) {
   a.j_chunk = per;
   a.nsplit = nsplit;
   const long tiles = (a.nx + S::TILE - 1) / S::TILE;
-  kern<<<dim3((unsigned)tiles, (unsigned)nsplit), 32 * KS, S::kSmem, st>>>(a);
-  return cudaGetLastError();
+  return launch(kern, dim3((unsigned)tiles, (unsigned)nsplit), 32 * KS, S::kSmem, st, a);
 }
 
 // Records one compiled warp-split kernel in the host table (see set_entry in gbk_dispatch.h): KS warps

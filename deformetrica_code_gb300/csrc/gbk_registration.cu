@@ -39,6 +39,7 @@ namespace {
 // the sum of the matches
 __global__ void data_terms_kernel(const double *match, const double *sigma2, int n, double *l_data,
                                   double *match_sum) {
+  pdl_entry();
   double acc = 0.0, m = 0.0;
   for (int k = 0; k < n; ++k) {
     acc -= match[k] / sigma2[k];
@@ -68,8 +69,10 @@ int gbk_registration::body() {
     RegObject &o = objs[k];
     if ((rc = o.surf.evaluate(c, xT + o.off * d, out + 8 + k, thetaT + o.off * d, 0.5 / o.sigma2, 0))) return rc;
   }
-  data_terms_kernel<<<1, 1, 0, c->stream>>>(out + 8, sigma2_dev, (int)objs.size(), out + 1, out + 3);
-  if ((rc = c->cuda(cudaGetLastError(), "data terms"))) return rc;
+  if ((rc = c->cuda(gbk::launch(data_terms_kernel, 1, 1, 0, c->stream, out + 8, sigma2_dev, (int)objs.size(),
+                                out + 1, out + 3),
+                    "data terms")))
+    return rc;
   // regularity: K p and ConvolveGradient(cp, p) in one fused pass, <K p, p> in FP64
   PairArgs a = pair_args(ncp, ncp, sigma_def);
   a.x = cp;

@@ -19,6 +19,7 @@ namespace gbk {
 // sum_i a_i * b_i over n doubles in FP64, one CTA, fixed order: bitwise reproducible.
 __global__ void __launch_bounds__(1024) dot_f64_kernel(const double *a, const double *b, long n,
                                                        double *out, int accumulate) {
+  pdl_entry();
   __shared__ double s[1024];
   double acc = 0.0;
   for (long i = threadIdx.x; i < n; i += blockDim.x) acc = fma(a[i], b[i], acc);
@@ -38,6 +39,7 @@ __global__ void __launch_bounds__(1024) dot_f64_kernel(const double *a, const do
 
 // Synthetic inputs for tuning: uniform [0,1) coordinates / uniform [-1,1) weights (hash based).
 __global__ void fill_uniform_kernel(double *p, long n, unsigned seed, double lo, double hi) {
+  pdl_entry();
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   unsigned long long z = (unsigned long long)i * 0x9E3779B97F4A7C15ull + seed * 0xD1B54A32D192ED03ull;

@@ -119,7 +119,8 @@ cudaError_t scalar_combine(cudaStream_t st, double *out, const double *a, double
 // loop bodies (device pointers only; shared with the registration object)
 // ---------------------------------------------------------------------------------------------
 int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *mom0, int T,
-                 double sigma, double *pos, double *mom, const DeformScratch &s, double span) {
+                 double sigma, double *pos, double *mom, const DeformScratch &s, double span,
+                 const cudaEvent_t *step_done, bool zero_tail) {
   const long n = ncp * d;
   const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
@@ -153,24 +154,33 @@ int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *m
     a.step1 = -dt;
     a.flag = s.flag;
     if ((rc = c->launch(OP_CONV_GRADA, d, d, a))) return rc;
+    if (step_done && (rc = c->cuda(cudaEventRecord(step_done[t], st), "event record"))) return rc;
   }
-  // nearly zero momenta: the reference leaves mom[t >= 1] at their initial zeros (:601-613)
+  return zero_tail ? zero_tail_device(c, d, ncp, T, mom, s) : GBK_OK;
+}
+
+// nearly zero momenta: the reference leaves mom[t >= 1] at their initial zeros (Diffeos.cxx:601-613)
+int zero_tail_device(gbk_ctx *c, int d, long ncp, int T, double *mom, const DeformScratch &s) {
+  const long n = ncp * d;
   c->launches += 1;
-  return c->cuda(launch(zero_if_flag_kernel, blocks_for((T - 1) * n), 256, 0, st, mom + n, (T - 1) * n, s.flag),
+  return c->cuda(launch(zero_if_flag_kernel, blocks_for((T - 1) * n), 256, 0, c->stream, mom + n, (T - 1) * n,
+                        s.flag),
                  "zero_if_flag_kernel");
 }
 
 int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                 double sigma, long nlm, const double *lm0, int heun, double *lm,
-                const DeformScratch &s, double span) {
+                const DeformScratch &s, double span, const cudaEvent_t *wait_step) {
   const long n = ncp * d, m = nlm * d;
   const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
   int rc;
+  if (wait_step && (rc = c->cuda(cudaStreamWaitEvent(st, wait_step[0], 0), "event wait"))) return rc;
   if ((rc = c->cuda(cudaMemcpyAsync(lm, lm0, m * sizeof(double), cudaMemcpyDeviceToDevice, st), "copy"))) return rc;
   if ((rc = c->cuda(small_norm_flag(st, mom, n, 1e-20, s.flag), "norm flag"))) return rc;
   c->launches += 1;
   for (int t = 0; t + 1 < T; ++t) {
+    if (wait_step && t > 0 && (rc = c->cuda(cudaStreamWaitEvent(st, wait_step[t], 0), "event wait"))) return rc;
     const double *lt = lm + t * m;
     double *lt1 = lm + (t + 1) * m;
     PairArgs a = pair_args(nlm, ncp, sigma);
@@ -205,7 +215,8 @@ int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mo
 int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
                              int T, double sigma, long nlm, const double *lm,
                              const double *theta_final, int heun, double *theta,
-                             const DeformScratch &s, double span, const AdjointJumps *jumps) {
+                             const DeformScratch &s, double span, const AdjointJumps *jumps,
+                             const cudaEvent_t *step_done) {
   const long n = ncp * d, m = nlm * d;
   const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
@@ -287,6 +298,7 @@ int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, con
         if ((rc = c->cuda(lincomb(st, th1, th1, 1.0, jumps->grads[k], 0.0, nullptr, m), "jump"))) return rc;
         c->launches += 1;
       }
+    if (step_done && (rc = c->cuda(cudaEventRecord(step_done[t], st), "event record"))) return rc;
   }
   return GBK_OK;
 }
@@ -331,14 +343,17 @@ int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const doubl
 
 int adjoint_diffeo_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                           double sigma, long nlm, const double *lm, const double *theta, int heun,
-                          double *xp, double *xm, const DeformScratch &s, double span) {
+                          double *xp, double *xm, const DeformScratch &s, double span,
+                          const cudaEvent_t *wait_step) {
   const long n = ncp * d, m = nlm * d;
   const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
   int rc;
+  if (wait_step && (rc = c->cuda(cudaStreamWaitEvent(st, wait_step[T - 1], 0), "event wait"))) return rc;
   if ((rc = c->cuda(cudaMemsetAsync(xp + (T - 1) * n, 0, n * sizeof(double), st), "memset"))) return rc;
   if ((rc = c->cuda(cudaMemsetAsync(xm + (T - 1) * n, 0, n * sizeof(double), st), "memset"))) return rc;
   for (int t = T - 1; t > 0; --t) {
+    if (wait_step && t < T - 1 && (rc = c->cuda(cudaStreamWaitEvent(st, wait_step[t], 0), "event wait"))) return rc;
     if ((rc = update_at_device(c, d, ncp, pos + t * n, mom + t * n, xp + t * n, xm + t * n, nlm,
                                nlm ? lm + t * m : nullptr, nlm ? theta + t * m : nullptr, sigma, s.va, s.vb)))
       return rc;

@@ -25,21 +25,34 @@ struct AdjointJumps {
 };
 
 // span = tn - t0: the time points are t0 + span k / (T - 1) (Diffeos::SetT0 / SetTN).
+//
+// Two loops may run on two streams one step apart (the registration's pipelined iteration): the
+// producer records step_done[k] on its stream after step k, the consumer's stream waits on
+// wait_step[k] before its step k (and on wait_step of its first step before anything else). Steps are
+// indexed by their t: shooting and flow t = 0 .. T-2 (the flow's step t reads the shooting's
+// positions and momenta at t and t + 1), the adjoints t = T-1 .. 1 (the parameter adjoint's step t
+// reads theta at t and t - 1, which the landmark adjoint's step t writes).
+// zero_tail = false leaves the zeroing of mom[t >= 1] for nearly zero momenta to the caller (after
+// a flow that reads mom has finished; its results do not depend on them then).
 int shoot_device(gbk_ctx *c, int d, long ncp, const double *cp0, const double *mom0, int T,
-                 double sigma, double *pos, double *mom, const DeformScratch &s, double span = 1.0);
+                 double sigma, double *pos, double *mom, const DeformScratch &s, double span = 1.0,
+                 const cudaEvent_t *step_done = nullptr, bool zero_tail = true);
+int zero_tail_device(gbk_ctx *c, int d, long ncp, int T, double *mom, const DeformScratch &s);
 int flow_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                 double sigma, long nlm, const double *lm0, int heun, double *lm,
-                const DeformScratch &s, double span = 1.0);
+                const DeformScratch &s, double span = 1.0, const cudaEvent_t *wait_step = nullptr);
 // theta_final: the final condition without jumps (ignored when jumps has observations)
 int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
                              int T, double sigma, long nlm, const double *lm,
                              const double *theta_final, int heun, double *theta,
-                             const DeformScratch &s, double span = 1.0, const AdjointJumps *jumps = nullptr);
+                             const DeformScratch &s, double span = 1.0, const AdjointJumps *jumps = nullptr,
+                             const cudaEvent_t *step_done = nullptr);
 int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
                      const double *xp, const double *xm, long nlm, const double *lm,
                      const double *theta, double sigma, double *dpos, double *dmom);
 int adjoint_diffeo_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                           double sigma, long nlm, const double *lm, const double *theta, int heun,
-                          double *xp, double *xm, const DeformScratch &s, double span = 1.0);
+                          double *xp, double *xm, const DeformScratch &s, double span = 1.0,
+                          const cudaEvent_t *wait_step = nullptr);
 
 }  // namespace gbk

@@ -35,6 +35,12 @@ using namespace gbk;
 
 namespace {
 
+// Single-subject registrations run their iteration pipelined on two streams unless GBK_PIPELINE=0.
+int pipeline_default() {
+  const char *e = getenv("GBK_PIPELINE");
+  return e && e[0] == '0' ? 0 : 1;
+}
+
 // L_data = 0.5 * (-sum_k match_k / sigma2_k) in object order (DeterministicAtlas.cxx:121-125) and
 // the sum of the matches
 __global__ void data_terms_kernel(const double *match, const double *sigma2, int n, double *l_data,
@@ -58,22 +64,67 @@ int gbk_registration::alloc(void **p, size_t bytes) {
   return GBK_OK;
 }
 
+// Helper context, second scratch set and events of the pipelined iteration (once per registration).
+int gbk_registration::enable_pipeline() {
+  if (c2) return GBK_OK;
+  gbk_ctx *h = nullptr;
+  if (gbk_create(c->device, &h) != GBK_OK)
+    return c->fail(GBK_ERR_CUDA, "pipelined registration: helper context: %s", gbk_last_error(nullptr));
+  c2 = h;
+  // the helper's kernel sums count into this context's pair counters and report into its status word;
+  // its own words stay allocated (its spatial order would use them) and are restored on release
+  c2_words = h->pair_counter;
+  h->pair_counter = c->pair_counter;
+  h->status = c->status;
+  const long rows = std::max(ncp, nv);
+  int rc = GBK_OK;
+  double **bufs[] = {&s2.va, &s2.vb, &s2.vc, &s2.vd};
+  for (double **b : bufs)
+    if (!rc) rc = alloc((void **)b, (size_t)rows * d * sizeof(double));
+  if (!rc) rc = alloc((void **)&s2.flag, 16);
+  ev.assign((size_t)(2 * T + 1), nullptr);
+  for (cudaEvent_t &e : ev)
+    if (!rc) rc = c->cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+  if (rc) {  // no helper: the iteration stays serial
+    c2->pair_counter = c2_words;
+    c2->status = reinterpret_cast<unsigned *>(c2_words + 3);
+    gbk_destroy(c2);
+    c2 = nullptr;
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    ev.clear();
+    pipeline = 0;
+  }
+  return rc;
+}
+
 int gbk_registration::body() {
   const long n = ncp * d;
   int rc;
-  if ((rc = shoot_device(c, d, ncp, cp, mom, T, sigma_def, pos, momt, s))) return rc;
-  if ((rc = flow_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm0, heun, lm, s))) return rc;
-  // data terms on the deformed template objects; thetaT = d match_k / d x_T / (2 sigma2_k)
-  const double *xT = lm + (long)(T - 1) * nv * d;
-  for (size_t k = 0; k < objs.size(); ++k) {
-    RegObject &o = objs[k];
-    if ((rc = o.surf.evaluate(c, xT + o.off * d, out + 8 + k, thetaT + o.off * d, 0.5 / o.sigma2, 0))) return rc;
+  // Pipelined: the flow and the control-point adjoint run on the helper's stream, one step behind
+  // the shooting and the landmark adjoint (their inputs at t and t + 1, resp. t and t - 1, are then
+  // written). Serial otherwise: one stream, same launches, same results bit for bit (every launch's
+  // inputs and reduction order are the same either way).
+  const bool two = c2 != nullptr;
+  gbk_ctx *cb = two ? c2 : c;
+  const DeformScratch &sb = two ? s2 : s;
+  const cudaEvent_t *ev_shoot = two ? ev.data() : nullptr, *ev_adj = two ? ev.data() + (T - 1) : nullptr;
+  const cudaEvent_t ev_join0 = two ? ev[2 * T - 1] : nullptr, ev_join1 = two ? ev[2 * T] : nullptr;
+  if (two) {  // the helper launches as this context would
+    c2->mode = c->mode;
+    c2->order = c->order;
+    c2->force_split = c->force_split;
+    c2->staging = c->staging;
+    c2->tune = c->tune;
+    c2->err.clear();
   }
-  if ((rc = c->cuda(gbk::launch(data_terms_kernel, 1, 1, 0, c->stream, out + 8, sigma2_dev, (int)objs.size(),
-                                out + 1, out + 3),
-                    "data terms")))
-    return rc;
-  // regularity: K p and ConvolveGradient(cp, p) in one fused pass, <K p, p> in FP64
+  auto helper = [&](int r) {  // a failure of the helper chain, reported in this context
+    if (r && two) c->err = c2->err;
+    return r;
+  };
+  if ((rc = shoot_device(c, d, ncp, cp, mom, T, sigma_def, pos, momt, s, 1.0, ev_shoot, !two))) return rc;
+  // regularity (reads cp and the initial momenta only: overlaps the flow): K p and
+  // ConvolveGradient(cp, p) in one fused pass, <K p, p> in FP64; out = [L, L_data, L_reg, match, <Kp,p>]
   PairArgs a = pair_args(ncp, ncp, sigma_def);
   a.x = cp;
   a.y = cp;
@@ -87,12 +138,39 @@ int gbk_registration::body() {
   a.out1_ld = d;
   if ((rc = c->launch(OP_CONV_GRADA, d, d, a))) return rc;
   if ((rc = c->cuda(dot_f64(c->stream, kp, mom, n, out + 4, 0), "dot"))) return rc;
-  // out = [L, L_data, L_reg, match, <Kp,p>]
   if ((rc = c->cuda(scalar_combine(c->stream, out + 2, out + 4, -0.5, nullptr, 0, nullptr, 0), "L"))) return rc;
+  c->launches += 2;
+  if ((rc = helper(flow_device(cb, d, ncp, pos, momt, T, sigma_def, nv, lm0, heun, lm, sb, 1.0, ev_shoot))))
+    return rc;
+  if (two) {
+    if ((rc = c->cuda(cudaEventRecord(ev_join0, c2->stream), "event record"))) return rc;
+    if ((rc = c->cuda(cudaStreamWaitEvent(c->stream, ev_join0, 0), "event wait"))) return rc;
+    if ((rc = zero_tail_device(c, d, ncp, T, momt, s))) return rc;
+  }
+  // data terms on the deformed template objects; thetaT = d match_k / d x_T / (2 sigma2_k)
+  const double *xT = lm + (long)(T - 1) * nv * d;
+  for (size_t k = 0; k < objs.size(); ++k) {
+    RegObject &o = objs[k];
+    if ((rc = o.surf.evaluate(c, xT + o.off * d, out + 8 + k, thetaT + o.off * d, 0.5 / o.sigma2, 0))) return rc;
+  }
+  if ((rc = c->cuda(gbk::launch(data_terms_kernel, 1, 1, 0, c->stream, out + 8, sigma2_dev, (int)objs.size(),
+                                out + 1, out + 3),
+                    "data terms")))
+    return rc;
   if ((rc = c->cuda(scalar_combine(c->stream, out + 0, out + 1, 1.0, out + 2, 1.0, nullptr, 0), "L"))) return rc;
-  c->launches += 4;
-  if ((rc = adjoint_landmarks_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm, thetaT, heun, theta, s))) return rc;
-  if ((rc = adjoint_diffeo_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm, theta, heun, xp, xm, s))) return rc;
+  c->launches += 2;
+  if ((rc = adjoint_landmarks_device(c, d, ncp, pos, momt, T, sigma_def, nv, lm, thetaT, heun, theta, s, 1.0, nullptr,
+                                     ev_adj)))
+    return rc;
+  if ((rc = helper(adjoint_diffeo_device(cb, d, ncp, pos, momt, T, sigma_def, nv, lm, theta, heun, xp, xm, sb, 1.0,
+                                         ev_adj))))
+    return rc;
+  if (two) {
+    if ((rc = c->cuda(cudaEventRecord(ev_join1, c2->stream), "event record"))) return rc;
+    if ((rc = c->cuda(cudaStreamWaitEvent(c->stream, ev_join1, 0), "event wait"))) return rc;
+    c->launches += c2->launches;
+    c2->launches = 0;
+  }
   if ((rc = c->cuda(lincomb(c->stream, gmom, nullptr, -1.0, xm, -1.0, kp, n), "grad"))) return rc;
   if ((rc = c->cuda(lincomb(c->stream, gcp, nullptr, -1.0, xp, -1.0, greg, n), "grad"))) return rc;
   c->launches += 2;
@@ -100,6 +178,9 @@ int gbk_registration::body() {
 }
 
 int gbk_registration::run() {
+  if (pipeline && !c2) {  // before any capture: creates a context, buffers and events
+    if (int rc = enable_pipeline()) return rc;
+  }
   cudaStream_t saved = c->stream;
   c->stream = stream;
   int rc = GBK_OK;
@@ -141,6 +222,15 @@ void gbk_registration::drop_graph() {
 
 void gbk_registration::release() {
   drop_graph();
+  if (c2) {  // waits for the helper's stream, then frees its buffers and its own counter words
+    c2->pair_counter = c2_words;
+    c2->status = reinterpret_cast<unsigned *>(c2_words + 3);
+    gbk_destroy(c2);
+    c2 = nullptr;
+  }
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
+  ev.clear();
   for (RegObject &o : objs) o.surf.release();
   for (void *p : owned) cudaFree(p);
   owned.clear();
@@ -273,8 +363,10 @@ int gbk_registration_create(gbk_ctx *c, int d, long ncp, long nv, const double *
                             gbk_registration **out) {
   if (!c || !out) return GBK_ERR_ARG;
   c->err.clear();
-  return registration_create(c, d, ncp, 1, &data_kind, &nv, tmpl_pts, &nf, tmpl_tris, &nv_t, tgt_pts, &nf_t, tgt_tris,
-                             &sigma_data, &data_sigma2, T, sigma_def, heun, nullptr, out);
+  int rc = registration_create(c, d, ncp, 1, &data_kind, &nv, tmpl_pts, &nf, tmpl_tris, &nv_t, tgt_pts, &nf_t,
+                               tgt_tris, &sigma_data, &data_sigma2, T, sigma_def, heun, nullptr, out);
+  if (!rc) (*out)->pipeline = pipeline_default();
+  return rc;
 }
 
 int gbk_registration_create_multi(gbk_ctx *c, int d, long ncp, int nobj, const int *data_kinds, const long *nv,
@@ -284,8 +376,10 @@ int gbk_registration_create_multi(gbk_ctx *c, int d, long ncp, int nobj, const i
                                   int heun, gbk_registration **out) {
   if (!c || !out) return GBK_ERR_ARG;
   c->err.clear();
-  return registration_create(c, d, ncp, nobj, data_kinds, nv, tmpl_pts, ncell, tmpl_cells, nv_t, tgt_pts, ncell_t,
-                             tgt_cells, sigma_data, data_sigma2, T, sigma_def, heun, nullptr, out);
+  int rc = registration_create(c, d, ncp, nobj, data_kinds, nv, tmpl_pts, ncell, tmpl_cells, nv_t, tgt_pts, ncell_t,
+                               tgt_cells, sigma_data, data_sigma2, T, sigma_def, heun, nullptr, out);
+  if (!rc) (*out)->pipeline = pipeline_default();
+  return rc;
 }
 
 int gbk_registration_set_template(gbk_registration *r, const double *pts) {

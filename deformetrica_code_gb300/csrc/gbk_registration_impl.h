@@ -38,7 +38,21 @@ struct gbk_registration {
   cudaGraphExec_t exec = nullptr;
   long long graph_launches = 0;
 
+  // Pipelined iteration (pipeline = 1; the single-subject registration of gbk_registration_create).
+  // The iteration is two chains of small dependent launches twice over: the flow of the template
+  // points needs the shooting's step t only, and the control-point adjoint needs the landmark
+  // adjoint's step t only. A helper context c2 (its own stream, split partials, tickets and packed
+  // coordinates) runs the flow and the control-point adjoint one step behind, so the two chains'
+  // launches overlap; its kernel sums count into c's pair counters and report into c's status word.
+  // The helper joins the capture of `stream` through events, so the graph holds both chains.
+  int pipeline = 0;
+  gbk_ctx *c2 = nullptr;
+  unsigned long long *c2_words = nullptr;  // the helper's own counter allocation (restored on release)
+  gbk::DeformScratch s2;                   // the helper chain's temporaries
+  std::vector<cudaEvent_t> ev;             // T - 1 shooting steps, T landmark-adjoint steps, 2 joins
+
   int alloc(void **p, size_t bytes);
+  int enable_pipeline();
   int body();   // the whole iteration on `stream`, device pointers only
   int run();    // eager, then captured, then replayed
   void drop_graph();

@@ -197,6 +197,29 @@ def test_registration_step_matches_oracle_and_graph_replay(gb, ctx, K, kind):
         reg.close()
 
 
+def test_pipelined_registration_equals_serial(gb, ctx, monkeypatch):
+    """The default two-stream iteration (flow and control-point adjoint on a helper stream, one step
+    behind) gives the one-stream iteration's loglik and gradients bit for bit, eager and replayed."""
+    from deformetrica_code_gb300.deformation import Registration
+    tp, tf, gp, gf, _, _ = _meshes()
+    cp = grid_cp(3, 0.25, 0.75)
+    mom = 0.01 * np.random.default_rng(5).standard_normal(cp.shape)
+    args = dict(T=6, sigma_def=0.25, sigma_data=0.15, data_sigma2=0.01)
+    for mode, _ in modes(gb):
+        ctx.set_mode(mode)
+        res = {}
+        for pipe in ("1", "0"):
+            monkeypatch.setenv("GBK_PIPELINE", pipe)
+            reg = Registration(cp.shape[0], tp, tf, gp, gf, context=ctx, **args)
+            res[pipe] = [reg.step(cp, mom) for _ in range(3)]  # eager, capture + replay, replay
+            tr = reg.trajectories()
+            res[pipe].append([tr[k] for k in ("pos", "mom", "lm", "theta", "xi_pos", "xi_mom")])
+            reg.close()
+        for a, b in zip(res["1"], res["0"]):
+            for x, y in zip(a, b):
+                assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
 @pytest.mark.parametrize("kind", ["currents", "varifold"])
 def test_batched_atlas_matches_per_subject_oracle(gb, ctx, K, kind):
     """One batched atlas iteration over subjects with uneven target meshes equals the sum of the

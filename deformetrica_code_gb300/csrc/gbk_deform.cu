@@ -93,6 +93,21 @@ __global__ void zero_if_flag_kernel(double *p, long n, const int *flag) {
   if (i < n && *flag) p[i] = 0.0;
 }
 
+// out = base + c1 v1 + c2 v2 + c3 v3 + c4 v4, added in that order (the Heun corrector of the
+// control-point adjoint with its landmark terms kept apart)
+__global__ void lincomb4_kernel(double *out, const double *base, double c1, const double *v1, double c2,
+                                const double *v2, double c3, const double *v3, double c4, const double *v4, long n) {
+  pdl_entry();
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double r = base[i];
+  r += c1 * v1[i];
+  r += c2 * v2[i];
+  r += c3 * v3[i];
+  r += c4 * v4[i];
+  out[i] = r;
+}
+
 static unsigned blocks_for(long n, int bs = 256) { return (unsigned)std::max(1L, (n + bs - 1) / bs); }
 
 cudaError_t lincomb(cudaStream_t st, double *out, const double *base, double c1, const double *v1,
@@ -303,9 +318,9 @@ int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, con
   return GBK_OK;
 }
 
-int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
-                     const double *xp, const double *xm, long nlm, const double *lm,
-                     const double *theta, double sigma, double *dpos, double *dmom) {
+// The control-point pass of ComputeUpdateAt (OpAdjointCP: dXi3 .. dXi6), written to dpos / dmom.
+static int update_cp_pass(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, const double *xp,
+                          const double *xm, double sigma, double *dpos, double *dmom) {
   PairArgs a = pair_args(ncp, ncp, sigma);
   a.x = pos;
   a.y = pos;
@@ -321,10 +336,15 @@ int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const doubl
   a.out0_ld = d;
   a.out1 = dmom;
   a.out1_ld = d;
-  int rc = c->launch(OP_ADJCP, d, d, a);
-  if (rc || nlm <= 0) return rc;
-  // landmark part: dXi1 = ConvolveGradient(pos, mom) and dXi2 = Convolve(pos) with sources lm,
-  // weights theta (AdjointEquationsIntegrator.cxx:519-521), one fused pass, added in place
+  return c->launch(OP_ADJCP, d, d, a);
+}
+
+// The landmark pass of ComputeUpdateAt: dXi1 = ConvolveGradient(pos, mom) and dXi2 = Convolve(pos)
+// with sources lm, weights theta (AdjointEquationsIntegrator.cxx:519-521), one fused pass, written
+// to (acc = 0) or added into (acc = 1) dpos / dmom.
+static int update_landmark_pass(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, long nlm,
+                                const double *lm, const double *theta, double sigma, double *dpos, double *dmom,
+                                int acc) {
   PairArgs b = pair_args(ncp, nlm, sigma);
   b.x = pos;
   b.ta = mom;
@@ -334,40 +354,83 @@ int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const doubl
   b.w_ld = d;
   b.out0 = dmom;
   b.out0_ld = d;
-  b.acc0 = 1;
+  b.acc0 = acc;
   b.out1 = dpos;
   b.out1_ld = d;
-  b.acc1 = 1;
+  b.acc1 = acc;
   return c->launch(OP_CONV_GRADA, d, d, b);
+}
+
+int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
+                     const double *xp, const double *xm, long nlm, const double *lm,
+                     const double *theta, double sigma, double *dpos, double *dmom) {
+  int rc = update_cp_pass(c, d, ncp, pos, mom, xp, xm, sigma, dpos, dmom);
+  if (rc || nlm <= 0) return rc;
+  return update_landmark_pass(c, d, ncp, pos, mom, nlm, lm, theta, sigma, dpos, dmom, 1);
 }
 
 int adjoint_diffeo_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                           double sigma, long nlm, const double *lm, const double *theta, int heun,
                           double *xp, double *xm, const DeformScratch &s, double span,
-                          const cudaEvent_t *wait_step) {
+                          const cudaEvent_t *wait_step, const LandmarkSplit *split) {
   const long n = ncp * d, m = nlm * d;
   const double dt = span / (T - 1);
   cudaStream_t st = c->stream;
   int rc;
+  const LandmarkSplit *ls = nlm > 0 ? split : nullptr;
+  // ComputeUpdateAt at time index k into (dpos, dmom); with a split, its landmark terms go to
+  // (lpos, lmom) instead, on the split's context (concurrently, between fork / join events e, e + 1)
+  // or on this one
+  auto update = [&](long k, const double *xpk, const double *xmk, double *dpos, double *dmom, double *lpos,
+                    double *lmom, int e) -> int {
+    const double *lmk = nlm ? lm + k * m : nullptr, *thk = nlm ? theta + k * m : nullptr;
+    if (!ls) return update_at_device(c, d, ncp, pos + k * n, mom + k * n, xpk, xmk, nlm, lmk, thk, sigma, dpos, dmom);
+    gbk_ctx *cl = ls->ctx ? ls->ctx : c;
+    int r;
+    if (ls->ctx) {
+      if ((r = c->cuda(cudaEventRecord(ls->ev[e], st), "event record"))) return r;
+      if ((r = c->cuda(cudaStreamWaitEvent(cl->stream, ls->ev[e], 0), "event wait"))) return r;
+    }
+    if ((r = update_landmark_pass(cl, d, ncp, pos + k * n, mom + k * n, nlm, lmk, thk, sigma, lpos, lmom, 0))) {
+      if (cl != c) c->err = cl->err;
+      return r;
+    }
+    if (ls->ctx && (r = c->cuda(cudaEventRecord(ls->ev[e + 1], cl->stream), "event record"))) return r;
+    if ((r = update_cp_pass(c, d, ncp, pos + k * n, mom + k * n, xpk, xmk, sigma, dpos, dmom))) return r;
+    if (ls->ctx && (r = c->cuda(cudaStreamWaitEvent(st, ls->ev[e + 1], 0), "event wait"))) return r;
+    return GBK_OK;
+  };
   if (wait_step && (rc = c->cuda(cudaStreamWaitEvent(st, wait_step[T - 1], 0), "event wait"))) return rc;
   if ((rc = c->cuda(cudaMemsetAsync(xp + (T - 1) * n, 0, n * sizeof(double), st), "memset"))) return rc;
   if ((rc = c->cuda(cudaMemsetAsync(xm + (T - 1) * n, 0, n * sizeof(double), st), "memset"))) return rc;
   for (int t = T - 1; t > 0; --t) {
     if (wait_step && t < T - 1 && (rc = c->cuda(cudaStreamWaitEvent(st, wait_step[t], 0), "event wait"))) return rc;
-    if ((rc = update_at_device(c, d, ncp, pos + t * n, mom + t * n, xp + t * n, xm + t * n, nlm,
-                               nlm ? lm + t * m : nullptr, nlm ? theta + t * m : nullptr, sigma, s.va, s.vb)))
+    const int e = 4 * (T - 1 - t);
+    if ((rc = update(t, xp + t * n, xm + t * n, s.va, s.vb, ls ? ls->s.va : nullptr, ls ? ls->s.vb : nullptr, e)))
       return rc;
     double *xp1 = xp + (t - 1) * n, *xm1 = xm + (t - 1) * n;
-    if ((rc = c->cuda(lincomb(st, xp1, xp + t * n, dt, s.va, 0, nullptr, n), "euler"))) return rc;
-    if ((rc = c->cuda(lincomb(st, xm1, xm + t * n, dt, s.vb, 0, nullptr, n), "euler"))) return rc;
+    if ((rc = c->cuda(lincomb(st, xp1, xp + t * n, dt, s.va, ls ? dt : 0, ls ? ls->s.va : nullptr, n), "euler")))
+      return rc;
+    if ((rc = c->cuda(lincomb(st, xm1, xm + t * n, dt, s.vb, ls ? dt : 0, ls ? ls->s.vb : nullptr, n), "euler")))
+      return rc;
     c->launches += 2;
     if (heun) {
-      if ((rc = update_at_device(c, d, ncp, pos + (t - 1) * n, mom + (t - 1) * n, xp1, xm1, nlm,
-                                 nlm ? lm + (t - 1) * m : nullptr, nlm ? theta + (t - 1) * m : nullptr,
-                                 sigma, s.vc, s.vd)))
+      if ((rc = update(t - 1, xp1, xm1, s.vc, s.vd, ls ? ls->s.vc : nullptr, ls ? ls->s.vd : nullptr, e + 2)))
         return rc;
-      if ((rc = c->cuda(lincomb(st, xp1, xp + t * n, 0.5 * dt, s.va, 0.5 * dt, s.vc, n), "heun"))) return rc;
-      if ((rc = c->cuda(lincomb(st, xm1, xm + t * n, 0.5 * dt, s.vb, 0.5 * dt, s.vd, n), "heun"))) return rc;
+      if (ls) {
+        const double h = 0.5 * dt;
+        if ((rc = c->cuda(launch(lincomb4_kernel, blocks_for(n), 256, 0, st, xp1, xp + t * n, h, s.va, h, ls->s.va, h,
+                                 s.vc, h, ls->s.vc, n),
+                          "heun")))
+          return rc;
+        if ((rc = c->cuda(launch(lincomb4_kernel, blocks_for(n), 256, 0, st, xm1, xm + t * n, h, s.vb, h, ls->s.vb, h,
+                                 s.vd, h, ls->s.vd, n),
+                          "heun")))
+          return rc;
+      } else {
+        if ((rc = c->cuda(lincomb(st, xp1, xp + t * n, 0.5 * dt, s.va, 0.5 * dt, s.vc, n), "heun"))) return rc;
+        if ((rc = c->cuda(lincomb(st, xm1, xm + t * n, 0.5 * dt, s.vb, 0.5 * dt, s.vd, n), "heun"))) return rc;
+      }
       c->launches += 2;
     }
   }

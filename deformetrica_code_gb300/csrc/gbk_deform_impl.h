@@ -50,9 +50,19 @@ int adjoint_landmarks_device(gbk_ctx *c, int d, long ncp, const double *pos, con
 int update_at_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom,
                      const double *xp, const double *xm, long nlm, const double *lm,
                      const double *theta, double sigma, double *dpos, double *dmom);
+// The control-point adjoint's landmark terms (dXi1, dXi2 of ComputeUpdateAt) kept apart from its
+// control-point terms: the landmark pass writes s.va / s.vb (predictor) and s.vc / s.vd (corrector),
+// which the Euler and Heun updates add in. With ctx set, the landmark pass runs on that context's
+// stream concurrently with the control-point pass (events ev[4 (T-1-t) .. +3] fork and join the two
+// passes of step t); with ctx null, on the same stream (same results bit for bit).
+struct LandmarkSplit {
+  gbk_ctx *ctx = nullptr;
+  DeformScratch s{};
+  const cudaEvent_t *ev = nullptr;
+};
 int adjoint_diffeo_device(gbk_ctx *c, int d, long ncp, const double *pos, const double *mom, int T,
                           double sigma, long nlm, const double *lm, const double *theta, int heun,
                           double *xp, double *xm, const DeformScratch &s, double span = 1.0,
-                          const cudaEvent_t *wait_step = nullptr);
+                          const cudaEvent_t *wait_step = nullptr, const LandmarkSplit *split = nullptr);
 
 }  // namespace gbk

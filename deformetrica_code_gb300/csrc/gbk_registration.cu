@@ -67,35 +67,53 @@ int gbk_registration::alloc(void **p, size_t bytes) {
 // Helper context, second scratch set and events of the pipelined iteration (once per registration).
 int gbk_registration::enable_pipeline() {
   if (c2) return GBK_OK;
-  gbk_ctx *h = nullptr;
-  if (gbk_create(c->device, &h) != GBK_OK)
-    return c->fail(GBK_ERR_CUDA, "pipelined registration: helper context: %s", gbk_last_error(nullptr));
-  c2 = h;
-  // the helper's kernel sums count into this context's pair counters and report into its status word;
-  // its own words stay allocated (its spatial order would use them) and are restored on release
-  c2_words = h->pair_counter;
-  h->pair_counter = c->pair_counter;
-  h->status = c->status;
-  const long rows = std::max(ncp, nv);
   int rc = GBK_OK;
+  gbk_ctx **helpers[2] = {&c2, &c3};
+  unsigned long long **words[2] = {&c2_words, &c3_words};
+  for (int k = 0; k < 2 && !rc; ++k) {
+    gbk_ctx *h = nullptr;
+    if (gbk_create(c->device, &h) != GBK_OK) {
+      rc = c->fail(GBK_ERR_CUDA, "pipelined registration: helper context: %s", gbk_last_error(nullptr));
+      break;
+    }
+    // the helper's kernel sums count into this context's pair counters and report into its status
+    // word; its own words stay allocated (its spatial order would use them) and are restored on release
+    *helpers[k] = h;
+    *words[k] = h->pair_counter;
+    h->pair_counter = c->pair_counter;
+    h->status = c->status;
+  }
+  const long rows = std::max(ncp, nv);
   double **bufs[] = {&s2.va, &s2.vb, &s2.vc, &s2.vd};
   for (double **b : bufs)
     if (!rc) rc = alloc((void **)b, (size_t)rows * d * sizeof(double));
   if (!rc) rc = alloc((void **)&s2.flag, 16);
-  ev.assign((size_t)(2 * T + 1), nullptr);
+  ev.assign((size_t)(2 * T + 1 + 4 * (T - 1)), nullptr);
   for (cudaEvent_t &e : ev)
     if (!rc) rc = c->cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
-  if (rc) {  // no helper: the iteration stays serial
-    c2->pair_counter = c2_words;
-    c2->status = reinterpret_cast<unsigned *>(c2_words + 3);
-    gbk_destroy(c2);
-    c2 = nullptr;
-    for (cudaEvent_t e : ev)
-      if (e) cudaEventDestroy(e);
-    ev.clear();
+  if (rc) {  // no helpers: the iteration stays serial
+    drop_helpers();
     pipeline = 0;
   }
   return rc;
+}
+
+// Waits for and destroys the helper contexts (their own counter words restored first) and the events.
+void gbk_registration::drop_helpers() {
+  gbk_ctx **helpers[2] = {&c2, &c3};
+  unsigned long long *words[2] = {c2_words, c3_words};
+  for (int k = 0; k < 2; ++k) {
+    gbk_ctx *h = *helpers[k];
+    if (!h) continue;
+    h->pair_counter = words[k];
+    h->status = reinterpret_cast<unsigned *>(words[k] + 3);
+    gbk_destroy(h);
+    *helpers[k] = nullptr;
+  }
+  c2_words = c3_words = nullptr;
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
+  ev.clear();
 }
 
 int gbk_registration::body() {
@@ -110,14 +128,21 @@ int gbk_registration::body() {
   const DeformScratch &sb = two ? s2 : s;
   const cudaEvent_t *ev_shoot = two ? ev.data() : nullptr, *ev_adj = two ? ev.data() + (T - 1) : nullptr;
   const cudaEvent_t ev_join0 = two ? ev[2 * T - 1] : nullptr, ev_join1 = two ? ev[2 * T] : nullptr;
-  if (two) {  // the helper launches as this context would
-    c2->mode = c->mode;
-    c2->order = c->order;
-    c2->force_split = c->force_split;
-    c2->staging = c->staging;
-    c2->tune = c->tune;
-    c2->err.clear();
+  if (two) {  // the helpers launch as this context would
+    for (gbk_ctx *h : {c2, c3}) {
+      h->mode = c->mode;
+      h->order = c->order;
+      h->force_split = c->force_split;
+      h->staging = c->staging;
+      h->tune = c->tune;
+      h->err.clear();
+    }
   }
+  // the control-point adjoint's landmark passes: beside its control-point passes on c3 when pipelined
+  LandmarkSplit ls;
+  ls.s = s3;
+  ls.ctx = two ? c3 : nullptr;
+  ls.ev = two ? ev.data() + (2 * T + 1) : nullptr;
   auto helper = [&](int r) {  // a failure of the helper chain, reported in this context
     if (r && two) c->err = c2->err;
     return r;
@@ -163,13 +188,13 @@ int gbk_registration::body() {
                                      ev_adj)))
     return rc;
   if ((rc = helper(adjoint_diffeo_device(cb, d, ncp, pos, momt, T, sigma_def, nv, lm, theta, heun, xp, xm, sb, 1.0,
-                                         ev_adj))))
+                                         ev_adj, &ls))))
     return rc;
-  if (two) {
+  if (two) {  // (c3's passes are joined into c2's stream step by step)
     if ((rc = c->cuda(cudaEventRecord(ev_join1, c2->stream), "event record"))) return rc;
     if ((rc = c->cuda(cudaStreamWaitEvent(c->stream, ev_join1, 0), "event wait"))) return rc;
-    c->launches += c2->launches;
-    c2->launches = 0;
+    c->launches += c2->launches + c3->launches;
+    c2->launches = c3->launches = 0;
   }
   if ((rc = c->cuda(lincomb(c->stream, gmom, nullptr, -1.0, xm, -1.0, kp, n), "grad"))) return rc;
   if ((rc = c->cuda(lincomb(c->stream, gcp, nullptr, -1.0, xp, -1.0, greg, n), "grad"))) return rc;
@@ -222,15 +247,7 @@ void gbk_registration::drop_graph() {
 
 void gbk_registration::release() {
   drop_graph();
-  if (c2) {  // waits for the helper's stream, then frees its buffers and its own counter words
-    c2->pair_counter = c2_words;
-    c2->status = reinterpret_cast<unsigned *>(c2_words + 3);
-    gbk_destroy(c2);
-    c2 = nullptr;
-  }
-  for (cudaEvent_t e : ev)
-    if (e) cudaEventDestroy(e);
-  ev.clear();
+  drop_helpers();
   for (RegObject &o : objs) o.surf.release();
   for (void *p : owned) cudaFree(p);
   owned.clear();
@@ -326,7 +343,8 @@ int registration_create(gbk_ctx *c, int d, long ncp, int nobj, const int *kinds,
               {&r->gcp, (size_t)n}, {&r->gmom, (size_t)n}, {&r->out, (size_t)8 + nobj},
               {&r->sigma2_dev, (size_t)nobj}, {&r->tgt, (size_t)nv_t * d},
               {&r->s.va, (size_t)rows * d}, {&r->s.vb, (size_t)rows * d}, {&r->s.vc, (size_t)rows * d},
-              {&r->s.vd, (size_t)rows * d}};
+              {&r->s.vd, (size_t)rows * d}, {&r->s3.va, (size_t)n}, {&r->s3.vb, (size_t)n}, {&r->s3.vc, (size_t)n},
+              {&r->s3.vd, (size_t)n}};
   for (auto &b : bufs)
     if (!rc) rc = r->alloc((void **)b.p, b.count * sizeof(double));
   if (!rc) rc = r->alloc((void **)&r->s.flag, 16);

@@ -43,16 +43,21 @@ struct gbk_registration {
   // points needs the shooting's step t only, and the control-point adjoint needs the landmark
   // adjoint's step t only. A helper context c2 (its own stream, split partials, tickets and packed
   // coordinates) runs the flow and the control-point adjoint one step behind, so the two chains'
-  // launches overlap; its kernel sums count into c's pair counters and report into c's status word.
-  // The helper joins the capture of `stream` through events, so the graph holds both chains.
+  // launches overlap, and a second helper c3 runs each control-point adjoint update's landmark pass
+  // beside its control-point pass. The helpers' kernel sums count into c's pair counters and report
+  // into c's status word; they join the capture of `stream` through events, so the graph holds every
+  // chain. The landmark terms are kept apart (s3) whether or not the iteration is pipelined.
   int pipeline = 0;
-  gbk_ctx *c2 = nullptr;
-  unsigned long long *c2_words = nullptr;  // the helper's own counter allocation (restored on release)
-  gbk::DeformScratch s2;                   // the helper chain's temporaries
-  std::vector<cudaEvent_t> ev;             // T - 1 shooting steps, T landmark-adjoint steps, 2 joins
+  gbk_ctx *c2 = nullptr, *c3 = nullptr;
+  unsigned long long *c2_words = nullptr, *c3_words = nullptr;  // the helpers' own counter allocations
+  gbk::DeformScratch s2;  // the helper chain's temporaries
+  gbk::DeformScratch s3;  // the control-point adjoint's landmark terms (predictor va/vb, corrector vc/vd)
+  // T - 1 shooting steps, T landmark-adjoint steps, 2 joins, 4 (T - 1) landmark-pass forks and joins
+  std::vector<cudaEvent_t> ev;
 
   int alloc(void **p, size_t bytes);
   int enable_pipeline();
+  void drop_helpers();
   int body();   // the whole iteration on `stream`, device pointers only
   int run();    // eager, then captured, then replayed
   void drop_graph();

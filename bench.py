@@ -234,7 +234,10 @@ def registration_bench(steps: int, cpu: bool = True):
     import deformetrica_code_gb300 as g
     from deformetrica_code_gb300.deformation import Registration
     cp, mom, tp, tf, gp, gf, kw = registration_workload()
-    res = {"workload": "1000 CP x 10242-vertex icosphere, T=11, sigma_def 0.15, currents sigma 0.1"}
+    res = {"workload": "1000 CP x 10242-vertex icosphere, T=11, sigma_def 0.15, currents sigma 0.1",
+           # the iteration's streams (GBK_PIPELINE=0: one) and programmatic dependent launch (GBK_PDL=0: off)
+           "streams": 1 if os.environ.get("GBK_PIPELINE", "1")[:1] == "0" else 3,
+           "programmatic_launch": os.environ.get("GBK_PDL", "1")[:1] != "0"}
     for name, mode, nsteps in (("f32c", g.GBK_MODE_F32C, steps), ("f64", g.GBK_MODE_F64, max(2, steps // 4))):
         ctx = g.Context(mode=mode)
         reg = Registration(cp.shape[0], tp, tf, gp, gf, context=ctx, **kw)

@@ -203,9 +203,9 @@ int gbk_registration::body() {
 }
 
 int gbk_registration::run() {
-  if (pipeline && !c2) {  // before any capture: creates a context, buffers and events
-    if (int rc = enable_pipeline()) return rc;
-  }
+  // before any capture: creates the helper contexts, buffers and events; if that fails (e.g. no device
+  // memory left), the iteration runs on one stream (same results) and the message is dropped
+  if (pipeline && !c2 && enable_pipeline() != GBK_OK) c->err.clear();
   cudaStream_t saved = c->stream;
   c->stream = stream;
   int rc = GBK_OK;

@@ -175,7 +175,10 @@ int gbk_mo_atlas_create(gbk_ctx *c, int d, long ncp, int nobj, const int *data_k
     rc = registration_create(c, d, ncp, nobj, data_kinds, nv, tmpl_pts, ncell, tmpl_cells, nv_t + (long)s * nobj,
                              tgt_pts + pt_off * d, ncell_t + (long)s * nobj, tgt_cells ? tgt_cells + cell_off : nullptr,
                              sigma_data, data_sigma2, T, sigma_def, heun, a->stream, &r);
-    if (!rc) a->subj.push_back(r);
+    if (!rc) {
+      r->pipeline = pipeline_default();  // each subject's iteration on three streams, as a registration's
+      a->subj.push_back(r);
+    }
     pt_off += pts;
     cell_off += cells;
   }

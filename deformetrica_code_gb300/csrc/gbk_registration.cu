@@ -33,13 +33,14 @@
 
 using namespace gbk;
 
-namespace {
-
-// Single-subject registrations run their iteration pipelined on two streams unless GBK_PIPELINE=0.
+namespace gbk {
 int pipeline_default() {
   const char *e = getenv("GBK_PIPELINE");
   return e && e[0] == '0' ? 0 : 1;
 }
+}  // namespace gbk
+
+namespace {
 
 // L_data = 0.5 * (-sum_k match_k / sigma2_k) in object order (DeterministicAtlas.cxx:121-125) and
 // the sum of the matches

@@ -38,7 +38,8 @@ struct gbk_registration {
   cudaGraphExec_t exec = nullptr;
   long long graph_launches = 0;
 
-  // Pipelined iteration (pipeline = 1; the single-subject registration of gbk_registration_create).
+  // Pipelined iteration (pipeline = 1: the registrations of gbk_registration_create and the subjects
+  // of the multi-object atlas).
   // The iteration is two chains of small dependent launches twice over: the flow of the template
   // points needs the shooting's step t only, and the control-point adjoint needs the landmark
   // adjoint's step t only. A helper context c2 (its own stream, split partials, tickets and packed
@@ -65,6 +66,10 @@ struct gbk_registration {
 };
 
 namespace gbk {
+
+// Registrations run their iteration pipelined on three streams unless GBK_PIPELINE=0 (the value for
+// gbk_registration::pipeline).
+int pipeline_default();
 
 // Creates a registration with nobj template objects: object k has kinds[k] (data_kind of
 // gbk_registration_create), nv[k] template points (concatenated in tmpl_pts) and nf[k] cells

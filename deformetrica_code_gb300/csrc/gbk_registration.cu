@@ -136,6 +136,7 @@ int gbk_registration::body() {
       h->force_split = c->force_split;
       h->staging = c->staging;
       h->tune = c->tune;
+      h->alloc_limit = c->alloc_limit;  // an injected allocation limit applies to the helpers too
       h->err.clear();
     }
   }

@@ -333,7 +333,10 @@ typedef struct gbk_registration gbk_registration;
  * (triangles, d = 3), 2 = curve currents, 3 = curve varifold (2-point segments, d = 2 or 3),
  * 4 = point cloud (nf = nv, nf_t = nv_t, the cell arrays are ignored and may be NULL; unit weights
  * until gbk_registration_set_point_weights), 5 = volume mesh (cells of d + 1 vertices), 6 =
- * landmarks (nv_t = nv, cells ignored). All device memory is allocated here. */
+ * landmarks (nv_t = nv, cells ignored). All device memory is allocated here, except that the first
+ * step creates two helper contexts (streams and small buffers, destroyed with the registration) so
+ * that the iteration runs on three streams, one step apart; GBK_PIPELINE=0 in the environment at
+ * creation keeps one stream (same results bit for bit). */
 int gbk_registration_create(gbk_ctx *ctx, int d, long ncp, long nv, const double *tmpl_pts,
                             long nf, const int *tmpl_tris, long nv_t, const double *tgt_pts,
                             long nf_t, const int *tgt_tris, int T, double sigma_def,
